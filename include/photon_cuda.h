@@ -1,0 +1,311 @@
+/*
+ * photon_cuda.h — C-ABI of libphoton_cuda.so, the GB300 (sm_103a) wavefront
+ * path tracer that stands in for Photon's ray back-ends and path tracer.
+ *
+ * Two levels of drop-in, both from Photon (jar091/photon):
+ *
+ *   Level B, the renderer seam.  Each phc_* renderer call replaces one method
+ *   of photon::bridge::Renderer (src/photon/anari/RenderBridge.h:175-214) with
+ *   the same argument meaning: scene upload, render(frame) with progressive
+ *   accumulation, and the colour / depth / normal / albedo channels the ANARI
+ *   device maps (src/photon/anari/Frame.cpp:139-241).  The structs below are
+ *   plain-old-data mirrors of bridge::SceneData, CameraData and RenderSettings
+ *   (RenderBridge.h:21-170): pointers plus counts instead of std::vector.
+ *
+ *   Level A, the ray back-end.  phc_accel_* and phc_trace_* replace
+ *   photon::pt::RayBackend::build_accel / trace_closest / trace_occluded
+ *   (include/photon/pt/backend/ray_backend.h:44-54) on device pointers, the
+ *   way the reference's OptiX back-end binds Kokkos::View::data()
+ *   (src/photon/pt/backend/optix_backend.cpp:724-814).
+ *
+ * Conventions (reference: RenderBridge.cpp:83-110, 274-281):
+ *   - every call returns PHC_OK (0) or a negative PHC_ERR_* code, and the
+ *     message of the last failure is kept per object (phc_last_error) or per
+ *     thread for calls without an object (phc_global_error);
+ *   - the caller owns every host buffer it passes; set_scene copies the scene
+ *     at call time; the library owns all device memory it allocates;
+ *   - calls on one renderer are serialised by the caller (one at a time, from
+ *     any thread) and block until their device work is done, as
+ *     bridge::Renderer's methods do (RenderBridge.h:172-174).
+ */
+#ifndef PHOTON_CUDA_H
+#define PHOTON_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHC_ABI_VERSION 1
+
+enum {
+  PHC_OK = 0,
+  PHC_ERR_INVALID = -1,    /* bad argument (null pointer, size 0, bad enum)   */
+  PHC_ERR_CUDA = -2,       /* a CUDA runtime call failed                       */
+  PHC_ERR_NO_SCENE = -3,   /* render before set_scene                          */
+  PHC_ERR_NO_FRAME = -4,   /* read_* before any render (RenderBridge.cpp:1089) */
+  PHC_ERR_OOM = -5,        /* device allocation failed                         */
+  PHC_ERR_DEVICE = -6,     /* a kernel reported an error word (iteration cap,
+                              queue overflow); the context stays usable        */
+  PHC_ERR_LIMIT = -7       /* size beyond a documented maximum                 */
+};
+
+typedef struct phc_renderer phc_renderer;
+typedef struct phc_accel phc_accel;
+
+/* Mirrors bridge::ParamSourceData (RenderBridge.h:21-25). */
+typedef struct phc_param_source {
+  int32_t kind;  /* 0 constant, 1 vertex attribute, 2 sampler */
+  int32_t index; /* attribute slot (0..3, 4 colour, 5 world position,
+                    6 world normal) or sampler index */
+} phc_param_source;
+
+/* Mirrors bridge::MaterialData (RenderBridge.h:27-56); phc_material_default
+   fills the reference's defaults. */
+typedef struct phc_material {
+  float base_color[3];
+  float opacity;
+  float metallic;
+  float roughness; /* perceptual: the GGX alpha is its square (RenderBridge.cpp:330) */
+  float ior;
+  float transmission;
+  float specular;  /* 0..1, becomes Disney specular 0.5*s (RenderBridge.cpp:334) */
+  float emission[3];
+  float clearcoat;
+  float clearcoat_roughness;
+  float sheen;
+  phc_param_source base_color_src;
+  phc_param_source opacity_src;
+  phc_param_source metallic_src;
+  phc_param_source roughness_src;
+  phc_param_source emission_src;
+  phc_param_source transmission_src;
+  phc_param_source normal_src;
+  int32_t alpha_mode; /* 0 blend, 1 opaque, 2 mask */
+  float alpha_cutoff;
+  int32_t base_color_alpha;
+  int32_t thin_walled;
+  int32_t emitter_only;
+  int32_t hidden_to_camera;
+  int32_t emission_side; /* 0 front, 1 back, 2 both */
+} phc_material;
+
+/* Mirrors bridge::SamplerData (RenderBridge.h:58-71). */
+typedef struct phc_sampler {
+  int32_t type; /* 0 image1D, 1 image2D, 2 image3D, 3 transform */
+  int32_t in_attribute;
+  int32_t linear;
+  int32_t wrap[3]; /* 0 clampToEdge, 1 repeat, 2 mirrorRepeat */
+  uint32_t size[3];
+  float in_transform[16];  /* row-major */
+  float in_offset[4];
+  float out_transform[16]; /* row-major */
+  float out_offset[4];
+  const float *texels;     /* RGBA, texel_count texels (may be short: the
+                              sampler then degrades to a transform, as in
+                              RenderBridge.cpp:559-562) */
+  uint64_t texel_count;
+} phc_sampler;
+
+/* Mirrors bridge::LightData (RenderBridge.h:73-85). */
+typedef struct phc_light {
+  int32_t type; /* 0 point, 1 directional, 2 spot */
+  float position[3];
+  float direction[3];
+  float color[3];
+  float intensity;
+  float radius;
+  float spot_angle;
+  float spot_falloff;
+} phc_light;
+
+/* Mirrors bridge::EnvironmentData (RenderBridge.h:87-97). */
+typedef struct phc_environment {
+  int32_t present;
+  int32_t visible;
+  uint32_t width;
+  uint32_t height;
+  const float *pixels; /* RGB radiance, width*height*3, row 0 = bottom row */
+  float world_to_map[9];
+} phc_environment;
+
+/* Mirrors bridge::VolumeData (RenderBridge.h:99-110). */
+typedef struct phc_volume {
+  float world_to_local[12]; /* row-major 3x4 */
+  float origin[3];
+  float spacing[3];
+  uint32_t dims[3];
+  const float *values; /* x fastest */
+  uint64_t value_count;
+  const float *transfer; /* RGBA entries */
+  uint32_t transfer_count; /* number of RGBA entries */
+  float value_range[2];
+  float density_scale;
+  int32_t linear;
+} phc_volume;
+
+/* Mirrors bridge::SceneData (RenderBridge.h:112-126). */
+typedef struct phc_scene_desc {
+  const float *positions; /* xyz per vertex */
+  uint64_t vertex_count;
+  const float *normals;   /* xyz per vertex or NULL */
+  const float *attributes[5]; /* RGBA per vertex or NULL */
+  const uint32_t *indices; /* three per triangle */
+  uint64_t triangle_count;
+  const uint32_t *material_ids; /* one per triangle, material_id_count of them */
+  uint64_t material_id_count;
+  const phc_material *materials;
+  uint32_t material_count;
+  const phc_sampler *samplers;
+  uint32_t sampler_count;
+  const phc_light *lights;
+  uint32_t light_count;
+  phc_environment environment;
+  const phc_volume *volumes;
+  uint32_t volume_count;
+} phc_scene_desc;
+
+/* Mirrors bridge::CameraData (RenderBridge.h:128-144). */
+typedef struct phc_camera {
+  float position[3];
+  float direction[3];
+  float up[3];
+  int32_t orthographic;
+  float fovy; /* radians */
+  float height;
+  float aspect; /* <= 0: width / height */
+  float aperture_radius;
+  float focus_distance;
+  float image_region[4];
+  float clip_near;
+  float clip_far; /* >= 1e30 or +inf: no far plane */
+} phc_camera;
+
+/* Mirrors bridge::RenderSettings (RenderBridge.h:146-170). */
+typedef struct phc_settings {
+  uint32_t width;
+  uint32_t height;
+  uint32_t pixel_samples;
+  uint32_t max_depth;
+  float background[4];
+  const float *background_image; /* RGBA, rows from the bottom, or NULL */
+  uint32_t background_width;
+  uint32_t background_height;
+  float ambient_color[3];
+  float ambient_radiance;
+  int32_t adaptive_sampling;
+  float throughput_clamp;
+  int32_t max_diffuse_bounces;
+  int32_t max_glossy_bounces;
+  int32_t max_transmission_bounces;
+  int32_t max_volume_bounces;
+  float clamp_direct;
+  float clamp_indirect;
+} phc_settings;
+
+/* Counters of the last render call, read by phc_render_stats. */
+typedef struct phc_render_stats {
+  uint64_t pixel_samples;   /* pixel-samples traced (adaptive: started ones)  */
+  uint64_t closest_rays;    /* rays given to closest-hit traversal            */
+  uint64_t shadow_rays;     /* rays given to any-hit traversal                */
+  uint64_t node_visits;     /* BVH8 nodes visited (when counters are enabled) */
+  uint64_t tri_tests;       /* triangle tests (when counters are enabled)     */
+  double render_ms;         /* device time of the render call                 */
+} phc_render_stats;
+
+/* ------------------------------------------------------------------ defaults */
+/* Fill the bridge's default values (RenderBridge.h:27-170). */
+void phc_material_default(phc_material *m);
+void phc_sampler_default(phc_sampler *s);
+void phc_light_default(phc_light *l);
+void phc_volume_default(phc_volume *v);
+void phc_camera_default(phc_camera *c);
+void phc_settings_default(phc_settings *s);
+void phc_scene_desc_default(phc_scene_desc *d);
+
+int phc_abi_version(void);
+/* Message of the last failure on this thread for calls without an object. */
+const char *phc_global_error(void);
+
+/* ------------------------------------------------------- Level B (renderer) */
+/* bridge::Renderer::Renderer + initialize (RenderBridge.cpp:1012-1034):
+   selects the current CUDA device and creates the renderer's stream. */
+int phc_create(phc_renderer **out);
+/* bridge::Renderer::~Renderer (RenderBridge.cpp:949-965). */
+void phc_destroy(phc_renderer *r);
+/* bridge::Renderer::backend_name (RenderBridge.cpp:1036-1039): "cuda". */
+const char *phc_backend_name(const phc_renderer *r);
+/* bridge::Renderer::set_scene (RenderBridge.cpp:1046-1058, scene build
+   441-826): uploads the scene, builds the BVH8 and the light tables.
+   Drops the accumulated frame. */
+int phc_set_scene(phc_renderer *r, const phc_scene_desc *scene);
+/* bridge::Renderer::render (RenderBridge.cpp:1060-1075, 828-928): renders
+   settings->pixel_samples more samples per pixel; reset != 0 drops the
+   accumulated ones. */
+int phc_render(phc_renderer *r, const phc_camera *camera, const phc_settings *settings, int reset);
+/* bridge::Renderer::accumulated_samples (RenderBridge.cpp:1077-1080). */
+uint32_t phc_accumulated_samples(const phc_renderer *r);
+/* bridge::Renderer::read_color / read_depth / read_normal / read_albedo
+   (RenderBridge.cpp:1082-1172): caller-owned host buffers of width*height
+   RGBA / 1 / 3 / 3 floats, row 0 = bottom row; depth is +inf on a miss. */
+int phc_read_color(phc_renderer *r, float *rgba);
+int phc_read_depth(phc_renderer *r, float *depth);
+int phc_read_normal(phc_renderer *r, float *xyz);
+int phc_read_albedo(phc_renderer *r, float *rgb);
+/* Counters of the last phc_render call. */
+int phc_render_stats_get(const phc_renderer *r, phc_render_stats *out);
+/* Message of the last failed call on this renderer ("" when none). */
+const char *phc_last_error(const phc_renderer *r);
+
+/* -------------------------------------------------- Level A (ray back-end) */
+/* Hit record of Level A, field for field photon::pt::HitResult
+   (include/photon/pt/backend/ray_backend.h:15-29), 88 bytes. */
+typedef struct phc_hit_result {
+  float t;
+  float position[3];
+  float normal[3];
+  float shading_normal[3];
+  float uv[2];
+  float bary[2];
+  float interpolated_color[3];
+  uint32_t prim_id;
+  uint32_t geom_id;
+  uint32_t inst_id;
+  uint32_t material_id;
+  uint8_t hit;
+  uint8_t has_interpolated_color;
+  uint8_t pad_[2];
+} phc_hit_result;
+
+/* RayBackend::build_accel (kokkos_backend.cpp:11-19): builds the BVH8 over
+   an indexed triangle mesh given in host memory (positions xyz, indices,
+   optional normals xyz and material ids). */
+int phc_accel_create(phc_accel **out, const float *positions, uint64_t vertex_count, const uint32_t *indices,
+    uint64_t triangle_count, const float *normals, const uint32_t *material_ids);
+void phc_accel_destroy(phc_accel *a);
+/* RayBackend::trace_closest (kokkos_backend.cpp:21-61) on device pointers:
+   origins/directions are xyz float triples (RayBatch, ray_backend.h:31-37),
+   tmin/tmax one float each; a ray with !(tmax > tmin) misses.  Writes n
+   phc_hit_result records.  stream is a cudaStream_t (NULL: the library's). */
+int phc_trace_closest(phc_accel *a, const float *origins, const float *directions, const float *tmin,
+    const float *tmax, uint32_t n, phc_hit_result *hits, void *stream);
+/* The same traversal with the compact 16-byte hit record the renderer uses:
+   hits4[i] = (t, prim_id bits, u, v); prim_id = 0xffffffff on a miss. */
+int phc_trace_closest_compact(phc_accel *a, const float *origins, const float *directions, const float *tmin,
+    const float *tmax, uint32_t n, float *hits4, void *stream);
+/* RayBackend::trace_occluded (kokkos_backend.cpp:63-86): occluded[i] = 1 when
+   anything is hit in [tmin, tmax]. */
+int phc_trace_occluded(phc_accel *a, const float *origins, const float *directions, const float *tmin,
+    const float *tmax, uint32_t n, uint32_t *occluded, void *stream);
+/* Node visits and triangle tests of the last trace call (counting build). */
+int phc_accel_counters(const phc_accel *a, uint64_t *node_visits, uint64_t *tri_tests);
+/* Size in bytes of the device BVH8 nodes, triangle records and node count. */
+int phc_accel_info(const phc_accel *a, uint64_t *node_bytes, uint64_t *tri_bytes, uint64_t *node_count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHOTON_CUDA_H */

@@ -1,0 +1,162 @@
+"""CPU oracles for the path-tracing hot path (TEST INFRASTRUCTURE ONLY).
+
+Two shared libraries, both built by oracle/Makefile:
+
+* ``_ref/libphoton_ref.so`` — Photon's own sources (pathtracer.cpp, bvh.cpp,
+  kokkos_backend.cpp, environment_map.cpp, RenderBridge.cpp) compiled
+  unmodified against the project's Kokkos stand-in.  Exists only where the
+  reference checkout was present at build time (not on the GPU host).
+* ``_build/libphoton_oracle.so`` — the project's CPU restatement of the same
+  algorithm (photon_oracle.cpp), bit-identical to the reference on the same
+  compiler and flags; it builds anywhere.
+
+Both expose the same renderer calls (create / set_scene / render / read_*),
+plus Level-A tracing and BSDF probes.  Only tests/, __graft_entry__.smoke()
+and bench.py's CPU-baseline leg may use this package; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_LIB = os.path.join(HERE, "_ref", "libphoton_ref.so")
+ORACLE_LIB = os.path.join(HERE, "_build", "libphoton_oracle.so")
+REFERENCE_DIR = os.environ.get("PHOTON_REFERENCE_DIR", "/root/reference")
+
+
+def build(ref: bool | None = None, jobs: int = 8, quiet: bool = True):
+    """Build the restatement (always) and the reference oracle (when the
+    reference checkout exists, or when ref=True)."""
+    if ref is None:
+        ref = os.path.isdir(os.path.join(REFERENCE_DIR, "src", "photon", "pt"))
+    targets = ["oracle"] + (["ref"] if ref else [])
+    out = subprocess.run(["make", "-C", HERE, f"-j{jobs}", f"REF={REFERENCE_DIR}"] + targets,
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout[-4000:] + out.stderr[-4000:])
+    return targets
+
+
+_libs = {}
+
+
+def _load(path, prefix):
+    if path in _libs:
+        return _libs[path]
+    if not os.path.exists(path):
+        raise FileNotFoundError(path)
+    lib = C.CDLL(path)
+    vp, cp = C.c_void_p, C.c_char_p
+    fn = lambda n: getattr(lib, prefix + n)  # noqa: E731
+    fn("renderer_create").restype = vp
+    fn("renderer_create").argtypes = []
+    fn("renderer_destroy").argtypes = [vp]
+    fn("last_error").restype = cp
+    fn("last_error").argtypes = [vp]
+    fn("set_scene").argtypes = [vp, vp]
+    fn("render").argtypes = [vp, vp, vp, C.c_int]
+    fn("accumulated_samples").restype = C.c_uint32
+    fn("accumulated_samples").argtypes = [vp]
+    for ch in ("color", "depth", "normal", "albedo"):
+        fn("read_" + ch).argtypes = [vp, vp]
+    fn("trace").argtypes = [vp, C.c_uint64, vp, C.c_uint64, vp, vp, vp, vp, vp, vp, C.c_uint32, C.c_int, vp, vp]
+    fn("bsdf_probe").argtypes = [vp, vp, vp, vp, vp, vp, C.c_uint32, vp, vp]
+    _libs[path] = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class CpuRenderer:
+    """bridge::Renderer-shaped wrapper over one of the two oracle libraries."""
+
+    def __init__(self, which: str = "oracle"):
+        self.which = which
+        self.prefix = "ref_" if which == "ref" else "orc_"
+        self.lib = _load(REF_LIB if which == "ref" else ORACLE_LIB, self.prefix)
+        self.h = self._fn("renderer_create")()
+        if not self.h:
+            raise RuntimeError(f"{which}: renderer_create failed")
+        self.width = self.height = 0
+        self._keep = None
+
+    def _fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    def close(self):
+        if self.h:
+            self._fn("renderer_destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{self.which} {what}: {self._fn('last_error')(self.h).decode()}")
+
+    def set_scene(self, scene):
+        desc, keep = scene.desc()
+        self._keep = (desc, keep)
+        self._check(self._fn("set_scene")(self.h, C.addressof(desc)), "set_scene")
+
+    def render(self, cam, settings, reset=True):
+        self.width, self.height = settings.width, settings.height
+        self._check(self._fn("render")(self.h, C.addressof(cam), C.addressof(settings), int(reset)), "render")
+
+    def accumulated_samples(self):
+        return self._fn("accumulated_samples")(self.h)
+
+    def read(self, channel):
+        n = {"color": 4, "depth": 1, "normal": 3, "albedo": 3}[channel]
+        out = np.empty((self.height, self.width, n), np.float32)
+        self._check(self._fn("read_" + channel)(self.h, out.ctypes.data), "read_" + channel)
+        return out[..., 0] if n == 1 else out
+
+
+def trace(which, positions, indices, orgs, dirs, tmin, tmax, any_hit=False, normals=None, material_ids=None):
+    """Level-A trace through the reference's KokkosBackend ('ref') or the
+    restatement ('oracle'); returns the HitResult records or occluded flags."""
+    from photon_gb300 import _abi
+    prefix = "ref_" if which == "ref" else "orc_"
+    lib = _load(REF_LIB if which == "ref" else ORACLE_LIB, prefix)
+    pos = np.ascontiguousarray(positions, np.float32)
+    idx = np.ascontiguousarray(indices, np.uint32)
+    o = np.ascontiguousarray(orgs, np.float32)
+    d = np.ascontiguousarray(dirs, np.float32)
+    t0 = np.ascontiguousarray(tmin, np.float32)
+    t1 = np.ascontiguousarray(tmax, np.float32)
+    nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+    mid = None if material_ids is None else np.ascontiguousarray(material_ids, np.uint32)
+    n = len(t0)
+    hits = np.zeros(n, _abi.hit_dtype())
+    occ = np.zeros(n, np.uint32)
+    rc = getattr(lib, prefix + "trace")(
+        _ptr(pos), pos.size // 3, _ptr(idx), idx.size // 3, _ptr(nrm), _ptr(mid), _ptr(o), _ptr(d), _ptr(t0),
+        _ptr(t1), n, int(any_hit), hits.ctypes.data, occ.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("trace failed")
+    return occ if any_hit else hits
+
+
+def bsdf_probe(which, material, n_geo, n_shade, wo, wi, seeds):
+    """Disney BSDF eval/pdf/sample at n cases (see ref_harness.cpp)."""
+    prefix = "ref_" if which == "ref" else "orc_"
+    lib = _load(REF_LIB if which == "ref" else ORACLE_LIB, prefix)
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (n_geo, n_shade, wo, wi)]
+    s = np.ascontiguousarray(seeds, np.uint32)
+    n = len(s)
+    out = np.zeros((n, 8), np.float32)
+    out2 = np.zeros((n, 4), np.float32)
+    getattr(lib, prefix + "bsdf_probe")(C.addressof(material), *[a.ctypes.data for a in arrs], s.ctypes.data, n,
+                                        out.ctypes.data, out2.ctypes.data)
+    return out, out2

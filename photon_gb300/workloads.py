@@ -1,0 +1,499 @@
+"""Seeded synthetic workloads.
+
+The reference's published numbers are on Bitterli pbrt-v4 scenes that are not
+available offline; these generators stand in for them with the shapes, sizes
+and value ranges of the five workloads the project is measured on:
+
+  box_room          ~36 triangles, 5 diffuse walls, two rotated boxes, a
+                    0.25 m^2 quad light of radiance (17, 12, 4); 512^2, 64 spp,
+                    depth 8.
+  procedural_500k   200 displaced icospheres and tori on a ground plane
+                    (~500K triangles), per-object Disney parameters, a
+                    1024x512 fp32 sun+sky environment map and 4 emissive
+                    triangles; 1024^2, 128 spp, depth 8.
+  instanced_2m      ~2M triangles (instances flattened, as the reference
+                    does), 12 RGBA8 2048^2 value-noise textures, emissive
+                    meshes and a 256^3 fBm density grid; 1920^2, 256 spp,
+                    depth 12, adaptive sampling.
+  batched_jobs      64 independent small renders of uneven size.
+  differentiable    50K triangles, 8 textured materials, homogeneous medium.
+
+Geometry and parameters come from numpy's PCG64 with the given seed; the
+path sampling itself uses the reference's per-(pixel, sample, dimension)
+hash streams, sample offset 0.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _abi
+from .scene import SceneData, camera, settings
+
+# ----------------------------------------------------------------- primitives
+
+
+def _quad(p0, p1, p2, p3):
+    """Two triangles (p0, p1, p2), (p0, p2, p3)."""
+    return np.array([p0, p1, p2, p3], np.float32), np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+
+
+def _box(center, size, angle_deg, bottom=True):
+    """Axis-aligned box rotated about +y; 10 or 12 triangles."""
+    cx, cy, cz = center
+    sx, sy, sz = size
+    c, s = np.cos(np.deg2rad(angle_deg)), np.sin(np.deg2rad(angle_deg))
+    corners = []
+    for y in (0.0, sy):
+        for (x, z) in ((-sx / 2, -sz / 2), (sx / 2, -sz / 2), (sx / 2, sz / 2), (-sx / 2, sz / 2)):
+            corners.append((cx + c * x + s * z, cy + y, cz - s * x + c * z))
+    v = np.array(corners, np.float32)
+    faces = [
+        (4, 7, 6, 5),  # top, normal +y
+        (0, 1, 5, 4), (1, 2, 6, 5), (2, 3, 7, 6), (3, 0, 4, 7),  # sides
+    ]
+    if bottom:
+        faces.append((0, 3, 2, 1))
+    idx = []
+    for a, b, cc, d in faces:
+        idx += [[a, b, cc], [a, cc, d]]
+    return v, np.array(idx, np.uint32)
+
+
+class _MeshBuilder:
+    def __init__(self):
+        self.pos, self.idx, self.mat, self.nrm = [], [], [], []
+        self.count = 0
+        self.with_normals = False
+
+    def add(self, v, i, mat, n=None):
+        self.pos.append(np.asarray(v, np.float32))
+        self.idx.append(np.asarray(i, np.uint32) + self.count)
+        self.mat.append(np.full(len(i), mat, np.uint32))
+        if n is None:
+            n = np.zeros_like(v, dtype=np.float32)
+        else:
+            self.with_normals = True
+        self.nrm.append(np.asarray(n, np.float32))
+        self.count += len(v)
+
+    def build(self, **kw):
+        return SceneData(
+            positions=np.concatenate(self.pos), indices=np.concatenate(self.idx),
+            material_ids=np.concatenate(self.mat),
+            normals=np.concatenate(self.nrm) if self.with_normals else None, **kw)
+
+
+def diffuse(rgb):
+    m = _abi.material_default()
+    m.base_color[:] = rgb
+    m.roughness = 1.0
+    return m
+
+
+def emitter(radiance, both_sides=False):
+    m = _abi.material_default()
+    m.base_color[:] = (0.0, 0.0, 0.0)
+    m.emission[:] = radiance
+    m.emitter_only = 1
+    m.emission_side = 2 if both_sides else 0
+    return m
+
+
+# ------------------------------------------------------------------ box room
+
+
+def box_room():
+    """Box room: 5 quads, two rotated boxes, a 0.5 x 0.5 m quad light."""
+    mb = _MeshBuilder()
+    W = 2.0
+    # floor, ceiling, back wall (white); left red; right green
+    mb.add(*_quad((-1, 0, -1), (-1, 0, 1), (1, 0, 1), (1, 0, -1)), 0)
+    mb.add(*_quad((-1, W, -1), (1, W, -1), (1, W, 1), (-1, W, 1)), 0)
+    mb.add(*_quad((-1, 0, -1), (1, 0, -1), (1, W, -1), (-1, W, -1)), 0)
+    mb.add(*_quad((-1, 0, -1), (-1, W, -1), (-1, W, 1), (-1, 0, 1)), 1)
+    mb.add(*_quad((1, 0, -1), (1, 0, 1), (1, W, 1), (1, W, -1)), 2)
+    mb.add(*_box((-0.33, 0.0, -0.3), (0.6, 1.2, 0.6), 17.0), 0)
+    mb.add(*_box((0.35, 0.0, 0.3), (0.6, 0.6, 0.6), -18.0), 0)
+    ly = W - 1e-3
+    mb.add(*_quad((-0.25, ly, -0.25), (0.25, ly, -0.25), (0.25, ly, 0.25), (-0.25, ly, 0.25)), 3)
+    sc = mb.build(name="box_room")
+    sc.materials = [diffuse((0.73, 0.73, 0.73)), diffuse((0.65, 0.05, 0.05)),
+                    diffuse((0.12, 0.45, 0.15)), emitter((17.0, 12.0, 4.0))]
+    cam = camera((0.0, 1.0, 3.9), (0.0, 1.0, 0.0), fovy_deg=40.0)
+    st = settings(512, 512, 64, 8, adaptive_sampling=0, throughput_clamp=0.0)
+    return sc, cam, st
+
+
+# ---------------------------------------------------------- procedural 500K
+
+
+def _icosphere(subdiv):
+    t = (1.0 + 5 ** 0.5) / 2
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    v = np.array(v, np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array(f, np.int64)
+    for _ in range(subdiv):
+        nv = len(v)
+        e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+        e.sort(axis=1)
+        key = e[:, 0] * nv + e[:, 1]
+        uniq, inv = np.unique(key, return_inverse=True)
+        a, b = uniq // nv, uniq % nv
+        mid = v[a] + v[b]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        m = inv.reshape(3, -1).T + nv  # midpoints of edges (01, 12, 20)
+        v = np.concatenate([v, mid])
+        f = np.concatenate([
+            np.stack([f[:, 0], m[:, 0], m[:, 2]], 1), np.stack([f[:, 1], m[:, 1], m[:, 0]], 1),
+            np.stack([f[:, 2], m[:, 2], m[:, 1]], 1), np.stack([m[:, 0], m[:, 1], m[:, 2]], 1)])
+    return v, f
+
+
+def _torus(nu, nv, R, r):
+    u = np.arange(nu) * (2 * np.pi / nu)
+    w = np.arange(nv) * (2 * np.pi / nv)
+    uu, ww = np.meshgrid(u, w, indexing="ij")
+    x = (R + r * np.cos(ww)) * np.cos(uu)
+    z = (R + r * np.cos(ww)) * np.sin(uu)
+    y = r * np.sin(ww)
+    v = np.stack([x, y, z], -1).reshape(-1, 3)
+    n = np.stack([np.cos(ww) * np.cos(uu), np.sin(ww), np.cos(ww) * np.sin(uu)], -1).reshape(-1, 3)
+    i = np.arange(nu)[:, None]
+    j = np.arange(nv)[None, :]
+    a = (i * nv + j)
+    b = (((i + 1) % nu) * nv + j)
+    c = (((i + 1) % nu) * nv + (j + 1) % nv)
+    d = (i * nv + (j + 1) % nv)
+    f = np.concatenate([np.stack([a, c, b], -1).reshape(-1, 3), np.stack([a, d, c], -1).reshape(-1, 3)])
+    return v, n, f
+
+
+def _vertex_normals(v, f):
+    fn = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    n = np.zeros_like(v)
+    for k in range(3):
+        np.add.at(n, f[:, k], fn)
+    n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-20)
+    return n
+
+
+def _displace(v, n, rng, amp):
+    """Radial displacement by a few random sinusoids (smooth, seeded)."""
+    d = np.zeros(len(v))
+    for _ in range(4):
+        k = rng.normal(size=3) * rng.uniform(2.0, 6.0)
+        d += np.sin(v @ k + rng.uniform(0, 2 * np.pi)) / 4
+    return v + n * (amp * d)[:, None]
+
+
+def sun_sky_env(width=1024, height=512, sun_dir=(0.35, 0.55, -0.75), seed=0):
+    """Procedural fp32 sun+sky environment (rows from the bottom, +y up)."""
+    sd = np.asarray(sun_dir, np.float64)
+    sd /= np.linalg.norm(sd)
+    # the reference maps texel (x, y) to phi = u*2pi - pi, theta = v*pi with
+    # direction (sin t cos p, cos t, sin t sin p) (environment_map.h:138-155)
+    u = (np.arange(width) + 0.5) / width
+    vv = (np.arange(height) + 0.5) / height
+    phi = u * 2 * np.pi - np.pi
+    theta = vv * np.pi
+    st = np.sin(theta)[:, None]
+    d = np.stack([st * np.cos(phi)[None, :], np.cos(theta)[:, None] * np.ones((1, width)),
+                  st * np.sin(phi)[None, :]], -1)
+    up = np.clip(d[..., 1], -1, 1)
+    zen = np.array([0.25, 0.45, 1.0])
+    hor = np.array([0.9, 0.85, 0.75])
+    gnd = np.array([0.18, 0.15, 0.12])
+    t = np.clip(up, 0, 1)[..., None] ** 0.5
+    sky = hor * (1 - t) + zen * t
+    sky = np.where(up[..., None] >= 0, sky, gnd * np.ones_like(sky))
+    cosang = np.clip(d @ sd, -1, 1)
+    halo = np.exp((cosang - 1) * 40.0)[..., None] * np.array([1.0, 0.9, 0.7]) * 2.0
+    sun = (cosang > np.cos(np.deg2rad(1.5)))[..., None] * np.array([4000.0, 3600.0, 3000.0])
+    img = (sky + halo + sun).astype(np.float32)
+    # texel rows here run v = 0 (theta 0, +y) upward in index; the bridge
+    # stores row 0 as given, the map looks texel (y, x) up at v = y / height
+    return np.ascontiguousarray(img)
+
+
+def procedural_500k(seed=0, n_objects=200, n_spheres=60, sphere_subdiv=4, torus_res=(36, 19)):
+    """~500K triangles: displaced icospheres and tori on a ground plane."""
+    rng = np.random.default_rng(seed)
+    mb = _MeshBuilder()
+    mats = []
+    G = 40.0
+    mb.add(*_quad((-G, 0, -G), (-G, 0, G), (G, 0, G), (G, 0, -G)), 0, n=np.tile([0, 1, 0], (4, 1)))
+    ground = _abi.material_default()
+    ground.base_color[:] = (0.5, 0.5, 0.5)
+    ground.roughness = 0.8
+    ground.specular = 0.5
+    mats.append(ground)
+    sv, sf = _icosphere(sphere_subdiv)
+    for k in range(n_objects):
+        px, pz = rng.uniform(-18, 18, 2)
+        scale = rng.uniform(0.5, 1.6)
+        if k < n_spheres:
+            v = sv.copy()
+            n = sv.copy()
+            v = _displace(v, n, rng, 0.12)
+            f = sf
+            v = v * scale
+            v[:, 1] += scale * 1.05
+        else:
+            R, r = 1.0, rng.uniform(0.25, 0.45)
+            v, n, f = _torus(torus_res[0], torus_res[1], R, r)
+            v = _displace(v, n, rng, 0.06)
+            ang = rng.uniform(0, np.pi)
+            ca, sa = np.cos(ang), np.sin(ang)
+            rot = np.array([[1, 0, 0], [0, ca, -sa], [0, sa, ca]])
+            v = v @ rot.T * scale
+            v[:, 1] += (R + r) * scale * abs(sa) + r * scale + 0.02
+        v[:, 0] += px
+        v[:, 2] += pz
+        nn = _vertex_normals(v, f)
+        mb.add(v.astype(np.float32), f, len(mats), n=nn.astype(np.float32))
+        m = _abi.material_default()
+        m.base_color[:] = rng.uniform(0.05, 0.95, 3).tolist()
+        m.metallic = float(rng.integers(0, 2))
+        m.roughness = float(rng.uniform(0.05, 1.0))
+        m.transmission = 1.0 if rng.uniform() < 0.1 else 0.0
+        m.clearcoat = float(rng.uniform(0, 1))
+        m.specular = 0.5
+        mats.append(m)
+    # 4 emissive triangles above the scene
+    for k in range(4):
+        cx, cz = rng.uniform(-12, 12, 2)
+        y = rng.uniform(9, 12)
+        s = 1.5
+        tri = np.array([[cx - s, y, cz - s], [cx + s, y, cz - s], [cx, y, cz + s]], np.float32)
+        mb.add(tri[[0, 2, 1]], np.array([[0, 1, 2]]), len(mats), n=np.tile([0, -1, 0], (3, 1)))
+        mats.append(emitter((30.0, 28.0, 24.0)))
+    sc = mb.build(name="procedural_500k")
+    sc.materials = mats
+    sc.env_pixels = sun_sky_env(1024, 512)
+    cam = camera((0.0, 9.0, 30.0), (0.0, 0.5, 0.0), fovy_deg=45.0)
+    st = settings(1024, 1024, 128, 8, adaptive_sampling=0, throughput_clamp=0.0)
+    return sc, cam, st
+
+
+# ------------------------------------------------------------ feature scenes
+
+
+def feature_scene(kind: str, seed=0, res=48):
+    """Small scenes that each switch on one part of the reference's shading
+    path, for parity tests: 'basic', 'glass', 'env', 'lights', 'volume',
+    'textures', 'alpha', 'limits', 'camera'."""
+    rng = np.random.default_rng(seed)
+    sc, cam, st = box_room()
+    st.width = st.height = res
+    st.pixel_samples = 1
+    mats = list(sc.materials)
+    if kind == "basic":
+        pass
+    elif kind == "glass":
+        g = _abi.material_default()
+        g.base_color[:] = (0.95, 0.95, 0.95)
+        g.transmission = 1.0
+        g.roughness = 0.0
+        g.ior = 1.5
+        g.specular = 1.0
+        metal = _abi.material_default()
+        metal.base_color[:] = (0.9, 0.7, 0.3)
+        metal.metallic = 1.0
+        metal.roughness = 0.3
+        coat = _abi.material_default()
+        coat.base_color[:] = (0.2, 0.3, 0.8)
+        coat.clearcoat = 1.0
+        coat.sheen = 0.5
+        coat.specular = 0.5
+        coat.roughness = 0.6
+        rough_glass = _abi.material_default()
+        rough_glass.transmission = 1.0
+        rough_glass.roughness = 0.4
+        rough_glass.thin_walled = 1
+        mats += [g, metal, coat, rough_glass]
+        ids = sc.material_ids.copy()
+        ids[10:22] = 4
+        ids[22:34] = 5
+        ids[np.arange(0, 2)] = 6
+        ids[np.arange(4, 6)] = 7
+        sc.material_ids = ids
+    elif kind == "env":
+        sc.env_pixels = sun_sky_env(64, 32, sun_dir=(0.3, 0.5, 0.8))
+        # open the room: drop ceiling and right wall
+        keep = np.ones(sc.triangle_count, bool)
+        keep[2:4] = False
+        keep[8:10] = False
+        sc.indices = sc.indices[keep]
+        sc.material_ids = sc.material_ids[keep]
+        ang = 0.6
+        sc.env_world_to_map = (np.cos(ang), 0, np.sin(ang), 0, 1, 0, -np.sin(ang), 0, np.cos(ang))
+    elif kind == "lights":
+        pl = _abi.light_default()
+        pl.type = 0
+        pl.position[:] = (0.3, 1.7, 0.5)
+        pl.color[:] = (1.0, 0.8, 0.6)
+        pl.intensity = 2.0
+        pl.radius = 0.05
+        dl = _abi.light_default()
+        dl.type = 1
+        dl.direction[:] = (-0.3, -1.0, -0.2)
+        dl.intensity = 0.8
+        dl.radius = 0.02
+        spl = _abi.light_default()
+        spl.type = 2
+        spl.position[:] = (-0.5, 1.9, 0.8)
+        spl.direction[:] = (0.3, -1.0, -0.4)
+        spl.intensity = 4.0
+        spl.spot_angle = 0.5
+        spl.spot_falloff = 0.2
+        sc.lights = [pl, dl, spl]
+        st.ambient_radiance = 0.3
+        st.ambient_color[:] = (0.6, 0.7, 1.0)
+    elif kind == "volume":
+        n = 24
+        g = np.linspace(-1, 1, n)
+        x, y, z = np.meshgrid(g, g, g, indexing="ij")
+        dens = np.clip(1.0 - np.sqrt(x ** 2 + y ** 2 + z ** 2), 0, 1) + 0.2 * np.sin(5 * x) * np.cos(4 * z)
+        vals = np.ascontiguousarray(np.transpose(dens, (2, 1, 0)), dtype=np.float32)  # x fastest
+        tf = np.array([[0.9, 0.9, 0.9, 0.0], [0.8, 0.6, 0.4, 0.5], [0.9, 0.3, 0.2, 1.0]], np.float32)
+        v = _abi.volume_default()
+        v.dims[:] = (n, n, n)
+        v.origin[:] = (-0.6, 0.2, -0.4)
+        v.spacing[:] = (1.2 / (n - 1),) * 3
+        v.value_range[:] = (0.0, 1.0)
+        v.density_scale = 4.0
+        hv = _abi.volume_default()
+        hv.dims[:] = (2, 2, 2)
+        hv.origin[:] = (-0.9, 0.05, 0.3)
+        hv.spacing[:] = (0.6, 0.5, 0.5)
+        hv.density_scale = 1.5
+        sc.volumes = [(v, vals, tf), (hv, np.ones(8, np.float32), np.array([[0.8, 0.8, 0.8, 1.0]], np.float32))]
+        st.max_volume_bounces = 6
+    elif kind == "textures":
+        V = sc.positions.shape[0]
+        uv = np.zeros((V, 4), np.float32)
+        uv[:, 0] = sc.positions[:, 0] * 0.7 + sc.positions[:, 2] * 0.3
+        uv[:, 1] = sc.positions[:, 1] * 0.6 + sc.positions[:, 2] * 0.2
+        uv[:, 3] = 1.0
+        sc.attributes = [uv, None, None, None, None]
+        col = np.zeros((V, 4), np.float32)
+        col[:, :3] = rng.uniform(0.2, 0.9, (V, 3))
+        col[:, 3] = 1.0
+        sc.attributes[4] = col
+        tex = rng.uniform(0, 1, (16, 16, 4)).astype(np.float32)
+        s0 = _abi.sampler_default()
+        s0.size[:] = (16, 16, 1)
+        s0.wrap[:] = (1, 2, 0)
+        s1 = _abi.sampler_default()
+        s1.type = 1
+        s1.linear = 0
+        s1.size[:] = (8, 8, 1)
+        nrm = np.zeros((8, 8, 4), np.float32)
+        nrm[..., 0] = 0.5 + 0.3 * np.sin(np.arange(8))[None, :]
+        nrm[..., 1] = 0.5 + 0.3 * np.cos(np.arange(8))[:, None]
+        nrm[..., 2] = 0.9
+        nrm[..., 3] = 1
+        s2 = _abi.sampler_default()
+        s2.type = 3
+        s2.in_attribute = 4
+        s2.out_transform[:] = (0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1)
+        s2.out_offset[:] = (0.1, 0.1, 0.1, 0)
+        s3 = _abi.sampler_default()
+        s3.type = 0
+        s3.size[:] = (5, 1, 1)
+        s3.wrap[0] = 2
+        s3.in_attribute = 5
+        ramp = np.stack([np.linspace(0, 1, 5)] * 4, -1).astype(np.float32)
+        s4 = _abi.sampler_default()
+        s4.type = 2
+        s4.size[:] = (3, 3, 3)
+        s4.in_attribute = 5
+        s4.in_transform[:] = (0.5, 0, 0, 0.5, 0, 0.5, 0, 0, 0, 0, 0.5, 0.5, 0, 0, 0, 1)
+        vol = rng.uniform(0, 1, (27, 4)).astype(np.float32)
+        sc.samplers = [(s0, tex), (s1, nrm), (s2, None), (s3, ramp), (s4, vol)]
+        m_tex = diffuse((1, 1, 1))
+        m_tex.base_color_src.kind, m_tex.base_color_src.index = 2, 0
+        m_tex.normal_src.kind, m_tex.normal_src.index = 2, 1
+        m_tex.roughness_src.kind, m_tex.roughness_src.index = 2, 3
+        m_tex.specular = 0.5
+        m_vc = diffuse((1, 1, 1))
+        m_vc.base_color_src.kind, m_vc.base_color_src.index = 1, 4
+        m_vc.metallic_src.kind, m_vc.metallic_src.index = 2, 4
+        m_vc.roughness = 0.5
+        m_tr = diffuse((1, 1, 1))
+        m_tr.base_color_src.kind, m_tr.base_color_src.index = 2, 2
+        m_em = emitter((0, 0, 0))
+        m_em.emitter_only = 0
+        m_em.emission_src.kind, m_em.emission_src.index = 2, 2
+        mats += [m_tex, m_vc, m_tr, m_em]
+        ids = sc.material_ids.copy()
+        ids[0:2] = 4
+        ids[4:6] = 4
+        ids[10:22] = 5
+        ids[22:34] = 6
+        ids[2:4] = 7
+        sc.material_ids = ids
+    elif kind == "alpha":
+        m_blend = diffuse((0.2, 0.8, 0.3))
+        m_blend.alpha_mode = 0
+        m_blend.opacity = 0.4
+        m_mask = diffuse((0.8, 0.2, 0.3))
+        m_mask.alpha_mode = 2
+        m_mask.opacity = 0.3
+        m_mask.alpha_cutoff = 0.5
+        m_hidden = diffuse((0.9, 0.9, 0.2))
+        m_hidden.hidden_to_camera = 1
+        mats += [m_blend, m_mask, m_hidden]
+        ids = sc.material_ids.copy()
+        ids[10:22] = 4
+        ids[22:28] = 5
+        ids[28:34] = 6
+        sc.material_ids = ids
+        st.background[:] = (0.1, 0.2, 0.3, 0.5)
+    elif kind == "limits":
+        st.max_diffuse_bounces = 1
+        st.max_glossy_bounces = 2
+        st.clamp_direct = 0.5
+        st.clamp_indirect = 0.2
+        st.throughput_clamp = 3.0
+        st.max_depth = 4
+        metal = _abi.material_default()
+        metal.base_color[:] = (0.9, 0.9, 0.9)
+        metal.metallic = 1.0
+        metal.roughness = 0.2
+        mats.append(metal)
+        ids = sc.material_ids.copy()
+        ids[22:34] = 4
+        sc.material_ids = ids
+    elif kind == "camera":
+        cam.aperture_radius = 0.05
+        cam.focus_distance = 3.5
+        cam.clip_near = 1.0
+        cam.clip_far = 4.5
+        cam.image_region[:] = (0.1, 0.2, 0.9, 0.8)
+    elif kind == "ortho":
+        cam.orthographic = 1
+        cam.height = 2.2
+        bg = rng.uniform(0, 1, (4, 6, 4)).astype(np.float32)
+        st._bg = bg
+        st.background_width = 6
+        st.background_height = 4
+        import ctypes as C
+        st.background_image = bg.ctypes.data_as(C.POINTER(C.c_float))
+        keep = np.ones(sc.triangle_count, bool)
+        keep[4:6] = False
+        sc.indices = sc.indices[keep]
+        sc.material_ids = sc.material_ids[keep]
+    else:
+        raise ValueError(kind)
+    sc.materials = mats
+    sc.name = "feature_" + kind
+    return sc, cam, st
+
+
+FEATURES = ("basic", "glass", "env", "lights", "volume", "textures", "alpha", "limits", "camera", "ortho")
