@@ -303,6 +303,18 @@ int phc_trace_occluded(phc_accel *a, const float *origins, const float *directio
 int phc_accel_counters(const phc_accel *a, uint64_t *node_visits, uint64_t *tri_tests);
 /* Size in bytes of the device BVH8 nodes, triangle records and node count. */
 int phc_accel_info(const phc_accel *a, uint64_t *node_bytes, uint64_t *tri_bytes, uint64_t *node_count);
+/* Message of the last failed phc_accel_* / phc_trace_* call on this thread. */
+const char *phc_accel_error(void);
+
+/* ------------------------------------------------------------ scheduling */
+/* Launch parameters picked by the autotuner (no reference counterpart; the
+   reference has no tunables on this path).  Keys: "wave_paths" (paths in
+   flight per wave), "trace_blocks_per_sm", "shade_blocks_per_sm",
+   "use_graph" (0/1), "count_traversal" (0/1), "max_leaf" (1..3, BVH8 leaf
+   size, read at the next scene upload).  Returns PHC_ERR_INVALID for an
+   unknown key or out-of-range value; get returns -1 for an unknown key. */
+int phc_tuning_set(const char *key, int64_t value);
+int64_t phc_tuning_get(const char *key);
 
 #ifdef __cplusplus
 }

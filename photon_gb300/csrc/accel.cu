@@ -1,0 +1,243 @@
+// Level A of the C-ABI: the ray back-end (RayBackend::build_accel,
+// trace_closest, trace_occluded; include/photon/pt/backend/ray_backend.h:44-54)
+// on caller-owned device arrays.
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/photon_cuda.h"
+#include "scene_build.h"
+#include "traverse.cuh"
+
+using namespace phc;
+
+struct phc_accel {
+  int device{0};
+  int sm_count{0};
+  cudaStream_t stream{nullptr};
+  DeviceScene scene;
+  uint64_t *counters{nullptr};
+  uint64_t last_nodes{0}, last_tris{0};
+  ~phc_accel()
+  {
+    if (counters)
+      cudaFree(counters);
+    if (stream)
+      cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+thread_local std::string g_accel_error;
+
+int fail(int code, const std::string &m)
+{
+  g_accel_error = m;
+  return code;
+}
+
+constexpr uint32_t FULL = 0xffffffffu;
+
+// One ray per thread; persistent warps take 32-ray batches.
+template <int MODE, bool COUNT> // 0 full hit record, 1 compact, 2 occluded
+__global__ void __launch_bounds__(128) k_level_a(DevScene sc, const float *__restrict__ orgs,
+    const float *__restrict__ dirs, const float *__restrict__ tmins, const float *__restrict__ tmaxs, uint32_t n,
+    void *out, uint32_t *fetch, unsigned long long *stats)
+{
+  TravCounters ctr{0u, 0u};
+  for (;;) {
+    uint32_t base = 0;
+    if ((threadIdx.x & 31u) == 0)
+      base = atomicAdd(fetch, 32u);
+    base = __shfl_sync(FULL, base, 0);
+    if (base >= n)
+      break;
+    const uint32_t i = base + (threadIdx.x & 31u);
+    if (i >= n)
+      continue;
+    const V3 o{orgs[3 * i], orgs[3 * i + 1], orgs[3 * i + 2]};
+    const V3 d{dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+    const float t0 = tmins[i], t1 = tmaxs[i];
+    if (MODE == 2) {
+      const RayHit h = trace_ray<true, COUNT>(sc, o, d, t0, t1, &ctr);
+      static_cast<uint32_t *>(out)[i] = h.prim != 0xffffffffu ? 1u : 0u;
+      continue;
+    }
+    const RayHit h = trace_ray<false, COUNT>(sc, o, d, t0, t1, &ctr);
+    if (MODE == 1) {
+      reinterpret_cast<float4 *>(out)[i] = make_float4(h.t, __uint_as_float(h.prim), h.u, h.v);
+      continue;
+    }
+    // HitResult (ray_backend.h:15-29); like KokkosBackend only `hit` is written
+    // for a miss, here the record is zeroed instead.
+    float rec[22];
+    for (int k = 0; k < 22; ++k)
+      rec[k] = 0.f;
+    uint32_t *urec = reinterpret_cast<uint32_t *>(rec);
+    if (h.prim != 0xffffffffu) {
+      const HitAttr a = hit_attributes(sc, o, d, h);
+      rec[0] = h.t;
+      rec[1] = a.p.x;
+      rec[2] = a.p.y;
+      rec[3] = a.p.z;
+      rec[4] = a.n.x;
+      rec[5] = a.n.y;
+      rec[6] = a.n.z;
+      rec[7] = a.sn.x;
+      rec[8] = a.sn.y;
+      rec[9] = a.sn.z;
+      rec[12] = h.u;
+      rec[13] = h.v;
+      urec[17] = h.prim;
+      urec[20] = a.material_id;
+      urec[21] = 1u; // hit = 1, has_interpolated_color = 0
+    }
+    float *dst = static_cast<float *>(out) + size_t(i) * 22;
+    for (int k = 0; k < 22; ++k)
+      dst[k] = rec[k];
+  }
+  if (COUNT) {
+    atomicAdd(&stats[0], (unsigned long long)ctr.nodes);
+    atomicAdd(&stats[1], (unsigned long long)ctr.tris);
+  }
+}
+
+template <int MODE>
+int launch(phc_accel *a, const float *o, const float *d, const float *t0, const float *t1, uint32_t n, void *out,
+    void *stream)
+{
+  if (!a)
+    return fail(PHC_ERR_INVALID, "null accel");
+  if (n == 0)
+    return PHC_OK;
+  if (!o || !d || !t0 || !t1 || !out)
+    return fail(PHC_ERR_INVALID, "null ray or output pointer");
+  cudaSetDevice(a->device);
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : a->stream;
+  uint32_t *fetch = reinterpret_cast<uint32_t *>(a->counters + 2);
+  cudaMemsetAsync(a->counters, 0, 4 * sizeof(uint64_t), s);
+  const int blocks = a->sm_count * 16;
+  const bool count = std::getenv("PHC_TUNE_COUNT_TRAVERSAL") && std::atoi(std::getenv("PHC_TUNE_COUNT_TRAVERSAL"));
+  auto *st = reinterpret_cast<unsigned long long *>(a->counters);
+  if (count)
+    k_level_a<MODE, true><<<blocks, 128, 0, s>>>(a->scene.dev, o, d, t0, t1, n, out, fetch, st);
+  else
+    k_level_a<MODE, false><<<blocks, 128, 0, s>>>(a->scene.dev, o, d, t0, t1, n, out, fetch, st);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess)
+    return fail(PHC_ERR_CUDA, std::string("trace: ") + cudaGetErrorString(e));
+  uint64_t c[2] = {0, 0};
+  if (count) {
+    cudaMemcpy(c, a->counters, sizeof(c), cudaMemcpyDeviceToHost);
+  }
+  a->last_nodes = c[0];
+  a->last_tris = c[1];
+  return PHC_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int phc_accel_create(phc_accel **out, const float *positions, uint64_t vertex_count, const uint32_t *indices,
+    uint64_t triangle_count, const float *normals, const uint32_t *material_ids)
+{
+  static_assert(sizeof(phc_hit_result) == 88, "HitResult layout");
+  if (!out)
+    return fail(PHC_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  if (!positions || !indices || vertex_count == 0 || triangle_count == 0)
+    return fail(PHC_ERR_INVALID, "empty mesh");
+  phc_accel *a = nullptr;
+  try {
+    a = new phc_accel();
+    cudaGetDevice(&a->device);
+    cudaDeviceGetAttribute(&a->sm_count, cudaDevAttrMultiProcessorCount, a->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+      e = cudaMalloc(&a->counters, 4 * sizeof(uint64_t));
+    if (e != cudaSuccess) {
+      delete a;
+      return fail(PHC_ERR_CUDA, std::string("accel: ") + cudaGetErrorString(e));
+    }
+    phc_scene_desc d{};
+    d.positions = positions;
+    d.vertex_count = vertex_count;
+    d.indices = indices;
+    d.triangle_count = triangle_count;
+    d.normals = normals;
+    d.material_ids = material_ids;
+    d.material_id_count = material_ids ? triangle_count : 0;
+    HostScene hs;
+    build_host_scene(d, hs);
+    // Level A keeps the caller's material ids as given (no material table).
+    if (material_ids)
+      for (uint64_t t = 0; t < triangle_count; ++t)
+        hs.prim_vidx[4 * t + 3] = material_ids[t];
+    if (hs.bvh.max_depth >= 64) {
+      delete a;
+      return fail(PHC_ERR_LIMIT, "BVH deeper than the traversal stack (64 levels)");
+    }
+    const std::string err = a->scene.upload(hs, a->stream);
+    if (!err.empty()) {
+      delete a;
+      return fail(PHC_ERR_CUDA, err);
+    }
+  } catch (const std::bad_alloc &) {
+    delete a;
+    return fail(PHC_ERR_OOM, "host allocation failed");
+  } catch (const std::exception &e) {
+    delete a;
+    return fail(PHC_ERR_INVALID, e.what());
+  }
+  *out = a;
+  return PHC_OK;
+}
+
+void phc_accel_destroy(phc_accel *a) { delete a; }
+
+int phc_trace_closest(phc_accel *a, const float *origins, const float *directions, const float *tmin,
+    const float *tmax, uint32_t n, phc_hit_result *hits, void *stream)
+{
+  return launch<0>(a, origins, directions, tmin, tmax, n, hits, stream);
+}
+
+int phc_trace_closest_compact(phc_accel *a, const float *origins, const float *directions, const float *tmin,
+    const float *tmax, uint32_t n, float *hits4, void *stream)
+{
+  return launch<1>(a, origins, directions, tmin, tmax, n, hits4, stream);
+}
+
+int phc_trace_occluded(phc_accel *a, const float *origins, const float *directions, const float *tmin,
+    const float *tmax, uint32_t n, uint32_t *occluded, void *stream)
+{
+  return launch<2>(a, origins, directions, tmin, tmax, n, occluded, stream);
+}
+
+int phc_accel_counters(const phc_accel *a, uint64_t *node_visits, uint64_t *tri_tests)
+{
+  if (!a || !node_visits || !tri_tests)
+    return fail(PHC_ERR_INVALID, "null argument");
+  *node_visits = a->last_nodes;
+  *tri_tests = a->last_tris;
+  return PHC_OK;
+}
+
+int phc_accel_info(const phc_accel *a, uint64_t *node_bytes, uint64_t *tri_bytes, uint64_t *node_count)
+{
+  if (!a || !node_bytes || !tri_bytes || !node_count)
+    return fail(PHC_ERR_INVALID, "null argument");
+  *node_bytes = a->scene.node_bytes;
+  *tri_bytes = a->scene.tri_bytes;
+  *node_count = a->scene.dev.node_count;
+  return PHC_OK;
+}
+
+const char *phc_accel_error(void) { return g_accel_error.c_str(); }
+
+} // extern "C"

@@ -1,0 +1,628 @@
+// libphoton_cuda.so: the renderer seam (Level B of include/photon_cuda.h).
+//
+// phc_renderer holds what photon::bridge::Renderer::Impl holds
+// (src/photon/anari/RenderBridge.cpp:416-439): the device scene, the wavefront
+// buffers of the path tracer, the accumulated frame and the sample counter
+// that decorrelates successive render calls.  Calls run on the renderer's own
+// CUDA stream and block until their device work is done.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <exception>
+#include <limits>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/photon_cuda.h"
+#include "pt_math.cuh"
+#include "scene_build.h"
+#include "tuning.h"
+#include "wavefront.h"
+
+using namespace phc;
+
+namespace {
+
+thread_local std::string g_error;
+
+struct Buf {
+  void *p{nullptr};
+  size_t bytes{0};
+  ~Buf() { release(); }
+  void release()
+  {
+    if (p)
+      cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // (Re)allocates to at least n bytes; contents are not kept.
+  cudaError_t ensure(size_t n)
+  {
+    if (n <= bytes && p)
+      return cudaSuccess;
+    release();
+    const cudaError_t e = cudaMalloc(&p, n ? n : 16);
+    if (e == cudaSuccess)
+      bytes = n;
+    else
+      p = nullptr;
+    return e;
+  }
+  template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct CudaError : std::runtime_error {
+  cudaError_t code;
+  CudaError(cudaError_t c, const char *what)
+      : std::runtime_error(std::string(what) + ": " + cudaGetErrorString(c)), code(c)
+  {
+  }
+};
+inline void ck(cudaError_t e, const char *what)
+{
+  if (e != cudaSuccess)
+    throw CudaError(e, what);
+}
+struct ApiError : std::runtime_error {
+  int code;
+  ApiError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+} // namespace
+
+struct phc_renderer {
+  int device{0};
+  int sm_count{0};
+  cudaStream_t stream{nullptr};
+  std::string error;
+  std::mutex mutex;
+
+  DeviceScene scene;
+  bool has_scene{false};
+  uint64_t scene_generation{0};
+
+  // wavefront buffers
+  size_t cap_paths{0};
+  Buf st_o[2], st_d[2], st_tp[2], st_info[2], st_dist[2], hits, sh_a, sh_b, sh_c;
+  size_t cap_slots{0};
+  Buf acc, acc_sq, acc_start, nsamp, aov_n, aov_a;
+  Buf counters; // count, scount, fetch, wave, error
+  Buf rc_buf, stats_buf, bg_buf;
+  size_t bg_floats{0};
+  // frame (RenderBridge.cpp:424-435)
+  Buf f_color, f_normal, f_albedo, read_buf;
+  uint32_t width{0}, height{0}, samples{0}, sample_counter{0};
+  // graph of one wave
+  cudaGraphExec_t graph{nullptr};
+  uint64_t graph_key[6]{};
+  phc_render_stats last{};
+  cudaEvent_t ev0{nullptr}, ev1{nullptr};
+
+  ~phc_renderer()
+  {
+    if (graph)
+      cudaGraphExecDestroy(graph);
+    if (ev0)
+      cudaEventDestroy(ev0);
+    if (ev1)
+      cudaEventDestroy(ev1);
+    if (stream)
+      cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int set_error(phc_renderer *r, int code, const std::string &msg)
+{
+  if (r)
+    r->error = msg;
+  g_error = msg;
+  return code;
+}
+
+template <class F> int guarded(phc_renderer *r, F &&f)
+{
+  try {
+    f();
+    if (r)
+      r->error.clear();
+    return PHC_OK;
+  } catch (const ApiError &e) {
+    return set_error(r, e.code, e.what());
+  } catch (const CudaError &e) {
+    return set_error(r, e.code == cudaErrorMemoryAllocation ? PHC_ERR_OOM : PHC_ERR_CUDA, e.what());
+  } catch (const std::bad_alloc &) {
+    return set_error(r, PHC_ERR_OOM, "host allocation failed");
+  } catch (const std::length_error &e) {
+    return set_error(r, PHC_ERR_LIMIT, e.what());
+  } catch (const std::invalid_argument &e) {
+    return set_error(r, PHC_ERR_INVALID, e.what());
+  } catch (const std::out_of_range &e) {
+    return set_error(r, PHC_ERR_INVALID, e.what());
+  } catch (const std::exception &e) {
+    return set_error(r, PHC_ERR_INVALID, e.what());
+  }
+}
+
+inline V3 hv3(const float *p) { return V3{p[0], p[1], p[2]}; }
+inline void put3(float *d, V3 v)
+{
+  d[0] = v.x;
+  d[1] = v.y;
+  d[2] = v.z;
+}
+
+// Camera of the render call: RenderBridge.cpp:872-891 with Camera::
+// make_perspective / make_orthographic (include/photon/pt/camera.h:32-77), in
+// float on the host with the reference's operation order.
+void make_camera(const phc_camera &c, uint32_t w, uint32_t h, RenderConst &rc)
+{
+  const V3 position = hv3(c.position);
+  V3 direction = normalize(hv3(c.direction));
+  if (length(direction) == 0.f)
+    direction = V3{0.f, 0.f, -1.f};
+  V3 up = hv3(c.up);
+  if (length(cross(direction, up)) < 1e-6f)
+    up = std::fabs(direction.y) < 0.9f ? V3{0.f, 1.f, 0.f} : V3{1.f, 0.f, 0.f};
+  const float aspect = c.aspect > 0.f ? c.aspect : float(w) / float(h);
+  const V3 at = position + direction;
+  V3 cw = normalize(position - at);
+  V3 cu = normalize(cross(up, cw));
+  V3 cv = cross(cw, cu);
+  V3 horizontal, vertical, lower_left;
+  float lens_radius = 0.f;
+  if (c.orthographic) {
+    horizontal = cu * (c.height * aspect);
+    vertical = cv * c.height;
+    lower_left = position - horizontal * 0.5f - vertical * 0.5f;
+  } else {
+    const float fovy_degrees = c.fovy * 180.f / 3.14159265358979f;
+    const bool lens = c.aperture_radius > 0.f && c.focus_distance > 0.f;
+    const float aperture = lens ? 2.f * c.aperture_radius : 0.f;
+    const float focus = lens ? c.focus_distance : 1.f;
+    const float theta = fovy_degrees * 3.1415926535f / 180.f;
+    const float hh = std::tan(theta * 0.5f);
+    const float vh = 2.f * hh;
+    const float vw = aspect * vh;
+    lens_radius = aperture * 0.5f;
+    horizontal = cu * (vw * focus);
+    vertical = cv * (vh * focus);
+    lower_left = position - horizontal * 0.5f - vertical * 0.5f - cw * focus;
+  }
+  put3(rc.origin, position);
+  put3(rc.lower_left, lower_left);
+  put3(rc.horizontal, horizontal);
+  put3(rc.vertical, vertical);
+  put3(rc.cu, cu);
+  put3(rc.cv, cv);
+  put3(rc.cw, cw);
+  rc.lens_radius = lens_radius;
+  rc.ortho = c.orthographic ? 1 : 0;
+  rc.clip_near = c.clip_near > 0.f ? c.clip_near : 0.f;
+  rc.clip_far = c.clip_far < 1e30f ? c.clip_far : 1e30f;
+  for (int i = 0; i < 4; ++i)
+    rc.region[i] = c.image_region[i];
+}
+
+void check_device(phc_renderer *r) { ck(cudaSetDevice(r->device), "cudaSetDevice"); }
+
+void ensure_paths(phc_renderer *r, size_t n)
+{
+  if (n <= r->cap_paths)
+    return;
+  for (int b = 0; b < 2; ++b) {
+    ck(r->st_o[b].ensure(n * 16), "alloc path state");
+    ck(r->st_d[b].ensure(n * 16), "alloc path state");
+    ck(r->st_tp[b].ensure(n * 16), "alloc path state");
+    ck(r->st_info[b].ensure(n * 16), "alloc path state");
+    ck(r->st_dist[b].ensure(n * 4), "alloc path state");
+  }
+  ck(r->hits.ensure(n * 16), "alloc hits");
+  ck(r->sh_a.ensure(n * 16), "alloc shadow queue");
+  ck(r->sh_b.ensure(n * 16), "alloc shadow queue");
+  ck(r->sh_c.ensure(n * 16), "alloc shadow queue");
+  r->cap_paths = n;
+}
+
+void ensure_slots(phc_renderer *r, size_t n)
+{
+  if (n <= r->cap_slots)
+    return;
+  ck(r->acc.ensure(n * 16), "alloc accumulators");
+  ck(r->acc_sq.ensure(n * 16), "alloc accumulators");
+  ck(r->acc_start.ensure(n * 16), "alloc accumulators");
+  ck(r->nsamp.ensure(n * 4), "alloc accumulators");
+  ck(r->aov_n.ensure(n * 16), "alloc accumulators");
+  ck(r->aov_a.ensure(n * 16), "alloc accumulators");
+  r->cap_slots = n;
+}
+
+PathSoA path_soa(phc_renderer *r, int b)
+{
+  return PathSoA{r->st_o[b].as<float4>(), r->st_d[b].as<float4>(), r->st_tp[b].as<float4>(),
+      r->st_info[b].as<uint4>(), r->st_dist[b].as<float>()};
+}
+Accum accum(phc_renderer *r)
+{
+  return Accum{r->acc.as<float4>(), r->acc_sq.as<float4>(), r->acc_start.as<float4>(), r->nsamp.as<uint32_t>(),
+      r->aov_n.as<float4>(), r->aov_a.as<float4>()};
+}
+WaveCounters wave_counters(phc_renderer *r, int max_iter)
+{
+  uint32_t *c = r->counters.as<uint32_t>();
+  WaveCounters wc;
+  wc.count = c;
+  wc.scount = c + (max_iter + 1);
+  wc.fetch = c + (2 * max_iter + 1);
+  wc.wave = c + (5 * max_iter + 2);
+  wc.error = c + (5 * max_iter + 3);
+  return wc;
+}
+size_t per_wave_counter_bytes(int max_iter) { return size_t(5 * max_iter + 2) * 4; }
+
+// One wave: counter reset, raygen, per iteration trace / shade / shadow, end.
+void record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, const RenderConst *rc, uint32_t npix,
+    int max_iter, int adaptive, bool counting)
+{
+  const WaveCounters wc = wave_counters(r, max_iter);
+  ck(cudaMemsetAsync(wc.count, 0, per_wave_counter_bytes(max_iter), s), "reset counters");
+  const DevScene sc = r->scene.dev;
+  const Accum ac = accum(r);
+  const ShadowSoA sh{r->sh_a.as<float4>(), r->sh_b.as<float4>(), r->sh_c.as<float4>()};
+  uint64_t *stats = r->stats_buf.as<uint64_t>();
+  launch_raygen(cfg, s, rc, sc, path_soa(r, 0), ac, wc);
+  for (int it = 0; it < max_iter; ++it) {
+    const PathSoA in = path_soa(r, it & 1), out = path_soa(r, (it + 1) & 1);
+    launch_trace(cfg, s, sc, in, r->hits.as<float4>(), wc, it, counting ? stats + 3 : nullptr);
+    launch_shade(cfg, s, rc, sc, in, out, r->hits.as<float4>(), sh, ac, wc, it);
+    launch_shadow(cfg, s, rc, sc, sh, ac, wc, it, counting ? stats + 3 : nullptr);
+  }
+  launch_wave_end(s, rc, ac, wc, npix, adaptive, max_iter, stats);
+}
+
+void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st, bool reset)
+{
+  const uint32_t w = st.width, h = st.height;
+  if (w == 0 || h == 0)
+    throw ApiError(PHC_ERR_INVALID, "invalid frame size");
+  if (!r->has_scene)
+    throw ApiError(PHC_ERR_NO_SCENE, "no scene");
+  if (uint64_t(w) * h > (1ull << 28))
+    throw ApiError(PHC_ERR_LIMIT, "frame larger than 2^28 pixels");
+  check_device(r);
+  cudaStream_t s = r->stream;
+  const uint32_t npix = w * h;
+  if (w != r->width || h != r->height) {
+    ck(r->f_color.ensure(size_t(npix) * 16), "alloc frame");
+    ck(r->f_normal.ensure(size_t(npix) * 16), "alloc frame");
+    ck(r->f_albedo.ensure(size_t(npix) * 16), "alloc frame");
+    ck(r->read_buf.ensure(size_t(npix) * 16), "alloc frame");
+    r->width = w;
+    r->height = h;
+    reset = true;
+  }
+  RenderConst rc{};
+  make_camera(cam, w, h, rc);
+  rc.w = w;
+  rc.h = h;
+  rc.npix = npix;
+  rc.spp = std::max<uint32_t>(st.pixel_samples, 1);
+  rc.max_depth = std::max<uint32_t>(st.max_depth, 1);
+  rc.max_iter = rc.max_depth + 1u + 8u;
+  rc.sample_offset = r->sample_counter;
+  std::memcpy(rc.bg, st.background, sizeof(rc.bg));
+  // background image (RenderBridge.cpp:848-870)
+  const size_t bg_n = size_t(st.background_width) * st.background_height * 4;
+  if (st.background_image && bg_n > 0) {
+    ck(r->bg_buf.ensure(bg_n * 4), "alloc background");
+    ck(cudaMemcpyAsync(r->bg_buf.p, st.background_image, bg_n * 4, cudaMemcpyHostToDevice, s), "upload background");
+    rc.bg_image = r->bg_buf.as<float4>();
+    rc.bg_w = st.background_width;
+    rc.bg_h = st.background_height;
+  }
+  for (int i = 0; i < 3; ++i)
+    rc.ambient[i] = st.ambient_color[i] * st.ambient_radiance;
+  rc.adaptive = st.adaptive_sampling ? 1 : 0;
+  rc.tp_clamp = st.throughput_clamp;
+  rc.max_diffuse = st.max_diffuse_bounces;
+  rc.max_glossy = st.max_glossy_bounces;
+  rc.max_transmission = st.max_transmission_bounces;
+  rc.max_volume = st.max_volume_bounces;
+  rc.clamp_direct = 3.f * std::max(st.clamp_direct, 0.f);
+  rc.clamp_indirect = 3.f * std::max(st.clamp_indirect, 0.f);
+  // samples of one pixel in flight: enough paths to fill the GPU, one when
+  // adaptive sampling needs the samples in order
+  const Tuning &tu = tuning();
+  uint32_t lanes = 1;
+  if (!rc.adaptive) {
+    const uint64_t target = tu.wave_paths;
+    lanes = uint32_t(std::min<uint64_t>(rc.spp, std::max<uint64_t>(1, (target + npix - 1) / npix)));
+    lanes = std::min<uint32_t>(lanes, std::max<uint32_t>(1u, uint32_t((1ull << 28) / npix)));
+  }
+  rc.lanes = lanes;
+  const int max_iter = int(rc.max_iter);
+  const size_t slots = size_t(lanes) * npix;
+  ensure_paths(r, slots);
+  ensure_slots(r, slots);
+  ck(r->counters.ensure(per_wave_counter_bytes(max_iter) + 16), "alloc counters");
+  ck(r->rc_buf.ensure(sizeof(RenderConst)), "alloc constants");
+  ck(r->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
+  ck(cudaMemcpyAsync(r->rc_buf.p, &rc, sizeof(rc), cudaMemcpyHostToDevice, s), "upload constants");
+  ck(cudaMemsetAsync(r->stats_buf.p, 0, 8 * sizeof(uint64_t), s), "reset stats");
+  ck(cudaMemsetAsync(r->acc.p, 0, slots * 16, s), "reset accumulators");
+  ck(cudaMemsetAsync(r->nsamp.p, 0, slots * 4, s), "reset accumulators");
+  ck(cudaMemsetAsync(r->aov_a.p, 0, slots * 16, s), "reset accumulators");
+  if (rc.adaptive)
+    ck(cudaMemsetAsync(r->acc_sq.p, 0, slots * 16, s), "reset accumulators");
+  const WaveCounters wc = wave_counters(r, max_iter);
+  ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
+
+  LaunchCfg cfg;
+  cfg.threads = 128;
+  cfg.blocks_trace = r->sm_count * std::max(1, std::min(tu.trace_blocks_per_sm, max_active_blocks(0, 128)));
+  cfg.blocks_shade = r->sm_count * std::max(1, std::min(tu.shade_blocks_per_sm, max_active_blocks(1, 128)));
+  cfg.blocks_raygen = int(std::min<size_t>((slots + 255) / 256, size_t(r->sm_count) * 8));
+  const bool counting = tu.count_traversal != 0;
+  const uint32_t waves = (rc.spp + lanes - 1) / lanes;
+  const RenderConst *drc = r->rc_buf.as<RenderConst>();
+
+  ck(cudaEventRecord(r->ev0, s), "event");
+  const uint64_t key[6] = {uint64_t(npix), uint64_t(lanes), uint64_t(max_iter), uint64_t(rc.adaptive),
+      r->scene_generation, uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32)};
+  if (tu.use_graph) {
+    if (!r->graph || std::memcmp(key, r->graph_key, sizeof(key)) != 0) {
+      if (r->graph) {
+        cudaGraphExecDestroy(r->graph);
+        r->graph = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+      try {
+        record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
+      } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g)
+          cudaGraphDestroy(g);
+        throw;
+      }
+      ck(cudaStreamEndCapture(s, &g), "end capture");
+      const cudaError_t e = cudaGraphInstantiate(&r->graph, g, 0);
+      cudaGraphDestroy(g);
+      ck(e, "graph instantiate");
+      std::memcpy(r->graph_key, key, sizeof(key));
+    }
+    for (uint32_t wv = 0; wv < waves; ++wv)
+      ck(cudaGraphLaunch(r->graph, s), "graph launch");
+  } else {
+    for (uint32_t wv = 0; wv < waves; ++wv)
+      record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
+  }
+  const bool first = reset || r->samples == 0;
+  const Frame fr{r->f_color.as<float4>(), r->f_normal.as<float4>(), r->f_albedo.as<float4>()};
+  launch_resolve(s, accum(r), fr, npix, lanes, float(rc.spp), first ? 1 : 0);
+  ck(cudaGetLastError(), "kernel launch");
+  ck(cudaEventRecord(r->ev1, s), "event");
+  uint64_t stats[8];
+  ck(cudaMemcpyAsync(stats, r->stats_buf.p, sizeof(stats), cudaMemcpyDeviceToHost, s), "read stats");
+  ck(cudaStreamSynchronize(s), "render");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, r->ev0, r->ev1);
+  r->last.pixel_samples = stats[0];
+  r->last.closest_rays = stats[1];
+  r->last.shadow_rays = stats[2];
+  r->last.node_visits = stats[3];
+  r->last.tri_tests = stats[4];
+  r->last.render_ms = ms;
+  r->sample_counter += rc.spp;
+  r->samples = first ? rc.spp : r->samples + rc.spp;
+}
+
+int read_channel(phc_renderer *r, float *out, int channel)
+{
+  if (!r)
+    return set_error(nullptr, PHC_ERR_INVALID, "null renderer");
+  std::lock_guard<std::mutex> lock(r->mutex);
+  if (!out)
+    return set_error(r, PHC_ERR_INVALID, "null output buffer");
+  if (r->samples == 0)
+    return set_error(r, PHC_ERR_NO_FRAME, "no frame has been rendered");
+  return guarded(r, [&] {
+    check_device(r);
+    const uint32_t npix = r->width * r->height;
+    const Frame fr{r->f_color.as<float4>(), r->f_normal.as<float4>(), r->f_albedo.as<float4>()};
+    launch_read(r->stream, fr, npix, 1.f / float(r->samples), channel, r->read_buf.as<float>());
+    ck(cudaGetLastError(), "read kernel");
+    const size_t n = size_t(npix) * (channel == 0 ? 4 : (channel == 1 ? 1 : 3));
+    ck(cudaMemcpyAsync(out, r->read_buf.p, n * 4, cudaMemcpyDeviceToHost, r->stream), "read back");
+    ck(cudaStreamSynchronize(r->stream), "read back");
+  });
+}
+
+} // namespace
+
+// ------------------------------------------------------------------ C-ABI
+extern "C" {
+
+int phc_abi_version(void) { return PHC_ABI_VERSION; }
+const char *phc_global_error(void) { return g_error.c_str(); }
+
+void phc_material_default(phc_material *m)
+{
+  if (!m)
+    return;
+  std::memset(m, 0, sizeof(*m));
+  m->base_color[0] = m->base_color[1] = m->base_color[2] = 0.8f;
+  m->opacity = 1.f;
+  m->roughness = 1.f;
+  m->ior = 1.5f;
+  m->clearcoat_roughness = 0.03f;
+  m->alpha_mode = 1;
+  m->alpha_cutoff = 0.5f;
+  m->emission_side = 2;
+}
+void phc_sampler_default(phc_sampler *s)
+{
+  if (!s)
+    return;
+  std::memset(s, 0, sizeof(*s));
+  s->type = 1;
+  s->linear = 1;
+  s->size[0] = s->size[1] = s->size[2] = 1;
+  for (int i = 0; i < 4; ++i)
+    s->in_transform[5 * i] = s->out_transform[5 * i] = 1.f;
+}
+void phc_light_default(phc_light *l)
+{
+  if (!l)
+    return;
+  std::memset(l, 0, sizeof(*l));
+  l->direction[2] = -1.f;
+  l->color[0] = l->color[1] = l->color[2] = 1.f;
+  l->intensity = 1.f;
+  l->spot_angle = 3.14159265f;
+}
+void phc_volume_default(phc_volume *v)
+{
+  if (!v)
+    return;
+  std::memset(v, 0, sizeof(*v));
+  v->world_to_local[0] = v->world_to_local[5] = v->world_to_local[10] = 1.f;
+  v->spacing[0] = v->spacing[1] = v->spacing[2] = 1.f;
+  v->dims[0] = v->dims[1] = v->dims[2] = 1;
+  v->value_range[1] = 1.f;
+  v->density_scale = 1.f;
+  v->linear = 1;
+}
+void phc_camera_default(phc_camera *c)
+{
+  if (!c)
+    return;
+  std::memset(c, 0, sizeof(*c));
+  c->direction[2] = -1.f;
+  c->up[1] = 1.f;
+  c->fovy = 1.0471976f;
+  c->height = 1.f;
+  c->aspect = 1.f;
+  c->focus_distance = 1.f;
+  c->image_region[2] = c->image_region[3] = 1.f;
+  c->clip_far = std::numeric_limits<float>::infinity();
+}
+void phc_settings_default(phc_settings *s)
+{
+  if (!s)
+    return;
+  std::memset(s, 0, sizeof(*s));
+  s->pixel_samples = 1;
+  s->max_depth = 6;
+  s->background[3] = 1.f;
+  s->ambient_color[0] = s->ambient_color[1] = s->ambient_color[2] = 1.f;
+  s->max_diffuse_bounces = s->max_glossy_bounces = s->max_transmission_bounces = s->max_volume_bounces = -1;
+}
+void phc_scene_desc_default(phc_scene_desc *d)
+{
+  if (d)
+    std::memset(d, 0, sizeof(*d));
+}
+
+int phc_create(phc_renderer **out)
+{
+  if (!out)
+    return set_error(nullptr, PHC_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  phc_renderer *r = nullptr;
+  try {
+    r = new phc_renderer();
+  } catch (const std::bad_alloc &) {
+    return set_error(nullptr, PHC_ERR_OOM, "host allocation failed");
+  }
+  const int rc = guarded(nullptr, [&] {
+    int count = 0;
+    ck(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+    if (count <= 0)
+      throw ApiError(PHC_ERR_CUDA, "no CUDA device found");
+    ck(cudaGetDevice(&r->device), "cudaGetDevice");
+    ck(cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, r->device), "device attribute");
+    ck(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaEventCreate(&r->ev0), "cudaEventCreate");
+    ck(cudaEventCreate(&r->ev1), "cudaEventCreate");
+  });
+  if (rc != PHC_OK) {
+    delete r;
+    return rc;
+  }
+  *out = r;
+  return PHC_OK;
+}
+
+void phc_destroy(phc_renderer *r)
+{
+  if (!r)
+    return;
+  cudaSetDevice(r->device);
+  if (r->stream)
+    cudaStreamSynchronize(r->stream);
+  delete r;
+}
+
+const char *phc_backend_name(const phc_renderer *) { return "cuda"; }
+
+int phc_set_scene(phc_renderer *r, const phc_scene_desc *desc)
+{
+  if (!r)
+    return set_error(nullptr, PHC_ERR_INVALID, "null renderer");
+  std::lock_guard<std::mutex> lock(r->mutex);
+  if (!desc)
+    return set_error(r, PHC_ERR_INVALID, "null scene");
+  return guarded(r, [&] {
+    check_device(r);
+    r->samples = 0;
+    r->has_scene = false;
+    HostScene hs;
+    build_host_scene(*desc, hs);
+    if (hs.bvh.max_depth >= 64)
+      throw ApiError(PHC_ERR_LIMIT, "BVH deeper than the traversal stack (64 levels)");
+    const std::string err = r->scene.upload(hs, r->stream);
+    if (!err.empty())
+      throw ApiError(err.find("out of memory") != std::string::npos ? PHC_ERR_OOM : PHC_ERR_CUDA, err);
+    r->has_scene = true;
+    r->scene_generation++;
+  });
+}
+
+int phc_render(phc_renderer *r, const phc_camera *camera, const phc_settings *settings, int reset)
+{
+  if (!r)
+    return set_error(nullptr, PHC_ERR_INVALID, "null renderer");
+  std::lock_guard<std::mutex> lock(r->mutex);
+  if (!camera || !settings)
+    return set_error(r, PHC_ERR_INVALID, "null camera or settings");
+  return guarded(r, [&] { render_impl(r, *camera, *settings, reset != 0); });
+}
+
+uint32_t phc_accumulated_samples(const phc_renderer *r) { return r ? r->samples : 0u; }
+
+int phc_read_color(phc_renderer *r, float *rgba) { return read_channel(r, rgba, 0); }
+int phc_read_depth(phc_renderer *r, float *depth) { return read_channel(r, depth, 1); }
+int phc_read_normal(phc_renderer *r, float *xyz) { return read_channel(r, xyz, 2); }
+int phc_read_albedo(phc_renderer *r, float *rgb) { return read_channel(r, rgb, 3); }
+
+int phc_render_stats_get(const phc_renderer *r, phc_render_stats *out)
+{
+  if (!r || !out)
+    return set_error(nullptr, PHC_ERR_INVALID, "null argument");
+  *out = r->last;
+  return PHC_OK;
+}
+
+const char *phc_last_error(const phc_renderer *r) { return r ? r->error.c_str() : g_error.c_str(); }
+
+} // extern "C"

@@ -1,0 +1,556 @@
+// Scene build of the GB300 renderer: the tables the reference's render bridge
+// and path tracer derive from a scene (src/photon/anari/RenderBridge.cpp:
+// 441-826, src/photon/pt/pathtracer.cpp:411-503, src/photon/pt/
+// environment_map.cpp:8-65), computed on the host with the same float
+// arithmetic (this file is compiled with -ffp-contract=off) so the device sees
+// identical CDFs, majorants and light densities, then uploaded to HBM.
+#include "scene_build.h"
+#include "tuning.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <stdexcept>
+
+namespace phc {
+namespace {
+
+struct F3 {
+  float x, y, z;
+};
+inline F3 f3(const float *p) { return {p[0], p[1], p[2]}; }
+inline F3 sub(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline F3 crs(F3 a, F3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float len(F3 v) { return std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+inline float lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+
+// The bridge's material conversion (RenderBridge.cpp:324-370).
+DevMaterial convert_material(const phc_material &in)
+{
+  DevMaterial m{};
+  std::memcpy(m.base_color, in.base_color, sizeof(m.base_color));
+  m.metallic = in.metallic;
+  m.roughness = in.roughness * in.roughness;
+  m.ior = in.ior;
+  m.transmission = in.transmission;
+  m.specular = 0.5f * in.specular;
+  m.clearcoat = in.clearcoat;
+  m.clearcoat_roughness = in.clearcoat_roughness;
+  m.sheen = in.sheen;
+  std::memcpy(m.emission, in.emission, sizeof(m.emission));
+  m.emission_strength = 1.f;
+  m.alpha = in.opacity;
+  const phc_param_source *src[7] = {&in.base_color_src, &in.opacity_src, &in.metallic_src, &in.roughness_src,
+      &in.emission_src, &in.transmission_src, &in.normal_src};
+  for (int k = 0; k < 7; ++k) {
+    m.src_kind[k] = src[k]->kind == 1 ? 1 : (src[k]->kind == 2 ? 2 : 0);
+    m.src_index[k] = src[k]->index;
+  }
+  m.base_color_alpha = in.base_color_alpha ? 1 : 0;
+  if (m.src_kind[SRC_ALPHA] != 0)
+    m.alpha = 1.f;
+  m.alpha_mode = in.alpha_mode == 0 ? 0 : (in.alpha_mode == 2 ? 2 : 1);
+  m.alpha_cutoff = in.alpha_cutoff;
+  m.thin = in.thin_walled ? 1 : 0;
+  m.flags = MF_REFRACTIVE;
+  if (in.emitter_only)
+    m.flags |= MF_EMITTER_ONLY;
+  if (in.hidden_to_camera)
+    m.flags |= MF_HIDDEN;
+  if (in.emission_side == 2)
+    m.flags |= MF_EMIT_BOTH;
+  else if (in.emission_side == 1)
+    m.flags |= MF_EMIT_BACK;
+  return m;
+}
+
+// photon::pt::Material{} defaults (material.h:35-82), used when the scene has
+// no material at all (RenderBridge.cpp:518-519).
+DevMaterial default_material()
+{
+  DevMaterial m{};
+  m.base_color[0] = m.base_color[1] = m.base_color[2] = 0.8f;
+  m.metallic = 0.f;
+  m.roughness = 0.5f;
+  m.ior = 1.5f;
+  m.transmission = 0.f;
+  m.specular = 0.5f;
+  m.clearcoat = 0.f;
+  m.clearcoat_roughness = 0.03f;
+  m.sheen = 0.f;
+  m.alpha = 1.f;
+  m.emission_strength = 0.f;
+  m.alpha_mode = 0;
+  m.alpha_cutoff = 0.5f;
+  m.flags = 0;
+  return m;
+}
+
+bool may_emit(const DevMaterial &m)
+{
+  if (m.emission_strength <= 0.f)
+    return false;
+  return m.src_kind[SRC_EMIT] != 0 || m.emission[0] > 0.f || m.emission[1] > 0.f || m.emission[2] > 0.f;
+}
+
+// EnvironmentMap::build_cdf (environment_map.cpp:8-65): row CDFs of texel
+// luminance and a marginal CDF of row sums weighted by sin(theta).
+void build_env_cdf(HostScene &s)
+{
+  const uint32_t w = s.env_w, h = s.env_h;
+  s.env_marginal.assign(h + 1, 0.f);
+  s.env_conditional.assign(size_t(h) * (w + 1), 0.f);
+  std::vector<float> row_w(h, 0.f);
+  const float PI = 3.14159265358979323846f;
+  for (uint32_t y = 0; y < h; ++y) {
+    float *c = &s.env_conditional[size_t(y) * (w + 1)];
+    c[0] = 0.f;
+    const float st = std::sin(((float)y + 0.5f) * (PI / (float)h));
+    float sum = 0.f;
+    for (uint32_t x = 0; x < w; ++x) {
+      const float *p = &s.env_pixels4[(size_t(y) * w + x) * 4];
+      sum += lum(p[0], p[1], p[2]);
+      c[x + 1] = sum;
+    }
+    if (sum > 0.f) {
+      const float inv = 1.f / sum;
+      for (uint32_t x = 0; x <= w; ++x)
+        c[x] *= inv;
+      c[w] = 1.f;
+    } else {
+      for (uint32_t x = 0; x <= w; ++x)
+        c[x] = (float)x / (float)w;
+    }
+    row_w[y] = sum * st;
+  }
+  float total = 0.f;
+  for (uint32_t y = 0; y < h; ++y) {
+    total += row_w[y];
+    s.env_marginal[y + 1] = total;
+  }
+  if (total > 0.f) {
+    const float inv = 1.f / total;
+    for (uint32_t y = 0; y <= h; ++y)
+      s.env_marginal[y] *= inv;
+    s.env_marginal[h] = 1.f;
+  } else {
+    for (uint32_t y = 0; y <= h; ++y)
+      s.env_marginal[y] = (float)y / (float)h;
+  }
+}
+
+// Volume tables and the macro-cell majorant grid (RenderBridge.cpp:622-778):
+// per macro cell the largest extinction the transfer function reaches over
+// the values the trilinear field can take inside it, with a 1% margin.
+void build_volumes(const phc_scene_desc &in, HostScene &s)
+{
+  size_t value_offset = 0, tf_offset = 0;
+  for (uint32_t i = 0; i < in.volume_count; ++i) {
+    const phc_volume &vd = in.volumes[i];
+    DevVolume v{};
+    std::memcpy(v.w2l, vd.world_to_local, sizeof(v.w2l));
+    std::memcpy(v.origin, vd.origin, sizeof(v.origin));
+    std::memcpy(v.spacing, vd.spacing, sizeof(v.spacing));
+    for (int d = 0; d < 3; ++d)
+      v.dims[d] = std::max<uint32_t>(vd.dims[d], 1);
+    v.data_offset = uint32_t(value_offset);
+    v.tf_offset = uint32_t(tf_offset);
+    const size_t table = vd.transfer ? vd.transfer_count : 0;
+    v.tf_size = uint32_t(table);
+    v.value_lo = vd.value_range[0];
+    v.value_hi = vd.value_range[1];
+    v.density_scale = vd.density_scale;
+    v.linear = vd.linear ? 1u : 0u;
+    float max_opacity = 0.f;
+    for (size_t t = 0; t < table; ++t) {
+      for (int k = 0; k < 4; ++k)
+        s.vol_tf.push_back(vd.transfer[4 * t + k]);
+      max_opacity = std::max(max_opacity, vd.transfer[4 * t + 3]);
+    }
+    v.majorant = max_opacity * vd.density_scale;
+    const size_t nvals = vd.values ? size_t(vd.value_count) : 0;
+    const bool complete = nvals >= size_t(v.dims[0]) * v.dims[1] * v.dims[2];
+    if (!complete)
+      v.majorant = 0.f;
+    v.macro_offset = uint32_t(s.vol_majorants.size());
+    uint32_t sub[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d) {
+      const uint32_t cells = v.dims[d] > 1 ? v.dims[d] - 1 : 1;
+      if (cells <= 32) {
+        sub[d] = std::min<uint32_t>(std::max<uint32_t>((32 + cells - 1) / cells, 1), 16);
+        v.macro_dims[d] = cells * sub[d];
+      } else {
+        v.macro_dims[d] = std::min<uint32_t>(std::max<uint32_t>((v.dims[d] + 2) / 4, 1), 128);
+      }
+    }
+    const float range = vd.value_range[1] - vd.value_range[0];
+    const bool refined = sub[0] > 0 && sub[1] > 0 && sub[2] > 0;
+    if (!refined)
+      for (int d = 0; d < 3; ++d)
+        if (sub[d] > 0)
+          v.macro_dims[d] = std::min<uint32_t>(std::max<uint32_t>((v.dims[d] + 2) / 4, 1), 128);
+    const float *vals = vd.values;
+    auto node = [&](uint32_t x, uint32_t y, uint32_t z) {
+      x = std::min(x, v.dims[0] - 1);
+      y = std::min(y, v.dims[1] - 1);
+      z = std::min(z, v.dims[2] - 1);
+      return vals[(size_t(z) * v.dims[1] + y) * v.dims[0] + x];
+    };
+    auto interp = [&](float gx, float gy, float gz) {
+      const uint32_t x = uint32_t(gx), y = uint32_t(gy), z = uint32_t(gz);
+      const float fx = gx - float(x), fy = gy - float(y), fz = gz - float(z);
+      const float c00 = node(x, y, z) * (1.f - fx) + node(x + 1, y, z) * fx;
+      const float c10 = node(x, y + 1, z) * (1.f - fx) + node(x + 1, y + 1, z) * fx;
+      const float c01 = node(x, y, z + 1) * (1.f - fx) + node(x + 1, y, z + 1) * fx;
+      const float c11 = node(x, y + 1, z + 1) * (1.f - fx) + node(x + 1, y + 1, z + 1) * fx;
+      return (c00 * (1.f - fy) + c10 * fy) * (1.f - fz) + (c01 * (1.f - fy) + c11 * fy) * fz;
+    };
+    const size_t cells_total = size_t(v.macro_dims[0]) * v.macro_dims[1] * v.macro_dims[2];
+    const size_t base = s.vol_majorants.size();
+    s.vol_majorants.resize(base + cells_total);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t mz = 0; mz < int64_t(v.macro_dims[2]); ++mz)
+      for (uint32_t my = 0; my < v.macro_dims[1]; ++my)
+        for (uint32_t mx = 0; mx < v.macro_dims[0]; ++mx) {
+          float bound = 0.f;
+          if (complete && table > 0) {
+            const uint32_t m[3] = {mx, my, uint32_t(mz)};
+            float vmin = std::numeric_limits<float>::max(), vmax = -std::numeric_limits<float>::max();
+            if (refined) {
+              for (int corner = 0; corner < 8; ++corner) {
+                float g[3];
+                for (int d = 0; d < 3; ++d)
+                  g[d] = float(m[d] + ((corner >> d) & 1)) / float(sub[d]);
+                const float value = interp(g[0], g[1], g[2]);
+                vmin = std::min(vmin, value);
+                vmax = std::max(vmax, value);
+              }
+            } else {
+              uint32_t first[3], last[3];
+              for (int d = 0; d < 3; ++d) {
+                const float cells = float(v.dims[d] > 1 ? v.dims[d] - 1 : 1);
+                const float lo = float(m[d]) / float(v.macro_dims[d]) * cells;
+                const float hi = float(m[d] + 1) / float(v.macro_dims[d]) * cells;
+                first[d] = uint32_t(std::max(std::floor(lo) - 1.f, 0.f));
+                last[d] = std::min<uint32_t>(uint32_t(std::ceil(hi)) + 1, v.dims[d] - 1);
+              }
+              for (uint32_t z = first[2]; z <= last[2]; ++z)
+                for (uint32_t y = first[1]; y <= last[1]; ++y)
+                  for (uint32_t x = first[0]; x <= last[0]; ++x) {
+                    const float value = vals[(size_t(z) * v.dims[1] + y) * v.dims[0] + x];
+                    vmin = std::min(vmin, value);
+                    vmax = std::max(vmax, value);
+                  }
+            }
+            auto tpos = [&](float value) {
+              float x = range != 0.f ? (value - vd.value_range[0]) / range : 0.f;
+              x = std::min(std::max(x, 0.f), 1.f);
+              return x * float(table - 1);
+            };
+            const size_t i0 = size_t(std::floor(tpos(vmin)));
+            const size_t i1 = std::min(size_t(std::ceil(tpos(vmax))), table - 1);
+            for (size_t t = i0; t <= i1; ++t)
+              bound = std::max(bound, vd.transfer[4 * t + 3]);
+            if (!(vmin <= vmax))
+              bound = max_opacity;
+          }
+          const size_t cell = (size_t(mz) * v.macro_dims[1] + my) * v.macro_dims[0] + mx;
+          s.vol_majorants[base + cell] = bound * vd.density_scale * 1.01f;
+        }
+    s.vol_values.insert(s.vol_values.end(), vals, vals + nvals);
+    value_offset += nvals;
+    tf_offset += table;
+    s.volumes.push_back(v);
+  }
+}
+
+} // namespace
+
+void build_host_scene(const phc_scene_desc &in, HostScene &s)
+{
+  s = HostScene{};
+  size_t vc = in.vertex_count, tc = in.triangle_count;
+  if ((vc && !in.positions) || (tc && !in.indices))
+    throw std::invalid_argument("scene: positions/indices pointer is null");
+  const bool empty = tc == 0 || vc == 0;
+  if (empty) { // one degenerate triangle, never hit (RenderBridge.cpp:445-453)
+    vc = 3;
+    tc = 1;
+  }
+  if (tc > 0x3fffffffull || vc > 0xffffffffull)
+    throw std::length_error("scene: too many triangles or vertices");
+  std::vector<float> pos3(vc * 3);
+  float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+  for (size_t i = 0; i < vc; ++i)
+    for (int a = 0; a < 3; ++a) {
+      const float p = empty ? 0.f : in.positions[3 * i + a];
+      pos3[3 * i + a] = p;
+      lo[a] = lo[a] < p ? lo[a] : p;
+      hi[a] = hi[a] > p ? hi[a] : p;
+    }
+  s.indices.resize(tc * 3);
+  for (size_t i = 0; i < tc * 3; ++i) {
+    const uint32_t v = empty ? uint32_t(i) : in.indices[i];
+    if (v >= vc)
+      throw std::out_of_range("scene: vertex index out of range");
+    s.indices[i] = v;
+  }
+  const uint32_t material_count = uint32_t(std::max<size_t>(in.material_count, 1));
+  s.material_ids.resize(tc);
+  for (size_t i = 0; i < tc; ++i) {
+    const uint32_t id = (!empty && in.material_ids && i < in.material_id_count) ? in.material_ids[i] : 0u;
+    s.material_ids[i] = id < material_count ? id : 0u;
+  }
+  s.positions4.resize(vc * 4);
+  for (size_t i = 0; i < vc; ++i) {
+    s.positions4[4 * i] = pos3[3 * i];
+    s.positions4[4 * i + 1] = pos3[3 * i + 1];
+    s.positions4[4 * i + 2] = pos3[3 * i + 2];
+    s.positions4[4 * i + 3] = 0.f;
+  }
+  if (!empty && in.normals) {
+    s.normals4.resize(vc * 4);
+    for (size_t i = 0; i < vc; ++i) {
+      s.normals4[4 * i] = in.normals[3 * i];
+      s.normals4[4 * i + 1] = in.normals[3 * i + 1];
+      s.normals4[4 * i + 2] = in.normals[3 * i + 2];
+      s.normals4[4 * i + 3] = 0.f;
+    }
+  }
+  s.prim_vidx.resize(tc * 4);
+  for (size_t t = 0; t < tc; ++t) {
+    s.prim_vidx[4 * t] = s.indices[3 * t];
+    s.prim_vidx[4 * t + 1] = s.indices[3 * t + 1];
+    s.prim_vidx[4 * t + 2] = s.indices[3 * t + 2];
+    s.prim_vidx[4 * t + 3] = s.material_ids[t];
+  }
+  build_prim_records(pos3.data(), s.indices.data(), tc, s.prim_geo);
+  // attributes (RenderBridge.cpp:489-511)
+  size_t total = 0;
+  for (int slot = 0; slot < 5; ++slot)
+    if (!empty && in.attributes[slot]) {
+      s.attr_offset[slot] = int32_t(total);
+      total += vc;
+    }
+  s.attr_values.resize(total * 4);
+  for (int slot = 0; slot < 5; ++slot)
+    if (s.attr_offset[slot] >= 0)
+      std::memcpy(&s.attr_values[size_t(s.attr_offset[slot]) * 4], in.attributes[slot], vc * 16);
+  for (uint32_t i = 0; i < in.material_count; ++i)
+    s.materials.push_back(convert_material(in.materials[i]));
+  if (s.materials.empty())
+    s.materials.push_back(default_material());
+  // samplers (RenderBridge.cpp:527-571)
+  size_t offset = 0;
+  for (uint32_t i = 0; i < in.sampler_count; ++i) {
+    const phc_sampler &sd = in.samplers[i];
+    DevSampler si{};
+    si.type = sd.type == 0 ? 0 : (sd.type == 2 ? 2 : (sd.type == 3 ? 3 : 1));
+    si.in_attribute = sd.in_attribute;
+    si.linear = sd.linear ? 1u : 0u;
+    for (int d = 0; d < 3; ++d) {
+      si.wrap[d] = sd.wrap[d] == 1 ? 1 : (sd.wrap[d] == 2 ? 2 : 0);
+      si.size[d] = std::max<uint32_t>(sd.size[d], 1);
+    }
+    si.offset = uint32_t(offset);
+    std::memcpy(si.in_t, sd.in_transform, sizeof(si.in_t));
+    std::memcpy(si.in_o, sd.in_offset, sizeof(si.in_o));
+    std::memcpy(si.out_t, sd.out_transform, sizeof(si.out_t));
+    std::memcpy(si.out_o, sd.out_offset, sizeof(si.out_o));
+    const size_t n = sd.texels ? size_t(sd.texel_count) : 0;
+    if (si.type != 3 && n < size_t(si.size[0]) * si.size[1] * si.size[2])
+      si.type = 3; // incomplete image: a transform keeps lookups in bounds
+    s.texels.insert(s.texels.end(), sd.texels, sd.texels + 4 * n);
+    offset += n;
+    s.samplers.push_back(si);
+  }
+  if (offset > 0xffffffffull)
+    throw std::length_error("scene: too many sampler texels");
+  for (uint32_t i = 0; i < in.light_count; ++i) {
+    const phc_light &ld = in.lights[i];
+    DevLight l{};
+    l.type = ld.type == 1 ? 1 : (ld.type == 2 ? 2 : 0);
+    std::memcpy(l.position, ld.position, sizeof(l.position));
+    std::memcpy(l.direction, ld.direction, sizeof(l.direction));
+    std::memcpy(l.color, ld.color, sizeof(l.color));
+    l.intensity = ld.intensity;
+    l.radius = ld.radius;
+    l.spot_angle = ld.spot_angle;
+    l.spot_falloff = ld.spot_falloff;
+    s.lights.push_back(l);
+  }
+  const phc_environment &env = in.environment;
+  if (env.present && env.width > 0 && env.height > 0 && env.pixels) {
+    s.env_w = env.width;
+    s.env_h = env.height;
+    const size_t n = size_t(env.width) * env.height;
+    s.env_pixels4.resize(n * 4);
+    for (size_t k = 0; k < n; ++k) {
+      for (int c = 0; c < 3; ++c) {
+        const float v = env.pixels[3 * k + c];
+        s.env_pixels4[4 * k + c] = std::isfinite(v) && v > 0.f ? v : 0.f;
+      }
+      s.env_pixels4[4 * k + 3] = 0.f;
+    }
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        s.env_w2t[r * 3 + c] = env.world_to_map[r * 3 + c];
+        s.env_t2w[c * 3 + r] = env.world_to_map[r * 3 + c];
+      }
+    build_env_cdf(s);
+    s.has_env = true;
+    s.env_visible = env.visible != 0;
+  }
+  build_volumes(in, s);
+  // emissive triangles (RenderBridge.cpp:780-813) and their selection CDF
+  // and area densities (pathtracer.cpp:439-487)
+  std::vector<uint32_t> ids;
+  std::vector<float> areas;
+  if (!empty) {
+    for (size_t t = 0; t < tc; ++t) {
+      const uint32_t mid = s.material_ids[t];
+      if (!may_emit(s.materials[mid]))
+        continue;
+      const F3 p0 = f3(&pos3[3 * size_t(s.indices[3 * t])]);
+      const F3 p1 = f3(&pos3[3 * size_t(s.indices[3 * t + 1])]);
+      const F3 p2 = f3(&pos3[3 * size_t(s.indices[3 * t + 2])]);
+      const float area = 0.5f * len(crs(sub(p1, p0), sub(p2, p0)));
+      if (!(area > 0.f))
+        continue;
+      ids.push_back(uint32_t(t));
+      areas.push_back(area);
+    }
+  }
+  if (!ids.empty()) {
+    const uint32_t n = uint32_t(ids.size());
+    std::vector<double> weights(n, 0.0);
+    double total_w = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+      const DevMaterial &m = s.materials[s.material_ids[ids[i]]];
+      const bool constant = m.src_kind[SRC_EMIT] == 0;
+      const float power = constant
+          ? lum(m.emission[0] * m.emission_strength, m.emission[1] * m.emission_strength,
+                m.emission[2] * m.emission_strength)
+          : m.emission_strength;
+      weights[i] = double(areas[i]) * double(power > 1e-6f ? power : 1e-6f);
+      if (!(areas[i] > 0.f))
+        weights[i] = 0.0;
+      total_w += weights[i];
+    }
+    if (total_w > 0.0) {
+      s.emissive_ids = ids;
+      s.emissive_cdf.assign(n, 0.f);
+      s.prim_light_pdf.assign(tc, 0.f);
+      double running = 0.0;
+      for (uint32_t i = 0; i < n; ++i) {
+        running += weights[i];
+        s.emissive_cdf[i] = float(running / total_w);
+        if (weights[i] > 0.0 && ids[i] < tc)
+          s.prim_light_pdf[ids[i]] = float(weights[i] / total_w / double(areas[i]));
+      }
+      s.emissive_cdf[n - 1] = 1.f;
+    }
+  }
+  // ray offset relative to the scene size (RenderBridge.cpp:815-820)
+  s.eps = 1e-3f;
+  if (!empty && hi[0] >= lo[0]) {
+    const F3 d{hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    const float e = 1e-4f * len(d);
+    s.eps = std::min(std::max(e, 1e-6f), 1e-2f);
+  }
+  s.strategy_count = uint32_t(s.lights.size()) + (s.emissive_cdf.empty() ? 0u : 1u) + (s.has_env ? 1u : 0u);
+  build_bvh8(pos3.data(), vc, s.indices.data(), tc, s.bvh, tuning().max_leaf);
+}
+
+// ------------------------------------------------------------------ upload
+
+DeviceScene::~DeviceScene() { release(); }
+
+void DeviceScene::release()
+{
+  for (void *p : allocations)
+    cudaFree(p);
+  allocations.clear();
+  dev = DevScene{};
+  bytes = 0;
+}
+
+template <class T> T *DeviceScene::put(const std::vector<T> &v, cudaStream_t s, std::string &err)
+{
+  if (v.empty() || !err.empty())
+    return nullptr;
+  void *p = nullptr;
+  const size_t n = v.size() * sizeof(T);
+  cudaError_t e = cudaMalloc(&p, n);
+  if (e != cudaSuccess) {
+    err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  allocations.push_back(p);
+  bytes += n;
+  e = cudaMemcpyAsync(p, v.data(), n, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess)
+    err = std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e);
+  return static_cast<T *>(p);
+}
+
+std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
+{
+  release();
+  std::string err;
+  DevScene d{};
+  d.nodes = reinterpret_cast<const uint4 *>(put(h.bvh.nodes, s, err));
+  d.tris = reinterpret_cast<const float4 *>(put(h.bvh.tris, s, err));
+  d.prim_geo = reinterpret_cast<const float4 *>(put(h.prim_geo, s, err));
+  d.prim_vidx = reinterpret_cast<const uint4 *>(put(h.prim_vidx, s, err));
+  d.normals = reinterpret_cast<const float4 *>(put(h.normals4, s, err));
+  d.positions = reinterpret_cast<const float4 *>(put(h.positions4, s, err));
+  d.node_count = h.bvh.node_count;
+  d.prim_count = uint32_t(h.material_ids.size());
+  d.materials = put(h.materials, s, err);
+  d.material_count = uint32_t(h.materials.size());
+  d.attr_values = reinterpret_cast<const float4 *>(put(h.attr_values, s, err));
+  std::memcpy(d.attr_offset, h.attr_offset, sizeof(d.attr_offset));
+  d.samplers = put(h.samplers, s, err);
+  d.sampler_count = uint32_t(h.samplers.size());
+  d.texels = reinterpret_cast<const float4 *>(put(h.texels, s, err));
+  d.lights = put(h.lights, s, err);
+  d.light_count = uint32_t(h.lights.size());
+  d.emissive_ids = put(h.emissive_ids, s, err);
+  d.emissive_cdf = put(h.emissive_cdf, s, err);
+  d.prim_light_pdf = put(h.prim_light_pdf, s, err);
+  d.emissive_count = uint32_t(h.emissive_cdf.size());
+  d.env_pixels = reinterpret_cast<const float4 *>(put(h.env_pixels4, s, err));
+  d.env_marginal = put(h.env_marginal, s, err);
+  d.env_conditional = put(h.env_conditional, s, err);
+  d.env_w = h.env_w;
+  d.env_h = h.env_h;
+  std::memcpy(d.env_w2t, h.env_w2t, sizeof(d.env_w2t));
+  std::memcpy(d.env_t2w, h.env_t2w, sizeof(d.env_t2w));
+  d.has_env = h.has_env ? 1 : 0;
+  d.env_visible = h.env_visible ? 1 : 0;
+  d.volumes = put(h.volumes, s, err);
+  d.volume_count = uint32_t(h.volumes.size());
+  d.vol_values = put(h.vol_values, s, err);
+  d.vol_tf = reinterpret_cast<const float4 *>(put(h.vol_tf, s, err));
+  d.vol_majorants = put(h.vol_majorants, s, err);
+  d.strategy_count = h.strategy_count;
+  d.eps = h.eps;
+  node_bytes = uint64_t(h.bvh.nodes.size()) * 4;
+  tri_bytes = uint64_t(h.bvh.tris.size()) * 4;
+  bvh_depth = h.bvh.max_depth;
+  if (!err.empty()) {
+    release();
+    return err;
+  }
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    release();
+    return std::string("scene upload: ") + cudaGetErrorString(e);
+  }
+  dev = d;
+  return std::string();
+}
+
+} // namespace phc

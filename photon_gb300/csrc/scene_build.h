@@ -1,0 +1,63 @@
+// Host-side scene build: phc_scene_desc -> device tables.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/photon_cuda.h"
+#include "bvh8.h"
+#include "scene_types.h"
+
+namespace phc {
+
+// Scene tables in host memory, exactly the content the reference's bridge
+// builds (RenderBridge.cpp:441-826) plus the light tables of
+// PathTracer::build_light_tables (pathtracer.cpp:411-503).
+struct HostScene {
+  std::vector<float> positions4;      // vertices as float4
+  std::vector<uint32_t> indices;      // 3 per triangle
+  std::vector<uint32_t> material_ids; // clamped like the bridge
+  std::vector<float> normals4;        // empty: none
+  std::vector<uint32_t> prim_vidx;    // (i0, i1, i2, material) per triangle
+  std::vector<float> prim_geo;        // 12 floats per triangle
+  std::vector<DevMaterial> materials;
+  std::vector<float> attr_values;     // float4
+  int32_t attr_offset[5]{-1, -1, -1, -1, -1};
+  std::vector<DevSampler> samplers;
+  std::vector<float> texels;          // float4
+  std::vector<DevLight> lights;
+  std::vector<uint32_t> emissive_ids;
+  std::vector<float> emissive_cdf, prim_light_pdf;
+  bool has_env{false}, env_visible{true};
+  uint32_t env_w{0}, env_h{0};
+  std::vector<float> env_pixels4, env_marginal, env_conditional;
+  float env_w2t[9]{1, 0, 0, 0, 1, 0, 0, 0, 1}, env_t2w[9]{1, 0, 0, 0, 1, 0, 0, 0, 1};
+  std::vector<DevVolume> volumes;
+  std::vector<float> vol_values, vol_tf, vol_majorants;
+  uint32_t strategy_count{0};
+  float eps{1e-3f};
+  Bvh8Host bvh;
+};
+
+void build_host_scene(const phc_scene_desc &in, HostScene &out);
+
+// Owns the device copies of a HostScene.
+struct DeviceScene {
+  std::vector<void *> allocations;
+  DevScene dev{};
+  size_t bytes{0};
+  uint64_t node_bytes{0}, tri_bytes{0};
+  uint32_t bvh_depth{0};
+  ~DeviceScene();
+  void release();
+  // Returns an empty string on success, else the failure message.
+  std::string upload(const HostScene &h, cudaStream_t stream);
+
+private:
+  template <class T> T *put(const std::vector<T> &v, cudaStream_t s, std::string &err);
+};
+
+} // namespace phc

@@ -1,0 +1,233 @@
+// BVH8 traversal on the SMs (GB300 has no RT cores).
+//
+// Closest-hit and any-hit queries over the quantised BVH8 of bvh8.h.  The
+// traversal keeps the current node group (child base, hit mask, internal
+// mask) in registers and pushes only groups with children left, so the stack
+// holds one 8-byte entry per tree level (a short stack, after Ylitie et al.
+// 2017).  Child boxes are tested with one FMA per plane from the 8-bit grid;
+// the far distance is widened by 4e-7 relative so the outward-rounded boxes
+// never cull a triangle the exact test would hit.
+//
+// The triangle test is the reference's Möller–Trumbore
+// (include/photon/pt/geom/triangle_intersect.h:18-52) with the same operation
+// order and the same e1/e2 roundings (precomputed on the host), compiled
+// without FMA contraction, so t, u, v and the accept/reject decisions are
+// bit-identical to the reference's for the same ray and triangle; the closest
+// hit therefore equals the reference's except for exact ties in t, which the
+// reference breaks by its own traversal order (mesh_intersector.h:92).
+//
+// The functions are __host__ __device__ so host-side tests can run the very
+// same traversal on the CPU against the oracle.
+#pragma once
+
+#include "pt_math.cuh"
+#include "scene_types.h"
+
+namespace phc {
+
+#ifndef PHC_STACK_SIZE
+#define PHC_STACK_SIZE 64
+#endif
+
+struct RayHit {
+  float t;
+  uint32_t prim; // 0xffffffff: miss
+  float u, v;
+};
+
+struct TravCounters {
+  uint32_t nodes;
+  uint32_t tris;
+};
+
+PHC_HD uint4 ldg4(const uint4 *p)
+{
+#ifdef __CUDA_ARCH__
+  return __ldg(p);
+#else
+  return *p;
+#endif
+}
+PHC_HD float4 ldg4(const float4 *p)
+{
+#ifdef __CUDA_ARCH__
+  return __ldg(p);
+#else
+  return *p;
+#endif
+}
+
+PHC_HD float safe_inv(float x) { return 1.f / (fabsf(x) > 1e-20f ? x : (x < 0.f ? -1e-20f : 1e-20f)); }
+
+// Möller–Trumbore exactly as triangle_intersect.h:18-52.
+PHC_HD bool tri_test(V3 o, V3 d, float4 r0, float4 r1, float4 r2, float tmin, float tmax, float &t, float &u, float &v)
+{
+  const V3 v0 = v3(r0), e1 = v3(r1), e2 = v3(r2);
+  const V3 p = cross(d, e2);
+  const float det = dot(e1, p);
+  if (fabsf(det) < 1e-30f)
+    return false;
+  const float inv_det = 1.f / det;
+  const V3 tv = o - v0;
+  u = dot(tv, p) * inv_det;
+  if (u < 0.f || u > 1.f)
+    return false;
+  const V3 q = cross(tv, e1);
+  v = dot(d, q) * inv_det;
+  if (v < 0.f || (u + v) > 1.f)
+    return false;
+  t = dot(e2, q) * inv_det;
+  if (t < tmin || t > tmax)
+    return false;
+  return true;
+}
+
+PHC_HD float byte_f(uint32_t w, int j) { return float((w >> (8 * j)) & 0xffu); }
+
+// Intersects the 8 child boxes of one node; returns the k-ordered hit mask of
+// internal children (bit k = slot k ^ oct) and the triangle mask.
+PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V3 idir, uint32_t oct, float tmin,
+    float tmax, uint32_t &child_base, uint32_t &hits, uint32_t &imask, uint32_t &tri_base, uint32_t &tri_hits)
+{
+  const uint4 w0 = ldg4(nodes + 5 * size_t(ni) + 0);
+  const uint4 w1 = ldg4(nodes + 5 * size_t(ni) + 1);
+  const uint4 w2 = ldg4(nodes + 5 * size_t(ni) + 2);
+  const uint4 w3 = ldg4(nodes + 5 * size_t(ni) + 3);
+  const uint4 w4 = ldg4(nodes + 5 * size_t(ni) + 4);
+  const float px = u2f(w0.x), py = u2f(w0.y), pz = u2f(w0.z);
+  const float sx = u2f((w0.w & 0xffu) << 23);
+  const float sy = u2f(((w0.w >> 8) & 0xffu) << 23);
+  const float sz = u2f(((w0.w >> 16) & 0xffu) << 23);
+  imask = w0.w >> 24;
+  child_base = w1.x;
+  tri_base = w1.y;
+  const float ax = sx * idir.x, ay = sy * idir.y, az = sz * idir.z;
+  const float bx = (px - o.x) * idir.x, by = (py - o.y) * idir.y, bz = (pz - o.z) * idir.z;
+  // near/far byte rows per axis (qlo for a positive direction component)
+  const bool nxl = idir.x >= 0.f, nyl = idir.y >= 0.f, nzl = idir.z >= 0.f;
+  const uint32_t nx0 = nxl ? w2.x : w3.z, nx1 = nxl ? w2.y : w3.w;
+  const uint32_t fx0 = nxl ? w3.z : w2.x, fx1 = nxl ? w3.w : w2.y;
+  const uint32_t ny0 = nyl ? w2.z : w4.x, ny1 = nyl ? w2.w : w4.y;
+  const uint32_t fy0 = nyl ? w4.x : w2.z, fy1 = nyl ? w4.y : w2.w;
+  const uint32_t nz0 = nzl ? w3.x : w4.z, nz1 = nzl ? w3.y : w4.w;
+  const uint32_t fz0 = nzl ? w4.z : w3.x, fz1 = nzl ? w4.w : w3.y;
+  hits = 0u;
+  tri_hits = 0u;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const uint32_t m4 = h ? w1.w : w1.z;
+    const uint32_t nxw = h ? nx1 : nx0, fxw = h ? fx1 : fx0;
+    const uint32_t nyw = h ? ny1 : ny0, fyw = h ? fy1 : fy0;
+    const uint32_t nzw = h ? nz1 : nz0, fzw = h ? fz1 : fz0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t mb = (m4 >> (8 * j)) & 0xffu;
+      const float tnx = fmaf(byte_f(nxw, j), ax, bx);
+      const float tny = fmaf(byte_f(nyw, j), ay, by);
+      const float tnz = fmaf(byte_f(nzw, j), az, bz);
+      const float tfx = fmaf(byte_f(fxw, j), ax, bx);
+      const float tfy = fmaf(byte_f(fyw, j), ay, by);
+      const float tfz = fmaf(byte_f(fzw, j), az, bz);
+      const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+      const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+      if (mb != 0u && t0 <= t1 * 1.0000004f) {
+        const int s = 4 * h + j;
+        if (mb & 0x80u)
+          hits |= 1u << (uint32_t(s) ^ oct);
+        else
+          tri_hits |= ((1u << (mb >> 5)) - 1u) << (mb & 31u);
+      }
+    }
+  }
+}
+
+// Full traversal of one ray.  ANY: stop at the first hit (occlusion).
+template <bool ANY, bool COUNT>
+PHC_HD RayHit trace_ray(const DevScene &sc, V3 o, V3 d, float tmin, float tmax, TravCounters *ctr)
+{
+  RayHit best{tmax, 0xffffffffu, 0.f, 0.f};
+  if (!(tmax > tmin))
+    return best;
+  const V3 idir{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+  const uint32_t oct = (d.x < 0.f ? 4u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 1u : 0u);
+  uint2 stack[PHC_STACK_SIZE];
+  int sp = 0;
+  uint32_t g_base = 0u, g_hits = 1u << oct, g_imask = 1u;
+  for (;;) {
+    if (g_hits == 0u) {
+      if (sp == 0)
+        break;
+      const uint2 e = stack[--sp];
+      g_base = e.x;
+      g_hits = e.y & 0xffu;
+      g_imask = e.y >> 8;
+    }
+    const uint32_t k = ffs32(g_hits) - 1u;
+    g_hits &= g_hits - 1u;
+    const uint32_t s = k ^ oct;
+    const uint32_t ni = g_base + popc32(g_imask & ((1u << s) - 1u));
+    if (g_hits != 0u && sp < PHC_STACK_SIZE) {
+      stack[sp].x = g_base;
+      stack[sp].y = g_hits | (g_imask << 8);
+      ++sp;
+    }
+    uint32_t tri_base, tri_hits;
+    intersect_node(sc.nodes, ni, o, idir, oct, tmin, best.t, g_base, g_hits, g_imask, tri_base, tri_hits);
+    if (COUNT)
+      ctr->nodes++;
+    while (tri_hits) {
+      const uint32_t b = ffs32(tri_hits) - 1u;
+      tri_hits &= tri_hits - 1u;
+      const float4 *r = sc.tris + 3 * size_t(tri_base + b);
+      const float4 r0 = ldg4(r), r1 = ldg4(r + 1), r2 = ldg4(r + 2);
+      if (COUNT)
+        ctr->tris++;
+      float t, u, v;
+      if (tri_test(o, d, r0, r1, r2, tmin, best.t, t, u, v)) {
+        best.t = t;
+        best.prim = f2u(r0.w);
+        best.u = u;
+        best.v = v;
+        if (ANY)
+          return best;
+      }
+    }
+  }
+  return best;
+}
+
+// Attributes of a hit as intersect_mesh_bvh computes them after the
+// traversal (mesh_intersector.h:129-178): position, geometric normal,
+// interpolated shading normal, material id.
+struct HitAttr {
+  V3 p, n, sn;
+  uint32_t material_id;
+  uint4 vidx;
+};
+PHC_HD HitAttr hit_attributes(const DevScene &sc, V3 o, V3 d, const RayHit &h)
+{
+  HitAttr a;
+  const float4 *g = sc.prim_geo + 3 * size_t(h.prim);
+  const V3 e1 = v3(ldg4(g + 1)), e2 = v3(ldg4(g + 2));
+#ifdef __CUDA_ARCH__
+  a.vidx = __ldg(sc.prim_vidx + h.prim);
+#else
+  a.vidx = sc.prim_vidx[h.prim];
+#endif
+  a.p = o + d * h.t;
+  const V3 nn = normalize(cross(e1, e2));
+  a.n = nn;
+  a.sn = nn;
+  if (sc.normals) {
+    const float w0 = 1.f - h.u - h.v, w1 = h.u, w2 = h.v;
+    const V3 n0 = v3(ldg4(sc.normals + a.vidx.x)), n1 = v3(ldg4(sc.normals + a.vidx.y));
+    const V3 n2 = v3(ldg4(sc.normals + a.vidx.z));
+    a.sn = normalize(n0 * w0 + n1 * w1 + n2 * w2);
+    if (dot(a.sn, nn) < 0.f)
+      a.sn = a.sn * -1.f;
+  }
+  a.material_id = a.vidx.w;
+  return a;
+}
+
+} // namespace phc

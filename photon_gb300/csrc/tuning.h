@@ -1,0 +1,21 @@
+// Launch and scheduling parameters of the renderer, set by the autotuner
+// (photon_gb300/autotune.py) through phc_tuning_set or the PHC_TUNE_<KEY>
+// environment variables, read once per render call.
+#pragma once
+
+#include <cstdint>
+
+namespace phc {
+
+struct Tuning {
+  int64_t wave_paths{1 << 21};       // paths in flight per wave (lanes = wave_paths / pixels)
+  int trace_blocks_per_sm{16};       // persistent grid of the traversal kernels (128 threads)
+  int shade_blocks_per_sm{8};        // persistent grid of the shading kernel (128 threads)
+  int use_graph{1};                  // replay each wave as a CUDA graph
+  int count_traversal{0};            // node-visit / triangle-test counters (roofline runs)
+  int max_leaf{3};                   // triangles per BVH8 leaf child (1..3), read at scene build
+};
+
+Tuning &tuning();
+
+} // namespace phc

@@ -1,0 +1,101 @@
+// Wavefront state and kernel launchers of the renderer (host/device view).
+//
+// One render call runs the samples of every pixel as waves of `lanes`
+// samples; one wave is a fixed sequence of launches (raygen, then per bounce
+// iteration: closest-hit trace, shade, shadow trace) over SoA queues in HBM
+// whose lengths live in device counters, so the host never waits between
+// bounces (the reference reduces the active count to the host every bounce,
+// pathtracer.cpp:1094-1126).  The sequence is captured once as a CUDA graph
+// and replayed per wave.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "scene_types.h"
+
+namespace phc {
+
+// Per-render-call constants (camera, settings), in device memory.
+struct RenderConst {
+  float origin[3], lower_left[3], horizontal[3], vertical[3], cu[3], cv[3], cw[3];
+  float lens_radius;
+  int32_t ortho;
+  float clip_near, clip_far;
+  float region[4];
+  uint32_t w, h, npix, spp;
+  uint32_t sample_offset; // bridge sample counter when the render call began
+  uint32_t max_depth, max_iter;
+  float bg[4];
+  const float4 *bg_image;
+  uint32_t bg_w, bg_h;
+  float ambient[3];
+  int32_t adaptive;
+  float tp_clamp;
+  int32_t max_diffuse, max_glossy, max_transmission, max_volume;
+  float clamp_direct, clamp_indirect;
+  uint32_t lanes; // samples of one pixel in flight per wave
+};
+
+// Path state, structure of arrays over `cap` slots (two copies, ping-pong).
+struct PathSoA {
+  float4 *ray_o; // org.xyz, tmin
+  float4 *ray_d; // dir.xyz, tmax
+  float4 *tp;    // throughput.xyz, prev_pdf (< 0: delta / none)
+  uint4 *info;   // pixel, sample index, bounce kinds, depth | primary << 16
+  float *pdist;  // distance travelled by the camera ray
+};
+
+// Shadow ray queue: (o.xyz, tmax), (d.xyz, contrib.x), (contrib.yz, slot, sample).
+struct ShadowSoA {
+  float4 *a, *b, *c;
+};
+
+// Per pixel-slot accumulators (slot = lane * npix + pixel).
+struct Accum {
+  float4 *acc;      // radiance.xyz, alpha
+  float4 *acc_sq;   // adaptive: squared sample values
+  float4 *start;    // adaptive: acc when the last sample began
+  uint32_t *nsamp;  // samples started
+  float4 *aov_n;    // normal.xyz, depth
+  float4 *aov_a;    // albedo.xyz, (sample index + 1) of the write as float bits, 0 unwritten
+};
+
+// Device counters of one wave.
+struct WaveCounters {
+  uint32_t *count;   // [max_iter + 1] paths entering iteration it
+  uint32_t *scount;  // [max_iter] shadow rays of iteration it
+  uint32_t *fetch;   // [3 * max_iter + 1] work-distribution counters
+  uint32_t *wave;    // current wave index within the render call
+  uint32_t *error;   // sticky error word
+};
+
+// Frame accumulated across render calls (RenderBridge.cpp:386-410).
+struct Frame {
+  float4 *color;  // rgb * weight sum, alpha
+  float4 *normal; // xyz, depth
+  float4 *albedo;
+};
+
+struct LaunchCfg {
+  int blocks_trace, blocks_shade, blocks_raygen;
+  int threads;
+};
+
+void launch_raygen(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA out, Accum acc,
+    WaveCounters wc);
+void launch_trace(const LaunchCfg &c, cudaStream_t s, DevScene sc, PathSoA in, float4 *hits, WaveCounters wc, int it,
+    uint64_t *stats);
+void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in, PathSoA out,
+    const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it);
+void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh, Accum acc,
+    WaveCounters wc, int it, uint64_t *stats);
+void launch_wave_end(cudaStream_t s, const RenderConst *rc, Accum acc, WaveCounters wc, uint32_t npix, int adaptive,
+    int max_iter, uint64_t *ray_totals);
+void launch_resolve(cudaStream_t s, Accum acc, Frame fr, uint32_t npix, uint32_t lanes, float weight, int first);
+void launch_read(cudaStream_t s, Frame fr, uint32_t npix, float inv_samples, int channel, float *out);
+// Resident blocks per SM of a kernel (0 trace, 1 shade, 2 shadow, 3 raygen).
+int max_active_blocks(int which, int threads);
+
+} // namespace phc

@@ -1,0 +1,167 @@
+"""Python mirror of photon::bridge::Renderer over the C-ABI.
+
+Method names, argument meaning and error behaviour follow
+src/photon/anari/RenderBridge.h:175-214: set_scene / render / read_* raise
+PhotonError where the reference returns false with a message, and
+accumulated_samples() counts the samples of the accumulated frame.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .native import PhotonError, load
+
+
+class Renderer:
+    """One GB300 path tracer: scene, BVH8, wavefront buffers, accumulated frame."""
+
+    def __init__(self):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.phc_create(C.byref(h))
+        if rc != 0:
+            raise PhotonError(rc, self.lib.phc_global_error().decode())
+        self.h = h
+        self.width = self.height = 0
+        self._keep = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.phc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise PhotonError(rc, self.lib.phc_last_error(self.h).decode())
+
+    def backend_name(self) -> str:
+        return self.lib.phc_backend_name(self.h).decode()
+
+    def set_scene(self, scene):
+        """Uploads a photon_gb300.scene.SceneData (bridge::SceneData)."""
+        desc, keep = scene.desc()
+        self._check(self.lib.phc_set_scene(self.h, C.addressof(desc)))
+
+    def render(self, camera, settings, reset=True):
+        self.width, self.height = settings.width, settings.height
+        self._check(self.lib.phc_render(self.h, C.addressof(camera), C.addressof(settings), int(reset)))
+
+    def accumulated_samples(self) -> int:
+        return int(self.lib.phc_accumulated_samples(self.h))
+
+    def read(self, channel: str, out: np.ndarray | None = None) -> np.ndarray:
+        """channel.color (h, w, 4) / depth (h, w) / normal, albedo (h, w, 3);
+        row 0 is the bottom row."""
+        n = {"color": 4, "depth": 1, "normal": 3, "albedo": 3}[channel]
+        if out is None:
+            out = np.empty((self.height, self.width, n), np.float32)
+        fn = getattr(self.lib, "phc_read_" + channel)
+        self._check(fn(self.h, out.ctypes.data))
+        return out[..., 0] if (n == 1 and out.ndim == 3) else out
+
+    def read_color(self):
+        return self.read("color")
+
+    def read_depth(self):
+        return self.read("depth")
+
+    def read_normal(self):
+        return self.read("normal")
+
+    def read_albedo(self):
+        return self.read("albedo")
+
+    def stats(self) -> dict:
+        s = _abi.RenderStats()
+        self._check(self.lib.phc_render_stats_get(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+def tuning_set(key: str, value: int):
+    lib = load()
+    if lib.phc_tuning_set(key.encode(), int(value)) != 0:
+        raise ValueError(f"bad tuning parameter {key}={value}")
+
+
+def tuning_get(key: str) -> int:
+    return int(load().phc_tuning_get(key.encode()))
+
+
+class Accel:
+    """Level A: the ray back-end over caller device pointers (torch tensors)."""
+
+    def __init__(self, positions, indices, normals=None, material_ids=None):
+        self.lib = load()
+        pos = np.ascontiguousarray(positions, np.float32)
+        idx = np.ascontiguousarray(indices, np.uint32)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+        mid = None if material_ids is None else np.ascontiguousarray(material_ids, np.uint32)
+        h = C.c_void_p()
+        rc = self.lib.phc_accel_create(C.byref(h), pos.ctypes.data, pos.size // 3, idx.ctypes.data, idx.size // 3,
+                                       None if nrm is None else nrm.ctypes.data,
+                                       None if mid is None else mid.ctypes.data)
+        if rc != 0:
+            raise PhotonError(rc, self.lib.phc_accel_error().decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.phc_accel_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _run(self, fn, o, d, t0, t1, out, stream=None):
+        n = int(t0.numel())
+        rc = fn(self.h, o.data_ptr(), d.data_ptr(), t0.data_ptr(), t1.data_ptr(), n, out.data_ptr(), stream)
+        if rc != 0:
+            raise PhotonError(rc, self.lib.phc_accel_error().decode())
+        return out
+
+    def trace_closest(self, o, d, tmin, tmax, out=None):
+        """88-byte HitResult records into a uint8 CUDA tensor (n, 88)."""
+        import torch
+        if out is None:
+            out = torch.empty((tmin.numel(), 88), dtype=torch.uint8, device=tmin.device)
+        return self._run(self.lib.phc_trace_closest, o, d, tmin, tmax, out)
+
+    def trace_closest_compact(self, o, d, tmin, tmax, out=None):
+        import torch
+        if out is None:
+            out = torch.empty((tmin.numel(), 4), dtype=torch.float32, device=tmin.device)
+        return self._run(self.lib.phc_trace_closest_compact, o, d, tmin, tmax, out)
+
+    def trace_occluded(self, o, d, tmin, tmax, out=None):
+        import torch
+        if out is None:
+            out = torch.empty((tmin.numel(),), dtype=torch.int32, device=tmin.device)
+        return self._run(self.lib.phc_trace_occluded, o, d, tmin, tmax, out)
+
+    def counters(self):
+        a, b = C.c_uint64(), C.c_uint64()
+        self.lib.phc_accel_counters(self.h, C.byref(a), C.byref(b))
+        return int(a.value), int(b.value)
+
+    def info(self):
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self.lib.phc_accel_info(self.h, C.byref(a), C.byref(b), C.byref(c))
+        return {"node_bytes": a.value, "tri_bytes": b.value, "node_count": c.value}

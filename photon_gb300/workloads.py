@@ -112,8 +112,10 @@ def box_room():
     mb.add(*_quad((-1, 0, -1), (1, 0, -1), (1, W, -1), (-1, W, -1)), 0)
     mb.add(*_quad((-1, 0, -1), (-1, W, -1), (-1, W, 1), (-1, 0, 1)), 1)
     mb.add(*_quad((1, 0, -1), (1, 0, 1), (1, W, 1), (1, W, -1)), 2)
-    mb.add(*_box((-0.33, 0.0, -0.3), (0.6, 1.2, 0.6), 17.0), 0)
-    mb.add(*_box((0.35, 0.0, 0.3), (0.6, 0.6, 0.6), -18.0), 0)
+    # the boxes float 1 mm above the floor: no coplanar faces, so no exact
+    # distance ties whose winner depends on the traversal order
+    mb.add(*_box((-0.33, 1e-3, -0.3), (0.6, 1.2, 0.6), 17.0), 0)
+    mb.add(*_box((0.35, 1e-3, 0.3), (0.6, 0.6, 0.6), -18.0), 0)
     ly = W - 1e-3
     mb.add(*_quad((-0.25, ly, -0.25), (0.25, ly, -0.25), (0.25, ly, 0.25), (-0.25, ly, 0.25)), 3)
     sc = mb.build(name="box_room")
