@@ -1,0 +1,344 @@
+"""Benchmark of the GB300 path tracer on the 500K-triangle workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step is one render call of the full workload: 498,726 triangles, 1024x1024
+pixels, 128 samples per pixel, max depth 8 (the reference's 1024^2 / depth-8
+metric), with a procedural 1024x512 fp32 sun+sky environment and 4 emissive
+triangles (seeded synthetic scene: the reference's published scenes are not
+available offline).
+
+Our arm prints one JSON line with
+  value      Msamples/s over the K timed steps, device time (CUDA events on the
+             renderer's stream), scene resident, L2 flushed before every step;
+  e2e        the same metric through the public API with host buffers: every
+             step renders from host-side camera/settings and reads the colour
+             channel back into pinned host memory;
+  roofline   the dominant kernel's algorithmic bytes / its event-timed
+             duration against the measured HBM copy bandwidth;
+  cpu_baseline  the CPU oracle (a restatement of the reference's algorithm)
+             on the host cores, on a bounded sample of the same workload.
+--impl reference times that CPU implementation as the main line.
+Under torchrun (N > 1) every rank renders its own replica (the path is
+replicated, not sharded) and rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Msamples/s @1024² d8 vs ref & plain; batched/plain ratio; adjoint/fwd time"
+NODE_BYTES = 80   # one BVH8 node
+TRI_BYTES = 48    # one triangle record (v0, e1, e2 as float4)
+RAY_BYTES = 32    # origin+tmin, direction+tmax
+HIT_BYTES = 16    # t, prim, u, v
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if n_gpus > 0 else "gloo")
+    return world, rank, local
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def workload():
+    from photon_gb300 import workloads
+    sc, cam, st = workloads.procedural_500k()
+    desc = (f"procedural_500k: {sc.triangle_count} tris (60 displaced icospheres + 140 tori on a ground plane), "
+            f"{st.width}x{st.height}, {st.pixel_samples} spp, max depth {st.max_depth}, "
+            "1024x512 fp32 sun+sky env + 4 emissive tris, Disney materials per object")
+    return sc, cam, st, desc
+
+
+def cpu_baseline(sc, cam, st, spp=1, frames=2):
+    """The CPU oracle on a bounded sample: `frames` full-resolution frames of
+    `spp` samples, all host threads."""
+    import oracle
+    oracle.build()
+    r = oracle.CpuRenderer("oracle")
+    r.set_scene(sc)
+    import ctypes as C
+    s = type(st).from_buffer_copy(bytes(st))
+    s.pixel_samples = spp
+    t = time.perf_counter()
+    for f in range(frames):
+        r.render(cam, s, True)
+    dt = time.perf_counter() - t
+    samples = s.width * s.height * spp * frames
+    return {"value": samples / dt / 1e6, "unit": "Msamples/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{frames} frames of {s.width}x{s.height} at {spp} spp of the same workload "
+                      f"({samples} pixel-samples, {dt:.1f} s)"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    sc, cam, st, desc = workload()
+    import oracle
+    oracle.build()
+    r = oracle.CpuRenderer("oracle")
+    r.set_scene(sc)
+    s = type(st).from_buffer_copy(bytes(st))
+    s.pixel_samples = 1
+    for _ in range(args.warmup):
+        r.render(cam, s, True)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        r.render(cam, s, True)
+    dt = time.perf_counter() - t
+    samples = s.width * s.height * args.steps
+    v = samples / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Msamples/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": desc, "sample_per_step": f"{s.width}x{s.height} at 1 spp",
+                   "parallelism": "host cores (OpenMP)"},
+        "cpu_baseline": {"value": v, "unit": "Msamples/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{args.steps} frames of {s.width}x{s.height} at 1 spp"},
+        "e2e": {"value": v, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    from photon_gb300 import build as pbuild
+    pbuild.build()
+    import photon_gb300 as p
+
+    sc, cam, st, desc = workload()
+    if args.spp:
+        st.pixel_samples = args.spp
+    r = p.Renderer()
+    t = time.perf_counter()
+    r.set_scene(sc)
+    scene_s = time.perf_counter() - t
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > 129 MB L2
+
+    for _ in range(args.warmup):
+        r.render(cam, st, True)
+
+    # ---- device-timed steps (scene resident)
+    barrier(world)
+    torch.cuda.synchronize()
+    dev_ms, samples, launches, closest, shadow = 0.0, 0, 0, 0, 0
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            r.render(cam, st, True)
+            s = r.stats()
+            dev_ms += s["render_ms"]
+            samples += s["pixel_samples"]
+            launches += s["kernel_launches"]
+            closest += s["closest_rays"]
+            shadow += s["shadow_rays"]
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t_wall
+    barrier(world)
+    t_max = dist_max(dev_ms / 1e3, world)
+    total_samples = dist_sum(samples, world)
+    value = total_samples / t_max / 1e6
+
+    # ---- end to end through the public API with host buffers
+    out = torch.empty((st.height, st.width, 4), dtype=torch.float32).pin_memory()
+    out_np = out.numpy()
+    barrier(world)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    e2e_samples = 0
+    for _ in range(args.steps):
+        r.render(cam, st, True)
+        r.read("color", out_np)
+        e2e_samples += r.stats()["pixel_samples"]
+    e2e_s = dist_max(time.perf_counter() - t, world)
+    e2e_value = dist_sum(e2e_samples, world) / e2e_s / 1e6
+
+    # ---- per-kernel times and traversal counters (events around every launch)
+    p.tuning_set("time_kernels", 1)
+    p.tuning_set("count_traversal", 1)
+    flush.zero_()
+    torch.cuda.synchronize()
+    r.render(cam, st, True)
+    prof = r.stats()
+    p.tuning_set("time_kernels", 0)
+    p.tuning_set("count_traversal", 0)
+    kinds = ["raygen", "trace_closest", "shade", "trace_shadow", "wave_end+resolve"]
+    kms = dict(zip(kinds, prof["kernel_ms"]))
+    kcount = dict(zip(kinds, prof["kernel_count"]))
+    # algorithmic bytes of the traversal kernels
+    b_closest = (prof["closest_rays"] * (RAY_BYTES + HIT_BYTES) + prof["node_visits"] * NODE_BYTES
+                 + prof["tri_tests"] * TRI_BYTES)
+    b_shadow = (prof["shadow_rays"] * (RAY_BYTES + 16) + prof["shadow_node_visits"] * NODE_BYTES
+                + prof["shadow_tri_tests"] * TRI_BYTES)
+    peak, peak_kind = peaks()
+    dom = max(kinds, key=lambda k: kms[k])
+    if dom == "trace_shadow":
+        bytes_alg, ms = b_shadow, kms["trace_shadow"]
+    else:
+        dom_t = "trace_closest"
+        bytes_alg, ms = b_closest, kms["trace_closest"]
+    achieved = bytes_alg / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    roofline = {
+        "kernel": "k_trace (BVH8 closest hit)" if dom != "trace_shadow" else "k_shadow (BVH8 any hit)",
+        "dominant_kernel_by_time": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "traffic": None,
+        "bytes_per_ray": bytes_alg / max(1, prof["closest_rays"] if dom != "trace_shadow" else prof["shadow_rays"]),
+        "nodes_per_ray": prof["node_visits"] / max(1, prof["closest_rays"]),
+        "tris_per_ray": prof["tri_tests"] / max(1, prof["closest_rays"]),
+        "launches": kcount["trace_closest"], "kernel_ms_total": kms["trace_closest"],
+    }
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, cam, st)
+
+    if rank == 0:
+        h2d = C.sizeof(cam) + C.sizeof(st)
+        line = {
+            "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": desc, "l2": "flushed before every step (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "lanes_paths_per_wave": p.tuning_get("wave_paths")},
+            "mrays_per_s": (closest + shadow) / (dev_ms / 1e3) / 1e6,
+            "wall_ms_per_step": wall * 1e3 / args.steps,
+            "scene_upload_s": scene_s,
+            "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": st.width * st.height * 16},
+            "roofline": roofline,
+            "kernel_ms": kms, "kernel_launches_profiled": kcount,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (testing only)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup(args.gpus if args.impl == "ours" else 0)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -210,9 +210,17 @@ typedef struct phc_render_stats {
   uint64_t pixel_samples;   /* pixel-samples traced (adaptive: started ones)  */
   uint64_t closest_rays;    /* rays given to closest-hit traversal            */
   uint64_t shadow_rays;     /* rays given to any-hit traversal                */
-  uint64_t node_visits;     /* BVH8 nodes visited (when counters are enabled) */
-  uint64_t tri_tests;       /* triangle tests (when counters are enabled)     */
+  uint64_t node_visits;     /* BVH8 nodes visited by closest-hit rays (when
+                               the "count_traversal" tuning key is 1)         */
+  uint64_t tri_tests;       /* triangle tests of closest-hit rays (same)      */
+  uint64_t shadow_node_visits; /* the same for the shadow (any-hit) rays      */
+  uint64_t shadow_tri_tests;
   double render_ms;         /* device time of the render call                 */
+  uint64_t kernel_launches; /* kernels launched by the call (graph nodes too) */
+  /* Device time per kernel kind (raygen, closest-hit trace, shade, shadow,
+     wave end + resolve) when the "time_kernels" tuning key is 1, else 0. */
+  double kernel_ms[5];
+  uint64_t kernel_count[5];
 } phc_render_stats;
 
 /* ------------------------------------------------------------------ defaults */

@@ -119,7 +119,10 @@ class RenderStats(C.Structure):
     _fields_ = [
         ("pixel_samples", C.c_uint64), ("closest_rays", C.c_uint64),
         ("shadow_rays", C.c_uint64), ("node_visits", C.c_uint64),
-        ("tri_tests", C.c_uint64), ("render_ms", C.c_double),
+        ("tri_tests", C.c_uint64), ("shadow_node_visits", C.c_uint64),
+        ("shadow_tri_tests", C.c_uint64), ("render_ms", C.c_double),
+        ("kernel_launches", C.c_uint64), ("kernel_ms", C.c_double * 5),
+        ("kernel_count", C.c_uint64 * 5),
     ]
 
 

@@ -269,9 +269,50 @@ WaveCounters wave_counters(phc_renderer *r, int max_iter)
 }
 size_t per_wave_counter_bytes(int max_iter) { return size_t(5 * max_iter + 2) * 4; }
 
+// Per-kind kernel times of a render call (time_kernels mode): events around
+// every launch of a wave, read after the wave.
+struct KernelTimer {
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kind;
+  size_t used{0};
+  double ms[5]{};
+  uint64_t count[5]{};
+  ~KernelTimer()
+  {
+    for (cudaEvent_t e : ev)
+      cudaEventDestroy(e);
+  }
+  void begin_wave() { used = 0; kind.clear(); }
+  void mark(cudaStream_t s, int k)
+  {
+    if (used + 2 > ev.size()) {
+      cudaEvent_t a, b;
+      ck(cudaEventCreate(&a), "cudaEventCreate");
+      ck(cudaEventCreate(&b), "cudaEventCreate");
+      ev.push_back(a);
+      ev.push_back(b);
+    }
+    kind.push_back(k);
+    ck(cudaEventRecord(ev[used], s), "cudaEventRecord");
+    used += 2;
+  }
+  void done(cudaStream_t s) { ck(cudaEventRecord(ev[used - 1], s), "cudaEventRecord"); }
+  void end_wave(cudaStream_t s)
+  {
+    ck(cudaStreamSynchronize(s), "timed wave");
+    for (size_t i = 0; i < kind.size(); ++i) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]);
+      ms[kind[i]] += t;
+      count[kind[i]]++;
+    }
+  }
+};
+
 // One wave: counter reset, raygen, per iteration trace / shade / shadow, end.
-void record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, const RenderConst *rc, uint32_t npix,
-    int max_iter, int adaptive, bool counting)
+// Returns the number of kernel launches.
+uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, const RenderConst *rc, uint32_t npix,
+    int max_iter, int adaptive, bool counting, KernelTimer *tm = nullptr)
 {
   const WaveCounters wc = wave_counters(r, max_iter);
   ck(cudaMemsetAsync(wc.count, 0, per_wave_counter_bytes(max_iter), s), "reset counters");
@@ -279,14 +320,26 @@ void record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, const Re
   const Accum ac = accum(r);
   const ShadowSoA sh{r->sh_a.as<float4>(), r->sh_b.as<float4>(), r->sh_c.as<float4>()};
   uint64_t *stats = r->stats_buf.as<uint64_t>();
-  launch_raygen(cfg, s, rc, sc, path_soa(r, 0), ac, wc);
+  auto timed = [&](int kind, auto &&launch) {
+    if (tm)
+      tm->mark(s, kind);
+    launch();
+    if (tm)
+      tm->done(s);
+  };
+  if (tm)
+    tm->begin_wave();
+  timed(0, [&] { launch_raygen(cfg, s, rc, sc, path_soa(r, 0), ac, wc); });
   for (int it = 0; it < max_iter; ++it) {
     const PathSoA in = path_soa(r, it & 1), out = path_soa(r, (it + 1) & 1);
-    launch_trace(cfg, s, sc, in, r->hits.as<float4>(), wc, it, counting ? stats + 3 : nullptr);
-    launch_shade(cfg, s, rc, sc, in, out, r->hits.as<float4>(), sh, ac, wc, it);
-    launch_shadow(cfg, s, rc, sc, sh, ac, wc, it, counting ? stats + 3 : nullptr);
+    timed(1, [&] { launch_trace(cfg, s, sc, in, r->hits.as<float4>(), wc, it, counting ? stats + 3 : nullptr); });
+    timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, r->hits.as<float4>(), sh, ac, wc, it); });
+    timed(3, [&] { launch_shadow(cfg, s, rc, sc, sh, ac, wc, it, counting ? stats + 5 : nullptr); });
   }
-  launch_wave_end(s, rc, ac, wc, npix, adaptive, max_iter, stats);
+  timed(4, [&] { launch_wave_end(s, rc, ac, wc, npix, adaptive, max_iter, stats); });
+  if (tm)
+    tm->end_wave(s);
+  return 2 + 3 * uint64_t(max_iter);
 }
 
 void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st, bool reset)
@@ -378,7 +431,12 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
   ck(cudaEventRecord(r->ev0, s), "event");
   const uint64_t key[6] = {uint64_t(npix), uint64_t(lanes), uint64_t(max_iter), uint64_t(rc.adaptive),
       r->scene_generation, uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32)};
-  if (tu.use_graph) {
+  uint64_t launches = 0;
+  KernelTimer timer;
+  if (tu.time_kernels) {
+    for (uint32_t wv = 0; wv < waves; ++wv)
+      launches += record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting, &timer);
+  } else if (tu.use_graph) {
     if (!r->graph || std::memcmp(key, r->graph_key, sizeof(key)) != 0) {
       if (r->graph) {
         cudaGraphExecDestroy(r->graph);
@@ -402,13 +460,25 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
     }
     for (uint32_t wv = 0; wv < waves; ++wv)
       ck(cudaGraphLaunch(r->graph, s), "graph launch");
+    launches = uint64_t(waves) * (2 + 3 * uint64_t(max_iter));
   } else {
     for (uint32_t wv = 0; wv < waves; ++wv)
-      record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
+      launches += record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
   }
   const bool first = reset || r->samples == 0;
   const Frame fr{r->f_color.as<float4>(), r->f_normal.as<float4>(), r->f_albedo.as<float4>()};
+  if (tu.time_kernels)
+    timer.mark(s, 4);
   launch_resolve(s, accum(r), fr, npix, lanes, float(rc.spp), first ? 1 : 0);
+  if (tu.time_kernels) {
+    timer.done(s);
+    ck(cudaStreamSynchronize(s), "resolve");
+    float t = 0.f;
+    cudaEventElapsedTime(&t, timer.ev[timer.used - 2], timer.ev[timer.used - 1]);
+    timer.ms[4] += t;
+    timer.count[4]++;
+  }
+  launches += 1;
   ck(cudaGetLastError(), "kernel launch");
   ck(cudaEventRecord(r->ev1, s), "event");
   uint64_t stats[8];
@@ -422,6 +492,13 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
   r->last.node_visits = stats[3];
   r->last.tri_tests = stats[4];
   r->last.render_ms = ms;
+  r->last.shadow_node_visits = stats[5];
+  r->last.shadow_tri_tests = stats[6];
+  r->last.kernel_launches = launches;
+  for (int k = 0; k < 5; ++k) {
+    r->last.kernel_ms[k] = timer.ms[k];
+    r->last.kernel_count[k] = timer.count[k];
+  }
   r->sample_counter += rc.spp;
   r->samples = first ? rc.spp : r->samples + rc.spp;
 }

@@ -29,6 +29,7 @@ Tuning &tuning()
     t.use_graph = int(env_or("PHC_TUNE_USE_GRAPH", t.use_graph));
     t.count_traversal = int(env_or("PHC_TUNE_COUNT_TRAVERSAL", t.count_traversal));
     t.max_leaf = int(env_or("PHC_TUNE_MAX_LEAF", t.max_leaf));
+    t.time_kernels = int(env_or("PHC_TUNE_TIME_KERNELS", t.time_kernels));
   });
   return g_tuning;
 }
@@ -56,6 +57,8 @@ int phc_tuning_set(const char *key, int64_t value)
     t.count_traversal = int(value);
   else if (!std::strcmp(key, "max_leaf") && value >= 1 && value <= 3)
     t.max_leaf = int(value);
+  else if (!std::strcmp(key, "time_kernels") && (value == 0 || value == 1))
+    t.time_kernels = int(value);
   else
     return PHC_ERR_INVALID;
   return PHC_OK;
@@ -78,6 +81,8 @@ int64_t phc_tuning_get(const char *key)
     return t.count_traversal;
   if (!std::strcmp(key, "max_leaf"))
     return t.max_leaf;
+  if (!std::strcmp(key, "time_kernels"))
+    return t.time_kernels;
   return -1;
 }
 

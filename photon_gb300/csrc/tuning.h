@@ -14,6 +14,7 @@ struct Tuning {
   int use_graph{1};                  // replay each wave as a CUDA graph
   int count_traversal{0};            // node-visit / triangle-test counters (roofline runs)
   int max_leaf{3};                   // triangles per BVH8 leaf child (1..3), read at scene build
+  int time_kernels{0};               // CUDA events around every launch (no graph), per-kind times
 };
 
 Tuning &tuning();

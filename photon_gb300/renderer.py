@@ -89,7 +89,11 @@ class Renderer:
     def stats(self) -> dict:
         s = _abi.RenderStats()
         self._check(self.lib.phc_render_stats_get(self.h, C.byref(s)))
-        return {k: getattr(s, k) for k, _ in s._fields_}
+        out = {}
+        for k, _ in s._fields_:
+            v = getattr(s, k)
+            out[k] = list(v) if hasattr(v, "__len__") else v
+        return out
 
 
 def tuning_set(key: str, value: int):
