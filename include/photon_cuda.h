@@ -314,6 +314,26 @@ int phc_accel_info(const phc_accel *a, uint64_t *node_bytes, uint64_t *tri_bytes
 /* Message of the last failed phc_accel_* / phc_trace_* call on this thread. */
 const char *phc_accel_error(void);
 
+/* Largest ray count phc_trace_closest_compact_static accepts. */
+#define PHC_STATIC_MAX_RAYS 0x40000000u
+/* No counterpart in the reference: an allocation-free form of
+   phc_trace_closest_compact, with the same arguments and the same results.
+   It is for callers that must not allocate device memory while they trace:
+   code holding a memory budget or pool that owns all device memory (a host
+   application embedding the renderer), and hot loops where cudaMalloc /
+   cudaFree would stall the device (they synchronise implicitly).  The
+   traversal's only scratch, its 32-ray batch counter, sits in a 256-byte
+   array compiled into the library, which every GPU that loads the library
+   holds until the process exits; the accel, rays and hit buffer are the
+   caller's as before.  The first call on a device looks the array's device
+   address up (cudaGetSymbolAddress) and caches it, so make that first call
+   before any stream capture.  Every call shares the one array and resets the
+   counter itself: calls that overlap on the GPU (two streams, two threads)
+   race and must be serialised by the caller.  n above PHC_STATIC_MAX_RAYS is
+   rejected with PHC_ERR_LIMIT.  Blocks until the trace is done. */
+int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const float *directions, const float *tmin,
+    const float *tmax, uint32_t n, float *hits4, void *stream);
+
 /* ------------------------------------------------------------ scheduling */
 /* Launch parameters picked by the autotuner (no reference counterpart; the
    reference has no tunables on this path).  Keys: "wave_paths" (paths in

@@ -3,6 +3,7 @@
 // on caller-owned device arrays.
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -241,3 +242,77 @@ int phc_accel_info(const phc_accel *a, uint64_t *node_bytes, uint64_t *tri_bytes
 const char *phc_accel_error(void) { return g_accel_error.c_str(); }
 
 } // extern "C"
+
+// ------------------------------------------- allocation-free closest-hit trace
+//
+// phc_trace_closest_compact_static runs the same traversal kernel as
+// phc_trace_closest_compact, but the kernel's only scratch memory, the counter
+// from which its persistent warps take 32-ray batches, lives in the
+// file-scope array below instead of memory the accel allocated.  The array is
+// part of the module image: every GPU that loads this library holds these
+// 256 bytes until the process exits.  Host code must not use the array's name
+// as a device address; it asks the runtime for the address once per device.
+#define PHC_STATIC_SCRATCH_WORDS 64
+static __device__ __align__(256) uint32_t g_static_scratch[PHC_STATIC_SCRATCH_WORDS];
+
+namespace {
+
+// Device address of g_static_scratch on `device`, looked up on the first call
+// made with that device current and cached (nullptr on failure, err set).
+uint32_t *static_scratch(int device, std::string &err)
+{
+  static std::mutex mu;
+  static uint32_t *ptrs[256] = {};
+  if (device < 0 || device >= 256) {
+    err = "device ordinal out of range";
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!ptrs[device]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) {
+      err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return nullptr;
+    }
+    ptrs[device] = static_cast<uint32_t *>(p);
+  }
+  return ptrs[device];
+}
+
+} // namespace
+
+extern "C" int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const float *directions,
+    const float *tmin, const float *tmax, uint32_t n, float *hits4, void *stream)
+{
+  if (!a)
+    return fail(PHC_ERR_INVALID, "null accel");
+  if (n > PHC_STATIC_MAX_RAYS)
+    return fail(PHC_ERR_LIMIT, "phc_trace_closest_compact_static: n = " + std::to_string(n) +
+        " rays exceeds the maximum of " + std::to_string(PHC_STATIC_MAX_RAYS) +
+        " a call can take with its fixed scratch counter");
+  if (n == 0)
+    return PHC_OK;
+  if (!origins || !directions || !tmin || !tmax || !hits4)
+    return fail(PHC_ERR_INVALID, "null ray or output pointer");
+  cudaError_t e = cudaSetDevice(a->device);
+  if (e != cudaSuccess)
+    return fail(PHC_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  std::string err;
+  uint32_t *scratch = static_scratch(a->device, err);
+  if (!scratch)
+    return fail(PHC_ERR_CUDA, err);
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : a->stream;
+  // the batch counter must start at zero; the array keeps the last call's value
+  e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess)
+    return fail(PHC_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+  k_level_a<1, false><<<a->sm_count * 16, 128, 0, s>>>(a->scene.dev, origins, directions, tmin, tmax, n, hits4,
+      scratch, nullptr);
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess)
+    return fail(PHC_ERR_CUDA, std::string("trace: ") + cudaGetErrorString(e));
+  return PHC_OK;
+}

@@ -45,6 +45,7 @@ SIGNATURES = {
     "phc_accel_counters": (C.c_int, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "phc_accel_info": (C.c_int, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "phc_accel_error": (C.c_char_p, []),
+    "phc_trace_closest_compact_static": (C.c_int, [vp, vp, vp, vp, vp, C.c_uint32, vp, vp]),
     "phc_tuning_set": (C.c_int, [C.c_char_p, C.c_int64]),
     "phc_tuning_get": (C.c_int64, [C.c_char_p]),
 }
