@@ -264,6 +264,23 @@ int phc_read_normal(phc_renderer *r, float *xyz);
 int phc_read_albedo(phc_renderer *r, float *rgb);
 /* Counters of the last phc_render call. */
 int phc_render_stats_get(const phc_renderer *r, phc_render_stats *out);
+
+/* One render call of a batch: the arguments of phc_render. */
+typedef struct phc_job {
+  phc_renderer *renderer;
+  const phc_camera *camera;
+  const phc_settings *settings;
+  int32_t reset;
+} phc_job;
+/* Batched mode (no reference counterpart; the reference renders one frame
+   per PathTracer::render call, pathtracer.cpp:564-1159): performs the n
+   render calls -- distinct renderers with their own scenes, sizes, sample
+   counts and depths, all on the current device -- in one wavefront whose
+   queues carry a job tag, as one replayed CUDA graph.  Each renderer ends in
+   exactly the state phc_render would leave it in, with the same image bit
+   for bit.  Jobs with adaptive sampling run through phc_render's path.
+   batch_stats (may be NULL) receives the counters of the whole batch. */
+int phc_render_batch(const phc_job *jobs, uint32_t n, phc_render_stats *batch_stats);
 /* Message of the last failed call on this renderer ("" when none). */
 const char *phc_last_error(const phc_renderer *r);
 

@@ -126,6 +126,13 @@ class RenderStats(C.Structure):
     ]
 
 
+class Job(C.Structure):
+    _fields_ = [
+        ("renderer", C.c_void_p), ("camera", C.POINTER(Camera)), ("settings", C.POINTER(Settings)),
+        ("reset", C.c_int32),
+    ]
+
+
 class HitResult(C.Structure):
     _fields_ = [
         ("t", C.c_float), ("position", f3), ("normal", f3), ("shading_normal", f3),

@@ -91,7 +91,7 @@ struct phc_renderer {
 
   // wavefront buffers
   size_t cap_paths{0};
-  Buf st_o[2], st_d[2], st_tp[2], st_info[2], st_dist[2], hits, sh_a, sh_b, sh_c;
+  Buf st_o[2], st_d[2], st_tp[2], st_info[2], st_dist[2], hits, sh_a, sh_b, sh_c, hitq, missq;
   size_t cap_slots{0};
   Buf acc, acc_sq, acc_start, nsamp, aov_n, aov_a;
   Buf counters; // count, scount, fetch, wave, error
@@ -103,6 +103,10 @@ struct phc_renderer {
   // graph of one wave
   cudaGraphExec_t graph{nullptr};
   uint64_t graph_key[6]{};
+  uint64_t graph_launches{0}; // kernels per replay of the wave graph
+  // batched renders led by this renderer: job table, wave schedule, and the
+  // job tags of the shadow queue
+  Buf b_jobs, b_entries, b_wave_entry, b_wave_items, sh_job;
   phc_render_stats last{};
   cudaEvent_t ev0{nullptr}, ev1{nullptr};
 
@@ -227,6 +231,8 @@ void ensure_paths(phc_renderer *r, size_t n)
     ck(r->st_dist[b].ensure(n * 4), "alloc path state");
   }
   ck(r->hits.ensure(n * 16), "alloc hits");
+  ck(r->hitq.ensure(n * 4), "alloc hit queue");
+  ck(r->missq.ensure(n * 4), "alloc miss queue");
   ck(r->sh_a.ensure(n * 16), "alloc shadow queue");
   ck(r->sh_b.ensure(n * 16), "alloc shadow queue");
   ck(r->sh_c.ensure(n * 16), "alloc shadow queue");
@@ -262,12 +268,15 @@ WaveCounters wave_counters(phc_renderer *r, int max_iter)
   WaveCounters wc;
   wc.count = c;
   wc.scount = c + (max_iter + 1);
-  wc.fetch = c + (2 * max_iter + 1);
-  wc.wave = c + (5 * max_iter + 2);
-  wc.error = c + (5 * max_iter + 3);
+  wc.hcount = c + (2 * max_iter + 1);
+  wc.mcount = c + (3 * max_iter + 1);
+  wc.fetch = c + (4 * max_iter + 1);
+  wc.wave = c + wave_counter_words(max_iter);
+  wc.error = c + wave_counter_words(max_iter) + 1;
   return wc;
 }
-size_t per_wave_counter_bytes(int max_iter) { return size_t(5 * max_iter + 2) * 4; }
+// Bytes of the counters reset at the start of every wave (not wave / error).
+size_t per_wave_counter_bytes(int max_iter) { return wave_counter_words(max_iter) * 4; }
 
 // Per-kind kernel times of a render call (time_kernels mode): events around
 // every launch of a wave, read after the wave.
@@ -327,32 +336,62 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
     if (tm)
       tm->done(s);
   };
+  // shading variants for this scene (shade_kernels.cu): the lean kernels
+  // without volume / source / analytic-light code when the scene uses none,
+  // misses and hits in separate kernels when no volume can scatter a miss
+  const Tuning &tu = tuning();
+  const bool full = (sc.features & (SCENE_VOLUMES | SCENE_SOURCES | SCENE_LIGHTS)) != 0 || !tu.shade_lean;
+  const bool split = (sc.features & SCENE_VOLUMES) == 0 && tu.split_shade;
+  const HitQueues hq = split ? HitQueues{r->hitq.as<uint32_t>(), r->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
+  uint64_t launches = 2;
   if (tm)
     tm->begin_wave();
   timed(0, [&] { launch_raygen(cfg, s, rc, sc, path_soa(r, 0), ac, wc); });
   for (int it = 0; it < max_iter; ++it) {
     const PathSoA in = path_soa(r, it & 1), out = path_soa(r, (it + 1) & 1);
-    timed(1, [&] { launch_trace(cfg, s, sc, in, r->hits.as<float4>(), wc, it, counting ? stats + 3 : nullptr); });
-    timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, r->hits.as<float4>(), sh, ac, wc, it); });
-    timed(3, [&] { launch_shadow(cfg, s, rc, sc, sh, ac, wc, it, counting ? stats + 5 : nullptr); });
+    float4 *hits = r->hits.as<float4>();
+    timed(1, [&] { launch_trace(cfg, s, sc, in, hits, wc, it, counting ? stats + 3 : nullptr, tu.trace_refill, hq); });
+    if (split) {
+      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 1}, hq); });
+      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 2}, hq); });
+      launches += 4;
+    } else {
+      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 0}, hq); });
+      launches += 3;
+    }
+    timed(3, [&] { launch_shadow(cfg, s, rc, sc, sh, ac, wc, it, counting ? stats + 5 : nullptr, tu.trace_refill); });
   }
   timed(4, [&] { launch_wave_end(s, rc, ac, wc, npix, adaptive, max_iter, stats); });
   if (tm)
     tm->end_wave(s);
-  return 2 + 3 * uint64_t(max_iter);
+  return launches;
 }
 
-void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st, bool reset)
+// What one render call of one renderer needs: its constants, sample lanes
+// and wave count; prepared (buffers sized, accumulators zeroed) on stream s.
+struct JobPlan {
+  RenderConst rc{};
+  uint32_t npix{0}, lanes{1}, waves{0};
+  int max_iter{0};
+  size_t slots{0};
+  bool first{true};
+};
+
+void validate_call(phc_renderer *r, const phc_settings &st)
 {
-  const uint32_t w = st.width, h = st.height;
-  if (w == 0 || h == 0)
+  if (st.width == 0 || st.height == 0)
     throw ApiError(PHC_ERR_INVALID, "invalid frame size");
   if (!r->has_scene)
     throw ApiError(PHC_ERR_NO_SCENE, "no scene");
-  if (uint64_t(w) * h > (1ull << 28))
+  if (uint64_t(st.width) * st.height > (1ull << 28))
     throw ApiError(PHC_ERR_LIMIT, "frame larger than 2^28 pixels");
+}
+
+JobPlan prepare_job(phc_renderer *r, const phc_camera &cam, const phc_settings &st, bool reset, cudaStream_t s)
+{
+  validate_call(r, st);
+  const uint32_t w = st.width, h = st.height;
   check_device(r);
-  cudaStream_t s = r->stream;
   const uint32_t npix = w * h;
   if (w != r->width || h != r->height) {
     ck(r->f_color.ensure(size_t(npix) * 16), "alloc frame");
@@ -402,35 +441,73 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
     lanes = std::min<uint32_t>(lanes, std::max<uint32_t>(1u, uint32_t((1ull << 28) / npix)));
   }
   rc.lanes = lanes;
-  const int max_iter = int(rc.max_iter);
-  const size_t slots = size_t(lanes) * npix;
-  ensure_paths(r, slots);
-  ensure_slots(r, slots);
-  ck(r->counters.ensure(per_wave_counter_bytes(max_iter) + 16), "alloc counters");
+  JobPlan p;
+  p.npix = npix;
+  p.lanes = lanes;
+  p.max_iter = int(rc.max_iter);
+  p.slots = size_t(lanes) * npix;
+  p.waves = (rc.spp + lanes - 1) / lanes;
+  p.first = reset || r->samples == 0;
+  ensure_slots(r, p.slots);
   ck(r->rc_buf.ensure(sizeof(RenderConst)), "alloc constants");
-  ck(r->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
   ck(cudaMemcpyAsync(r->rc_buf.p, &rc, sizeof(rc), cudaMemcpyHostToDevice, s), "upload constants");
-  ck(cudaMemsetAsync(r->stats_buf.p, 0, 8 * sizeof(uint64_t), s), "reset stats");
-  ck(cudaMemsetAsync(r->acc.p, 0, slots * 16, s), "reset accumulators");
-  ck(cudaMemsetAsync(r->nsamp.p, 0, slots * 4, s), "reset accumulators");
-  ck(cudaMemsetAsync(r->aov_a.p, 0, slots * 16, s), "reset accumulators");
+  ck(cudaMemsetAsync(r->acc.p, 0, p.slots * 16, s), "reset accumulators");
+  ck(cudaMemsetAsync(r->nsamp.p, 0, p.slots * 4, s), "reset accumulators");
+  ck(cudaMemsetAsync(r->aov_a.p, 0, p.slots * 16, s), "reset accumulators");
   if (rc.adaptive)
-    ck(cudaMemsetAsync(r->acc_sq.p, 0, slots * 16, s), "reset accumulators");
-  const WaveCounters wc = wave_counters(r, max_iter);
-  ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
+    ck(cudaMemsetAsync(r->acc_sq.p, 0, p.slots * 16, s), "reset accumulators");
+  p.rc = rc;
+  return p;
+}
 
+Frame frame_of(phc_renderer *r)
+{
+  return Frame{r->f_color.as<float4>(), r->f_normal.as<float4>(), r->f_albedo.as<float4>()};
+}
+
+// After the device work: the bridge's sample bookkeeping (RenderBridge.cpp:920-927).
+void commit_job(phc_renderer *r, const JobPlan &p)
+{
+  r->sample_counter += p.rc.spp;
+  r->samples = p.first ? p.rc.spp : r->samples + p.rc.spp;
+}
+
+LaunchCfg launch_cfg(phc_renderer *r, size_t raygen_items)
+{
+  const Tuning &tu = tuning();
   LaunchCfg cfg;
   cfg.threads = 128;
   cfg.blocks_trace = r->sm_count * std::max(1, std::min(tu.trace_blocks_per_sm, max_active_blocks(0, 128)));
   cfg.blocks_shade = r->sm_count * std::max(1, std::min(tu.shade_blocks_per_sm, max_active_blocks(1, 128)));
-  cfg.blocks_raygen = int(std::min<size_t>((slots + 255) / 256, size_t(r->sm_count) * 8));
+  cfg.blocks_raygen = int(std::max<size_t>(1, std::min<size_t>((raygen_items + 255) / 256, size_t(r->sm_count) * 8)));
+  return cfg;
+}
+
+void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st, bool reset)
+{
+  cudaStream_t s = r->stream;
+  const JobPlan plan = prepare_job(r, cam, st, reset, s);
+  const RenderConst &rc = plan.rc;
+  const uint32_t npix = plan.npix, lanes = plan.lanes, waves = plan.waves;
+  const int max_iter = plan.max_iter;
+  const bool first = plan.first;
+  const Tuning &tu = tuning();
+  ensure_paths(r, plan.slots);
+  ck(r->counters.ensure(per_wave_counter_bytes(max_iter) + 16), "alloc counters");
+  ck(r->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
+  ck(cudaMemsetAsync(r->stats_buf.p, 0, 8 * sizeof(uint64_t), s), "reset stats");
+  const WaveCounters wc = wave_counters(r, max_iter);
+  ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
+  const LaunchCfg cfg = launch_cfg(r, plan.slots);
   const bool counting = tu.count_traversal != 0;
-  const uint32_t waves = (rc.spp + lanes - 1) / lanes;
   const RenderConst *drc = r->rc_buf.as<RenderConst>();
 
   ck(cudaEventRecord(r->ev0, s), "event");
-  const uint64_t key[6] = {uint64_t(npix), uint64_t(lanes), uint64_t(max_iter), uint64_t(rc.adaptive),
-      r->scene_generation, uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32)};
+  // everything the recorded launch sequence depends on
+  const uint64_t key[6] = {uint64_t(npix) | (uint64_t(lanes) << 32),
+      uint64_t(max_iter) | (uint64_t(rc.adaptive) << 32), r->scene_generation,
+      uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32),
+      uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16), 0};
   uint64_t launches = 0;
   KernelTimer timer;
   if (tu.time_kernels) {
@@ -445,7 +522,7 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
       cudaGraph_t g = nullptr;
       ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
       try {
-        record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
+        r->graph_launches = record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
       } catch (...) {
         cudaStreamEndCapture(s, &g);
         if (g)
@@ -460,13 +537,12 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
     }
     for (uint32_t wv = 0; wv < waves; ++wv)
       ck(cudaGraphLaunch(r->graph, s), "graph launch");
-    launches = uint64_t(waves) * (2 + 3 * uint64_t(max_iter));
+    launches = uint64_t(waves) * r->graph_launches;
   } else {
     for (uint32_t wv = 0; wv < waves; ++wv)
       launches += record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
   }
-  const bool first = reset || r->samples == 0;
-  const Frame fr{r->f_color.as<float4>(), r->f_normal.as<float4>(), r->f_albedo.as<float4>()};
+  const Frame fr = frame_of(r);
   if (tu.time_kernels)
     timer.mark(s, 4);
   launch_resolve(s, accum(r), fr, npix, lanes, float(rc.spp), first ? 1 : 0);
@@ -499,8 +575,217 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
     r->last.kernel_ms[k] = timer.ms[k];
     r->last.kernel_count[k] = timer.count[k];
   }
-  r->sample_counter += rc.spp;
-  r->samples = first ? rc.spp : r->samples + rc.spp;
+  commit_job(r, plan);
+}
+
+// ---------------------------------------------------------------- batches
+//
+// Several renderers' render calls in one wavefront: every job keeps the
+// sample lanes its own render would use (so its per-pixel sums and its image
+// are bit-identical), and a batch wave packs at most one "chunk" (one plain
+// wave: lanes samples of every pixel) per job, round-robin, until the wave
+// holds batch_wave_paths paths.  One CUDA graph of one batch wave is
+// replayed for all waves; the wave index selects the wave's table.
+struct BatchPlan {
+  std::vector<BatchJob> jobs;
+  std::vector<BatchEntry> entries;
+  std::vector<uint32_t> wave_entry, wave_items;
+  uint32_t max_items{0};
+  int max_iter{0};
+  uint32_t features{0};
+};
+
+BatchPlan plan_batch(const std::vector<phc_renderer *> &rs, const std::vector<JobPlan> &plans, uint64_t cap)
+{
+  BatchPlan b;
+  const size_t n = rs.size();
+  std::vector<uint32_t> next(n, 0);
+  for (size_t j = 0; j < n; ++j) {
+    b.jobs.push_back(BatchJob{rs[j]->scene.dev, plans[j].rc, accum(rs[j])});
+    b.max_iter = std::max(b.max_iter, plans[j].max_iter);
+    b.features |= rs[j]->scene.dev.features;
+  }
+  size_t start = 0;
+  b.wave_entry.push_back(0);
+  for (;;) {
+    uint64_t items = 0;
+    bool any = false;
+    for (size_t k = 0; k < n; ++k) {
+      const size_t j = (start + k) % n;
+      const JobPlan &p = plans[j];
+      if (next[j] >= p.waves)
+        continue;
+      const uint32_t s0 = next[j] * p.lanes;
+      const uint32_t ns = std::min(p.lanes, p.rc.spp - s0);
+      const uint64_t paths = uint64_t(ns) * p.npix;
+      if (items > 0 && items + paths > cap)
+        continue;
+      b.entries.push_back(BatchEntry{uint32_t(j), s0, ns, uint32_t(items)});
+      items += paths;
+      next[j]++;
+      any = true;
+    }
+    if (!any)
+      break;
+    if (items > 0xffffffffull)
+      throw ApiError(PHC_ERR_LIMIT, "batch wave larger than 2^32 paths");
+    b.wave_entry.push_back(uint32_t(b.entries.size()));
+    b.wave_items.push_back(uint32_t(items));
+    b.max_items = std::max(b.max_items, uint32_t(items));
+    start = (start + 1) % n;
+  }
+  return b;
+}
+
+void record_batch_wave(phc_renderer *lead, cudaStream_t s, const LaunchCfg &cfg, const BatchTable &bt, int max_iter,
+    uint32_t features)
+{
+  const Tuning &tu = tuning();
+  const WaveCounters wc = wave_counters(lead, max_iter);
+  ck(cudaMemsetAsync(wc.count, 0, per_wave_counter_bytes(max_iter), s), "reset counters");
+  const ShadowSoA sh{lead->sh_a.as<float4>(), lead->sh_b.as<float4>(), lead->sh_c.as<float4>(),
+      lead->sh_job.as<uint32_t>()};
+  const bool full = (features & (SCENE_VOLUMES | SCENE_SOURCES | SCENE_LIGHTS)) != 0 || !tu.shade_lean;
+  const bool split = (features & SCENE_VOLUMES) == 0 && tu.split_shade;
+  const HitQueues hq =
+      split ? HitQueues{lead->hitq.as<uint32_t>(), lead->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
+  float4 *hits = lead->hits.as<float4>();
+  launch_raygen_batch(cfg, s, bt, path_soa(lead, 0), wc);
+  for (int it = 0; it < max_iter; ++it) {
+    const PathSoA in = path_soa(lead, it & 1), out = path_soa(lead, (it + 1) & 1);
+    launch_trace_batch(cfg, s, bt, in, hits, wc, it, tu.trace_refill, hq);
+    if (split) {
+      launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 1}, hq);
+      launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 2}, hq);
+    } else {
+      launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 0}, hq);
+    }
+    launch_shadow_batch(cfg, s, bt, sh, wc, it, tu.trace_refill);
+  }
+  launch_wave_end(s, nullptr, Accum{}, wc, 0, 0, max_iter, lead->stats_buf.as<uint64_t>());
+}
+
+template <class T> void upload_vec(Buf &b, const std::vector<T> &v, cudaStream_t s, const char *what)
+{
+  ck(b.ensure(std::max<size_t>(v.size(), 1) * sizeof(T)), what);
+  if (!v.empty())
+    ck(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), what);
+}
+
+void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_stats)
+{
+  std::vector<phc_renderer *> rs;
+  std::vector<JobPlan> plans;
+  std::vector<const phc_job *> batch_jobs;
+  phc_renderer *lead = jobs[0].renderer;
+  int device = lead->device;
+  for (uint32_t i = 0; i < n; ++i) {
+    const phc_job &jb = jobs[i];
+    if (!jb.renderer || !jb.camera || !jb.settings)
+      throw ApiError(PHC_ERR_INVALID, "batch job " + std::to_string(i) + ": null renderer, camera or settings");
+    if (jb.renderer->device != device)
+      throw ApiError(PHC_ERR_INVALID, "batch jobs must share one device");
+    for (uint32_t k = 0; k < i; ++k)
+      if (jobs[k].renderer == jb.renderer)
+        throw ApiError(PHC_ERR_INVALID, "a renderer appears twice in the batch");
+    validate_call(jb.renderer, *jb.settings);
+  }
+  if (n > MAX_BATCH_JOBS)
+    throw ApiError(PHC_ERR_LIMIT, "more than 32768 jobs in one batch");
+  check_device(lead);
+  cudaStream_t s = lead->stream;
+  // adaptive sampling needs the samples of a pixel in order: such jobs run
+  // through their own render path first
+  for (uint32_t i = 0; i < n; ++i) {
+    if (jobs[i].settings->adaptive_sampling) {
+      render_impl(jobs[i].renderer, *jobs[i].camera, *jobs[i].settings, jobs[i].reset != 0);
+      continue;
+    }
+    batch_jobs.push_back(&jobs[i]);
+  }
+  if (batch_jobs.empty())
+    return;
+  for (const phc_job *jb : batch_jobs) {
+    rs.push_back(jb->renderer);
+    plans.push_back(prepare_job(jb->renderer, *jb->camera, *jb->settings, jb->reset != 0, s));
+  }
+  const Tuning &tu = tuning();
+  const BatchPlan bp = plan_batch(rs, plans, uint64_t(std::max<int64_t>(tu.batch_wave_paths, 1024)));
+  upload_vec(lead->b_jobs, bp.jobs, s, "upload batch jobs");
+  upload_vec(lead->b_entries, bp.entries, s, "upload batch entries");
+  upload_vec(lead->b_wave_entry, bp.wave_entry, s, "upload batch waves");
+  upload_vec(lead->b_wave_items, bp.wave_items, s, "upload batch waves");
+  ensure_paths(lead, bp.max_items);
+  ck(lead->sh_job.ensure(size_t(std::max<uint32_t>(bp.max_items, 1)) * 4), "alloc shadow jobs");
+  ck(lead->counters.ensure(per_wave_counter_bytes(bp.max_iter) + 16), "alloc counters");
+  ck(lead->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
+  ck(cudaMemsetAsync(lead->stats_buf.p, 0, 8 * sizeof(uint64_t), s), "reset stats");
+  const WaveCounters wc = wave_counters(lead, bp.max_iter);
+  ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
+  const BatchTable bt{lead->b_jobs.as<BatchJob>(), lead->b_entries.as<BatchEntry>(),
+      lead->b_wave_entry.as<uint32_t>(), lead->b_wave_items.as<uint32_t>()};
+  const LaunchCfg cfg = launch_cfg(lead, bp.max_items);
+  const uint32_t waves = uint32_t(bp.wave_items.size());
+  ck(cudaEventRecord(lead->ev0, s), "event");
+  uint64_t launches = 0;
+  if (tu.use_graph) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    try {
+      record_batch_wave(lead, s, cfg, bt, bp.max_iter, bp.features);
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g)
+        cudaGraphDestroy(g);
+      throw;
+    }
+    ck(cudaStreamEndCapture(s, &g), "end capture");
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    ck(e, "graph instantiate");
+    for (uint32_t wv = 0; wv < waves; ++wv) {
+      const cudaError_t le = cudaGraphLaunch(ge, s);
+      if (le != cudaSuccess) {
+        cudaGraphExecDestroy(ge);
+        ck(le, "graph launch");
+      }
+    }
+    launches = uint64_t(waves) * (nodes > 0 ? nodes - 1 : 0); // minus the counter memset node
+    ck(cudaStreamSynchronize(s), "batch");
+    cudaGraphExecDestroy(ge);
+  } else {
+    for (uint32_t wv = 0; wv < waves; ++wv)
+      record_batch_wave(lead, s, cfg, bt, bp.max_iter, bp.features);
+  }
+  for (size_t j = 0; j < rs.size(); ++j)
+    launch_resolve(s, accum(rs[j]), frame_of(rs[j]), plans[j].npix, plans[j].lanes, float(plans[j].rc.spp),
+        plans[j].first ? 1 : 0);
+  launches += rs.size();
+  ck(cudaGetLastError(), "kernel launch");
+  ck(cudaEventRecord(lead->ev1, s), "event");
+  uint64_t stats[8];
+  ck(cudaMemcpyAsync(stats, lead->stats_buf.p, sizeof(stats), cudaMemcpyDeviceToHost, s), "read stats");
+  ck(cudaStreamSynchronize(s), "batch");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, lead->ev0, lead->ev1);
+  phc_render_stats st{};
+  st.pixel_samples = stats[0];
+  st.closest_rays = stats[1];
+  st.shadow_rays = stats[2];
+  st.render_ms = ms;
+  st.kernel_launches = launches;
+  for (size_t j = 0; j < rs.size(); ++j) {
+    commit_job(rs[j], plans[j]);
+    rs[j]->last = phc_render_stats{};
+    rs[j]->last.pixel_samples = uint64_t(plans[j].npix) * plans[j].rc.spp;
+    rs[j]->last.render_ms = ms;
+  }
+  lead->last = st;
+  if (out_stats)
+    *out_stats = st;
 }
 
 int read_channel(phc_renderer *r, float *out, int channel)
@@ -683,6 +968,27 @@ int phc_render(phc_renderer *r, const phc_camera *camera, const phc_settings *se
   if (!camera || !settings)
     return set_error(r, PHC_ERR_INVALID, "null camera or settings");
   return guarded(r, [&] { render_impl(r, *camera, *settings, reset != 0); });
+}
+
+int phc_render_batch(const phc_job *jobs, uint32_t n, phc_render_stats *batch_stats)
+{
+  if (!jobs || n == 0)
+    return set_error(nullptr, PHC_ERR_INVALID, "empty batch");
+  for (uint32_t i = 0; i < n; ++i)
+    if (!jobs[i].renderer)
+      return set_error(nullptr, PHC_ERR_INVALID, "batch job with a null renderer");
+  // lock every renderer of the batch, in address order
+  std::vector<phc_renderer *> order;
+  for (uint32_t i = 0; i < n; ++i)
+    order.push_back(jobs[i].renderer);
+  std::sort(order.begin(), order.end());
+  order.erase(std::unique(order.begin(), order.end()), order.end());
+  for (phc_renderer *r : order)
+    r->mutex.lock();
+  const int rc = guarded(jobs[0].renderer, [&] { render_batch_impl(jobs, n, batch_stats); });
+  for (phc_renderer *r : order)
+    r->mutex.unlock();
+  return rc;
 }
 
 uint32_t phc_accumulated_samples(const phc_renderer *r) { return r ? r->samples : 0u; }

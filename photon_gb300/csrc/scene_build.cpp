@@ -537,6 +537,15 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   d.vol_majorants = put(h.vol_majorants, s, err);
   d.strategy_count = h.strategy_count;
   d.eps = h.eps;
+  d.features = 0u;
+  if (!h.volumes.empty())
+    d.features |= SCENE_VOLUMES;
+  if (!h.lights.empty())
+    d.features |= SCENE_LIGHTS;
+  for (const DevMaterial &m : h.materials)
+    for (int k = 0; k < 7; ++k)
+      if (m.src_kind[k] != 0)
+        d.features |= SCENE_SOURCES;
   node_bytes = uint64_t(h.bvh.nodes.size()) * 4;
   tri_bytes = uint64_t(h.bvh.tris.size()) * 4;
   bvh_depth = h.bvh.max_depth;

@@ -133,6 +133,13 @@ struct DevScene {
   const float *vol_majorants;
   uint32_t strategy_count;
   float eps;
+  uint32_t features; // SCENE_* bits: which shading features the scene uses
+};
+
+enum : uint32_t {
+  SCENE_VOLUMES = 1u,  // transfer-function volumes (delta / ratio tracking)
+  SCENE_SOURCES = 2u,  // material parameters from attributes or samplers, normal maps
+  SCENE_LIGHTS = 4u    // analytic point / directional / spot lights
 };
 
 } // namespace phc

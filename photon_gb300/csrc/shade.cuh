@@ -195,7 +195,7 @@ __device__ __forceinline__ V3 eval_coat(const Mat &m, V3 wo, V3 wi, V3 n)
   const float w = m.clearcoat * 0.25f;
   return F * (w * D * G / denom);
 }
-__device__ __noinline__ V3 bsdf_eval(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
+static __device__ __noinline__ V3 bsdf_eval(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
 {
   if (dot(wo, n) <= 0.f || dot(wi, n) <= 0.f)
     return V3{0.f, 0.f, 0.f};
@@ -211,7 +211,7 @@ __device__ __noinline__ V3 bsdf_eval(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
   f = f + eval_coat(m, wo, wi, sn);
   return f;
 }
-__device__ __noinline__ float bsdf_pdf(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
+static __device__ __noinline__ float bsdf_pdf(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
 {
   if (dot(wo, n) <= 0.f || dot(wi, n) <= 0.f)
     return 0.f;
@@ -256,7 +256,7 @@ struct BSample {
   float pdf;
   bool spec, diff;
 };
-__device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3 sn, Rng &rng)
+static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3 sn, Rng &rng)
 {
   BSample out{V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, 0.f, false, false};
   const BSample none = out;
@@ -398,7 +398,7 @@ __device__ __forceinline__ int32_t wrap_index(int32_t i, int32_t n, int32_t mode
   }
   return i < 0 ? 0 : (i >= n ? n - 1 : i);
 }
-__device__ __noinline__ float4 sampler_sample(const DevScene &sc, int32_t id, float4 attr)
+static __device__ __noinline__ float4 sampler_sample(const DevScene &sc, int32_t id, float4 attr)
 {
   if (id < 0 || uint32_t(id) >= sc.sampler_count)
     return make_float4(0.f, 0.f, 0.f, 1.f);
@@ -462,7 +462,7 @@ __device__ __forceinline__ float4 eval_source(const DevScene &sc, int32_t kind, 
   const int32_t slot = sc.samplers[uint32_t(index)].in_attribute;
   return sampler_sample(sc, index, fetch_attribute(sc, slot, q));
 }
-__device__ __noinline__ V3 apply_normal_map(const DevScene &sc, int32_t kind, int32_t index, const Query &q, V3 sn)
+static __device__ __noinline__ V3 apply_normal_map(const DevScene &sc, int32_t kind, int32_t index, const Query &q, V3 sn)
 {
   const float4 c = eval_source(sc, kind, index, q);
   const V3 nm{2.f * c.x - 1.f, 2.f * c.y - 1.f, 2.f * c.z - 1.f};
@@ -497,7 +497,10 @@ __device__ __noinline__ V3 apply_normal_map(const DevScene &sc, int32_t kind, in
   return dot(n, n) > 0.f ? normalize(n) : sn;
 }
 // resolve_material, pathtracer.cpp:188-247 (seam materials: no atlas textures)
-__device__ __noinline__ Mat resolve_material(const DevScene &sc, const DevMaterial &dm, const Query &q, float &alpha)
+// SRC = false: the scene has no attribute / sampler sources, the constants
+// are the parameters (the source branches are not compiled).
+template <bool SRC>
+static __device__ __noinline__ Mat resolve_material(const DevScene &sc, const DevMaterial &dm, const Query &q, float &alpha)
 {
   Mat m;
   m.base_color = V3{dm.base_color[0], dm.base_color[1], dm.base_color[2]};
@@ -514,23 +517,23 @@ __device__ __noinline__ Mat resolve_material(const DevScene &sc, const DevMateri
   m.flags = dm.flags;
   m.thin = dm.thin;
   alpha = dm.alpha;
-  if (dm.src_kind[SRC_BASE] != 0) {
+  if (SRC && dm.src_kind[SRC_BASE] != 0) {
     const float4 c = eval_source(sc, dm.src_kind[SRC_BASE], dm.src_index[SRC_BASE], q);
     m.base_color = V3{fmaxf(c.x, 0.f), fmaxf(c.y, 0.f), fmaxf(c.z, 0.f)};
     if (dm.base_color_alpha)
       alpha *= c.w;
   }
-  if (dm.src_kind[SRC_ALPHA] != 0)
+  if (SRC && dm.src_kind[SRC_ALPHA] != 0)
     alpha *= eval_source(sc, dm.src_kind[SRC_ALPHA], dm.src_index[SRC_ALPHA], q).x;
-  if (dm.src_kind[SRC_METAL] != 0)
+  if (SRC && dm.src_kind[SRC_METAL] != 0)
     m.metallic = eval_source(sc, dm.src_kind[SRC_METAL], dm.src_index[SRC_METAL], q).x;
-  if (dm.src_kind[SRC_ROUGH] != 0) {
+  if (SRC && dm.src_kind[SRC_ROUGH] != 0) {
     const float r = clamp01(eval_source(sc, dm.src_kind[SRC_ROUGH], dm.src_index[SRC_ROUGH], q).x);
     m.roughness = r * r;
   }
-  if (dm.src_kind[SRC_TRANS] != 0)
+  if (SRC && dm.src_kind[SRC_TRANS] != 0)
     m.transmission = eval_source(sc, dm.src_kind[SRC_TRANS], dm.src_index[SRC_TRANS], q).x;
-  if (dm.src_kind[SRC_EMIT] != 0) {
+  if (SRC && dm.src_kind[SRC_EMIT] != 0) {
     const float4 e = eval_source(sc, dm.src_kind[SRC_EMIT], dm.src_index[SRC_EMIT], q);
     m.emission = V3{fmaxf(e.x, 0.f), fmaxf(e.y, 0.f), fmaxf(e.z, 0.f)};
   }
@@ -584,7 +587,7 @@ __device__ __forceinline__ float env_pdf(const DevScene &sc, V3 dir)
   const float denom = TWO_PI * PI * fmaxf(sinf(theta), 1e-6f);
   return (row_pdf * col_pdf) * float(sc.env_w) * float(sc.env_h) / denom;
 }
-__device__ __noinline__ V3 env_sample(const DevScene &sc, Rng &rng, float &pdf_out)
+static __device__ __noinline__ V3 env_sample(const DevScene &sc, Rng &rng, float &pdf_out)
 {
   const float u1 = rng.next();
   const float u2 = rng.next();
@@ -639,7 +642,7 @@ __device__ __forceinline__ V3 sphere_point(const DevLight &l, V3 p, Rng &rng)
   concentric_disk(rng, dx, dy);
   return pos + (t * dx + b * dy) * l.radius;
 }
-__device__ __noinline__ LightSample sample_light(const DevLight &l, V3 p, Rng &rng)
+static __device__ __noinline__ LightSample sample_light(const DevLight &l, V3 p, Rng &rng)
 {
   const V3 color{l.color[0], l.color[1], l.color[2]};
   const V3 pos{l.position[0], l.position[1], l.position[2]};
@@ -690,7 +693,9 @@ struct DirectSample {
   bool mis, valid;
 };
 // sample_direct, pathtracer.cpp:270-367
-__device__ __noinline__ DirectSample sample_direct(const DevScene &sc, V3 p, Rng &rng)
+// FULL = false: no analytic lights and no material sources in the scene.
+template <bool FULL>
+static __device__ __noinline__ DirectSample sample_direct(const DevScene &sc, V3 p, Rng &rng)
 {
   DirectSample ds{V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, 0.f, 0.f, false, false};
   if (sc.strategy_count == 0)
@@ -699,7 +704,7 @@ __device__ __noinline__ DirectSample sample_direct(const DevScene &sc, V3 p, Rng
   uint32_t pick = uint32_t(rng.next() * float(sc.strategy_count));
   if (pick >= sc.strategy_count)
     pick = sc.strategy_count - 1;
-  if (pick < sc.light_count) {
+  if (FULL && pick < sc.light_count) {
     const LightSample ls = sample_light(sc.lights[pick], p, rng);
     if (!(ls.pdf > 0.f))
       return ds;
@@ -756,7 +761,7 @@ __device__ __noinline__ DirectSample sample_direct(const DevScene &sc, V3 p, Rng
     q.sn = ln;
     float alpha = 1.f;
     const DevMaterial &dm = sc.materials[vidx.w];
-    const Mat em = resolve_material(sc, dm, q, alpha);
+    const Mat em = resolve_material<FULL>(sc, dm, q, alpha);
     if (!emits_on_side(em.flags, cos_light > 0.f))
       return ds;
     ds.wi = wi;
@@ -876,7 +881,7 @@ __device__ __forceinline__ float4 vol_classify(const DevScene &sc, const DevVolu
   return c;
 }
 // VolumeSet::track, tf_volume.h:150-232
-__device__ __noinline__ float vol_track(const DevScene &sc, const DevVolume &v, V3 org, V3 dir, float t0, float t1,
+static __device__ __noinline__ float vol_track(const DevScene &sc, const DevVolume &v, V3 org, V3 dir, float t0, float t1,
     Rng &rng, bool scatter, V3 &albedo, float &tr)
 {
   const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
@@ -948,7 +953,7 @@ __device__ __noinline__ float vol_track(const DevScene &sc, const DevVolume &v, 
   }
   return -1.f;
 }
-__device__ __noinline__ float vol_sample_scatter(const DevScene &sc, V3 ro, V3 rd, float tmin, float tmax, Rng &rng,
+static __device__ __noinline__ float vol_sample_scatter(const DevScene &sc, V3 ro, V3 rd, float tmin, float tmax, Rng &rng,
     V3 &albedo)
 {
   float t_event = -1.f, t_limit = tmax, unused = 1.f;
@@ -970,7 +975,7 @@ __device__ __noinline__ float vol_sample_scatter(const DevScene &sc, V3 ro, V3 r
   }
   return t_event;
 }
-__device__ __noinline__ float vol_transmittance(const DevScene &sc, V3 ro, V3 rd, float tmin, float tmax, Rng &rng)
+static __device__ __noinline__ float vol_transmittance(const DevScene &sc, V3 ro, V3 rd, float tmin, float tmax, Rng &rng)
 {
   float tr = 1.f;
   V3 unused{0.f, 0.f, 0.f};

@@ -82,7 +82,17 @@ PHC_HD bool tri_test(V3 o, V3 d, float4 r0, float4 r1, float4 r2, float tmin, fl
   return true;
 }
 
-PHC_HD float byte_f(uint32_t w, int j) { return float((w >> (8 * j)) & 0xffu); }
+// Byte j of w as a float, exactly: the byte becomes the low mantissa bits of
+// 2^23 (one byte permute) and 2^23 is subtracted (one add), which avoids the
+// integer-to-float conversion unit that throttled the box tests.
+PHC_HD float byte_f(uint32_t w, int j)
+{
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + uint32_t(j))) - 8388608.f;
+#else
+  return u2f(0x4B000000u | ((w >> (8 * j)) & 0xffu)) - 8388608.f;
+#endif
+}
 
 // Intersects the 8 child boxes of one node; returns the k-ordered hit mask of
 // internal children (bit k = slot k ^ oct) and the triangle mask.
@@ -141,59 +151,92 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
   }
 }
 
+// Resumable traversal state of one ray: the current node group (child base,
+// k-ordered hit mask, internal mask) and the stack depth; the stack itself
+// is a per-thread array owned by the caller.
+struct TravState {
+  V3 o, d, idir;
+  uint32_t oct;
+  float tmin;
+  RayHit best;
+  uint32_t g_base, g_hits, g_imask;
+  int sp;
+};
+
+PHC_HD void trav_init(TravState &s, V3 o, V3 d, float tmin, float tmax)
+{
+  s.o = o;
+  s.d = d;
+  s.idir = V3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+  s.oct = (d.x < 0.f ? 4u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 1u : 0u);
+  s.tmin = tmin;
+  s.best = RayHit{tmax, 0xffffffffu, 0.f, 0.f};
+  s.g_base = 0u;
+  s.g_hits = (tmax > tmin) ? 1u << s.oct : 0u; // the root, or nothing for an empty ray
+  s.g_imask = 1u;
+  s.sp = 0;
+}
+
+// One step: the next node of the current group (or of the stack), its box
+// tests and the triangles of its hit leaves.  Returns false when the ray is
+// finished (nothing left, or an any-hit query found a hit).
+template <bool ANY, bool COUNT>
+PHC_HD bool trav_step(const uint4 *__restrict__ nodes, const float4 *__restrict__ tris, TravState &s, uint2 *stack,
+    TravCounters *ctr)
+{
+  if (s.g_hits == 0u) {
+    if (s.sp == 0)
+      return false;
+    const uint2 e = stack[--s.sp];
+    s.g_base = e.x;
+    s.g_hits = e.y & 0xffu;
+    s.g_imask = e.y >> 8;
+  }
+  const uint32_t k = ffs32(s.g_hits) - 1u;
+  s.g_hits &= s.g_hits - 1u;
+  const uint32_t slot = k ^ s.oct;
+  const uint32_t ni = s.g_base + popc32(s.g_imask & ((1u << slot) - 1u));
+  if (s.g_hits != 0u && s.sp < PHC_STACK_SIZE) {
+    stack[s.sp].x = s.g_base;
+    stack[s.sp].y = s.g_hits | (s.g_imask << 8);
+    ++s.sp;
+  }
+  uint32_t tri_base, tri_hits;
+  intersect_node(nodes, ni, s.o, s.idir, s.oct, s.tmin, s.best.t, s.g_base, s.g_hits, s.g_imask, tri_base,
+      tri_hits);
+  if (COUNT)
+    ctr->nodes++;
+  while (tri_hits) {
+    const uint32_t b = ffs32(tri_hits) - 1u;
+    tri_hits &= tri_hits - 1u;
+    const float4 *r = tris + 3 * size_t(tri_base + b);
+    const float4 r0 = ldg4(r), r1 = ldg4(r + 1), r2 = ldg4(r + 2);
+    if (COUNT)
+      ctr->tris++;
+    float t, u, v;
+    if (tri_test(s.o, s.d, r0, r1, r2, s.tmin, s.best.t, t, u, v)) {
+      s.best.t = t;
+      s.best.prim = f2u(r0.w);
+      s.best.u = u;
+      s.best.v = v;
+      if (ANY)
+        return false;
+    }
+  }
+  return s.g_hits != 0u || s.sp != 0;
+}
+
 // Full traversal of one ray.  ANY: stop at the first hit (occlusion).
 template <bool ANY, bool COUNT>
 PHC_HD RayHit trace_ray(const DevScene &sc, V3 o, V3 d, float tmin, float tmax, TravCounters *ctr)
 {
-  RayHit best{tmax, 0xffffffffu, 0.f, 0.f};
-  if (!(tmax > tmin))
-    return best;
-  const V3 idir{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
-  const uint32_t oct = (d.x < 0.f ? 4u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 1u : 0u);
+  TravState s;
+  trav_init(s, o, d, tmin, tmax);
   uint2 stack[PHC_STACK_SIZE];
-  int sp = 0;
-  uint32_t g_base = 0u, g_hits = 1u << oct, g_imask = 1u;
-  for (;;) {
-    if (g_hits == 0u) {
-      if (sp == 0)
-        break;
-      const uint2 e = stack[--sp];
-      g_base = e.x;
-      g_hits = e.y & 0xffu;
-      g_imask = e.y >> 8;
+  if (s.g_hits != 0u)
+    while (trav_step<ANY, COUNT>(sc.nodes, sc.tris, s, stack, ctr)) {
     }
-    const uint32_t k = ffs32(g_hits) - 1u;
-    g_hits &= g_hits - 1u;
-    const uint32_t s = k ^ oct;
-    const uint32_t ni = g_base + popc32(g_imask & ((1u << s) - 1u));
-    if (g_hits != 0u && sp < PHC_STACK_SIZE) {
-      stack[sp].x = g_base;
-      stack[sp].y = g_hits | (g_imask << 8);
-      ++sp;
-    }
-    uint32_t tri_base, tri_hits;
-    intersect_node(sc.nodes, ni, o, idir, oct, tmin, best.t, g_base, g_hits, g_imask, tri_base, tri_hits);
-    if (COUNT)
-      ctr->nodes++;
-    while (tri_hits) {
-      const uint32_t b = ffs32(tri_hits) - 1u;
-      tri_hits &= tri_hits - 1u;
-      const float4 *r = sc.tris + 3 * size_t(tri_base + b);
-      const float4 r0 = ldg4(r), r1 = ldg4(r + 1), r2 = ldg4(r + 2);
-      if (COUNT)
-        ctr->tris++;
-      float t, u, v;
-      if (tri_test(o, d, r0, r1, r2, tmin, best.t, t, u, v)) {
-        best.t = t;
-        best.prim = f2u(r0.w);
-        best.u = u;
-        best.v = v;
-        if (ANY)
-          return best;
-      }
-    }
-  }
-  return best;
+  return s.best;
 }
 
 // Attributes of a hit as intersect_mesh_bvh computes them after the

@@ -9,27 +9,67 @@
 namespace phc {
 
 namespace {
+
 std::once_flag g_once;
 Tuning g_tuning;
 
-int64_t env_or(const char *name, int64_t v)
+struct Key {
+  const char *name;
+  const char *env;
+  int64_t lo, hi;
+  int64_t *wide;
+  int *narrow;
+};
+
+// Every tunable with its environment override and admissible range.
+const Key *keys(size_t &n)
 {
-  const char *s = std::getenv(name);
-  return s && *s ? std::strtoll(s, nullptr, 10) : v;
+  static Key k[] = {
+      {"wave_paths", "PHC_TUNE_WAVE_PATHS", 1024, int64_t(1) << 28, &g_tuning.wave_paths, nullptr},
+      {"trace_blocks_per_sm", "PHC_TUNE_TRACE_BLOCKS_PER_SM", 1, 32, nullptr, &g_tuning.trace_blocks_per_sm},
+      {"shade_blocks_per_sm", "PHC_TUNE_SHADE_BLOCKS_PER_SM", 1, 32, nullptr, &g_tuning.shade_blocks_per_sm},
+      {"use_graph", "PHC_TUNE_USE_GRAPH", 0, 1, nullptr, &g_tuning.use_graph},
+      {"count_traversal", "PHC_TUNE_COUNT_TRAVERSAL", 0, 1, nullptr, &g_tuning.count_traversal},
+      {"max_leaf", "PHC_TUNE_MAX_LEAF", 1, 3, nullptr, &g_tuning.max_leaf},
+      {"time_kernels", "PHC_TUNE_TIME_KERNELS", 0, 1, nullptr, &g_tuning.time_kernels},
+      {"trace_refill", "PHC_TUNE_TRACE_REFILL", 1, 32, nullptr, &g_tuning.trace_refill},
+      {"split_shade", "PHC_TUNE_SPLIT_SHADE", 0, 1, nullptr, &g_tuning.split_shade},
+      {"shade_lean", "PHC_TUNE_SHADE_LEAN", 0, 1, nullptr, &g_tuning.shade_lean},
+      {"batch_wave_paths", "PHC_TUNE_BATCH_WAVE_PATHS", 1024, int64_t(1) << 30, &g_tuning.batch_wave_paths, nullptr},
+  };
+  n = sizeof(k) / sizeof(k[0]);
+  return k;
 }
+
+const Key *find(const char *name)
+{
+  size_t n;
+  const Key *k = keys(n);
+  for (size_t i = 0; i < n; ++i)
+    if (!std::strcmp(k[i].name, name))
+      return &k[i];
+  return nullptr;
+}
+
 } // namespace
 
 Tuning &tuning()
 {
   std::call_once(g_once, [] {
-    Tuning &t = g_tuning;
-    t.wave_paths = env_or("PHC_TUNE_WAVE_PATHS", t.wave_paths);
-    t.trace_blocks_per_sm = int(env_or("PHC_TUNE_TRACE_BLOCKS_PER_SM", t.trace_blocks_per_sm));
-    t.shade_blocks_per_sm = int(env_or("PHC_TUNE_SHADE_BLOCKS_PER_SM", t.shade_blocks_per_sm));
-    t.use_graph = int(env_or("PHC_TUNE_USE_GRAPH", t.use_graph));
-    t.count_traversal = int(env_or("PHC_TUNE_COUNT_TRAVERSAL", t.count_traversal));
-    t.max_leaf = int(env_or("PHC_TUNE_MAX_LEAF", t.max_leaf));
-    t.time_kernels = int(env_or("PHC_TUNE_TIME_KERNELS", t.time_kernels));
+    size_t n;
+    const Key *k = keys(n);
+    for (size_t i = 0; i < n; ++i) {
+      const char *s = std::getenv(k[i].env);
+      if (!s || !*s)
+        continue;
+      const int64_t v = std::strtoll(s, nullptr, 10);
+      if (v < k[i].lo || v > k[i].hi)
+        continue;
+      if (k[i].wide)
+        *k[i].wide = v;
+      else
+        *k[i].narrow = int(v);
+    }
   });
   return g_tuning;
 }
@@ -42,48 +82,28 @@ extern "C" {
 // value out of range.  Not synchronised with concurrent render calls.
 int phc_tuning_set(const char *key, int64_t value)
 {
-  phc::Tuning &t = phc::tuning();
+  phc::tuning();
   if (!key)
     return PHC_ERR_INVALID;
-  if (!std::strcmp(key, "wave_paths") && value >= 1024 && value <= (int64_t(1) << 28))
-    t.wave_paths = value;
-  else if (!std::strcmp(key, "trace_blocks_per_sm") && value >= 1 && value <= 32)
-    t.trace_blocks_per_sm = int(value);
-  else if (!std::strcmp(key, "shade_blocks_per_sm") && value >= 1 && value <= 32)
-    t.shade_blocks_per_sm = int(value);
-  else if (!std::strcmp(key, "use_graph") && (value == 0 || value == 1))
-    t.use_graph = int(value);
-  else if (!std::strcmp(key, "count_traversal") && (value == 0 || value == 1))
-    t.count_traversal = int(value);
-  else if (!std::strcmp(key, "max_leaf") && value >= 1 && value <= 3)
-    t.max_leaf = int(value);
-  else if (!std::strcmp(key, "time_kernels") && (value == 0 || value == 1))
-    t.time_kernels = int(value);
-  else
+  const phc::Key *k = phc::find(key);
+  if (!k || value < k->lo || value > k->hi)
     return PHC_ERR_INVALID;
+  if (k->wide)
+    *k->wide = value;
+  else
+    *k->narrow = int(value);
   return PHC_OK;
 }
 
 int64_t phc_tuning_get(const char *key)
 {
-  const phc::Tuning &t = phc::tuning();
+  phc::tuning();
   if (!key)
     return -1;
-  if (!std::strcmp(key, "wave_paths"))
-    return t.wave_paths;
-  if (!std::strcmp(key, "trace_blocks_per_sm"))
-    return t.trace_blocks_per_sm;
-  if (!std::strcmp(key, "shade_blocks_per_sm"))
-    return t.shade_blocks_per_sm;
-  if (!std::strcmp(key, "use_graph"))
-    return t.use_graph;
-  if (!std::strcmp(key, "count_traversal"))
-    return t.count_traversal;
-  if (!std::strcmp(key, "max_leaf"))
-    return t.max_leaf;
-  if (!std::strcmp(key, "time_kernels"))
-    return t.time_kernels;
-  return -1;
+  const phc::Key *k = phc::find(key);
+  if (!k)
+    return -1;
+  return k->wide ? *k->wide : int64_t(*k->narrow);
 }
 
 } // extern "C"

@@ -15,6 +15,10 @@ struct Tuning {
   int count_traversal{0};            // node-visit / triangle-test counters (roofline runs)
   int max_leaf{3};                   // triangles per BVH8 leaf child (1..3), read at scene build
   int time_kernels{0};               // CUDA events around every launch (no graph), per-kind times
+  int trace_refill{8};               // closest-hit warps refill once this many lanes idle (32: never)
+  int split_shade{1};                // misses and hits shaded by separate kernels (no-volume scenes)
+  int shade_lean{1};                 // lean shading kernels for scenes without volumes/sources/lights
+  int64_t batch_wave_paths{1 << 22}; // paths per wave of a batched render
 };
 
 Tuning &tuning();

@@ -47,9 +47,11 @@ struct PathSoA {
   float *pdist;  // distance travelled by the camera ray
 };
 
-// Shadow ray queue: (o.xyz, tmax), (d.xyz, contrib.x), (contrib.yz, slot, sample).
+// Shadow ray queue: (o.xyz, tmax), (d.xyz, contrib.x), (contrib.yz, slot,
+// sample); job: the batch job of each ray (batched renders only).
 struct ShadowSoA {
   float4 *a, *b, *c;
+  uint32_t *job;
 };
 
 // Per pixel-slot accumulators (slot = lane * npix + pixel).
@@ -66,9 +68,26 @@ struct Accum {
 struct WaveCounters {
   uint32_t *count;   // [max_iter + 1] paths entering iteration it
   uint32_t *scount;  // [max_iter] shadow rays of iteration it
-  uint32_t *fetch;   // [3 * max_iter + 1] work-distribution counters
+  uint32_t *hcount;  // [max_iter] closest-hit results that hit (split queues)
+  uint32_t *mcount;  // [max_iter] closest-hit results that missed (split queues)
+  uint32_t *fetch;   // [4 * max_iter] work counters: trace, shade (all/hits), shade misses, shadow
   uint32_t *wave;    // current wave index within the render call
   uint32_t *error;   // sticky error word
+};
+inline size_t wave_counter_words(int max_iter) { return size_t(9 * max_iter + 1); }
+
+// Indices (into the iteration's path queue) of the paths whose closest-hit
+// query hit / missed, when the shading of misses and hits is split.
+struct HitQueues {
+  uint32_t *hitq;
+  uint32_t *missq;
+};
+
+// Shading kernel variants: FULL compiles volumes, material sources and
+// analytic lights; PART 0 shades every path, 1 the hit queue, 2 the misses.
+struct ShadeVariant {
+  bool full;
+  int part;
 };
 
 // Frame accumulated across render calls (RenderBridge.cpp:386-410).
@@ -83,14 +102,51 @@ struct LaunchCfg {
   int threads;
 };
 
+// ---------------------------------------------------------------- batches
+// One job of a batched render: its scene, constants and accumulators.  Paths
+// of all jobs share the queues; bits 17..31 of PathSoA::info.w hold the job.
+struct BatchJob {
+  DevScene sc;
+  RenderConst rc;
+  Accum acc;
+};
+// One entry of a batch wave: `nsamples` consecutive samples (from
+// sample_begin) of every pixel of `job`, as items [item_begin, item_begin +
+// nsamples * npix) of the wave.
+struct BatchEntry {
+  uint32_t job;
+  uint32_t sample_begin;
+  uint32_t nsamples;
+  uint32_t item_begin;
+};
+struct BatchTable {
+  const BatchJob *jobs;
+  const BatchEntry *entries;  // all waves' entries
+  const uint32_t *wave_entry; // [waves + 1] first entry of each wave
+  const uint32_t *wave_items; // [waves] paths of each wave
+};
+constexpr uint32_t BATCH_JOB_SHIFT = 17;
+constexpr uint32_t MAX_BATCH_JOBS = 1u << (32 - BATCH_JOB_SHIFT);
+
+void launch_raygen_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA out, WaveCounters wc);
+void launch_trace_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA in, float4 *hits,
+    WaveCounters wc, int it, int refill, HitQueues hq);
+void launch_shade_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA in, PathSoA out,
+    const float4 *hits, ShadowSoA sh, WaveCounters wc, int it, ShadeVariant v, HitQueues hq);
+void launch_shadow_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, ShadowSoA sh, WaveCounters wc, int it,
+    int refill);
+
 void launch_raygen(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA out, Accum acc,
     WaveCounters wc);
+// refill: a warp takes new rays once at least this many of its lanes are
+// idle (32: only when all are).  hq.hitq != nullptr: also write the hit and
+// miss index queues.
 void launch_trace(const LaunchCfg &c, cudaStream_t s, DevScene sc, PathSoA in, float4 *hits, WaveCounters wc, int it,
-    uint64_t *stats);
+    uint64_t *stats, int refill, HitQueues hq);
 void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in, PathSoA out,
-    const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it);
+    const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, ShadeVariant v, HitQueues hq);
 void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh, Accum acc,
-    WaveCounters wc, int it, uint64_t *stats);
+    WaveCounters wc, int it, uint64_t *stats, int refill);
 void launch_wave_end(cudaStream_t s, const RenderConst *rc, Accum acc, WaveCounters wc, uint32_t npix, int adaptive,
     int max_iter, uint64_t *ray_totals);
 void launch_resolve(cudaStream_t s, Accum acc, Frame fr, uint32_t npix, uint32_t lanes, float weight, int first);

@@ -36,6 +36,7 @@ SIGNATURES = {
     "phc_read_normal": (C.c_int, [vp, vp]),
     "phc_read_albedo": (C.c_int, [vp, vp]),
     "phc_render_stats_get": (C.c_int, [vp, vp]),
+    "phc_render_batch": (C.c_int, [vp, C.c_uint32, vp]),
     "phc_last_error": (C.c_char_p, [vp]),
     "phc_accel_create": (C.c_int, [C.POINTER(vp), vp, C.c_uint64, vp, C.c_uint64, vp, vp]),
     "phc_accel_destroy": (None, [vp]),

@@ -96,6 +96,31 @@ class Renderer:
         return out
 
 
+def render_batch(jobs) -> dict:
+    """Batched mode: jobs is a list of (Renderer, camera, settings, reset);
+    all render calls run as one wavefront (phc_render_batch).  Returns the
+    batch counters."""
+    lib = load()
+    arr = (_abi.Job * len(jobs))()
+    keep = []
+    for k, (r, cam, st, reset) in enumerate(jobs):
+        r.width, r.height = st.width, st.height
+        arr[k].renderer = r.h
+        arr[k].camera = C.pointer(cam)
+        arr[k].settings = C.pointer(st)
+        arr[k].reset = int(reset)
+        keep.append((cam, st))
+    s = _abi.RenderStats()
+    rc = lib.phc_render_batch(C.addressof(arr), len(jobs), C.byref(s))
+    if rc != 0:
+        raise PhotonError(rc, lib.phc_last_error(jobs[0][0].h).decode())
+    out = {}
+    for k, _ in s._fields_:
+        v = getattr(s, k)
+        out[k] = list(v) if hasattr(v, "__len__") else v
+    return out
+
+
 def tuning_set(key: str, value: int):
     lib = load()
     if lib.phc_tuning_set(key.encode(), int(value)) != 0:

@@ -222,7 +222,7 @@ def sun_sky_env(width=1024, height=512, sun_dir=(0.35, 0.55, -0.75), seed=0):
     return np.ascontiguousarray(img)
 
 
-def procedural_500k(seed=0, n_objects=200, n_spheres=60, sphere_subdiv=4, torus_res=(36, 19)):
+def procedural_500k(seed=0, n_objects=200, n_spheres=60, sphere_subdiv=4, torus_res=(36, 19), env_res=(1024, 512)):
     """~500K triangles: displaced icospheres and tori on a ground plane."""
     rng = np.random.default_rng(seed)
     mb = _MeshBuilder()
@@ -276,10 +276,39 @@ def procedural_500k(seed=0, n_objects=200, n_spheres=60, sphere_subdiv=4, torus_
         mats.append(emitter((30.0, 28.0, 24.0)))
     sc = mb.build(name="procedural_500k")
     sc.materials = mats
-    sc.env_pixels = sun_sky_env(1024, 512)
+    sc.env_pixels = sun_sky_env(*env_res)
     cam = camera((0.0, 9.0, 30.0), (0.0, 0.5, 0.0), fovy_deg=45.0)
     st = settings(1024, 1024, 128, 8, adaptive_sampling=0, throughput_clamp=0.0)
     return sc, cam, st
+
+
+# ----------------------------------------------------------- batched jobs
+
+
+def batched_jobs(seed=0, n=64, min_tris=1_000, max_tris=200_000, min_res=128, max_res=1024, spp=(4, 64),
+                 depth=(4, 12)):
+    """n independent renders: procedural scenes of log-uniform triangle
+    counts, square resolutions log-uniform in [min_res, max_res], samples per
+    pixel and depths uniform in the given ranges.  Returns a list of
+    (SceneData, camera, settings)."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(n):
+        tris = float(np.exp(rng.uniform(np.log(min_tris), np.log(max_tris))))
+        n_obj = 24
+        budget = tris / n_obj
+        subdiv = int(np.clip(np.round(np.log(max(budget, 20) / 20.0) / np.log(4.0)), 0, 5))
+        nu = int(np.clip(np.sqrt(budget), 3, 80))
+        nv = int(np.clip(budget / (2 * nu), 3, 80))
+        res = int(np.exp(rng.uniform(np.log(min_res), np.log(max_res))))
+        sc, cam, st = procedural_500k(seed=1000 + k, n_objects=n_obj, n_spheres=n_obj // 2, sphere_subdiv=subdiv,
+                                      torus_res=(nu, nv), env_res=(256, 128))
+        st.width = st.height = res
+        st.pixel_samples = int(rng.integers(spp[0], spp[1] + 1))
+        st.max_depth = int(rng.integers(depth[0], depth[1] + 1))
+        sc.name = f"job{k}"
+        jobs.append((sc, cam, st))
+    return jobs
 
 
 # ------------------------------------------------------------ feature scenes
