@@ -112,24 +112,27 @@ def dist_setup(n_gpus):
     return world, rank, local
 
 
-def dist_max(x, world):
+def _reduce(x, world, op):
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([float(x)], device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def dist_max(x, world):
+    """Largest value over the ranks (the slowest replica's time)."""
+    import torch.distributed as dist
+    return _reduce(x, world, dist.ReduceOp.MAX) if world > 1 else x
 
 
 def dist_sum(x, world):
-    if world == 1:
-        return x
-    import torch
+    """Sum over the ranks (all replicas' samples)."""
     import torch.distributed as dist
-    t = torch.tensor([float(x)], device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(x, world, dist.ReduceOp.SUM) if world > 1 else x
 
 
 def barrier(world):
@@ -165,6 +168,50 @@ def cpu_baseline(sc, cam, st, spp=1, frames=2):
     return {"value": samples / dt / 1e6, "unit": "Msamples/s", "cores": os.cpu_count(), "kind": "port",
             "sample": f"{frames} frames of {s.width}x{s.height} at {spp} spp of the same workload "
                       f"({samples} pixel-samples, {dt:.1f} s)"}
+
+
+def batched_vs_plain(p, n_jobs=64, seed=0):
+    """The 64-job mix: the same render calls one at a time (phc_render per
+    renderer) and as one batch (phc_render_batch), wall-clock, scenes
+    resident, after one warm-up of each; images compared bit for bit."""
+    import numpy as np
+    import torch
+    from photon_gb300 import workloads
+    jobs = workloads.batched_jobs(seed=seed, n=n_jobs)
+    rs = []
+    for sc, cam, st in jobs:
+        r = p.Renderer()
+        r.set_scene(sc)
+        rs.append(r)
+    samples = sum(st.width * st.height * st.pixel_samples for _, _, st in jobs)
+
+    def plain():
+        for r, (sc, cam, st) in zip(rs, jobs):
+            r.render(cam, st, True)
+
+    def batch():
+        p.render_batch([(r, cam, st, True) for r, (sc, cam, st) in zip(rs, jobs)])
+
+    plain()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    plain()
+    plain_s = time.perf_counter() - t
+    ref = [r.read("color").copy() for r in rs]
+    batch()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    batch()
+    batch_s = time.perf_counter() - t
+    same = all(np.array_equal(a.view(np.uint32), r.read("color").view(np.uint32)) for a, r in zip(ref, rs))
+    tris = [sc.triangle_count for sc, _, _ in jobs]
+    for r in rs:
+        r.close()
+    return {"jobs": n_jobs, "pixel_samples": samples, "plain_s": plain_s, "batched_s": batch_s,
+            "plain_msamples_per_s": samples / plain_s / 1e6, "batched_msamples_per_s": samples / batch_s / 1e6,
+            "ratio": plain_s / batch_s, "identical_images": bool(same),
+            "mix": f"{n_jobs} seeded procedural scenes, {min(tris)}-{max(tris)} tris (log-uniform), "
+                   "128^2-1024^2, 4-64 spp, depth 4-12"}
 
 
 def run_reference(args, world, rank):
@@ -259,15 +306,21 @@ def run_ours(args, world, rank, local):
     e2e_s = dist_max(time.perf_counter() - t, world)
     e2e_value = dist_sum(e2e_samples, world) / e2e_s / 1e6
 
-    # ---- per-kernel times and traversal counters (events around every launch)
+    # ---- per-kernel times (events around every launch, one render) and the
+    # traversal counters (a second render with counting on: the counts are
+    # deterministic, the timing of that render is not used)
     p.tuning_set("time_kernels", 1)
-    p.tuning_set("count_traversal", 1)
     flush.zero_()
     torch.cuda.synchronize()
     r.render(cam, st, True)
     prof = r.stats()
     p.tuning_set("time_kernels", 0)
+    p.tuning_set("count_traversal", 1)
+    r.render(cam, st, True)
+    cnt = r.stats()
     p.tuning_set("count_traversal", 0)
+    for k in ("node_visits", "tri_tests", "shadow_node_visits", "shadow_tri_tests"):
+        prof[k] = cnt[k]
     kinds = ["raygen", "trace_closest", "shade", "trace_shadow", "wave_end+resolve"]
     kms = dict(zip(kinds, prof["kernel_ms"]))
     kcount = dict(zip(kinds, prof["kernel_count"]))
@@ -297,6 +350,10 @@ def run_ours(args, world, rank, local):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, cam, st)
+    batched = None
+    if rank == 0 and not args.no_batch:
+        r.close()
+        batched = batched_vs_plain(p)
 
     if rank == 0:
         h2d = C.sizeof(cam) + C.sizeof(st)
@@ -315,6 +372,7 @@ def run_ours(args, world, rank, local):
             "roofline": roofline,
             "kernel_ms": kms, "kernel_launches_profiled": kcount,
             "cpu_baseline": cpu,
+            "batched_vs_plain": batched,
             "clocks": clk.summary(),
             "gpu_launches": launches,
         }
@@ -329,6 +387,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched/plain measurement")
     args = ap.parse_args()
     world, rank, local = dist_setup(args.gpus if args.impl == "ours" else 0)
     if args.impl == "reference":
