@@ -41,6 +41,14 @@ RAY_BYTES = 32    # origin+tmin, direction+tmax
 HIT_BYTES = 16    # t, prim, u, v
 
 
+_T0 = time.perf_counter()
+
+
+def _log(msg):
+    """Progress on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -170,48 +178,123 @@ def cpu_baseline(sc, cam, st, spp=1, frames=2):
                       f"({samples} pixel-samples, {dt:.1f} s)"}
 
 
-def batched_vs_plain(p, n_jobs=64, seed=0):
+def batched_vs_plain(p, n_jobs=64, seed=0, check_jobs=8):
     """The 64-job mix: the same render calls one at a time (phc_render per
     renderer) and as one batch (phc_render_batch), wall-clock, scenes
-    resident, after one warm-up of each; images compared bit for bit."""
+    resident, after one warm-up of each.  Measured twice: with one sample of
+    every pixel per wavefront (the reference's plain structure,
+    pathtracer.cpp:688-1127; wave_paths = 1) and with the renderer's default
+    sample lanes.  Image identity is checked on `check_jobs` jobs rendered by
+    two fresh renderer sets with the same call history (the bridge's sample
+    counter advances per call)."""
     import numpy as np
     import torch
     from photon_gb300 import workloads
     jobs = workloads.batched_jobs(seed=seed, n=n_jobs)
-    rs = []
-    for sc, cam, st in jobs:
-        r = p.Renderer()
-        r.set_scene(sc)
-        rs.append(r)
     samples = sum(st.width * st.height * st.pixel_samples for _, _, st in jobs)
+    tris = [sc.triangle_count for sc, _, _ in jobs]
+    old = p.tuning_get("wave_paths")
 
-    def plain():
-        for r, (sc, cam, st) in zip(rs, jobs):
+    def make(js):
+        rs = []
+        for sc, cam, st in js:
+            r = p.Renderer()
+            r.set_scene(sc)
+            rs.append(r)
+        return rs
+
+    def plain(rs, js):
+        for r, (sc, cam, st) in zip(rs, js):
             r.render(cam, st, True)
 
-    def batch():
-        p.render_batch([(r, cam, st, True) for r, (sc, cam, st) in zip(rs, jobs)])
+    def batch(rs, js):
+        p.render_batch([(r, cam, st, True) for r, (sc, cam, st) in zip(rs, js)])
 
-    plain()
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    plain()
-    plain_s = time.perf_counter() - t
-    ref = [r.read("color").copy() for r in rs]
-    batch()
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    batch()
-    batch_s = time.perf_counter() - t
-    same = all(np.array_equal(a.view(np.uint32), r.read("color").view(np.uint32)) for a, r in zip(ref, rs))
-    tris = [sc.triangle_count for sc, _, _ in jobs]
-    for r in rs:
-        r.close()
-    return {"jobs": n_jobs, "pixel_samples": samples, "plain_s": plain_s, "batched_s": batch_s,
-            "plain_msamples_per_s": samples / plain_s / 1e6, "batched_msamples_per_s": samples / batch_s / 1e6,
-            "ratio": plain_s / batch_s, "identical_images": bool(same),
-            "mix": f"{n_jobs} seeded procedural scenes, {min(tris)}-{max(tris)} tris (log-uniform), "
-                   "128^2-1024^2, 4-64 spp, depth 4-12"}
+    out = {"jobs": n_jobs, "pixel_samples": samples,
+           "mix": f"{n_jobs} seeded procedural scenes, {min(tris)}-{max(tris)} tris (log-uniform), "
+                  "128^2-1024^2, 4-64 spp, depth 4-12"}
+    _log("batched: jobs generated")
+    try:
+        rs = make(jobs)
+        _log("batched: scenes uploaded")
+        for label, wave_paths in (("one_sample_per_wave", 1024), ("lanes", old)):
+            p.tuning_set("wave_paths", wave_paths)
+            res = {}
+            for name, fn in (("plain", plain), ("batched", batch)):
+                fn(rs, jobs)
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                fn(rs, jobs)
+                res[name + "_s"] = time.perf_counter() - t
+            res["plain_msamples_per_s"] = samples / res["plain_s"] / 1e6
+            res["batched_msamples_per_s"] = samples / res["batched_s"] / 1e6
+            res["ratio"] = res["plain_s"] / res["batched_s"]
+            _log(f"batched: {label} timed")
+            a, b = make(jobs[:check_jobs]), make(jobs[:check_jobs])
+            for _ in range(2):
+                plain(a, jobs[:check_jobs])
+                batch(b, jobs[:check_jobs])
+            res["identical_images"] = bool(all(
+                np.array_equal(x.read("color").view(np.uint32), y.read("color").view(np.uint32))
+                for x, y in zip(a, b)))
+            for r in a + b:
+                r.close()
+            out[label] = res
+        for r in rs:
+            r.close()
+    finally:
+        p.tuning_set("wave_paths", old)
+    out["ratio"] = out["one_sample_per_wave"]["ratio"]
+    out["identical_images"] = out["one_sample_per_wave"]["identical_images"] and out["lanes"]["identical_images"]
+    return out
+
+
+def adjoint_vs_forward(p, reps=3):
+    """Differentiable workload (50K triangles, 8 materials with 512^2 fp32
+    base-colour textures, homogeneous medium, 256^2, depth 6): device time
+    of the 64-spp forward render and of the 16-spp path-replay adjoint with
+    material, texel and medium gradients, on an L2 loss against a 1024-spp
+    image of perturbed parameters.  Reports both times, their ratio (the
+    workload's own numbers) and the ratio per sample."""
+    import numpy as np
+
+    from photon_gb300 import workloads
+    sc_t, cam, st_t = workloads.differentiable(target=True)
+    st_t.pixel_samples = 1024
+    rt = p.Renderer()
+    rt.set_scene(sc_t)
+    rt.render(cam, st_t, True)
+    target = rt.read_color()[..., :3].copy()
+    rt.close()
+    sc, cam, st = workloads.differentiable()
+    r = p.Renderer()
+    r.set_scene(sc)
+    fwd, adj, adj_wall = [], [], []
+    for k in range(reps + 1):
+        r.render(cam, st, True)
+        fwd.append(r.stats()["render_ms"])
+        img = r.read_color()[..., :3]
+        d = np.zeros((st.height, st.width, 4), np.float32)
+        d[..., :3] = 2.0 * (img - target)
+        sa = type(st).from_buffer_copy(bytes(st))
+        sa.pixel_samples = 16
+        t = time.perf_counter()
+        g = r.adjoint(cam, sa, d, sample_offset=(1 << 28) + 16 * k)
+        adj_wall.append((time.perf_counter() - t) * 1e3)
+        adj.append(g["adjoint_ms"])
+    r.close()
+    f = float(np.median(fwd[1:]))
+    a = float(np.median(adj[1:]))
+    loss = float(np.sum((img - target) ** 2))
+    return {"workload": f"differentiable: {sc.triangle_count} tris, 8 materials x 512^2 fp32 base-colour "
+                        f"textures, homogeneous medium; {st.width}x{st.height}, depth {st.max_depth}",
+            "forward_spp": st.pixel_samples, "adjoint_spp": 16,
+            "forward_ms": f, "adjoint_ms": a, "adjoint_wall_ms": float(np.median(adj_wall[1:])),
+            "adjoint_over_forward": a / f,
+            "adjoint_over_forward_per_sample": (a / 16) / (f / st.pixel_samples),
+            "loss": loss, "grad_norm_materials": float(np.linalg.norm(g["materials"])),
+            "grad_norm_texels": float(np.linalg.norm(g["texels"])),
+            "grad_volume": g["volumes"][0].tolist()}
 
 
 def run_reference(args, world, rank):
@@ -257,13 +340,16 @@ def run_ours(args, world, rank, local):
     pbuild.build()
     import photon_gb300 as p
 
+    _log("build done")
     sc, cam, st, desc = workload()
+    _log("workload generated")
     if args.spp:
         st.pixel_samples = args.spp
     r = p.Renderer()
     t = time.perf_counter()
     r.set_scene(sc)
     scene_s = time.perf_counter() - t
+    _log(f"scene uploaded ({scene_s:.1f}s)")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > 129 MB L2
 
     for _ in range(args.warmup):
@@ -292,6 +378,7 @@ def run_ours(args, world, rank, local):
     total_samples = dist_sum(samples, world)
     value = total_samples / t_max / 1e6
 
+    _log("device-timed steps done")
     # ---- end to end through the public API with host buffers
     out = torch.empty((st.height, st.width, 4), dtype=torch.float32).pin_memory()
     out_np = out.numpy()
@@ -347,13 +434,20 @@ def run_ours(args, world, rank, local):
         "launches": kcount["trace_closest"], "kernel_ms_total": kms["trace_closest"],
     }
 
+    _log("e2e and kernel profile done")
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, cam, st)
+        _log("cpu baseline done")
     batched = None
     if rank == 0 and not args.no_batch:
         r.close()
         batched = batched_vs_plain(p)
+        _log("batched/plain done")
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = adjoint_vs_forward(p)
+        _log("adjoint/forward done")
 
     if rank == 0:
         h2d = C.sizeof(cam) + C.sizeof(st)
@@ -373,6 +467,7 @@ def run_ours(args, world, rank, local):
             "kernel_ms": kms, "kernel_launches_profiled": kcount,
             "cpu_baseline": cpu,
             "batched_vs_plain": batched,
+            "adjoint": adjoint,
             "clocks": clk.summary(),
             "gpu_launches": launches,
         }
@@ -388,6 +483,7 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched/plain measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
     args = ap.parse_args()
     world, rank, local = dist_setup(args.gpus if args.impl == "ours" else 0)
     if args.impl == "reference":

@@ -284,6 +284,48 @@ int phc_render_batch(const phc_job *jobs, uint32_t n, phc_render_stats *batch_st
 /* Message of the last failed call on this renderer ("" when none). */
 const char *phc_last_error(const phc_renderer *r);
 
+/* ------------------------------------------------------------ adjoint */
+/* Gradient layout.  Per material: base colour r, g, b, roughness (the
+   bridge's perceptual roughness; GGX alpha = roughness^2), metallic,
+   specTrans (transmission), sheen, clearcoat.  Per volume: density scale,
+   albedo r, g, b (the transfer function's colour, taken as constant over the
+   volume).  Per texel: r, g, b, 0, for the texels of every sampler in the
+   order of phc_scene_desc::samplers (sampler i's texels follow those of
+   samplers 0..i-1). */
+#define PHC_ADJ_MATERIAL_PARAMS 8
+#define PHC_ADJ_VOLUME_PARAMS 4
+#define PHC_ADJ_MAX_VOLUMES 4
+typedef struct phc_adjoint_grads {
+  float *materials; /* material_count * PHC_ADJ_MATERIAL_PARAMS (required)   */
+  float *volumes;   /* volume_count * PHC_ADJ_VOLUME_PARAMS, or NULL          */
+  float *texels;    /* 4 * total texel count, or NULL (no texel gradients)   */
+  float *color;     /* width*height*4: the image of the pass's own samples
+                       (RGB, alpha 0), or NULL                                */
+  double adjoint_ms; /* out: device time of the call                          */
+  uint64_t longest_sample_cycles; /* out: SM clock cycles of the slowest pixel
+                       sample (both passes); a pixel sample that runs past
+                       2^31 cycles or a ray past 2^20 traversal steps stops
+                       the call with PHC_ERR_LIMIT                             */
+} phc_adjoint_grads;
+/* No counterpart in the reference (it has no derivatives).  Path-replay
+   backpropagation: gradients of a loss of the image I that phc_render would
+   produce with these camera/settings from settings->pixel_samples samples
+   starting at sample index sample_offset (a fresh renderer's first render
+   uses sample_offset 0), given d_color = dLoss/dI (width*height RGBA floats
+   in the phc_read_color layout; alpha is ignored).  Each path is traced
+   again from its seed, so the memory does not grow with the depth.  Lobe
+   selection, Russian roulette, MIS weights, clamps and stochastic
+   transparency are held constant; visibility (edge) derivatives are not
+   computed.  Parameters that come from attributes get no gradient; a base
+   colour from an image sampler sends its gradient to the texels.  Leaves
+   the accumulated frame and the sample counter unchanged.  Every output
+   buffer is host memory and is overwritten.  Volume gradients need
+   volume_count <= PHC_ADJ_MAX_VOLUMES (else PHC_ERR_LIMIT). */
+int phc_adjoint(phc_renderer *r, const phc_camera *camera, const phc_settings *settings, uint32_t sample_offset,
+    const float *d_color, phc_adjoint_grads *grads);
+/* Element counts of the scene's gradient buffers (any pointer may be NULL). */
+int phc_adjoint_sizes(const phc_renderer *r, uint64_t *materials, uint64_t *volumes, uint64_t *texels);
+
 /* -------------------------------------------------- Level A (ray back-end) */
 /* Hit record of Level A, field for field photon::pt::HitResult
    (include/photon/pt/backend/ray_backend.h:15-29), 88 bytes. */

@@ -126,6 +126,21 @@ class RenderStats(C.Structure):
     ]
 
 
+ADJ_MATERIAL_PARAMS = 8
+ADJ_VOLUME_PARAMS = 4
+ADJ_MAX_VOLUMES = 4
+# names of the per-material gradient entries, in buffer order
+ADJ_MATERIAL_NAMES = ("base_r", "base_g", "base_b", "roughness", "metallic", "transmission", "sheen", "clearcoat")
+ADJ_VOLUME_NAMES = ("density_scale", "albedo_r", "albedo_g", "albedo_b")
+
+
+class AdjointGrads(C.Structure):
+    _fields_ = [
+        ("materials", C.c_void_p), ("volumes", C.c_void_p), ("texels", C.c_void_p),
+        ("color", C.c_void_p), ("adjoint_ms", C.c_double), ("longest_sample_cycles", C.c_uint64),
+    ]
+
+
 class Job(C.Structure):
     _fields_ = [
         ("renderer", C.c_void_p), ("camera", C.POINTER(Camera)), ("settings", C.POINTER(Settings)),

@@ -1,0 +1,1015 @@
+// Path-replay adjoint (no reference counterpart: the reference has no
+// derivatives).  Gradients of an image loss with respect to the Disney
+// parameters of the materials (base colour, roughness, metallic, specTrans,
+// sheen, clearcoat), the base-colour texels of sampler textures, and the
+// extinction scale and albedo of homogeneous volumes.
+//
+// Path replay backpropagation (Vicini, Speierer and Jakob, "Path Replay
+// Backpropagation", SIGGRAPH 2021): one thread per pixel sample re-runs the
+// path from its seed twice.  Pass 1 computes the path's radiance L exactly as
+// the forward renderer (same reference RNG streams, same shading code).
+// Pass 2 replays it, subtracts every contribution from L as it is collected,
+// and at every vertex adds  delta . (remaining radiance) * d log f / d theta
+// for the sampled BSDF weight and  delta . C * d log f_nee / d theta  for the
+// next-event contribution C, so memory stays O(1) per path whatever its
+// depth.  d f / d theta comes from a forward-mode dual-number instantiation of
+// the Disney eval (dual.cuh) over the 8 parameters.  Lobe selection, Russian
+// roulette, MIS weights, clamps and stochastic transparency are detached
+// (held constant); visibility and edge terms are not computed.  Medium: the majorants scale with the density scale, so the
+// derivative of a tracked segment's log weight is the score of its Poisson
+// process of tentative collisions, (collisions - majorant optical depth) /
+// scale, for delta tracking and ratio tracking alike; a real scattering event
+// multiplies the path by the albedo.
+//
+// Gradients accumulate per block in shared memory (materials, volumes) and in
+// global memory through warp-aggregated atomics (texels: lanes that hit the
+// same texel combine before one atomic).
+#include "adjoint.h"
+#include "dual.cuh"
+#include "wave_common.cuh"
+
+namespace phc {
+namespace {
+
+constexpr int NP = ADJ_MATERIAL_PARAMS; // base r, g, b, roughness, metallic, specTrans, sheen, clearcoat
+using D = Dual<NP>;
+constexpr int MAX_SMEM_MATERIALS = 64;
+constexpr int MAX_VOLUMES = ADJ_MAX_VOLUMES;
+
+struct D3 {
+  D x, y, z;
+};
+__device__ __forceinline__ D3 d3(V3 v) { return D3{dconst<NP>(v.x), dconst<NP>(v.y), dconst<NP>(v.z)}; }
+__device__ __forceinline__ D3 operator+(const D3 &a, const D3 &b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ D3 operator*(const D3 &a, const D &s) { return D3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ D dlum(const D3 &c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+// lerp(a, b, t) = a + (b - a) * t
+__device__ __forceinline__ D dlerp(const D &a, const D &b, const D &t) { return a + (b - a) * t; }
+
+// Material with the differentiable parameters as duals.
+struct MatD {
+  D3 base;
+  D metallic, rough, trans, sheen, coat;
+  float ior, specular, coat_rough;
+};
+
+// d/d(bridge roughness r) of the GGX alpha = r^2 is 2 r.
+__device__ __forceinline__ MatD make_matd(const Mat &m)
+{
+  MatD d;
+  d.base = D3{dvar<NP>(m.base_color.x, 0), dvar<NP>(m.base_color.y, 1), dvar<NP>(m.base_color.z, 2)};
+  d.rough = dconst<NP>(m.roughness);
+  d.rough.d[3] = 2.f * sqrtf(fmaxf(m.roughness, 0.f));
+  d.metallic = dvar<NP>(m.metallic, 4);
+  d.trans = dvar<NP>(m.transmission, 5);
+  d.sheen = dvar<NP>(m.sheen, 6);
+  d.coat = dvar<NP>(m.clearcoat, 7);
+  d.ior = m.ior;
+  d.specular = m.specular;
+  d.coat_rough = m.clearcoat_roughness;
+  return d;
+}
+
+__device__ __forceinline__ float f0_of(float ior)
+{
+  const float a = (1.f - ior) / (1.f + ior);
+  return a * a;
+}
+__device__ __forceinline__ void spec_f0_f90_d(const MatD &m, D3 &F0, D3 &F90)
+{
+  const float scale = fmaxf(2.f * m.specular, 0.f);
+  const D opaque = 1.f - dsat(m.trans);
+  const D f0d = opaque * fminf(f0_of(m.ior) * scale, 1.f);
+  F0 = D3{dlerp(f0d, m.base.x, m.metallic), dlerp(f0d, m.base.y, m.metallic), dlerp(f0d, m.base.z, m.metallic)};
+  const D f90d = opaque * fminf(scale, 1.f);
+  const D one = dconst<NP>(1.f);
+  const D f90 = dlerp(f90d, one, m.metallic);
+  F90 = D3{f90, f90, f90};
+}
+__device__ __forceinline__ D3 schlick_d(float c, const D3 &F0, const D3 &F90)
+{
+  const float k = 1.f - fminf(1.f, fmaxf(0.f, c));
+  const float k2 = k * k;
+  const float k5 = k2 * k2 * k;
+  return D3{F0.x + (F90.x - F0.x) * k5, F0.y + (F90.y - F0.y) * k5, F0.z + (F90.z - F0.z) * k5};
+}
+__device__ __forceinline__ float diffuse_scale_f(const MatD &m, float NoV)
+{
+  const float scale = fmaxf(2.f * m.specular, 0.f);
+  const float f0d = fminf(f0_of(m.ior) * scale, 1.f);
+  const float f90d = fminf(scale, 1.f);
+  const float c = 1.f - fminf(1.f, fmaxf(0.f, NoV));
+  const float c2 = c * c;
+  return 1.f - (f0d + (f90d - f0d) * c2 * c2 * c);
+}
+__device__ __forceinline__ D D_ggx_d(float NoH, const D &a)
+{
+  const D a2 = a * a;
+  const D d = (a2 - 1.f) * (NoH * NoH) + 1.f;
+  return a2 / (d * d * PI);
+}
+__device__ __forceinline__ D G1_d(float NoV, const D &a)
+{
+  const D a2 = a * a;
+  const D denom = dsqrt(a2 + (1.f - a2) * (NoV * NoV)) + NoV;
+  if (denom.v <= 0.f)
+    return dconst<NP>(0.f);
+  return (2.f * NoV) / denom;
+}
+__device__ __forceinline__ float D_ggx_f(float NoH, float a)
+{
+  const float a2 = a * a;
+  const float d = NoH * NoH * (a2 - 1.f) + 1.f;
+  return a2 / (PI * d * d);
+}
+__device__ __forceinline__ float G1_f(float NoV, float a)
+{
+  const float a2 = a * a;
+  const float denom = NoV + sqrtf(a2 + (1.f - a2) * NoV * NoV);
+  return denom <= 0.f ? 0.f : (2.f * NoV) / denom;
+}
+
+// Disney BSDF times cosine (disney_bsdf.h:288-307) with dual parameters.
+__device__ __noinline__ D3 bsdf_eval_d(const MatD &m, V3 wo, V3 wi, V3 n, V3 sn)
+{
+  const D3 zero = d3(V3{0.f, 0.f, 0.f});
+  if (dot(wo, n) <= 0.f || dot(wi, n) <= 0.f)
+    return zero;
+  const float NoL = saturate(dot(sn, wi));
+  const float NoV = saturate(dot(sn, wo));
+  if (NoL <= 0.f || NoV <= 0.f)
+    return zero;
+  D3 f = zero;
+  { // diffuse
+    const D w = (1.f - m.metallic) * (1.f - m.trans) * diffuse_scale_f(m, NoV);
+    if (w.v > 0.f)
+      f = m.base * (w * (INV_PI * NoL));
+  }
+  const D a = dmax(m.rough, 0.001f);
+  if (!(m.rough.v < 0.001f)) { // GGX reflection (not the delta lobe)
+    const V3 h = normalize(wi + wo);
+    const float NoH = saturate(dot(sn, h));
+    const float VoH = saturate(dot(wo, h));
+    D3 F0, F90;
+    spec_f0_f90_d(m, F0, F90);
+    const D3 F = schlick_d(VoH, F0, F90);
+    const D s = D_ggx_d(NoH, a) * G1_d(NoV, a) * G1_d(NoL, a) / (4.f * fmaxf(NoV, 1e-7f));
+    f = f + F * s;
+  }
+  if (m.sheen.v > 0.f && m.metallic.v < 1.f) {
+    const V3 h = normalize(wi + wo);
+    const float HoL = fabsf(dot(h, wi));
+    const D l = dlum(m.base);
+    D3 tint = d3(V3{1.f, 1.f, 1.f});
+    if (l.v > 0.f)
+      tint = D3{m.base.x / l, m.base.y / l, m.base.z / l};
+    const D half = dconst<NP>(0.5f);
+    const D one = dconst<NP>(1.f);
+    const D3 cs = D3{dlerp(one, tint.x, half), dlerp(one, tint.y, half), dlerp(one, tint.z, half)};
+    const float c = 1.f - HoL;
+    const float c2 = c * c;
+    const float c5 = c2 * c2 * c;
+    const D w = (1.f - m.metallic) * (1.f - m.trans);
+    f = f + cs * (m.sheen * w * (c5 * NoL));
+  }
+  if (m.coat.v > 0.f) {
+    const float ac = fmaxf(m.coat_rough, 0.001f);
+    const V3 h = normalize(wi + wo);
+    const float NoH = saturate(dot(sn, h));
+    const float VoH = saturate(dot(wo, h));
+    const float F0 = f0_of(1.5f);
+    const float c = 1.f - saturate(VoH);
+    const float c2 = c * c;
+    const float F = F0 + (1.f - F0) * (c2 * c2 * c);
+    const float s = F * D_ggx_f(NoH, ac) * G1_f(NoV, ac) * G1_f(NoL, ac) / (4.f * fmaxf(NoV, 1e-7f));
+    const D w = m.coat * (0.25f * s);
+    f = f + D3{w, w, w};
+  }
+  return f;
+}
+
+// Weight of a delta lobe (the path weight bsdf_sample returns) up to the
+// constant factor 1 / (selection probability), as duals.
+__device__ __forceinline__ D3 delta_weight_d(const MatD &m, int lobe, V3 wo, V3 n, V3 sn)
+{
+  const bool front = dot(wo, n) > 0.f;
+  if (lobe == LOBE_SPEC_DELTA) {
+    D3 F0, F90;
+    spec_f0_f90_d(m, F0, F90);
+    return schlick_d(saturate(dot(wo, sn)), F0, F90);
+  }
+  // dielectric boundary: t_energy / p_t, times the base colour when transmitted
+  const D w = front ? dsat(m.trans) * (1.f - dsat(m.metallic)) : dconst<NP>(1.f);
+  if (lobe == LOBE_TRANS)
+    return D3{m.base.x * w, m.base.y * w, m.base.z * w};
+  return D3{w, w, w};
+}
+
+// lobe_weights (disney_bsdf.h) with dual parameters.
+__device__ __forceinline__ void lobe_weights_d(const MatD &m, float NoV, D &wd, D &ws, D &wt, D &wc)
+{
+  const D opaque = 1.f - dsat(m.trans);
+  const D dielectric = 1.f - dsat(m.metallic);
+  const D de = dielectric * opaque * diffuse_scale_f(m, NoV);
+  wd = de.v > 0.f ? de * dmax(dlum(m.base), 0.05f) : dconst<NP>(0.f);
+  if (m.sheen.v > 0.f && (dielectric * opaque).v > 0.f)
+    wd = wd + m.sheen * 0.1f;
+  D3 F0, F90;
+  spec_f0_f90_d(m, F0, F90);
+  const D spec = dlum(schlick_d(NoV, F0, F90));
+  ws = spec.v > 0.f ? dmax(spec, 0.05f) : dconst<NP>(0.f);
+  wt = dsat(m.trans) * dielectric;
+  wc = dconst<NP>(0.f);
+  if (m.coat.v > 0.f) {
+    const float c = 1.f - saturate(NoV);
+    const float c2 = c * c;
+    wc = dmax(m.coat * (0.25f * (0.04f + 0.96f * c2 * c2 * c)), 0.02f);
+  }
+}
+
+__device__ __forceinline__ D ggx_pdf_refl_d(float NoH, float VoH, const D &a)
+{
+  return D_ggx_d(NoH, a) * (NoH / (4.f * fmaxf(VoH, 1e-7f)));
+}
+__device__ __forceinline__ float ggx_pdf_refl_f(float NoH, float VoH, float a)
+{
+  return D_ggx_f(NoH, a) * NoH / (4.f * fmaxf(VoH, 1e-7f));
+}
+
+// The direction density of bsdf_sample's non-delta lobes, two ways:
+//   pu  the mixture pdf the estimator divides by (bsdf_pdf, disney_bsdf.h);
+//   pt  the density the sampler actually draws from.  Its diffuse lobe maps
+//       the unit square through sample_concentric_disk (sampling.h:53-75),
+//       whose radius |u| (resp. |v|) folds the disk onto the half x + y > 0
+//       with twice the density, so the diffuse part is 2 cos / pi on that
+//       half of the hemisphere (in the onb of the shading normal) and 0 on
+//       the other.
+// The renderer's expected image is the integral of pt * f / pu, so its
+// derivative carries d log pt - d log pu besides d log f.
+__device__ __noinline__ void pdf_pair_d(const MatD &m, V3 wo, V3 wi, V3 n, V3 sn, D &pu, D &pt)
+{
+  pu = dconst<NP>(0.f);
+  pt = pu;
+  if (dot(wo, n) <= 0.f || dot(wi, n) <= 0.f)
+    return;
+  const float NoL = saturate(dot(sn, wi));
+  const float NoV = saturate(dot(sn, wo));
+  if (NoL <= 0.f || NoV <= 0.f)
+    return;
+  D wd, ws, wt, wc;
+  lobe_weights_d(m, NoV, wd, ws, wt, wc);
+  const D sum = wd + ws + wt + wc;
+  if (!(sum.v > 0.f))
+    return;
+  const D pd = wd / sum, ps = ws / sum, pc = wc / sum;
+  if (pd.v > 0.f) {
+    V3 t, b;
+    onb(sn, t, b);
+    pu = pu + pd * (NoL * INV_PI);
+    if (dot(wi, t) + dot(wi, b) > 0.f)
+      pt = pt + pd * (2.f * NoL * INV_PI);
+  }
+  if (ps.v > 0.f && !(m.rough.v < 0.001f)) {
+    const V3 h = normalize(wi + wo);
+    const D gs = ggx_pdf_refl_d(saturate(dot(sn, h)), saturate(dot(wo, h)), dmax(m.rough, 0.001f));
+    pu = pu + ps * gs;
+    pt = pt + ps * gs;
+  }
+  if (pc.v > 0.f) {
+    const V3 h = normalize(wi + wo);
+    const float gc = ggx_pdf_refl_f(saturate(dot(sn, h)), saturate(dot(wo, h)), fmaxf(m.coat_rough, 0.001f));
+    pu = pu + pc * gc;
+    pt = pt + pc * gc;
+  }
+}
+
+// ----------------------------------------------------------------- grads
+struct Grads {
+  float *smat;      // shared: material_count * NP (or nullptr: global)
+  float *gmat;      // global material grads
+  float *svol;      // shared: volume_count * 4
+  float4 *texels;   // global texel grads
+  uint32_t nmat;
+};
+
+// Atomic add in which the lanes of a warp that target the same address
+// combine their values first (one atomic per distinct address).
+__device__ __forceinline__ void warp_agg_add(float *p, float v)
+{
+  const uint32_t act = __activemask();
+  const uint32_t grp = __match_any_sync(act, reinterpret_cast<unsigned long long>(p));
+  const uint32_t need = __ballot_sync(act, __popc(grp) > 1);
+  const uint32_t lane = threadIdx.x & 31u;
+  if (!((need >> lane) & 1u)) {
+    atomicAdd(p, v);
+    return;
+  }
+  const uint32_t leader = uint32_t(__ffs(int(grp)) - 1);
+  float s = 0.f;
+  for (uint32_t src = 0; src < 32; ++src) {
+    if (!((need >> src) & 1u))
+      continue;
+    const float o = __shfl_sync(need, v, int(src));
+    if (lane == leader && ((grp >> src) & 1u))
+      s += o;
+  }
+  if (lane == leader)
+    atomicAdd(p, s);
+}
+
+__device__ __forceinline__ void add_mat(Grads &g, uint32_t m, int k, float v)
+{
+  if (v == 0.f || !(v == v))
+    return;
+  if (g.smat)
+    atomicAdd(&g.smat[m * NP + k], v);
+  else
+    atomicAdd(&g.gmat[m * NP + k], v);
+}
+
+// Base-colour texture taps at a hit: texel indices, weights and the chain
+// factor d base_i / d acc_j (out transform, clamp at 0) of sampler_sample.
+struct Taps {
+  int n;
+  uint32_t idx[8];
+  float w[8];
+  float dbase[3][4];
+};
+__device__ Taps base_color_taps(const DevScene &sc, const DevMaterial &dm, const Query &q)
+{
+  Taps t;
+  t.n = 0;
+  if (dm.src_kind[SRC_BASE] != 2)
+    return t;
+  const int32_t id = dm.src_index[SRC_BASE];
+  if (id < 0 || uint32_t(id) >= sc.sampler_count)
+    return t;
+  const DevSampler &si = sc.samplers[uint32_t(id)];
+  if (si.type == 3)
+    return t;
+  const float4 attr = fetch_attribute(sc, si.in_attribute, q);
+  float4 c = mat4_mul(si.in_t, attr);
+  c.x += si.in_o[0];
+  c.y += si.in_o[1];
+  c.z += si.in_o[2];
+  const int dims = si.type == 0 ? 1 : (si.type == 1 ? 2 : 3);
+  const float coord[3] = {c.x, c.y, c.z};
+  int32_t i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0};
+  float fr[3] = {0.f, 0.f, 0.f};
+  for (int d = 0; d < dims; ++d) {
+    const int32_t n = int32_t(si.size[d]);
+    float x = coord[d];
+    if (!(x > -1e6f && x < 1e6f))
+      x = 0.f;
+    if (si.linear) {
+      const float f = x * float(n) - 0.5f;
+      const float fl = floorf(f);
+      fr[d] = f - fl;
+      i0[d] = wrap_index(int32_t(fl), n, si.wrap[d]);
+      i1[d] = wrap_index(int32_t(fl) + 1, n, si.wrap[d]);
+    } else {
+      i0[d] = wrap_index(int32_t(floorf(x * float(n))), n, si.wrap[d]);
+      i1[d] = i0[d];
+    }
+  }
+  const uint32_t sx = si.size[0], sxy = si.size[0] * si.size[1];
+  const int nz = dims > 2 ? 2 : 1, ny = dims > 1 ? 2 : 1;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int kz = 0; kz < nz; ++kz) {
+    const float wz = dims > 2 ? (kz ? fr[2] : 1.f - fr[2]) : 1.f;
+    const uint32_t z = uint32_t(kz ? i1[2] : i0[2]);
+    for (int ky = 0; ky < ny; ++ky) {
+      const float wy = dims > 1 ? (ky ? fr[1] : 1.f - fr[1]) : 1.f;
+      const uint32_t y = uint32_t(ky ? i1[1] : i0[1]);
+      for (int kx = 0; kx < 2; ++kx) {
+        const uint32_t x = uint32_t(kx ? i1[0] : i0[0]);
+        const float w = (kx ? fr[0] : 1.f - fr[0]) * (wy * wz);
+        const uint32_t ti = si.offset + z * sxy + y * sx + x;
+        t.idx[t.n] = ti;
+        t.w[t.n] = w;
+        ++t.n;
+        acc = add4(acc, mul4(__ldg(sc.texels + ti), w));
+      }
+    }
+  }
+  const float4 out = mat4_mul(si.out_t, acc);
+  const float o[3] = {out.x + si.out_o[0], out.y + si.out_o[1], out.z + si.out_o[2]};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 4; ++j)
+      t.dbase[i][j] = o[i] > 0.f ? si.out_t[4 * i + j] : 0.f;
+  return t;
+}
+
+// gp += sum_c k_c * (d f_c / d theta) / f_c
+__device__ __forceinline__ void add_dlog3(const D3 &f, V3 k, float *gp)
+{
+  const D *fc[3] = {&f.x, &f.y, &f.z};
+  const float kc[3] = {k.x, k.y, k.z};
+  for (int c = 0; c < 3; ++c) {
+    const float fv = fc[c]->v;
+    if (!(fv > 0.f) || kc[c] == 0.f)
+      continue;
+    const float s = kc[c] / fv;
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+      gp[p] += s * fc[c]->d[p];
+  }
+}
+// gp += K * d log x / d theta
+__device__ __forceinline__ void add_dlog(const D &x, float K, float *gp)
+{
+  if (!(x.v > 0.f) || K == 0.f)
+    return;
+  const float s = K / x.v;
+#pragma unroll
+  for (int p = 0; p < NP; ++p)
+    gp[p] += s * x.d[p];
+}
+
+// Scatters a vertex's parameter gradient gp into its material (constant
+// parameters) and, for a base colour read from an image, its texels.
+__device__ void scatter_grads(Grads &g, const DevMaterial &dm, uint32_t mat_id, const Taps &taps, const float *gp)
+{
+  const int src_of[NP] = {SRC_BASE, SRC_BASE, SRC_BASE, SRC_ROUGH, SRC_METAL, SRC_TRANS, -1, -1};
+  for (int p = 0; p < NP; ++p)
+    if (src_of[p] < 0 || dm.src_kind[src_of[p]] == 0)
+      add_mat(g, mat_id, p, gp[p]);
+  if (taps.n > 0 && g.texels) {
+    for (int t = 0; t < taps.n; ++t) {
+      float *tp = reinterpret_cast<float *>(g.texels + taps.idx[t]);
+      for (int j = 0; j < 3; ++j) {
+        const float v = taps.w[t] * (gp[0] * taps.dbase[0][j] + gp[1] * taps.dbase[1][j] + gp[2] * taps.dbase[2][j]);
+        if (v != 0.f)
+          warp_agg_add(tp + j, v);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------- volumes with d log weight
+// VolumeSet::track (tf_volume.h:150-232) that also adds to dlog the
+// derivative of the log tracking weight per unit of the volume's density
+// scale.
+__device__ float vol_track_d(const DevScene &sc, const DevVolume &v, V3 org, V3 dir, float t0, float t1, Rng &rng,
+    bool scatter, V3 &albedo, float &tr, float &dlog)
+{
+  const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
+  const float ds = v.density_scale;
+  int cell[3], step[3];
+  float t_next[3], t_delta[3];
+  for (int a = 0; a < 3; ++a) {
+    const int m = int(v.macro_dims[a]);
+    const float extent = v.spacing[a] * float(v.dims[a] > 1 ? v.dims[a] - 1 : 1);
+    const float cpu = float(m) / extent;
+    const float g = (o[a] + d[a] * t0 - v.origin[a]) * cpu;
+    int c = int(g);
+    c = c < 0 ? 0 : (c > m - 1 ? m - 1 : c);
+    cell[a] = c;
+    const float speed = d[a] * cpu;
+    if (speed > 0.f) {
+      step[a] = 1;
+      t_delta[a] = 1.f / speed;
+      t_next[a] = t0 + (float(c + 1) - g) * t_delta[a];
+    } else if (speed < 0.f) {
+      step[a] = -1;
+      t_delta[a] = -1.f / speed;
+      t_next[a] = t0 + (g - float(c)) * t_delta[a];
+    } else {
+      step[a] = 0;
+      t_delta[a] = 1e30f;
+      t_next[a] = 1e30f;
+    }
+  }
+  // Every majorant (macro cell) is proportional to the density scale ds, so
+  // the real / null split and the ratio-tracking factors do not depend on it:
+  // only the Poisson process of tentative collisions does.  Its log density
+  // is  n log mu - tau  (n collisions, tau = majorant optical depth covered),
+  // whose derivative per unit of ds is (n - tau) / ds.
+  float t = t0;
+  int lookups = 0;
+  float n = 0.f, tau = 0.f;
+  auto finish = [&]() {
+    if (ds > 0.f)
+      dlog += (n - tau) / ds;
+  };
+  for (int visited = 0; visited < 4096; ++visited) {
+    const int axis = t_next[0] < t_next[1] ? (t_next[0] < t_next[2] ? 0 : 2) : (t_next[1] < t_next[2] ? 1 : 2);
+    const float t_exit = t_next[axis] < t1 ? t_next[axis] : t1;
+    const float bound = __ldg(sc.vol_majorants + v.macro_offset +
+        (uint32_t(cell[2]) * v.macro_dims[1] + uint32_t(cell[1])) * v.macro_dims[0] + uint32_t(cell[0]));
+    if (bound > 0.f) {
+      const float inv_bound = 1.f / bound;
+      const float cell_start = t;
+      while (lookups < 8192) {
+        t -= logf(1.f - rng.next()) * inv_bound;
+        if (t >= t_exit)
+          break;
+        ++lookups;
+        n += 1.f;
+        const float4 c = vol_classify(sc, v, org + dir * t);
+        if (scatter) {
+          if (rng.next() * bound < c.w) {
+            albedo = V3{c.x, c.y, c.z};
+            tau += bound * (t - cell_start);
+            finish();
+            return t;
+          }
+        } else {
+          tr *= 1.f - c.w * inv_bound;
+          if (tr < 0.05f) {
+            if (!(tr > 0.f) || rng.next() * 0.05f >= tr) {
+              tr = 0.f;
+              tau += bound * (t - cell_start);
+              finish();
+              return -1.f;
+            }
+            tr = 0.05f;
+          }
+        }
+      }
+      tau += bound * (fminf(t, t_exit) - cell_start);
+    }
+    t = t_exit;
+    if (t_exit >= t1 || lookups >= 8192)
+      break;
+    cell[axis] += step[axis];
+    if (cell[axis] < 0 || cell[axis] >= int(v.macro_dims[axis]))
+      break;
+    t_next[axis] += t_delta[axis];
+  }
+  finish();
+  return -1.f;
+}
+
+__device__ float vol_scatter_d(const DevScene &sc, V3 ro, V3 rd, float tmin, float tmax, Rng &rng, V3 &albedo,
+    float *dlog, int &event_vol)
+{
+  float t_event = -1.f, t_limit = tmax, unused = 1.f;
+  event_vol = -1;
+  for (uint32_t vi = 0; vi < sc.volume_count; ++vi) {
+    const DevVolume &v = sc.volumes[vi];
+    if (v.majorant <= 0.f || v.tf_size == 0)
+      continue;
+    const V3 org = vol_point(v, ro), dir = vol_vector(v, rd);
+    float t0 = tmin, t1 = t_limit;
+    if (!vol_clip(v, org, dir, t0, t1))
+      continue;
+    V3 ea{0.f, 0.f, 0.f};
+    float dl = 0.f;
+    const float t = vol_track_d(sc, v, org, dir, t0, t1, rng, true, ea, unused, dl);
+    if (vi < uint32_t(MAX_VOLUMES))
+      dlog[vi] += dl;
+    if (t >= 0.f) {
+      t_event = t;
+      t_limit = t;
+      albedo = ea;
+      event_vol = int(vi);
+    }
+  }
+  return t_event;
+}
+
+__device__ float vol_transmittance_d(const DevScene &sc, V3 ro, V3 rd, float tmin, float tmax, Rng &rng, float *dlog)
+{
+  float tr = 1.f;
+  V3 unused{0.f, 0.f, 0.f};
+  for (uint32_t vi = 0; vi < sc.volume_count; ++vi) {
+    const DevVolume &v = sc.volumes[vi];
+    if (v.majorant <= 0.f || v.tf_size == 0)
+      continue;
+    const V3 org = vol_point(v, ro), dir = vol_vector(v, rd);
+    float t0 = tmin, t1 = tmax;
+    if (!vol_clip(v, org, dir, t0, t1))
+      continue;
+    float dl = 0.f;
+    vol_track_d(sc, v, org, dir, t0, t1, rng, false, unused, tr, dl);
+    if (vi < uint32_t(MAX_VOLUMES))
+      dlog[vi] += dl;
+    if (tr <= 0.f)
+      return 0.f;
+  }
+  return tr;
+}
+
+__device__ __forceinline__ void add_vol(Grads &g, const float *dlog, uint32_t nvol, float k)
+{
+  for (uint32_t vi = 0; vi < nvol && vi < uint32_t(MAX_VOLUMES); ++vi)
+    if (dlog[vi] != 0.f && k != 0.f)
+      atomicAdd(&g.svol[4 * vi], k * dlog[vi]);
+}
+
+// trace_ray with a step limit: a ray that needs more than
+// ADJ_MAX_TRAVERSAL_STEPS node visits stops and flags the status word.
+template <bool ANY>
+__device__ RayHit trace_capped(const DevScene &sc, V3 o, V3 d, float tmin, float tmax, unsigned long long *status)
+{
+  TravState s;
+  trav_init(s, o, d, tmin, tmax);
+  uint2 stack[PHC_STACK_SIZE];
+  uint32_t steps = 0;
+  if (s.g_hits != 0u)
+    while (trav_step<ANY, false>(sc.nodes, sc.tris, s, stack, nullptr))
+      if (++steps >= ADJ_MAX_TRAVERSAL_STEPS) {
+        atomicCAS(status, 0ull, 0x10000ull);
+        break;
+      }
+  return s.best;
+}
+
+// ---------------------------------------------------------------- the path
+// One path of one pixel sample, as the forward renderer traces and shades it
+// (shade_kernels.cu shade_path, wavefront.cu k_shadow), in one thread.
+// ADJ = false: returns the path's radiance.  ADJ = true: L is that radiance;
+// accumulates the gradients for the pixel's loss gradient `delta`.
+template <bool ADJ>
+__device__ V3 replay(const RenderConst &rc, const DevScene &sc, uint32_t pixel, uint32_t sample_index, V3 L,
+    V3 delta, Grads &g, unsigned long long *status, long long t_start, unsigned long long budget)
+{
+  V3 collected{0.f, 0.f, 0.f};
+  V3 rem = L; // ADJ: radiance still to be collected from here on
+  auto collect = [&](V3 c) {
+    if (ADJ)
+      rem = rem - c;
+    else
+      collected = collected + c;
+  };
+  V3 ro, rd;
+  float tmin, tmax;
+  camera_ray(rc, pixel, sample_index, ro, rd, tmin, tmax);
+  V3 tp{1.f, 1.f, 1.f};
+  float prev_pdf = -1.f, pdist = 0.f;
+  uint32_t depth = 0, kinds = 0;
+  bool primary = true;
+  const uint32_t max_depth = rc.max_depth;
+  const float eps = sc.eps;
+  const uint32_t nvol = sc.volume_count;
+  // ADJ: the last surface vertex whose non-delta sample set prev_pdf:
+  // d log pu / d theta of that sample, for the MIS weight of the emission
+  // the sampled ray finds
+  bool prev_valid = false;
+  float gprev[NP];
+  uint32_t prev_mat = 0;
+  const DevMaterial *prev_dm = nullptr;
+  Taps prev_taps;
+  prev_taps.n = 0;
+  // d log w_b / d theta = 2 (1 - w_b) d log pu (power heuristic, BSDF side)
+  auto mis_prev = [&](V3 e, float w) {
+    if (!ADJ || !prev_valid || !(w < 1.f))
+      return;
+    const float K = dot(delta, e) * 2.f * (1.f - w);
+    if (K == 0.f)
+      return;
+    float gp[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q)
+      gp[q] = K * gprev[q];
+    scatter_grads(g, *prev_dm, prev_mat, prev_taps, gp);
+  };
+  for (uint32_t it = 0; it < rc.max_iter; ++it) {
+    if (static_cast<unsigned long long>(clock64() - t_start) > budget) {
+      atomicCAS(status, 0ull, 1ull + it);
+      break;
+    }
+    const RayHit hit = trace_capped<false>(sc, ro, rd, tmin, tmax, status);
+    const bool is_hit = hit.prim != 0xffffffffu;
+    const bool emission_only = (kinds & EMISSION_ONLY) != 0u;
+    Rng rng = path_rng(pixel, sample_index, 1u + it);
+    if (nvol > 0) { // volume segment (pathtracer.cpp:789-858)
+      V3 albedo{0.f, 0.f, 0.f};
+      float dlog[MAX_VOLUMES] = {0.f, 0.f, 0.f, 0.f};
+      int ev = -1;
+      const float t_end = is_hit ? hit.t : tmax;
+      const float t_sc = vol_scatter_d(sc, ro, rd, tmin, t_end, rng, albedo, dlog, ev);
+      if (ADJ) { // the segment's weight scales everything collected from here on
+        add_vol(g, dlog, nvol, dot(delta, rem));
+        if (t_sc >= 0.f && ev >= 0 && ev < MAX_VOLUMES) { // the scatter weight is the albedo
+          if (albedo.x > 0.f)
+            atomicAdd(&g.svol[4 * ev + 1], delta.x * rem.x / albedo.x);
+          if (albedo.y > 0.f)
+            atomicAdd(&g.svol[4 * ev + 2], delta.y * rem.y / albedo.y);
+          if (albedo.z > 0.f)
+            atomicAdd(&g.svol[4 * ev + 3], delta.z * rem.z / albedo.z);
+        }
+      }
+      if (t_sc >= 0.f) {
+        const V3 p = ro + rd * t_sc;
+        primary = false;
+        if (depth >= max_depth || emission_only)
+          break;
+        const V3 tpa = tp * albedo;
+        const float phase = 0.25f * INV_PI;
+        const DirectSample ds = sample_direct<true>(sc, p, rng);
+        if (ds.valid) {
+          const float w_mis = ds.mis ? power_heuristic(ds.pdf, phase) : 1.f;
+          V3 c = clamp_contrib(tpa * ds.radiance * (phase * w_mis / ds.pdf), int(depth), rc.clamp_direct,
+              rc.clamp_indirect);
+          const float stmax = ds.dist < 1e29f ? ds.dist * (1.f - 1e-4f) : 1e30f;
+          if (trace_capped<true>(sc, p, ds.wi, 0.f, stmax, status).prim == 0xffffffffu) {
+            Rng rs = path_rng(pixel, sample_index, 0x10000u + it);
+            float dlt[MAX_VOLUMES] = {0.f, 0.f, 0.f, 0.f};
+            c = c * vol_transmittance_d(sc, p, ds.wi, 0.f, stmax, rs, dlt);
+            if (finite3(c)) {
+              collect(c);
+              if (ADJ)
+                add_vol(g, dlt, nvol, dot(delta, c));
+            }
+          }
+        }
+        V3 tp_next = tpa;
+        if (depth >= 2) {
+          const float max_tp = fmaxf(tpa.x, fmaxf(tpa.y, tpa.z));
+          const float survive = fminf(fmaxf(max_tp, 0.05f), 0.95f);
+          if (rng.next() >= survive)
+            break;
+          tp_next = tpa * (1.f / survive);
+        }
+        if (count_bounce(kinds, 24u, rc.max_volume))
+          kinds |= EMISSION_ONLY;
+        tp = tp_next;
+        prev_pdf = phase;
+        prev_valid = false;
+        depth += 1;
+        ro = p;
+        rd = uniform_sphere(rng);
+        tmin = 0.f;
+        tmax = 1e30f;
+        continue;
+      }
+    }
+    if (!is_hit) { // miss: background / environment (pathtracer.cpp:860-899)
+      V3 Lm{0.f, 0.f, 0.f};
+      if (primary) {
+        if (sc.has_env && sc.env_visible)
+          Lm = env_eval(sc, rd);
+        else if (rc.bg_image) {
+          const uint32_t x = pixel % rc.w, y = pixel / rc.w;
+          const float4 bg = bg_image(rc, (float(x) + 0.5f) / float(rc.w), (float(y) + 0.5f) / float(rc.h));
+          Lm = V3{bg.x, bg.y, bg.z} * bg.w;
+        } else
+          Lm = rc3(rc.bg) * rc.bg[3];
+      } else {
+        Lm = rc3(rc.ambient);
+        if (sc.has_env) {
+          float w_mis = 1.f;
+          if (prev_pdf > 0.f)
+            w_mis = power_heuristic(prev_pdf, env_pdf(sc, rd) / float(sc.strategy_count));
+          const V3 le = env_eval(sc, rd);
+          Lm = Lm + le * w_mis;
+          mis_prev(tp * le * w_mis, w_mis);
+        }
+      }
+      V3 c = tp * Lm;
+      if (!primary || (sc.has_env && sc.env_visible))
+        c = clamp_contrib(c, int(depth) - 1, rc.clamp_direct, rc.clamp_indirect);
+      collect(c);
+      break;
+    }
+    const HitAttr ha = hit_attributes(sc, ro, rd, hit);
+    const V3 p = ha.p;
+    const V3 wo = -rd;
+    V3 hit_sn = ha.sn;
+    if (!(dot(hit_sn, hit_sn) > 0.25f))
+      hit_sn = ha.n;
+    else if (dot(hit_sn, ha.n) < 0.f)
+      hit_sn = hit_sn * -1.f;
+    Query q;
+    q.prim = hit.prim;
+    q.vidx = ha.vidx;
+    q.b1 = hit.u;
+    q.b2 = hit.v;
+    q.p = p;
+    q.sn = hit_sn;
+    float alpha_val = 1.f;
+    const DevMaterial &dm = sc.materials[ha.material_id];
+    const Mat mat = resolve_material<true>(sc, dm, q, alpha_val);
+    const bool hidden = (mat.flags & MF_HIDDEN) != 0 && primary;
+    if (hidden || (alpha_val < 1.f && rng.next() >= alpha_val)) {
+      const float nd = pdist + hit.t;
+      tmin = eps;
+      tmax = 1e30f;
+      if (primary) {
+        float tn, tf;
+        clip_range(rc, rd, tn, tf);
+        if (tf < 1e30f) {
+          tmax = tf - nd;
+          if (tmax < eps) {
+            tmin = 1.f;
+            tmax = 0.f;
+          }
+        }
+      }
+      pdist = nd;
+      ro = p;
+      prev_pdf = -1.f;
+      prev_valid = false;
+      continue;
+    }
+    V3 n = ha.n, sn = hit_sn;
+    const bool front = dot(n, wo) >= 0.f;
+    if (!(mat.transmission > 0.f) && !front) {
+      n = n * -1.f;
+      sn = sn * -1.f;
+    }
+    if (dm.src_kind[SRC_NORMAL] != 0)
+      sn = apply_normal_map(sc, dm.src_kind[SRC_NORMAL], dm.src_index[SRC_NORMAL], q, sn);
+    primary = false;
+    if (may_emit(dm) && emits_on_side(mat.flags, front)) {
+      float w_mis = 1.f;
+      if (prev_pdf > 0.f && sc.emissive_count > 0) {
+        const float pdf_area = __ldg(sc.prim_light_pdf + hit.prim);
+        const float cos_light = fabsf(dot(ha.n, wo));
+        if (pdf_area > 0.f && cos_light > 0.f)
+          w_mis = power_heuristic(prev_pdf, pdf_area * hit.t * hit.t / cos_light / float(sc.strategy_count));
+      }
+      const V3 e = clamp_contrib(tp * mat_emission(mat) * w_mis, int(depth) - 1, rc.clamp_direct, rc.clamp_indirect);
+      collect(e);
+      mis_prev(e, w_mis);
+    }
+    if ((mat.flags & MF_EMITTER_ONLY) != 0 || depth >= max_depth || emission_only)
+      break;
+    MatD md;
+    Taps taps;
+    if (ADJ) {
+      md = make_matd(mat);
+      taps = base_color_taps(sc, dm, q);
+    }
+    { // next event estimation
+      const DirectSample ds = sample_direct<true>(sc, p, rng);
+      if (ds.valid) {
+        const V3 f = bsdf_eval(mat, wo, ds.wi, n, sn);
+        if (f.x > 0.f || f.y > 0.f || f.z > 0.f) {
+          float w_mis = 1.f;
+          if (ds.mis)
+            w_mis = power_heuristic(ds.pdf, bsdf_pdf(mat, wo, ds.wi, n, sn));
+          V3 c = clamp_contrib(tp * f * ds.radiance * (w_mis / ds.pdf), int(depth), rc.clamp_direct,
+              rc.clamp_indirect);
+          const V3 so = p + n * eps;
+          V3 sd;
+          float stmax;
+          if (ds.dist < 1e29f) {
+            const V3 to_light = p + ds.wi * ds.dist - so;
+            const float sdist = length(to_light);
+            sd = sdist > 0.f ? to_light * (1.f / sdist) : ds.wi;
+            stmax = sdist * (1.f - 1e-3f);
+          } else {
+            sd = ds.wi;
+            stmax = 1e30f;
+          }
+          if (trace_capped<true>(sc, so, sd, 0.f, stmax, status).prim == 0xffffffffu) {
+            float dlt[MAX_VOLUMES] = {0.f, 0.f, 0.f, 0.f};
+            if (nvol > 0) {
+              Rng rs = path_rng(pixel, sample_index, 0x10000u + it);
+              c = c * vol_transmittance_d(sc, so, sd, 0.f, stmax, rs, dlt);
+            }
+            if (finite3(c)) {
+              collect(c);
+              if (ADJ) {
+                float gp[NP];
+#pragma unroll
+                for (int q = 0; q < NP; ++q)
+                  gp[q] = 0.f;
+                add_dlog3(bsdf_eval_d(md, wo, ds.wi, n, sn), delta * c, gp);
+                if (ds.mis && w_mis < 1.f) { // d log w_nee = -2 (1 - w_nee) d log pu
+                  D pu, pt;
+                  pdf_pair_d(md, wo, ds.wi, n, sn, pu, pt);
+                  add_dlog(pu, -2.f * (1.f - w_mis) * dot(delta, c), gp);
+                }
+                scatter_grads(g, dm, ha.material_id, taps, gp);
+                add_vol(g, dlt, nvol, dot(delta, c));
+              }
+            }
+          }
+        }
+      }
+    }
+    const BSample bs = bsdf_sample(mat, wo, n, sn, rng);
+    if (bs.pdf <= 0.f || (bs.f.x <= 0.f && bs.f.y <= 0.f && bs.f.z <= 0.f))
+      break;
+    if (ADJ) { // everything still to come passes through this vertex's weight
+      const V3 k = delta * rem;
+      const float K = k.x + k.y + k.z;
+      float gp[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q)
+        gp[q] = 0.f;
+      prev_valid = false;
+      if (bs.lobe == LOBE_DIFFUSE || bs.lobe == LOBE_GLOSSY || bs.lobe == LOBE_COAT) {
+        // weight f / pu of a direction drawn from pt
+        D pu, pt;
+        pdf_pair_d(md, wo, bs.wi, n, sn, pu, pt);
+        add_dlog3(bsdf_eval_d(md, wo, bs.wi, n, sn), k, gp);
+        add_dlog(pt, K, gp);
+        add_dlog(pu, -K, gp);
+        if (pu.v > 0.f) {
+          prev_valid = true;
+#pragma unroll
+          for (int q = 0; q < NP; ++q)
+            gprev[q] = pu.d[q] / pu.v;
+          prev_mat = ha.material_id;
+          prev_dm = &dm;
+          prev_taps = taps;
+        }
+      } else {
+        add_dlog3(delta_weight_d(md, bs.lobe, wo, n, sn), k, gp);
+        if (bs.noh > 0.f) // the microfacet normal's density D(h) cos (ggx_half)
+          add_dlog(D_ggx_d(bs.noh, dmax(md.rough, 0.001f)), K, gp);
+      }
+      scatter_grads(g, dm, ha.material_id, taps, gp);
+    }
+    V3 tpn = tp * (bs.f * (1.f / bs.pdf));
+    if (depth >= 2) {
+      const float max_tp = fmaxf(tpn.x, fmaxf(tpn.y, tpn.z));
+      const float survive = fminf(fmaxf(max_tp, 0.05f), 0.95f);
+      if (rng.next() >= survive)
+        break;
+      tpn = tpn * (1.f / survive);
+    }
+    if (rc.tp_clamp > 0.f) {
+      const float mx = fmaxf(tpn.x, fmaxf(tpn.y, tpn.z));
+      if (mx > rc.tp_clamp)
+        tpn = tpn * (rc.tp_clamp / mx);
+    }
+    if (!finite3(tpn))
+      break;
+    tp = tpn;
+    prev_pdf = bs.spec ? -1.f : bs.pdf;
+    depth += 1;
+    const V3 wi = normalize(bs.wi);
+    const float side = dot(wi, ha.n) < 0.f ? -1.f : 1.f;
+    const bool through = (dot(wi, ha.n) < 0.f) != (dot(wo, ha.n) < 0.f);
+    const bool exceeded = through ? count_bounce(kinds, 16u, rc.max_transmission)
+                                  : (bs.diff ? count_bounce(kinds, 0u, rc.max_diffuse)
+                                             : count_bounce(kinds, 8u, rc.max_glossy));
+    if (exceeded)
+      kinds |= EMISSION_ONLY;
+    ro = p + ha.n * (side * eps);
+    rd = wi;
+    tmin = 0.f;
+    tmax = 1e30f;
+  }
+  return collected;
+}
+
+__global__ void __launch_bounds__(128) k_adjoint(const RenderConst *__restrict__ rcp, DevScene sc, AdjointArgs a)
+{
+  __shared__ float smat[MAX_SMEM_MATERIALS * NP];
+  __shared__ float svol[MAX_VOLUMES * 4];
+  const bool shared_mat = sc.material_count <= uint32_t(MAX_SMEM_MATERIALS);
+  for (uint32_t i = threadIdx.x; i < MAX_SMEM_MATERIALS * NP; i += blockDim.x)
+    smat[i] = 0.f;
+  for (uint32_t i = threadIdx.x; i < MAX_VOLUMES * 4; i += blockDim.x)
+    svol[i] = 0.f;
+  __syncthreads();
+  Grads g{shared_mat ? smat : nullptr, a.mat_grads, svol, a.texel_grads, sc.material_count};
+  const RenderConst &rc = *rcp;
+  const uint64_t total = uint64_t(a.npix) * a.spp;
+  unsigned long long longest = 0;
+  for (uint64_t item = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; item < total;
+       item += uint64_t(gridDim.x) * blockDim.x) {
+    if (*reinterpret_cast<volatile unsigned long long *>(a.status) != 0ull)
+      break;
+    const long long t0 = clock64();
+    const uint32_t pixel = uint32_t(item % a.npix);
+    const uint32_t s = uint32_t(item / a.npix);
+    const uint32_t sample_index = a.sample_offset + s;
+    const V3 L = replay<false>(rc, sc, pixel, sample_index, V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, g, a.status, t0,
+        a.cycle_budget);
+    if (a.radiance) {
+      atomicAdd(a.radiance + 3 * pixel, L.x);
+      atomicAdd(a.radiance + 3 * pixel + 1, L.y);
+      atomicAdd(a.radiance + 3 * pixel + 2, L.z);
+    }
+    const float4 dI = a.d_image[pixel];
+    const V3 delta{dI.x * a.inv_spp, dI.y * a.inv_spp, dI.z * a.inv_spp};
+    if (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f)
+      replay<true>(rc, sc, pixel, sample_index, L, delta, g, a.status, t0, a.cycle_budget);
+    const unsigned long long dt = static_cast<unsigned long long>(clock64() - t0);
+    longest = dt > longest ? dt : longest;
+  }
+  atomicMax(a.status + 1, longest);
+  __syncthreads();
+  if (shared_mat)
+    for (uint32_t i = threadIdx.x; i < sc.material_count * NP; i += blockDim.x)
+      if (smat[i] != 0.f)
+        atomicAdd(&a.mat_grads[i], smat[i]);
+  for (uint32_t i = threadIdx.x; i < MAX_VOLUMES * 4 && i < sc.volume_count * 4; i += blockDim.x)
+    if (svol[i] != 0.f)
+      atomicAdd(&a.vol_grads[i], svol[i]);
+}
+
+} // namespace
+
+void launch_adjoint(cudaStream_t s, int blocks, const RenderConst *rc, DevScene sc, AdjointArgs a)
+{
+  k_adjoint<<<blocks, 128, 0, s>>>(rc, sc, a);
+}
+
+int adjoint_max_active_blocks(int threads)
+{
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adjoint, threads, 0) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
+
+} // namespace phc

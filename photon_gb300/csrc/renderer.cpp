@@ -24,6 +24,7 @@
 #include "pt_math.cuh"
 #include "scene_build.h"
 #include "tuning.h"
+#include "adjoint.h"
 #include "wavefront.h"
 
 using namespace phc;
@@ -107,6 +108,8 @@ struct phc_renderer {
   // batched renders led by this renderer: job table, wave schedule, and the
   // job tags of the shadow queue
   Buf b_jobs, b_entries, b_wave_entry, b_wave_items, sh_job;
+  // adjoint: constants, background, loss gradient, gradients, radiance
+  Buf adj_rc, adj_bg, adj_dimg, adj_rad, adj_mat, adj_vol, adj_tex, adj_status;
   phc_render_stats last{};
   cudaEvent_t ev0{nullptr}, ev1{nullptr};
 
@@ -273,6 +276,7 @@ WaveCounters wave_counters(phc_renderer *r, int max_iter)
   wc.fetch = c + (4 * max_iter + 1);
   wc.wave = c + wave_counter_words(max_iter);
   wc.error = c + wave_counter_words(max_iter) + 1;
+  wc.dbg = c + wave_counter_words(max_iter) + 4;
   return wc;
 }
 // Bytes of the counters reset at the start of every wave (not wave / error).
@@ -360,11 +364,39 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
       launches += 3;
     }
     timed(3, [&] { launch_shadow(cfg, s, rc, sc, sh, ac, wc, it, counting ? stats + 5 : nullptr, tu.trace_refill); });
+    if (sc.volume_count > 0)
+      launches += 1; // k_shadow_volume
   }
   timed(4, [&] { launch_wave_end(s, rc, ac, wc, npix, adaptive, max_iter, stats); });
   if (tm)
     tm->end_wave(s);
   return launches;
+}
+
+// The sticky error word of the wave kernels (WAVE_TRIP_CAP self-check) and
+// the record of the failing warp.
+void check_wave_error(uint32_t w, const WaveCounters &wc, cudaStream_t s)
+{
+  if (w == 0u)
+    return;
+  uint32_t d[WAVE_DBG_WORDS] = {};
+  cudaMemcpyAsync(d, wc.dbg, sizeof(d), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  auto f = [&](int i) {
+    float x;
+    std::memcpy(&x, &d[i], 4);
+    return std::to_string(x);
+  };
+  const uint32_t kind = w >> 16;
+  throw ApiError(PHC_ERR_DEVICE, std::string("a ") + (kind == WAVE_ERR_TRACE ? "closest-hit" : "shadow") +
+          " traversal warp exceeded its loop-trip cap at bounce iteration " + std::to_string(w & 0xffffu) +
+          " (queue " + std::to_string(d[0]) + ", fetched " + std::to_string(d[1]) + ", busy " +
+          std::to_string(d[2]) + ", exhausted " + std::to_string(d[3]) + "; ray " + std::to_string(d[4]) + " o " +
+          f(5) + " " + f(6) + " " + f(7) + " tmax " + f(8) + " d " + f(9) + " " + f(10) + " " + f(11) + " sp " +
+          std::to_string(d[12]) + " base " + std::to_string(d[13]) + " hits " + std::to_string(d[14]) + " imask " +
+          std::to_string(d[15]) + " steps " + std::to_string(d[16]) + " rays of the lane " + std::to_string(d[17]) + "; warp fetch trips " + std::to_string(d[18]) +
+          " step trips " + std::to_string(d[19]) + " longest ray " + std::to_string(d[20]) + " steps (ray " +
+          std::to_string(d[21]) + "); trips " + std::to_string(d[22]) + " active " + std::to_string(d[23]) + ")");
 }
 
 // What one render call of one renderer needs: its constants, sample lanes
@@ -387,6 +419,43 @@ void validate_call(phc_renderer *r, const phc_settings &st)
     throw ApiError(PHC_ERR_LIMIT, "frame larger than 2^28 pixels");
 }
 
+// The constants of one render call of a w x h frame (everything but the
+// sample offset and lanes); a background image goes to `bg`.
+RenderConst render_const(const phc_camera &cam, const phc_settings &st, Buf &bg, cudaStream_t s)
+{
+  const uint32_t w = st.width, h = st.height;
+  const uint32_t npix = w * h;
+  RenderConst rc{};
+  make_camera(cam, w, h, rc);
+  rc.w = w;
+  rc.h = h;
+  rc.npix = npix;
+  rc.spp = std::max<uint32_t>(st.pixel_samples, 1);
+  rc.max_depth = std::max<uint32_t>(st.max_depth, 1);
+  rc.max_iter = rc.max_depth + 1u + 8u;
+  std::memcpy(rc.bg, st.background, sizeof(rc.bg));
+  // background image (RenderBridge.cpp:848-870)
+  const size_t bg_n = size_t(st.background_width) * st.background_height * 4;
+  if (st.background_image && bg_n > 0) {
+    ck(bg.ensure(bg_n * 4), "alloc background");
+    ck(cudaMemcpyAsync(bg.p, st.background_image, bg_n * 4, cudaMemcpyHostToDevice, s), "upload background");
+    rc.bg_image = bg.as<float4>();
+    rc.bg_w = st.background_width;
+    rc.bg_h = st.background_height;
+  }
+  for (int i = 0; i < 3; ++i)
+    rc.ambient[i] = st.ambient_color[i] * st.ambient_radiance;
+  rc.adaptive = st.adaptive_sampling ? 1 : 0;
+  rc.tp_clamp = st.throughput_clamp;
+  rc.max_diffuse = st.max_diffuse_bounces;
+  rc.max_glossy = st.max_glossy_bounces;
+  rc.max_transmission = st.max_transmission_bounces;
+  rc.max_volume = st.max_volume_bounces;
+  rc.clamp_direct = 3.f * std::max(st.clamp_direct, 0.f);
+  rc.clamp_indirect = 3.f * std::max(st.clamp_indirect, 0.f);
+  return rc;
+}
+
 JobPlan prepare_job(phc_renderer *r, const phc_camera &cam, const phc_settings &st, bool reset, cudaStream_t s)
 {
   validate_call(r, st);
@@ -402,35 +471,8 @@ JobPlan prepare_job(phc_renderer *r, const phc_camera &cam, const phc_settings &
     r->height = h;
     reset = true;
   }
-  RenderConst rc{};
-  make_camera(cam, w, h, rc);
-  rc.w = w;
-  rc.h = h;
-  rc.npix = npix;
-  rc.spp = std::max<uint32_t>(st.pixel_samples, 1);
-  rc.max_depth = std::max<uint32_t>(st.max_depth, 1);
-  rc.max_iter = rc.max_depth + 1u + 8u;
+  RenderConst rc = render_const(cam, st, r->bg_buf, s);
   rc.sample_offset = r->sample_counter;
-  std::memcpy(rc.bg, st.background, sizeof(rc.bg));
-  // background image (RenderBridge.cpp:848-870)
-  const size_t bg_n = size_t(st.background_width) * st.background_height * 4;
-  if (st.background_image && bg_n > 0) {
-    ck(r->bg_buf.ensure(bg_n * 4), "alloc background");
-    ck(cudaMemcpyAsync(r->bg_buf.p, st.background_image, bg_n * 4, cudaMemcpyHostToDevice, s), "upload background");
-    rc.bg_image = r->bg_buf.as<float4>();
-    rc.bg_w = st.background_width;
-    rc.bg_h = st.background_height;
-  }
-  for (int i = 0; i < 3; ++i)
-    rc.ambient[i] = st.ambient_color[i] * st.ambient_radiance;
-  rc.adaptive = st.adaptive_sampling ? 1 : 0;
-  rc.tp_clamp = st.throughput_clamp;
-  rc.max_diffuse = st.max_diffuse_bounces;
-  rc.max_glossy = st.max_glossy_bounces;
-  rc.max_transmission = st.max_transmission_bounces;
-  rc.max_volume = st.max_volume_bounces;
-  rc.clamp_direct = 3.f * std::max(st.clamp_direct, 0.f);
-  rc.clamp_indirect = 3.f * std::max(st.clamp_indirect, 0.f);
   // samples of one pixel in flight: enough paths to fill the GPU, one when
   // adaptive sampling needs the samples in order
   const Tuning &tu = tuning();
@@ -493,11 +535,12 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
   const bool first = plan.first;
   const Tuning &tu = tuning();
   ensure_paths(r, plan.slots);
-  ck(r->counters.ensure(per_wave_counter_bytes(max_iter) + 16), "alloc counters");
+  ck(r->counters.ensure(wave_counter_alloc_bytes(max_iter)), "alloc counters");
   ck(r->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
   ck(cudaMemsetAsync(r->stats_buf.p, 0, 8 * sizeof(uint64_t), s), "reset stats");
   const WaveCounters wc = wave_counters(r, max_iter);
   ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
+  ck(cudaMemsetAsync(wc.dbg, 0, WAVE_DBG_WORDS * 4, s), "reset wave");
   const LaunchCfg cfg = launch_cfg(r, plan.slots);
   const bool counting = tu.count_traversal != 0;
   const RenderConst *drc = r->rc_buf.as<RenderConst>();
@@ -558,8 +601,11 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
   ck(cudaGetLastError(), "kernel launch");
   ck(cudaEventRecord(r->ev1, s), "event");
   uint64_t stats[8];
+  uint32_t err_word = 0;
   ck(cudaMemcpyAsync(stats, r->stats_buf.p, sizeof(stats), cudaMemcpyDeviceToHost, s), "read stats");
+  ck(cudaMemcpyAsync(&err_word, wc.error, 4, cudaMemcpyDeviceToHost, s), "read error word");
   ck(cudaStreamSynchronize(s), "render");
+  check_wave_error(err_word, wc, s);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, r->ev0, r->ev1);
   r->last.pixel_samples = stats[0];
@@ -660,7 +706,7 @@ void record_batch_wave(phc_renderer *lead, cudaStream_t s, const LaunchCfg &cfg,
     } else {
       launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 0}, hq);
     }
-    launch_shadow_batch(cfg, s, bt, sh, wc, it, tu.trace_refill);
+    launch_shadow_batch(cfg, s, bt, sh, wc, it, tu.trace_refill, (features & SCENE_VOLUMES) != 0);
   }
   launch_wave_end(s, nullptr, Accum{}, wc, 0, 0, max_iter, lead->stats_buf.as<uint64_t>());
 }
@@ -717,11 +763,12 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
   upload_vec(lead->b_wave_items, bp.wave_items, s, "upload batch waves");
   ensure_paths(lead, bp.max_items);
   ck(lead->sh_job.ensure(size_t(std::max<uint32_t>(bp.max_items, 1)) * 4), "alloc shadow jobs");
-  ck(lead->counters.ensure(per_wave_counter_bytes(bp.max_iter) + 16), "alloc counters");
+  ck(lead->counters.ensure(wave_counter_alloc_bytes(bp.max_iter)), "alloc counters");
   ck(lead->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
   ck(cudaMemsetAsync(lead->stats_buf.p, 0, 8 * sizeof(uint64_t), s), "reset stats");
   const WaveCounters wc = wave_counters(lead, bp.max_iter);
   ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
+  ck(cudaMemsetAsync(wc.dbg, 0, WAVE_DBG_WORDS * 4, s), "reset wave");
   const BatchTable bt{lead->b_jobs.as<BatchJob>(), lead->b_entries.as<BatchEntry>(),
       lead->b_wave_entry.as<uint32_t>(), lead->b_wave_items.as<uint32_t>()};
   const LaunchCfg cfg = launch_cfg(lead, bp.max_items);
@@ -767,8 +814,11 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
   ck(cudaGetLastError(), "kernel launch");
   ck(cudaEventRecord(lead->ev1, s), "event");
   uint64_t stats[8];
+  uint32_t err_word = 0;
   ck(cudaMemcpyAsync(stats, lead->stats_buf.p, sizeof(stats), cudaMemcpyDeviceToHost, s), "read stats");
+  ck(cudaMemcpyAsync(&err_word, wc.error, 4, cudaMemcpyDeviceToHost, s), "read error word");
   ck(cudaStreamSynchronize(s), "batch");
+  check_wave_error(err_word, wc, s);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, lead->ev0, lead->ev1);
   phc_render_stats st{};
@@ -786,6 +836,89 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
   lead->last = st;
   if (out_stats)
     *out_stats = st;
+}
+
+// ---------------------------------------------------------------- adjoint
+void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st, uint32_t sample_offset,
+    const float *d_color, phc_adjoint_grads &g)
+{
+  validate_call(r, st);
+  if (st.adaptive_sampling)
+    throw ApiError(PHC_ERR_INVALID, "the adjoint takes every sample: adaptive sampling must be off");
+  if (!g.materials)
+    throw ApiError(PHC_ERR_INVALID, "null material gradient buffer");
+  const DevScene &sc = r->scene.dev;
+  if (g.volumes && sc.volume_count > uint32_t(PHC_ADJ_MAX_VOLUMES))
+    throw ApiError(PHC_ERR_LIMIT, "volume gradients for more than PHC_ADJ_MAX_VOLUMES volumes");
+  check_device(r);
+  cudaStream_t s = r->stream;
+  RenderConst rc = render_const(cam, st, r->adj_bg, s);
+  rc.sample_offset = sample_offset;
+  rc.lanes = 1;
+  const uint32_t npix = rc.npix;
+  const size_t nmat = size_t(sc.material_count) * ADJ_MATERIAL_PARAMS;
+  const size_t nvol = size_t(std::min<uint32_t>(sc.volume_count, ADJ_MAX_VOLUMES)) * ADJ_VOLUME_PARAMS;
+  const size_t ntex = g.texels ? size_t(r->scene.texel_count) : 0;
+  ck(r->adj_rc.ensure(sizeof(RenderConst)), "alloc constants");
+  ck(r->adj_dimg.ensure(size_t(npix) * 16), "alloc adjoint");
+  ck(r->adj_rad.ensure(size_t(npix) * 12), "alloc adjoint");
+  ck(r->adj_mat.ensure(nmat * 4), "alloc adjoint");
+  ck(r->adj_vol.ensure(std::max<size_t>(nvol, 1) * 4), "alloc adjoint");
+  if (ntex)
+    ck(r->adj_tex.ensure(ntex * 16), "alloc adjoint");
+  ck(r->adj_status.ensure(16), "alloc adjoint");
+  ck(cudaEventRecord(r->ev0, s), "event");
+  ck(cudaMemsetAsync(r->adj_status.p, 0, 16, s), "clear adjoint");
+  ck(cudaMemcpyAsync(r->adj_rc.p, &rc, sizeof(rc), cudaMemcpyHostToDevice, s), "upload constants");
+  ck(cudaMemcpyAsync(r->adj_dimg.p, d_color, size_t(npix) * 16, cudaMemcpyHostToDevice, s), "upload loss gradient");
+  ck(cudaMemsetAsync(r->adj_rad.p, 0, size_t(npix) * 12, s), "clear adjoint");
+  ck(cudaMemsetAsync(r->adj_mat.p, 0, nmat * 4, s), "clear adjoint");
+  ck(cudaMemsetAsync(r->adj_vol.p, 0, std::max<size_t>(nvol, 1) * 4, s), "clear adjoint");
+  if (ntex)
+    ck(cudaMemsetAsync(r->adj_tex.p, 0, ntex * 16, s), "clear adjoint");
+  AdjointArgs a{};
+  a.d_image = r->adj_dimg.as<float4>();
+  a.radiance = g.color ? r->adj_rad.as<float>() : nullptr;
+  a.mat_grads = r->adj_mat.as<float>();
+  a.vol_grads = r->adj_vol.as<float>();
+  a.texel_grads = ntex ? r->adj_tex.as<float4>() : nullptr;
+  a.status = r->adj_status.as<unsigned long long>();
+  a.cycle_budget = 1ull << 31; // about 1 s at the SM clock, per pixel sample
+  a.npix = npix;
+  a.spp = rc.spp;
+  a.sample_offset = sample_offset;
+  a.inv_spp = 1.f / float(rc.spp);
+  const int blocks = r->sm_count * adjoint_max_active_blocks(128);
+  launch_adjoint(s, blocks, r->adj_rc.as<RenderConst>(), sc, a);
+  ck(cudaGetLastError(), "adjoint kernel");
+  ck(cudaEventRecord(r->ev1, s), "event");
+  ck(cudaMemcpyAsync(g.materials, r->adj_mat.p, nmat * 4, cudaMemcpyDeviceToHost, s), "read gradients");
+  if (g.volumes && nvol)
+    ck(cudaMemcpyAsync(g.volumes, r->adj_vol.p, nvol * 4, cudaMemcpyDeviceToHost, s), "read gradients");
+  if (ntex)
+    ck(cudaMemcpyAsync(g.texels, r->adj_tex.p, ntex * 16, cudaMemcpyDeviceToHost, s), "read gradients");
+  unsigned long long status[2] = {0, 0};
+  ck(cudaMemcpyAsync(status, r->adj_status.p, 16, cudaMemcpyDeviceToHost, s), "read status");
+  std::vector<float> rad;
+  if (g.color) {
+    rad.resize(size_t(npix) * 3);
+    ck(cudaMemcpyAsync(rad.data(), r->adj_rad.p, rad.size() * 4, cudaMemcpyDeviceToHost, s), "read radiance");
+  }
+  ck(cudaStreamSynchronize(s), "adjoint");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, r->ev0, r->ev1);
+  g.adjoint_ms = ms;
+  g.longest_sample_cycles = status[1];
+  if (status[0] != 0)
+    throw ApiError(PHC_ERR_LIMIT, status[0] >= 0x10000ull
+            ? "adjoint: a ray exceeded the traversal step limit"
+            : "adjoint: a pixel sample exceeded its time budget at bounce " + std::to_string(status[0] - 1));
+  if (g.color)
+    for (size_t p = 0; p < npix; ++p) {
+      for (int c = 0; c < 3; ++c)
+        g.color[4 * p + c] = rad[3 * p + c] * a.inv_spp;
+      g.color[4 * p + 3] = 0.f;
+    }
 }
 
 int read_channel(phc_renderer *r, float *out, int channel)
@@ -989,6 +1122,32 @@ int phc_render_batch(const phc_job *jobs, uint32_t n, phc_render_stats *batch_st
   for (phc_renderer *r : order)
     r->mutex.unlock();
   return rc;
+}
+
+int phc_adjoint(phc_renderer *r, const phc_camera *camera, const phc_settings *settings, uint32_t sample_offset,
+    const float *d_color, phc_adjoint_grads *grads)
+{
+  if (!r)
+    return set_error(nullptr, PHC_ERR_INVALID, "null renderer");
+  std::lock_guard<std::mutex> lock(r->mutex);
+  if (!camera || !settings || !d_color || !grads)
+    return set_error(r, PHC_ERR_INVALID, "null camera, settings, loss gradient or gradient buffers");
+  return guarded(r, [&] { adjoint_impl(r, *camera, *settings, sample_offset, d_color, *grads); });
+}
+
+int phc_adjoint_sizes(const phc_renderer *r, uint64_t *materials, uint64_t *volumes, uint64_t *texels)
+{
+  if (!r)
+    return set_error(nullptr, PHC_ERR_INVALID, "null renderer");
+  if (!r->has_scene)
+    return set_error(nullptr, PHC_ERR_NO_SCENE, "no scene");
+  if (materials)
+    *materials = uint64_t(r->scene.dev.material_count) * PHC_ADJ_MATERIAL_PARAMS;
+  if (volumes)
+    *volumes = uint64_t(r->scene.dev.volume_count) * PHC_ADJ_VOLUME_PARAMS;
+  if (texels)
+    *texels = r->scene.texel_count * 4;
+  return PHC_OK;
 }
 
 uint32_t phc_accumulated_samples(const phc_renderer *r) { return r ? r->samples : 0u; }

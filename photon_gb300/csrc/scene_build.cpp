@@ -549,6 +549,7 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   node_bytes = uint64_t(h.bvh.nodes.size()) * 4;
   tri_bytes = uint64_t(h.bvh.tris.size()) * 4;
   bvh_depth = h.bvh.max_depth;
+  texel_count = uint64_t(h.texels.size() / 4);
   if (!err.empty()) {
     release();
     return err;

@@ -50,6 +50,7 @@ struct DeviceScene {
   DevScene dev{};
   size_t bytes{0};
   uint64_t node_bytes{0}, tri_bytes{0};
+  uint64_t texel_count{0};
   uint32_t bvh_depth{0};
   ~DeviceScene();
   void release();

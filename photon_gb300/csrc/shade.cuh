@@ -251,14 +251,21 @@ __device__ __forceinline__ V3 ggx_half(V3 n, float a, Rng &rng)
   const float phi = 2.f * PI * r2;
   return normalize(t * (st * cosf(phi)) + b * (st * sinf(phi)) + n * ct);
 }
+// Sampled lobe: 1 diffuse, 2 GGX reflection, 3 smooth (delta) specular,
+// 4 dielectric reflection, 5 dielectric transmission, 6 clearcoat.  noh > 0:
+// the dielectric lobes went through a GGX-sampled microfacet normal h, with
+// noh = dot(n, h) (the derivative code needs its density).
+enum : int { LOBE_NONE = 0, LOBE_DIFFUSE, LOBE_GLOSSY, LOBE_SPEC_DELTA, LOBE_TRANS_REFL, LOBE_TRANS, LOBE_COAT };
 struct BSample {
   V3 wi, f;
   float pdf;
   bool spec, diff;
+  int lobe;
+  float noh;
 };
 static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3 sn, Rng &rng)
 {
-  BSample out{V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, 0.f, false, false};
+  BSample out{V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, 0.f, false, false, LOBE_NONE, 0.f};
   const BSample none = out;
   const bool front = dot(wo, n) > 0.f;
   if (!front && m.transmission <= 0.f)
@@ -283,6 +290,7 @@ static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3
   if (xi < pd) {
     out.wi = cosine_hemisphere(sn, rng);
     out.diff = true;
+    out.lobe = LOBE_DIFFUSE;
     out.f = bsdf_eval(m, wo, out.wi, n, sn);
     out.pdf = bsdf_pdf(m, wo, out.wi, n, sn);
     return out;
@@ -299,6 +307,7 @@ static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3
       out.f = schlick(saturate(dot(wo, sn)), F0, F90) * (1.f / ps);
       out.pdf = 1.f;
       out.spec = true;
+      out.lobe = LOBE_SPEC_DELTA;
       return out;
     }
     const V3 h = ggx_half(sn, rough, rng);
@@ -307,6 +316,7 @@ static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3
       return none;
     out.f = bsdf_eval(m, wo, out.wi, n, sn);
     out.pdf = bsdf_pdf(m, wo, out.wi, n, sn);
+    out.lobe = LOBE_GLOSSY;
     return out;
   }
   if (xi < pd + ps + pt && m.transmission > 0.f) {
@@ -319,6 +329,8 @@ static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3
       h = ggx_half(snf, rough, rng);
       if (dot(h, wo) <= 0.f)
         h = snf;
+      else
+        out.noh = dot(snf, h);
     }
     const bool refractive = (m.flags & MF_REFRACTIVE) != 0 && m.thin == 0;
     const float ior = fmaxf(m.ior, 1.0001f);
@@ -336,23 +348,30 @@ static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3
     out.spec = true;
     if (rng.next() < F) {
       out.wi = reflect(-wo, h);
-      if (dot(out.wi, nn) <= 0.f)
+      if (dot(out.wi, nn) <= 0.f) {
         out.wi = reflect(-wo, nn);
+        out.noh = 0.f;
+      }
       if (dot(out.wi, nn) <= 0.f)
         return none;
       out.f = V3{1.f, 1.f, 1.f} * lobe_weight;
+      out.lobe = LOBE_TRANS_REFL;
       return out;
     }
     if (refractive) {
       out.wi = normalize(refract(-wo, h, eta));
-      if (dot(out.wi, nn) >= 0.f)
+      if (dot(out.wi, nn) >= 0.f) {
         out.wi = normalize(refract(-wo, snf, eta));
+        out.noh = 0.f;
+      }
       if (dot(out.wi, nn) >= 0.f)
         return none;
     } else {
       out.wi = normalize(-wo);
+      out.noh = 0.f;
     }
     out.f = m.base_color * lobe_weight;
+    out.lobe = LOBE_TRANS;
     return out;
   }
   if (pc > 0.f) {
@@ -362,6 +381,7 @@ static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3
       return none;
     out.f = bsdf_eval(m, wo, out.wi, n, sn);
     out.pdf = bsdf_pdf(m, wo, out.wi, n, sn);
+    out.lobe = LOBE_COAT;
     return out;
   }
   return out;

@@ -11,9 +11,13 @@ constexpr uint32_t EMISSION_ONLY = 0x80000000u;
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
-// Next `k`-item batch of a warp; uniform across the warp.
+// Next `k`-item batch of a warp; uniform across the warp.  Every lane of
+// the warp calls it.  The __syncwarp makes the reconvergence explicit: a
+// lane that ran long divergent work (a tracking loop, a shading call) must
+// be back before the warp votes, or the lanes' views of the batch differ.
 __device__ __forceinline__ uint32_t warp_fetch(uint32_t *ctr, uint32_t k = 32u)
 {
+  __syncwarp();
   uint32_t base = 0;
   if (lane_id() == 0)
     base = atomicAdd(ctr, k);
@@ -24,6 +28,7 @@ __device__ __forceinline__ uint32_t warp_fetch(uint32_t *ctr, uint32_t k = 32u)
 // lanes of the warp call it (ballot + popc prefix, one atomic per warp).
 __device__ __forceinline__ uint32_t warp_append(uint32_t *ctr, bool pred)
 {
+  __syncwarp();
   const uint32_t mask = __ballot_sync(WARP_FULL, pred);
   if (mask == 0u)
     return 0u;
@@ -74,6 +79,37 @@ __device__ __forceinline__ void clip_range(const RenderConst &rc, V3 dir, float 
     tn = rc.clip_near / ca;
   if (rc.clip_far < 1e30f)
     tf = rc.clip_far / ca;
+}
+
+// Jittered camera ray of one pixel sample (pathtracer.cpp:727-743 with
+// Camera::ray and clip_range, camera.h:118-157).
+__device__ __forceinline__ void camera_ray(const RenderConst &rc, uint32_t pixel, uint32_t sample_index, V3 &ro,
+    V3 &rd, float &tmin, float &tmax)
+{
+  const uint32_t x = pixel % rc.w, y = pixel / rc.w;
+  Rng rng = path_rng(pixel, sample_index, 0u);
+  float u = (float(x) + rng.next()) / float(rc.w);
+  float v = (float(y) + rng.next()) / float(rc.h); // rows from the bottom (bridge: bottom_up)
+  u = rc.region[0] + (rc.region[2] - rc.region[0]) * u;
+  v = rc.region[1] + (rc.region[3] - rc.region[1]) * v;
+  const V3 ll = rc3(rc.lower_left), hz = rc3(rc.horizontal), vt = rc3(rc.vertical), org = rc3(rc.origin);
+  if (rc.ortho) {
+    ro = ll + hz * u + vt * v;
+    rd = -rc3(rc.cw);
+  } else if (rc.lens_radius <= 0.f) {
+    ro = org;
+    rd = normalize(ll + hz * u + vt * v - org);
+  } else {
+    float dx, dy;
+    concentric_disk(rng, dx, dy);
+    dx = dx * rc.lens_radius;
+    dy = dy * rc.lens_radius;
+    const V3 off = rc3(rc.cu) * dx + rc3(rc.cv) * dy;
+    const V3 target = ll + hz * u + vt * v;
+    ro = org + off;
+    rd = normalize(target - org - off);
+  }
+  clip_range(rc, rd, tmin, tmax);
 }
 
 // sample_background_image, pathtracer.cpp:370-389

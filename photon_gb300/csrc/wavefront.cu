@@ -3,6 +3,8 @@
 //   k_raygen   pt_init_sample      pathtracer.cpp:691-760
 //   k_trace    trace_closest       kokkos_backend.cpp:21-61 (BVH8, traverse.cuh)
 //   k_shadow   trace_occluded + pt_nee_accum_pack  pathtracer.cpp:1092-1123
+//   k_shadow_volume  the transmittance of the unoccluded shadow rays of
+//              volume scenes (the tracking loop, out of the voting loop)
 //   k_wave_end pt_update_variance  pathtracer.cpp:1129-1139 (+ wave bookkeeping)
 //   k_resolve  pt_resolve + frame accumulation  pathtracer.cpp:1143-1155,
 //              RenderBridge.cpp:386-410
@@ -19,37 +21,6 @@ namespace phc {
 namespace {
 
 // ----------------------------------------------------------------- raygen
-// Jittered camera ray of one pixel sample (pathtracer.cpp:727-743 with
-// Camera::ray and clip_range, camera.h:118-157).
-__device__ __forceinline__ void camera_ray(const RenderConst &rc, uint32_t pixel, uint32_t sample_index, V3 &ro,
-    V3 &rd, float &tmin, float &tmax)
-{
-  const uint32_t x = pixel % rc.w, y = pixel / rc.w;
-  Rng rng = path_rng(pixel, sample_index, 0u);
-  float u = (float(x) + rng.next()) / float(rc.w);
-  float v = (float(y) + rng.next()) / float(rc.h); // rows from the bottom (bridge: bottom_up)
-  u = rc.region[0] + (rc.region[2] - rc.region[0]) * u;
-  v = rc.region[1] + (rc.region[3] - rc.region[1]) * v;
-  const V3 ll = rc3(rc.lower_left), hz = rc3(rc.horizontal), vt = rc3(rc.vertical), org = rc3(rc.origin);
-  if (rc.ortho) {
-    ro = ll + hz * u + vt * v;
-    rd = -rc3(rc.cw);
-  } else if (rc.lens_radius <= 0.f) {
-    ro = org;
-    rd = normalize(ll + hz * u + vt * v - org);
-  } else {
-    float dx, dy;
-    concentric_disk(rng, dx, dy);
-    dx = dx * rc.lens_radius;
-    dy = dy * rc.lens_radius;
-    const V3 off = rc3(rc.cu) * dx + rc3(rc.cv) * dy;
-    const V3 target = ll + hz * u + vt * v;
-    ro = org + off;
-    rd = normalize(target - org - off);
-  }
-  clip_range(rc, rd, tmin, tmax);
-}
-
 // Batched raygen: the items of this wave are the entries of its table (job,
 // sample range, every pixel); each path lands in its job's lane of the
 // sample (lane = sample % job lanes), exactly as the job's own render would.
@@ -150,6 +121,64 @@ __global__ void __launch_bounds__(256) k_raygen(const RenderConst *__restrict__ 
   }
 }
 
+// Loop-trip cap reached (WAVE_TRIP_CAP): the first warp to report writes the
+// error word and its record (the state of its first busy lane).  Called by
+// every lane of the warp.
+__device__ __forceinline__ void record_cap(const WaveCounters &wc, uint32_t code, uint32_t n, uint32_t fetched,
+    bool busy, bool exhausted, uint32_t idx, float4 o, float4 d, const TravState &s, uint32_t steps, uint32_t rays,
+    uint32_t fetch_trips, uint32_t step_trips, uint32_t max_steps, uint32_t max_idx, uint32_t trips)
+{
+  const uint32_t active = __activemask();
+  const uint32_t bm = __ballot_sync(WARP_FULL, busy);
+  // the busy lane with the most steps on its current ray
+  uint32_t best = busy ? steps : 0u;
+  for (int off = 16; off > 0; off >>= 1)
+    best = max(best, __shfl_xor_sync(WARP_FULL, best, off));
+  const uint32_t cand = __ballot_sync(WARP_FULL, busy && steps == best);
+  uint32_t won = 0;
+  if (lane_id() == 0)
+    won = atomicCAS(wc.error, 0u, code) == 0u ? 1u : 0u;
+  won = __shfl_sync(WARP_FULL, won, 0);
+  if (!won)
+    return;
+  uint32_t *r = wc.dbg;
+  if (lane_id() == 0) {
+    r[0] = n;
+    r[1] = fetched;
+    r[2] = bm;
+    r[3] = exhausted ? 1u : 0u;
+  }
+  if (cand != 0u && lane_id() == uint32_t(__ffs(int(cand)) - 1)) {
+    r[4] = idx;
+    r[5] = __float_as_uint(o.x);
+    r[6] = __float_as_uint(o.y);
+    r[7] = __float_as_uint(o.z);
+    r[8] = __float_as_uint(o.w);
+    r[9] = __float_as_uint(d.x);
+    r[10] = __float_as_uint(d.y);
+    r[11] = __float_as_uint(d.z);
+    r[12] = uint32_t(s.sp);
+    r[13] = s.g_base;
+    r[14] = s.g_hits;
+    r[15] = s.g_imask;
+    r[16] = steps;
+    r[17] = rays;
+  }
+  uint32_t ms = max_steps;
+  for (int off = 16; off > 0; off >>= 1)
+    ms = max(ms, __shfl_xor_sync(WARP_FULL, ms, off));
+  const uint32_t mc = __ballot_sync(WARP_FULL, max_steps == ms);
+  if (lane_id() == 0) {
+    r[18] = fetch_trips;
+    r[19] = step_trips;
+    r[20] = ms;
+    r[22] = trips;
+    r[23] = active;
+  }
+  if (lane_id() == uint32_t(__ffs(int(mc)) - 1))
+    r[21] = max_idx;
+}
+
 // ------------------------------------------------------------ closest hit
 // Persistent warps with dynamic refill: a lane whose ray is finished idles
 // until `refill` lanes of its warp are idle, then the warp fetches that many
@@ -169,14 +198,21 @@ __global__ void __launch_bounds__(128) k_trace(DevScene sc, BatchTable bt, PathS
   TravState s;
   uint2 stack[PHC_STACK_SIZE];
   bool busy = false, exhausted = false;
-  uint32_t idx = 0;
+  uint32_t idx = 0, steps = 0, rays = 0, fetch_trips = 0, step_trips = 0, max_steps = 0, max_idx = 0;
   const uint4 *nodes = sc.nodes;
   const float4 *tris = sc.tris;
-  for (;;) {
+  for (uint32_t trips = 0;; ++trips) {
+    if (trips >= WAVE_TRIP_CAP) { // warp-uniform: every lane counts the same trips
+      record_cap(wc, (WAVE_ERR_TRACE << 16) | uint32_t(it), n, *fetch, busy, exhausted, idx, in.ray_o[idx],
+          in.ray_d[idx], s, steps, rays, fetch_trips, step_trips, max_steps, max_idx, trips);
+      break;
+    }
+    __syncwarp(); // every lane back from the last trip's divergent work before the votes
     const uint32_t idle = __ballot_sync(WARP_FULL, !busy);
     if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= refill)) {
       const uint32_t k = uint32_t(__popc(idle));
       const uint32_t base = warp_fetch(fetch, k);
+      ++fetch_trips;
       if (base + k >= n)
         exhausted = true;
       if (!busy) {
@@ -190,6 +226,8 @@ __global__ void __launch_bounds__(128) k_trace(DevScene sc, BatchTable bt, PathS
             tris = job.sc.tris;
           }
           trav_init(s, v3(o), v3(d), o.w, d.w);
+          steps = 0;
+          ++rays;
           busy = true;
         }
       }
@@ -200,8 +238,15 @@ __global__ void __launch_bounds__(128) k_trace(DevScene sc, BatchTable bt, PathS
       continue;
     }
     bool done = false;
-    if (busy)
+    ++step_trips;
+    if (busy) {
       done = !trav_step<false, COUNT>(nodes, tris, s, stack, &ctr);
+      ++steps;
+      if (steps > max_steps) {
+        max_steps = steps;
+        max_idx = idx;
+      }
+    }
     if (SPLIT) {
       const bool is_hit = done && s.best.prim != 0xffffffffu;
       const uint32_t ph = warp_append(wc.hcount + it, is_hit);
@@ -236,15 +281,22 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
   TravState s;
   uint2 stack[PHC_STACK_SIZE];
   bool busy = false, exhausted = false;
-  uint32_t idx = 0, job = 0;
+  uint32_t idx = 0, job = 0, steps = 0, rays = 0, fetch_trips = 0, step_trips = 0, max_steps = 0, max_idx = 0;
   const uint4 *nodes = sc.nodes;
   const float4 *tris = sc.tris;
   // persistent warps with dynamic refill, as in k_trace
-  for (;;) {
+  for (uint32_t trips = 0;; ++trips) {
+    if (trips >= WAVE_TRIP_CAP) {
+      record_cap(wc, (WAVE_ERR_SHADOW << 16) | uint32_t(it), n, *fetch, busy, exhausted, idx, sh.a[idx], sh.b[idx],
+          s, steps, rays, fetch_trips, step_trips, max_steps, max_idx, trips);
+      break;
+    }
+    __syncwarp(); // every lane back from the last trip's divergent work before the votes
     const uint32_t idle = __ballot_sync(WARP_FULL, !busy);
     if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= refill)) {
       const uint32_t k = uint32_t(__popc(idle));
       const uint32_t base = warp_fetch(fetch, k);
+      ++fetch_trips;
       if (base + k >= n)
         exhausted = true;
       if (!busy) {
@@ -258,6 +310,8 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
             tris = bt.jobs[job].sc.tris;
           }
           trav_init(s, v3(a), v3(b), 0.f, a.w);
+          steps = 0;
+          ++rays;
           busy = true;
         }
       }
@@ -267,19 +321,27 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
         break;
       continue;
     }
+    ++step_trips;
+    if (busy) {
+      ++steps;
+      if (steps > max_steps) {
+        max_steps = steps;
+        max_idx = idx;
+      }
+    }
     if (busy && !trav_step<true, COUNT>(nodes, tris, s, stack, &ctr)) {
       busy = false;
-      if (s.best.prim == 0xffffffffu) { // unoccluded
-        const DevScene &S = BATCH ? bt.jobs[job].sc : sc;
+      // Unoccluded: add the contribution here when the ray's scene has no
+      // volume; otherwise leave the ray (tmax >= 0) to k_shadow_volume, so
+      // that no lane runs a tracking loop inside this warp-voting loop.
+      // Occluded or done: tmax < 0.
+      const bool vol = (BATCH ? bt.jobs[job].sc.volume_count : sc.volume_count) > 0;
+      const bool open = s.best.prim == 0xffffffffu;
+      if (open && !vol) {
         const Accum &acc = BATCH ? bt.jobs[job].acc : acc_param;
-        const uint32_t npix = BATCH ? bt.jobs[job].rc.npix : rcp->npix;
         const float4 b = sh.b[idx], c = sh.c[idx];
-        V3 contrib{b.w, c.x, c.y};
-        const uint32_t slot = __float_as_uint(c.z), sample_index = __float_as_uint(c.w);
-        if (S.volume_count > 0) {
-          Rng rs = path_rng(slot % npix, sample_index, 0x10000u + uint32_t(it));
-          contrib = contrib * vol_transmittance(S, s.o, s.d, 0.f, s.best.t, rs);
-        }
+        const V3 contrib{b.w, c.x, c.y};
+        const uint32_t slot = __float_as_uint(c.z);
         if (finite3(contrib)) {
           float4 v = acc.acc[slot];
           v.x = v.x + contrib.x;
@@ -288,11 +350,43 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
           acc.acc[slot] = v;
         }
       }
+      if (!(open && vol))
+        sh.a[idx].w = -1.f;
     }
   }
   if (COUNT) {
     atomicAdd((unsigned long long *)&stats[0], (unsigned long long)ctr.nodes);
     atomicAdd((unsigned long long *)&stats[1], (unsigned long long)ctr.tris);
+  }
+}
+
+// The unoccluded shadow rays of volume scenes (tmax >= 0 after k_shadow):
+// contribution times the ratio-tracking transmittance of the volumes along
+// [0, tmax] (stream dimension 0x10000 + iteration), added to the path's slot.
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__restrict__ rcp, DevScene sc,
+    BatchTable bt, ShadowSoA sh, Accum acc_param, WaveCounters wc, int it)
+{
+  const uint32_t n = wc.scount[it];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 a = sh.a[i];
+    if (!(a.w >= 0.f))
+      continue;
+    const uint32_t job = BATCH ? sh.job[i] : 0u;
+    const DevScene &S = BATCH ? bt.jobs[job].sc : sc;
+    const Accum &acc = BATCH ? bt.jobs[job].acc : acc_param;
+    const uint32_t npix = BATCH ? bt.jobs[job].rc.npix : rcp->npix;
+    const float4 b = sh.b[i], c = sh.c[i];
+    const uint32_t slot = __float_as_uint(c.z), sample_index = __float_as_uint(c.w);
+    Rng rs = path_rng(slot % npix, sample_index, 0x10000u + uint32_t(it));
+    const V3 contrib = V3{b.w, c.x, c.y} * vol_transmittance(S, v3(a), v3(b), 0.f, a.w, rs);
+    if (finite3(contrib)) {
+      float4 v = acc.acc[slot];
+      v.x = v.x + contrib.x;
+      v.y = v.y + contrib.y;
+      v.z = v.z + contrib.z;
+      acc.acc[slot] = v;
+    }
   }
 }
 
@@ -428,6 +522,8 @@ void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, De
     k_shadow<true, false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, stats, r);
   else
     k_shadow<false, false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, nullptr, r);
+  if (sc.volume_count > 0)
+    k_shadow_volume<false><<<c.blocks_shade, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it);
 }
 
 void launch_raygen_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA out, WaveCounters wc)
@@ -447,10 +543,12 @@ void launch_trace_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathS
 }
 
 void launch_shadow_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, ShadowSoA sh, WaveCounters wc, int it,
-    int refill)
+    int refill, bool volumes)
 {
   const uint32_t r = uint32_t(refill < 1 ? 1 : (refill > 32 ? 32 : refill));
   k_shadow<false, true><<<c.blocks_trace, 128, 0, s>>>(nullptr, DevScene{}, bt, sh, Accum{}, wc, it, nullptr, r);
+  if (volumes)
+    k_shadow_volume<true><<<c.blocks_shade, 128, 0, s>>>(nullptr, DevScene{}, bt, sh, Accum{}, wc, it);
 }
 
 void launch_wave_end(cudaStream_t s, const RenderConst *rc, Accum acc, WaveCounters wc, uint32_t npix, int adaptive,

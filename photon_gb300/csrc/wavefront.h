@@ -73,8 +73,22 @@ struct WaveCounters {
   uint32_t *fetch;   // [4 * max_iter] work counters: trace, shade (all/hits), shade misses, shadow
   uint32_t *wave;    // current wave index within the render call
   uint32_t *error;   // sticky error word
+  uint32_t *dbg;     // [WAVE_DBG_WORDS] record of the first self-check failure
 };
 inline size_t wave_counter_words(int max_iter) { return size_t(9 * max_iter + 1); }
+
+// Self-check of the persistent traversal loops: a warp that makes more than
+// WAVE_TRIP_CAP loop trips (each trip is one traversal step of every busy
+// lane; legitimate work needs a few thousand) stops and records
+// (kernel << 16) | iteration in the error word, first writer wins.
+constexpr uint32_t WAVE_TRIP_CAP = 1u << 24;
+enum : uint32_t { WAVE_ERR_TRACE = 1u, WAVE_ERR_SHADOW = 2u };
+// dbg words: queue length, fetch counter, busy ballot, exhausted, then for
+// the warp's first busy lane: ray index, origin xyz, tmax, direction xyz,
+// stack depth, group base, group hits, group internal mask, steps of the ray.
+constexpr uint32_t WAVE_DBG_WORDS = 24;
+// Counter words after the per-wave block: wave, error, 2 spare, dbg.
+inline size_t wave_counter_alloc_bytes(int max_iter) { return (wave_counter_words(max_iter) + 4 + WAVE_DBG_WORDS) * 4; }
 
 // Indices (into the iteration's path queue) of the paths whose closest-hit
 // query hit / missed, when the shading of misses and hits is split.
@@ -133,8 +147,9 @@ void launch_trace_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathS
     WaveCounters wc, int it, int refill, HitQueues hq);
 void launch_shade_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA in, PathSoA out,
     const float4 *hits, ShadowSoA sh, WaveCounters wc, int it, ShadeVariant v, HitQueues hq);
+// volumes: some job of the batch has volumes (k_shadow_volume runs too).
 void launch_shadow_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, ShadowSoA sh, WaveCounters wc, int it,
-    int refill);
+    int refill, bool volumes);
 
 void launch_raygen(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA out, Accum acc,
     WaveCounters wc);

@@ -86,6 +86,47 @@ class Renderer:
     def read_albedo(self):
         return self.read("albedo")
 
+    def adjoint_sizes(self):
+        """Element counts of the material, volume and texel gradient buffers."""
+        m, v, t = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._check(self.lib.phc_adjoint_sizes(self.h, C.byref(m), C.byref(v), C.byref(t)))
+        return int(m.value), int(v.value), int(t.value)
+
+    def adjoint(self, camera, settings, d_color, sample_offset=0, texels=True, volumes=True, color=False):
+        """Path-replay gradients of a loss given dLoss/dImage (h, w, 4) or
+        (h, w, 3) float32 (row 0 = bottom row) for the image of
+        settings.pixel_samples samples from sample index sample_offset.
+
+        Returns {"materials": (M, 8), "volumes": (V, 4), "texels": (T, 4),
+        "color": (h, w, 4) when color=True, "adjoint_ms": float}.
+        """
+        h, w = settings.height, settings.width
+        d = np.asarray(d_color, np.float32)
+        if d.shape[:2] != (h, w) or d.ndim != 3 or d.shape[2] not in (3, 4):
+            raise ValueError(f"d_color must be ({h}, {w}, 3|4)")
+        if d.shape[2] == 3:
+            d = np.concatenate([d, np.zeros((h, w, 1), np.float32)], axis=2)
+        d = np.ascontiguousarray(d)
+        nm, nv, nt = self.adjoint_sizes()
+        g_mat = np.zeros((nm // _abi.ADJ_MATERIAL_PARAMS, _abi.ADJ_MATERIAL_PARAMS), np.float32)
+        g_vol = np.zeros((nv // _abi.ADJ_VOLUME_PARAMS, _abi.ADJ_VOLUME_PARAMS), np.float32)
+        g_tex = np.zeros((nt // 4, 4), np.float32) if texels else None
+        img = np.zeros((h, w, 4), np.float32) if color else None
+        g = _abi.AdjointGrads()
+        g.materials = g_mat.ctypes.data
+        g.volumes = g_vol.ctypes.data if (volumes and nv) else None
+        g.texels = g_tex.ctypes.data if (g_tex is not None and nt) else None
+        g.color = img.ctypes.data if img is not None else None
+        self._check(self.lib.phc_adjoint(self.h, C.addressof(camera), C.addressof(settings),
+                                         int(sample_offset), d.ctypes.data, C.byref(g)))
+        out = {"materials": g_mat, "volumes": g_vol, "adjoint_ms": float(g.adjoint_ms),
+               "longest_sample_cycles": int(g.longest_sample_cycles)}
+        if g_tex is not None:
+            out["texels"] = g_tex
+        if img is not None:
+            out["color"] = img
+        return out
+
     def stats(self) -> dict:
         s = _abi.RenderStats()
         self._check(self.lib.phc_render_stats_get(self.h, C.byref(s)))

@@ -193,7 +193,7 @@ def _displace(v, n, rng, amp):
     return v + n * (amp * d)[:, None]
 
 
-def sun_sky_env(width=1024, height=512, sun_dir=(0.35, 0.55, -0.75), seed=0):
+def sun_sky_env(width=1024, height=512, sun_dir=(0.35, 0.55, -0.75), seed=0, sun_radiance=(4000.0, 3600.0, 3000.0)):
     """Procedural fp32 sun+sky environment (rows from the bottom, +y up)."""
     sd = np.asarray(sun_dir, np.float64)
     sd /= np.linalg.norm(sd)
@@ -215,7 +215,7 @@ def sun_sky_env(width=1024, height=512, sun_dir=(0.35, 0.55, -0.75), seed=0):
     sky = np.where(up[..., None] >= 0, sky, gnd * np.ones_like(sky))
     cosang = np.clip(d @ sd, -1, 1)
     halo = np.exp((cosang - 1) * 40.0)[..., None] * np.array([1.0, 0.9, 0.7]) * 2.0
-    sun = (cosang > np.cos(np.deg2rad(1.5)))[..., None] * np.array([4000.0, 3600.0, 3000.0])
+    sun = (cosang > np.cos(np.deg2rad(1.5)))[..., None] * np.asarray(sun_radiance, np.float64)
     img = (sky + halo + sun).astype(np.float32)
     # texel rows here run v = 0 (theta 0, +y) upward in index; the bridge
     # stores row 0 as given, the map looks texel (y, x) up at v = y / height
@@ -309,6 +309,134 @@ def batched_jobs(seed=0, n=64, min_tris=1_000, max_tris=200_000, min_res=128, ma
         sc.name = f"job{k}"
         jobs.append((sc, cam, st))
     return jobs
+
+
+# ------------------------------------------------------------ differentiable
+
+
+def value_noise(rng, size=512, octaves=(4, 8, 16, 32, 64), channels=4):
+    """(size, size, channels) float32 value noise in [0, 1]: random lattices
+    of the given resolutions, bilinearly upsampled (wrapping), summed with
+    weights halving per octave."""
+    out = np.zeros((size, size, channels), np.float64)
+    total = 0.0
+    for k, res in enumerate(octaves):
+        lat = rng.uniform(0, 1, (res + 1, res + 1, channels))
+        lat[res, :] = lat[0, :]
+        lat[:, res] = lat[:, 0]
+        x = (np.arange(size) + 0.5) * (res / size)
+        i = np.floor(x).astype(np.int64)
+        f = (x - i)[:, None]
+        rows = lat[i] * (1 - f)[..., None] + lat[i + 1] * f[..., None]
+        img = rows[:, i] * (1 - f.T)[..., None] + rows[:, i + 1] * f.T[..., None]
+        w = 0.5 ** k
+        out += w * img
+        total += w
+    return (out / total).astype(np.float32)
+
+
+DIFF_MATERIALS = 8
+DIFF_TEXTURE = 512
+
+
+def differentiable(seed=0, res=256, spp=64, depth=6, texture=DIFF_TEXTURE, target=False):
+    """Differentiable workload: ~50K triangles of displaced icospheres and tori
+    on a ground plane, 8 materials whose base colour is a texture x texture
+    fp32 value-noise image (sampler i for material i, uv in attribute 0) with
+    scalar roughness / metallic / specTrans / sheen / clearcoat, a soft sky
+    environment and a homogeneous box medium (constant transfer function of
+    albedo 0.8, density scale 0.5).  target=True gives the perturbed
+    parameters a reference image is rendered from.  Returns
+    (SceneData, camera, settings)."""
+    rng = np.random.default_rng(seed)
+    mb = _MeshBuilder()
+    uvs = []
+    G = 12.0
+    gv, gf = _quad((-G, 0, -G), (-G, 0, G), (G, 0, G), (G, 0, -G))
+    mb.add(gv, gf, 0, n=np.tile([0, 1, 0], (4, 1)))
+    uvs.append(np.stack([gv[:, 0] / 6.0, gv[:, 2] / 6.0], -1))
+    sv, sf = _icosphere(3)
+    for k in range(40):
+        px, pz = rng.uniform(-8, 8, 2)
+        scale = rng.uniform(0.5, 1.3)
+        if k < 20:
+            n = sv.copy()
+            v = _displace(sv.copy(), n, rng, 0.1) * scale
+            f = sf
+            uv = np.stack([np.arctan2(sv[:, 2], sv[:, 0]) / (2 * np.pi) + 0.5, np.arccos(np.clip(sv[:, 1], -1, 1)) / np.pi],
+                          -1)
+            v[:, 1] += scale * 1.05
+        else:
+            R, r = 1.0, rng.uniform(0.25, 0.4)
+            nu, nv = 36, 17
+            v, n, f = _torus(nu, nv, R, r)
+            v = _displace(v, n, rng, 0.05)
+            ang = rng.uniform(0, np.pi)
+            ca, sa = np.cos(ang), np.sin(ang)
+            v = v @ np.array([[1, 0, 0], [0, ca, -sa], [0, sa, ca]]).T * scale
+            v[:, 1] += (R + r) * scale * abs(sa) + r * scale + 0.02
+            uu, ww = np.meshgrid(np.arange(nu) / nu, np.arange(nv) / nv, indexing="ij")
+            uv = np.stack([uu.reshape(-1) * 2.0, ww.reshape(-1)], -1)
+        v[:, 0] += px
+        v[:, 2] += pz
+        mb.add(v.astype(np.float32), f, k % DIFF_MATERIALS, n=_vertex_normals(v, f).astype(np.float32))
+        uvs.append(uv)
+    sc = mb.build(name="differentiable")
+    attr = np.zeros((sc.positions.shape[0], 4), np.float32)
+    attr[:, :2] = np.concatenate(uvs)
+    attr[:, 3] = 1.0
+    sc.attributes = [attr, None, None, None, None]
+    prng = np.random.default_rng(seed + 7)
+    mats, samplers = [], []
+    for i in range(DIFF_MATERIALS):
+        tint = prng.uniform(0.25, 0.9, 3)
+        tex = value_noise(prng, texture)
+        tex[..., :3] = np.clip(tex[..., :3] * 0.6 + 0.4 * tint, 0, 1)
+        tex[..., 3] = 1.0
+        m = _abi.material_default()
+        m.base_color[:] = (1.0, 1.0, 1.0)
+        m.base_color_src.kind, m.base_color_src.index = 2, i
+        m.roughness = float(prng.uniform(0.3, 0.8))
+        m.metallic = float(prng.uniform(0.05, 0.5))
+        m.transmission = float(prng.uniform(0.05, 0.3)) if i % 4 == 3 else 0.0
+        m.sheen = float(prng.uniform(0.1, 0.6))
+        m.clearcoat = float(prng.uniform(0.1, 0.6))
+        m.specular = 0.5
+        s = _abi.sampler_default()
+        s.type = 1
+        s.in_attribute = 0
+        s.linear = 1
+        s.wrap[:] = (1, 1, 0)
+        s.size[:] = (texture, texture, 1)
+        mats.append(m)
+        samplers.append((s, tex.reshape(-1, 4)))
+    vol = _abi.volume_default()
+    vol.dims[:] = (2, 2, 2)
+    vol.origin[:] = (-6.0, 0.0, -6.0)
+    vol.spacing[:] = (12.0, 3.0, 12.0)
+    vol.value_range[:] = (0.0, 1.0)
+    vol.density_scale = 0.5
+    albedo = np.array([0.8, 0.8, 0.8], np.float32)
+    if target:
+        trng = np.random.default_rng(seed + 99)
+        for m, (s, tex) in zip(mats, samplers):
+            m.roughness = float(np.clip(m.roughness + trng.uniform(-0.15, 0.15), 0.05, 1.0))
+            m.metallic = float(np.clip(m.metallic + trng.uniform(-0.1, 0.1), 0.0, 1.0))
+            m.sheen = float(np.clip(m.sheen + trng.uniform(-0.1, 0.1), 0.0, 1.0))
+            m.clearcoat = float(np.clip(m.clearcoat + trng.uniform(-0.1, 0.1), 0.0, 1.0))
+            if m.transmission > 0:
+                m.transmission = float(np.clip(m.transmission + trng.uniform(-0.05, 0.05), 0.0, 1.0))
+            tex[:, :3] = np.clip(tex[:, :3] * trng.uniform(0.8, 1.2, 3).astype(np.float32), 0, 1)
+        vol.density_scale = 0.5 * float(trng.uniform(0.8, 1.2))
+        albedo = np.clip(albedo * trng.uniform(0.9, 1.1, 3), 0, 1).astype(np.float32)
+    tf = np.array([list(albedo) + [1.0], list(albedo) + [1.0]], np.float32)
+    sc.materials = mats
+    sc.samplers = samplers
+    sc.volumes = [(vol, np.ones(8, np.float32), tf)]
+    sc.env_pixels = sun_sky_env(256, 128, sun_radiance=(0.0, 0.0, 0.0))
+    cam = camera((0.0, 7.0, 17.0), (0.0, 0.8, 0.0), fovy_deg=45.0)
+    st = settings(res, res, spp, depth, adaptive_sampling=0, throughput_clamp=0.0)
+    return sc, cam, st
 
 
 # ------------------------------------------------------------ feature scenes
