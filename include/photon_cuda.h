@@ -306,14 +306,18 @@ typedef struct phc_adjoint_grads {
                        sample (both passes); a pixel sample that runs past
                        2^31 cycles or a ray past 2^20 traversal steps stops
                        the call with PHC_ERR_LIMIT                             */
+  uint64_t replay_mismatches; /* out: pixel samples whose replayed radiance
+                       differed from the forward pass's (0 when the replay
+                       walks every forward path)                               */
 } phc_adjoint_grads;
 /* No counterpart in the reference (it has no derivatives).  Path-replay
    backpropagation: gradients of a loss of the image I that phc_render would
    produce with these camera/settings from settings->pixel_samples samples
    starting at sample index sample_offset (a fresh renderer's first render
    uses sample_offset 0), given d_color = dLoss/dI (width*height RGBA floats
-   in the phc_read_color layout; alpha is ignored).  Each path is traced
-   again from its seed, so the memory does not grow with the depth.  Lobe
+   in the phc_read_color layout; alpha is ignored).  The forward wavefront
+   gives each pixel sample's radiance; each path is then traced again from
+   its seed, so the memory does not grow with the depth.  Lobe
    selection, Russian roulette, MIS weights, clamps and stochastic
    transparency are held constant; visibility (edge) derivatives are not
    computed.  Parameters that come from attributes get no gradient; a base

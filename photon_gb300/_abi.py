@@ -138,6 +138,7 @@ class AdjointGrads(C.Structure):
     _fields_ = [
         ("materials", C.c_void_p), ("volumes", C.c_void_p), ("texels", C.c_void_p),
         ("color", C.c_void_p), ("adjoint_ms", C.c_double), ("longest_sample_cycles", C.c_uint64),
+        ("replay_mismatches", C.c_uint64),
     ]
 
 

@@ -5,10 +5,11 @@
 // extinction scale and albedo of homogeneous volumes.
 //
 // Path replay backpropagation (Vicini, Speierer and Jakob, "Path Replay
-// Backpropagation", SIGGRAPH 2021): one thread per pixel sample re-runs the
-// path from its seed twice.  Pass 1 computes the path's radiance L exactly as
-// the forward renderer (same reference RNG streams, same shading code).
-// Pass 2 replays it, subtracts every contribution from L as it is collected,
+// Backpropagation", SIGGRAPH 2021).  Pass 1 is the wavefront renderer itself,
+// run with one pixel sample per accumulator slot: it leaves the radiance L of
+// every pixel sample.  Pass 2, one thread per pixel sample, re-runs the path
+// from its seed (same reference RNG streams, same shading code, so the same
+// path), subtracts every contribution from L as it is collected,
 // and at every vertex adds  delta . (remaining radiance) * d log f / d theta
 // for the sampled BSDF weight and  delta . C * d log f_nee / d theta  for the
 // next-event contribution C, so memory stays O(1) per path whatever its
@@ -21,9 +22,13 @@
 // scale, for delta tracking and ratio tracking alike; a real scattering event
 // multiplies the path by the albedo.
 //
-// Gradients accumulate per block in shared memory (materials, volumes) and in
-// global memory through warp-aggregated atomics (texels: lanes that hit the
-// same texel combine before one atomic).
+// The primal radiance of every pixel sample comes from the wavefront
+// renderer (one sample per accumulator slot), so each thread only runs the
+// replay.  Material gradients gather in a per-thread cache of the current
+// material, then in block shared memory, then one global atomic per block and
+// parameter; volume gradients in shared memory; texel gradients go straight
+// to global memory with atomics (taps of neighbouring pixels rarely coincide
+// within a warp).
 #include "adjoint.h"
 #include "dual.cuh"
 #include "wave_common.cuh"
@@ -290,41 +295,39 @@ struct Grads {
   float *svol;      // shared: volume_count * 4
   float4 *texels;   // global texel grads
   uint32_t nmat;
+  // per-thread cache of one material's gradient, flushed when another
+  // material comes (consecutive vertices, and NEE + sample of one vertex,
+  // mostly share one): fewer contended shared-memory atomics
+  uint32_t cur;
+  float cache[NP];
 };
 
-// Atomic add in which the lanes of a warp that target the same address
-// combine their values first (one atomic per distinct address).
-__device__ __forceinline__ void warp_agg_add(float *p, float v)
+__device__ __forceinline__ void flush_mat(Grads &g)
 {
-  const uint32_t act = __activemask();
-  const uint32_t grp = __match_any_sync(act, reinterpret_cast<unsigned long long>(p));
-  const uint32_t need = __ballot_sync(act, __popc(grp) > 1);
-  const uint32_t lane = threadIdx.x & 31u;
-  if (!((need >> lane) & 1u)) {
-    atomicAdd(p, v);
+  if (g.cur == 0xffffffffu)
     return;
-  }
-  const uint32_t leader = uint32_t(__ffs(int(grp)) - 1);
-  float s = 0.f;
-  for (uint32_t src = 0; src < 32; ++src) {
-    if (!((need >> src) & 1u))
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    const float v = g.cache[k];
+    g.cache[k] = 0.f;
+    if (v == 0.f || !(v == v))
       continue;
-    const float o = __shfl_sync(need, v, int(src));
-    if (lane == leader && ((grp >> src) & 1u))
-      s += o;
+    if (g.smat)
+      atomicAdd(&g.smat[g.cur * NP + k], v);
+    else
+      atomicAdd(&g.gmat[g.cur * NP + k], v);
   }
-  if (lane == leader)
-    atomicAdd(p, s);
 }
-
-__device__ __forceinline__ void add_mat(Grads &g, uint32_t m, int k, float v)
+__device__ __forceinline__ void add_mat(Grads &g, uint32_t m, const float *gp, uint32_t allowed)
 {
-  if (v == 0.f || !(v == v))
-    return;
-  if (g.smat)
-    atomicAdd(&g.smat[m * NP + k], v);
-  else
-    atomicAdd(&g.gmat[m * NP + k], v);
+  if (m != g.cur) {
+    flush_mat(g);
+    g.cur = m;
+  }
+#pragma unroll
+  for (int k = 0; k < NP; ++k)
+    if ((allowed >> k) & 1u)
+      g.cache[k] += gp[k];
 }
 
 // Base-colour texture taps at a hit: texel indices, weights and the chain
@@ -431,16 +434,19 @@ __device__ __forceinline__ void add_dlog(const D &x, float K, float *gp)
 __device__ void scatter_grads(Grads &g, const DevMaterial &dm, uint32_t mat_id, const Taps &taps, const float *gp)
 {
   const int src_of[NP] = {SRC_BASE, SRC_BASE, SRC_BASE, SRC_ROUGH, SRC_METAL, SRC_TRANS, -1, -1};
+  uint32_t allowed = 0;
+#pragma unroll
   for (int p = 0; p < NP; ++p)
     if (src_of[p] < 0 || dm.src_kind[src_of[p]] == 0)
-      add_mat(g, mat_id, p, gp[p]);
+      allowed |= 1u << p;
+  add_mat(g, mat_id, gp, allowed);
   if (taps.n > 0 && g.texels) {
     for (int t = 0; t < taps.n; ++t) {
       float *tp = reinterpret_cast<float *>(g.texels + taps.idx[t]);
       for (int j = 0; j < 3; ++j) {
         const float v = taps.w[t] * (gp[0] * taps.dbase[0][j] + gp[1] * taps.dbase[1][j] + gp[2] * taps.dbase[2][j]);
-        if (v != 0.f)
-          warp_agg_add(tp + j, v);
+        if (v != 0.f && v == v)
+          atomicAdd(tp + j, v);
       }
     }
   }
@@ -630,8 +636,7 @@ __device__ V3 replay(const RenderConst &rc, const DevScene &sc, uint32_t pixel, 
   auto collect = [&](V3 c) {
     if (ADJ)
       rem = rem - c;
-    else
-      collected = collected + c;
+    collected = collected + c;
   };
   V3 ro, rd;
   float tmin, tmax;
@@ -960,7 +965,16 @@ __global__ void __launch_bounds__(128) k_adjoint(const RenderConst *__restrict__
   for (uint32_t i = threadIdx.x; i < MAX_VOLUMES * 4; i += blockDim.x)
     svol[i] = 0.f;
   __syncthreads();
-  Grads g{shared_mat ? smat : nullptr, a.mat_grads, svol, a.texel_grads, sc.material_count};
+  Grads g;
+  g.smat = shared_mat ? smat : nullptr;
+  g.gmat = a.mat_grads;
+  g.svol = svol;
+  g.texels = a.texel_grads;
+  g.nmat = sc.material_count;
+  g.cur = 0xffffffffu;
+#pragma unroll
+  for (int k = 0; k < NP; ++k)
+    g.cache[k] = 0.f;
   const RenderConst &rc = *rcp;
   const uint64_t total = uint64_t(a.npix) * a.spp;
   unsigned long long longest = 0;
@@ -972,8 +986,8 @@ __global__ void __launch_bounds__(128) k_adjoint(const RenderConst *__restrict__
     const uint32_t pixel = uint32_t(item % a.npix);
     const uint32_t s = uint32_t(item / a.npix);
     const uint32_t sample_index = a.sample_offset + s;
-    const V3 L = replay<false>(rc, sc, pixel, sample_index, V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, g, a.status, t0,
-        a.cycle_budget);
+    const float4 p4 = a.primal[item];
+    const V3 L{p4.x, p4.y, p4.z};
     if (a.radiance) {
       atomicAdd(a.radiance + 3 * pixel, L.x);
       atomicAdd(a.radiance + 3 * pixel + 1, L.y);
@@ -981,11 +995,17 @@ __global__ void __launch_bounds__(128) k_adjoint(const RenderConst *__restrict__
     }
     const float4 dI = a.d_image[pixel];
     const V3 delta{dI.x * a.inv_spp, dI.y * a.inv_spp, dI.z * a.inv_spp};
-    if (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f)
-      replay<true>(rc, sc, pixel, sample_index, L, delta, g, a.status, t0, a.cycle_budget);
+    if (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) {
+      const V3 Lr = replay<true>(rc, sc, pixel, sample_index, L, delta, g, a.status, t0, a.cycle_budget);
+      // the replay must walk the primal path: same radiance up to rounding
+      const float tol = 1e-4f * fmaxf(fabsf(L.x) + fabsf(L.y) + fabsf(L.z), 1e-2f);
+      if (!(fabsf(Lr.x - L.x) + fabsf(Lr.y - L.y) + fabsf(Lr.z - L.z) <= tol))
+        atomicAdd(a.status + 2, 1ull);
+    }
     const unsigned long long dt = static_cast<unsigned long long>(clock64() - t0);
     longest = dt > longest ? dt : longest;
   }
+  flush_mat(g);
   atomicMax(a.status + 1, longest);
   __syncthreads();
   if (shared_mat)

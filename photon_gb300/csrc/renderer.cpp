@@ -104,6 +104,8 @@ struct phc_renderer {
   // graph of one wave
   cudaGraphExec_t graph{nullptr};
   uint64_t graph_key[6]{};
+  // bumped whenever a buffer a recorded wave graph points to is reallocated
+  uint64_t buf_gen{0};
   uint64_t graph_launches{0}; // kernels per replay of the wave graph
   // batched renders led by this renderer: job table, wave schedule, and the
   // job tags of the shadow queue
@@ -226,6 +228,7 @@ void ensure_paths(phc_renderer *r, size_t n)
 {
   if (n <= r->cap_paths)
     return;
+  r->buf_gen++;
   for (int b = 0; b < 2; ++b) {
     ck(r->st_o[b].ensure(n * 16), "alloc path state");
     ck(r->st_d[b].ensure(n * 16), "alloc path state");
@@ -246,6 +249,7 @@ void ensure_slots(phc_renderer *r, size_t n)
 {
   if (n <= r->cap_slots)
     return;
+  r->buf_gen++;
   ck(r->acc.ensure(n * 16), "alloc accumulators");
   ck(r->acc_sq.ensure(n * 16), "alloc accumulators");
   ck(r->acc_start.ensure(n * 16), "alloc accumulators");
@@ -253,6 +257,17 @@ void ensure_slots(phc_renderer *r, size_t n)
   ck(r->aov_n.ensure(n * 16), "alloc accumulators");
   ck(r->aov_a.ensure(n * 16), "alloc accumulators");
   r->cap_slots = n;
+}
+
+// Counters, statistics and constants buffers of the wave kernels.
+void ensure_wave_buffers(phc_renderer *r, int max_iter)
+{
+  const void *before[3] = {r->counters.p, r->stats_buf.p, r->rc_buf.p};
+  ck(r->counters.ensure(wave_counter_alloc_bytes(max_iter)), "alloc counters");
+  ck(r->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
+  ck(r->rc_buf.ensure(sizeof(RenderConst)), "alloc constants");
+  if (before[0] != r->counters.p || before[1] != r->stats_buf.p || before[2] != r->rc_buf.p)
+    r->buf_gen++;
 }
 
 PathSoA path_soa(phc_renderer *r, int b)
@@ -491,7 +506,7 @@ JobPlan prepare_job(phc_renderer *r, const phc_camera &cam, const phc_settings &
   p.waves = (rc.spp + lanes - 1) / lanes;
   p.first = reset || r->samples == 0;
   ensure_slots(r, p.slots);
-  ck(r->rc_buf.ensure(sizeof(RenderConst)), "alloc constants");
+  ensure_wave_buffers(r, p.max_iter);
   ck(cudaMemcpyAsync(r->rc_buf.p, &rc, sizeof(rc), cudaMemcpyHostToDevice, s), "upload constants");
   ck(cudaMemsetAsync(r->acc.p, 0, p.slots * 16, s), "reset accumulators");
   ck(cudaMemsetAsync(r->nsamp.p, 0, p.slots * 4, s), "reset accumulators");
@@ -535,8 +550,7 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
   const bool first = plan.first;
   const Tuning &tu = tuning();
   ensure_paths(r, plan.slots);
-  ck(r->counters.ensure(wave_counter_alloc_bytes(max_iter)), "alloc counters");
-  ck(r->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
+  ensure_wave_buffers(r, max_iter);
   ck(cudaMemsetAsync(r->stats_buf.p, 0, 8 * sizeof(uint64_t), s), "reset stats");
   const WaveCounters wc = wave_counters(r, max_iter);
   ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
@@ -550,7 +564,7 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
   const uint64_t key[6] = {uint64_t(npix) | (uint64_t(lanes) << 32),
       uint64_t(max_iter) | (uint64_t(rc.adaptive) << 32), r->scene_generation,
       uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32),
-      uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16), 0};
+      uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16), r->buf_gen};
   uint64_t launches = 0;
   KernelTimer timer;
   if (tu.time_kernels) {
@@ -762,9 +776,8 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
   upload_vec(lead->b_wave_entry, bp.wave_entry, s, "upload batch waves");
   upload_vec(lead->b_wave_items, bp.wave_items, s, "upload batch waves");
   ensure_paths(lead, bp.max_items);
+  ensure_wave_buffers(lead, bp.max_iter);
   ck(lead->sh_job.ensure(size_t(std::max<uint32_t>(bp.max_items, 1)) * 4), "alloc shadow jobs");
-  ck(lead->counters.ensure(wave_counter_alloc_bytes(bp.max_iter)), "alloc counters");
-  ck(lead->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
   ck(cudaMemsetAsync(lead->stats_buf.p, 0, 8 * sizeof(uint64_t), s), "reset stats");
   const WaveCounters wc = wave_counters(lead, bp.max_iter);
   ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
@@ -852,10 +865,18 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
     throw ApiError(PHC_ERR_LIMIT, "volume gradients for more than PHC_ADJ_MAX_VOLUMES volumes");
   check_device(r);
   cudaStream_t s = r->stream;
-  RenderConst rc = render_const(cam, st, r->adj_bg, s);
-  rc.sample_offset = sample_offset;
-  rc.lanes = 1;
-  const uint32_t npix = rc.npix;
+  const RenderConst base = render_const(cam, st, r->adj_bg, s);
+  const uint32_t npix = base.npix, spp = base.spp;
+  const int max_iter = int(base.max_iter);
+  // pass 1 runs the wavefront over chunks of `chunk` samples, one sample per
+  // accumulator slot (slot = sample-in-chunk * npix + pixel)
+  const Tuning &tu = tuning();
+  const uint64_t per_chunk = std::max<uint64_t>(uint64_t(tu.wave_paths), npix);
+  const uint32_t chunk = uint32_t(std::min<uint64_t>(spp, std::max<uint64_t>(1, per_chunk / npix)));
+  const size_t slots = size_t(chunk) * npix;
+  ensure_slots(r, slots);
+  ensure_paths(r, slots);
+  ensure_wave_buffers(r, max_iter);
   const size_t nmat = size_t(sc.material_count) * ADJ_MATERIAL_PARAMS;
   const size_t nvol = size_t(std::min<uint32_t>(sc.volume_count, ADJ_MAX_VOLUMES)) * ADJ_VOLUME_PARAMS;
   const size_t ntex = g.texels ? size_t(r->scene.texel_count) : 0;
@@ -866,49 +887,69 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
   ck(r->adj_vol.ensure(std::max<size_t>(nvol, 1) * 4), "alloc adjoint");
   if (ntex)
     ck(r->adj_tex.ensure(ntex * 16), "alloc adjoint");
-  ck(r->adj_status.ensure(16), "alloc adjoint");
+  ck(r->adj_status.ensure(32), "alloc adjoint");
   ck(cudaEventRecord(r->ev0, s), "event");
-  ck(cudaMemsetAsync(r->adj_status.p, 0, 16, s), "clear adjoint");
-  ck(cudaMemcpyAsync(r->adj_rc.p, &rc, sizeof(rc), cudaMemcpyHostToDevice, s), "upload constants");
+  ck(cudaMemsetAsync(r->adj_status.p, 0, 32, s), "clear adjoint");
   ck(cudaMemcpyAsync(r->adj_dimg.p, d_color, size_t(npix) * 16, cudaMemcpyHostToDevice, s), "upload loss gradient");
   ck(cudaMemsetAsync(r->adj_rad.p, 0, size_t(npix) * 12, s), "clear adjoint");
   ck(cudaMemsetAsync(r->adj_mat.p, 0, nmat * 4, s), "clear adjoint");
   ck(cudaMemsetAsync(r->adj_vol.p, 0, std::max<size_t>(nvol, 1) * 4, s), "clear adjoint");
   if (ntex)
     ck(cudaMemsetAsync(r->adj_tex.p, 0, ntex * 16, s), "clear adjoint");
-  AdjointArgs a{};
-  a.d_image = r->adj_dimg.as<float4>();
-  a.radiance = g.color ? r->adj_rad.as<float>() : nullptr;
-  a.mat_grads = r->adj_mat.as<float>();
-  a.vol_grads = r->adj_vol.as<float>();
-  a.texel_grads = ntex ? r->adj_tex.as<float4>() : nullptr;
-  a.status = r->adj_status.as<unsigned long long>();
-  a.cycle_budget = 1ull << 31; // about 1 s at the SM clock, per pixel sample
-  a.npix = npix;
-  a.spp = rc.spp;
-  a.sample_offset = sample_offset;
-  a.inv_spp = 1.f / float(rc.spp);
+  const WaveCounters wc = wave_counters(r, max_iter);
+  const LaunchCfg cfg = launch_cfg(r, slots);
   const int blocks = r->sm_count * adjoint_max_active_blocks(128);
-  launch_adjoint(s, blocks, r->adj_rc.as<RenderConst>(), sc, a);
-  ck(cudaGetLastError(), "adjoint kernel");
+  for (uint32_t s0 = 0; s0 < spp; s0 += chunk) {
+    const uint32_t cnt = std::min(chunk, spp - s0);
+    RenderConst rc = base;
+    rc.spp = cnt;
+    rc.lanes = cnt;
+    rc.adaptive = 0;
+    rc.sample_offset = sample_offset + s0;
+    ck(cudaMemcpyAsync(r->adj_rc.p, &rc, sizeof(rc), cudaMemcpyHostToDevice, s), "upload constants");
+    ck(cudaMemsetAsync(r->acc.p, 0, size_t(cnt) * npix * 16, s), "reset accumulators");
+    ck(cudaMemsetAsync(r->nsamp.p, 0, size_t(cnt) * npix * 4, s), "reset accumulators");
+    ck(cudaMemsetAsync(r->aov_a.p, 0, size_t(cnt) * npix * 16, s), "reset accumulators");
+    ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
+    record_wave(r, s, cfg, r->adj_rc.as<RenderConst>(), npix, max_iter, 0, false);
+    AdjointArgs a{};
+    a.primal = r->acc.as<float4>();
+    a.d_image = r->adj_dimg.as<float4>();
+    a.radiance = g.color ? r->adj_rad.as<float>() : nullptr;
+    a.mat_grads = r->adj_mat.as<float>();
+    a.vol_grads = r->adj_vol.as<float>();
+    a.texel_grads = ntex ? r->adj_tex.as<float4>() : nullptr;
+    a.status = r->adj_status.as<unsigned long long>();
+    a.cycle_budget = 1ull << 31; // about 1 s at the SM clock, per pixel sample
+    a.npix = npix;
+    a.spp = cnt;
+    a.sample_offset = sample_offset + s0;
+    a.inv_spp = 1.f / float(spp);
+    launch_adjoint(s, blocks, r->adj_rc.as<RenderConst>(), sc, a);
+    ck(cudaGetLastError(), "adjoint kernel");
+  }
   ck(cudaEventRecord(r->ev1, s), "event");
   ck(cudaMemcpyAsync(g.materials, r->adj_mat.p, nmat * 4, cudaMemcpyDeviceToHost, s), "read gradients");
   if (g.volumes && nvol)
     ck(cudaMemcpyAsync(g.volumes, r->adj_vol.p, nvol * 4, cudaMemcpyDeviceToHost, s), "read gradients");
   if (ntex)
     ck(cudaMemcpyAsync(g.texels, r->adj_tex.p, ntex * 16, cudaMemcpyDeviceToHost, s), "read gradients");
-  unsigned long long status[2] = {0, 0};
-  ck(cudaMemcpyAsync(status, r->adj_status.p, 16, cudaMemcpyDeviceToHost, s), "read status");
+  unsigned long long status[3] = {0, 0, 0};
+  uint32_t err_word = 0;
+  ck(cudaMemcpyAsync(status, r->adj_status.p, 24, cudaMemcpyDeviceToHost, s), "read status");
+  ck(cudaMemcpyAsync(&err_word, wc.error, 4, cudaMemcpyDeviceToHost, s), "read error word");
   std::vector<float> rad;
   if (g.color) {
     rad.resize(size_t(npix) * 3);
     ck(cudaMemcpyAsync(rad.data(), r->adj_rad.p, rad.size() * 4, cudaMemcpyDeviceToHost, s), "read radiance");
   }
   ck(cudaStreamSynchronize(s), "adjoint");
+  check_wave_error(err_word, wc, s);
   float ms = 0.f;
   cudaEventElapsedTime(&ms, r->ev0, r->ev1);
   g.adjoint_ms = ms;
   g.longest_sample_cycles = status[1];
+  g.replay_mismatches = status[2];
   if (status[0] != 0)
     throw ApiError(PHC_ERR_LIMIT, status[0] >= 0x10000ull
             ? "adjoint: a ray exceeded the traversal step limit"
@@ -916,7 +957,7 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
   if (g.color)
     for (size_t p = 0; p < npix; ++p) {
       for (int c = 0; c < 3; ++c)
-        g.color[4 * p + c] = rad[3 * p + c] * a.inv_spp;
+        g.color[4 * p + c] = rad[3 * p + c] / float(spp);
       g.color[4 * p + 3] = 0.f;
     }
 }
