@@ -302,10 +302,6 @@ typedef struct phc_adjoint_grads {
   float *color;     /* width*height*4: the image of the pass's own samples
                        (RGB, alpha 0), or NULL                                */
   double adjoint_ms; /* out: device time of the call                          */
-  uint64_t longest_sample_cycles; /* out: SM clock cycles of the slowest pixel
-                       sample (both passes); a pixel sample that runs past
-                       2^31 cycles or a ray past 2^20 traversal steps stops
-                       the call with PHC_ERR_LIMIT                             */
   uint64_t replay_mismatches; /* out: pixel samples whose replayed radiance
                        differed from the forward pass's (0 when the replay
                        walks every forward path)                               */

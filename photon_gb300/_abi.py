@@ -137,8 +137,7 @@ ADJ_VOLUME_NAMES = ("density_scale", "albedo_r", "albedo_g", "albedo_b")
 class AdjointGrads(C.Structure):
     _fields_ = [
         ("materials", C.c_void_p), ("volumes", C.c_void_p), ("texels", C.c_void_p),
-        ("color", C.c_void_p), ("adjoint_ms", C.c_double), ("longest_sample_cycles", C.c_uint64),
-        ("replay_mismatches", C.c_uint64),
+        ("color", C.c_void_p), ("adjoint_ms", C.c_double), ("replay_mismatches", C.c_uint64),
     ]
 
 

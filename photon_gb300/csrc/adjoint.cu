@@ -5,27 +5,36 @@
 // extinction scale and albedo of homogeneous volumes.
 //
 // Path replay backpropagation (Vicini, Speierer and Jakob, "Path Replay
-// Backpropagation", SIGGRAPH 2021).  Pass 1 is the wavefront renderer itself,
-// run with one pixel sample per accumulator slot: it leaves the radiance L of
-// every pixel sample.  Pass 2, one thread per pixel sample, re-runs the path
+// Backpropagation", SIGGRAPH 2021), on the wavefront.  Pass 1 is the
+// wavefront renderer itself, run with one pixel sample per accumulator slot:
+// it leaves the radiance L of every pixel sample.  Pass 2 replays every path
 // from its seed (same reference RNG streams, same shading code, so the same
-// path), subtracts every contribution from L as it is collected,
-// and at every vertex adds  delta . (remaining radiance) * d log f / d theta
-// for the sampled BSDF weight and  delta . C * d log f_nee / d theta  for the
-// next-event contribution C, so memory stays O(1) per path whatever its
-// depth.  d f / d theta comes from a forward-mode dual-number instantiation of
-// the Disney eval (dual.cuh) over the 8 parameters.  Lobe selection, Russian
-// roulette, MIS weights, clamps and stochastic transparency are detached
-// (held constant); visibility and edge terms are not computed.  Medium: the majorants scale with the density scale, so the
-// derivative of a tracked segment's log weight is the score of its Poisson
-// process of tentative collisions, (collisions - majorant optical depth) /
-// scale, for delta tracking and ratio tracking alike; a real scattering event
-// multiplies the path by the albedo.
+// path) bounce by bounce with the renderer's queues: k_trace, k_adj_shade,
+// k_shadow (deferred) and k_adj_resolve per bounce.  Each path carries the
+// radiance it has yet to collect; every contribution is subtracted as it is
+// collected, and each weight w the path picks up adds
+//   delta . (radiance collected after w) * d log w / d theta,
+// so the memory is one state per path whatever its depth.
 //
-// The primal radiance of every pixel sample comes from the wavefront
-// renderer (one sample per accumulator slot), so each thread only runs the
-// replay.  Material gradients gather in a per-thread cache of the current
-// material, then in block shared memory, then one global atomic per block and
+// The derivative is that of the renderer's own expected image.  The sampled
+// BSDF weight is f / pu with the direction drawn from the sampler's true
+// density pt (pt != pu: see pdf_pair_d), so d log w = d log f - d log pu +
+// d log pt; delta lobes give d log of their weight; the power-heuristic MIS
+// weights contribute 2 (1 - w) d log pu (BSDF side, at the previous vertex)
+// and -2 (1 - w) d log pu (light side); a rough dielectric sample adds the
+// score of its GGX microfacet normal.  Lobe choice and Russian roulette
+// probabilities cancel from the estimator (their weights divide by them).
+// d f / d theta and the pdfs' derivatives come from forward-mode dual numbers
+// (dual.cuh) over the 8 material parameters.  Clamps and stochastic
+// transparency are held constant; visibility (edge) terms are not computed.
+// Medium: the majorants scale with the density scale, so the derivative of a
+// tracked segment's log weight is the score of its Poisson process of
+// tentative collisions, (collisions - majorant optical depth) / scale, for
+// delta and ratio tracking alike; a real scattering event multiplies the path
+// by the albedo.
+//
+// Material gradients gather in a per-thread cache of the current material,
+// then in block shared memory, then one global atomic per block and
 // parameter; volume gradients in shared memory; texel gradients go straight
 // to global memory with atomics (taps of neighbouring pixels rarely coincide
 // within a warp).
@@ -604,361 +613,12 @@ __device__ __forceinline__ void add_vol(Grads &g, const float *dlog, uint32_t nv
       atomicAdd(&g.svol[4 * vi], k * dlog[vi]);
 }
 
-// trace_ray with a step limit: a ray that needs more than
-// ADJ_MAX_TRAVERSAL_STEPS node visits stops and flags the status word.
-template <bool ANY>
-__device__ RayHit trace_capped(const DevScene &sc, V3 o, V3 d, float tmin, float tmax, unsigned long long *status)
+// ---------------------------------------------------------------- grads
+// Per-block gradient accumulators: materials in shared memory (up to
+// MAX_SMEM_MATERIALS, else straight to global), volumes in shared memory;
+// flushed to global memory once per block.
+__device__ __forceinline__ Grads begin_grads(float *smat, float *svol, const DevScene &sc, const AdjointArgs &a)
 {
-  TravState s;
-  trav_init(s, o, d, tmin, tmax);
-  uint2 stack[PHC_STACK_SIZE];
-  uint32_t steps = 0;
-  if (s.g_hits != 0u)
-    while (trav_step<ANY, false>(sc.nodes, sc.tris, s, stack, nullptr))
-      if (++steps >= ADJ_MAX_TRAVERSAL_STEPS) {
-        atomicCAS(status, 0ull, 0x10000ull);
-        break;
-      }
-  return s.best;
-}
-
-// ---------------------------------------------------------------- the path
-// One path of one pixel sample, as the forward renderer traces and shades it
-// (shade_kernels.cu shade_path, wavefront.cu k_shadow), in one thread.
-// ADJ = false: returns the path's radiance.  ADJ = true: L is that radiance;
-// accumulates the gradients for the pixel's loss gradient `delta`.
-template <bool ADJ>
-__device__ V3 replay(const RenderConst &rc, const DevScene &sc, uint32_t pixel, uint32_t sample_index, V3 L,
-    V3 delta, Grads &g, unsigned long long *status, long long t_start, unsigned long long budget)
-{
-  V3 collected{0.f, 0.f, 0.f};
-  V3 rem = L; // ADJ: radiance still to be collected from here on
-  auto collect = [&](V3 c) {
-    if (ADJ)
-      rem = rem - c;
-    collected = collected + c;
-  };
-  V3 ro, rd;
-  float tmin, tmax;
-  camera_ray(rc, pixel, sample_index, ro, rd, tmin, tmax);
-  V3 tp{1.f, 1.f, 1.f};
-  float prev_pdf = -1.f, pdist = 0.f;
-  uint32_t depth = 0, kinds = 0;
-  bool primary = true;
-  const uint32_t max_depth = rc.max_depth;
-  const float eps = sc.eps;
-  const uint32_t nvol = sc.volume_count;
-  // ADJ: the last surface vertex whose non-delta sample set prev_pdf:
-  // d log pu / d theta of that sample, for the MIS weight of the emission
-  // the sampled ray finds
-  bool prev_valid = false;
-  float gprev[NP];
-  uint32_t prev_mat = 0;
-  const DevMaterial *prev_dm = nullptr;
-  Taps prev_taps;
-  prev_taps.n = 0;
-  // d log w_b / d theta = 2 (1 - w_b) d log pu (power heuristic, BSDF side)
-  auto mis_prev = [&](V3 e, float w) {
-    if (!ADJ || !prev_valid || !(w < 1.f))
-      return;
-    const float K = dot(delta, e) * 2.f * (1.f - w);
-    if (K == 0.f)
-      return;
-    float gp[NP];
-#pragma unroll
-    for (int q = 0; q < NP; ++q)
-      gp[q] = K * gprev[q];
-    scatter_grads(g, *prev_dm, prev_mat, prev_taps, gp);
-  };
-  for (uint32_t it = 0; it < rc.max_iter; ++it) {
-    if (static_cast<unsigned long long>(clock64() - t_start) > budget) {
-      atomicCAS(status, 0ull, 1ull + it);
-      break;
-    }
-    const RayHit hit = trace_capped<false>(sc, ro, rd, tmin, tmax, status);
-    const bool is_hit = hit.prim != 0xffffffffu;
-    const bool emission_only = (kinds & EMISSION_ONLY) != 0u;
-    Rng rng = path_rng(pixel, sample_index, 1u + it);
-    if (nvol > 0) { // volume segment (pathtracer.cpp:789-858)
-      V3 albedo{0.f, 0.f, 0.f};
-      float dlog[MAX_VOLUMES] = {0.f, 0.f, 0.f, 0.f};
-      int ev = -1;
-      const float t_end = is_hit ? hit.t : tmax;
-      const float t_sc = vol_scatter_d(sc, ro, rd, tmin, t_end, rng, albedo, dlog, ev);
-      if (ADJ) { // the segment's weight scales everything collected from here on
-        add_vol(g, dlog, nvol, dot(delta, rem));
-        if (t_sc >= 0.f && ev >= 0 && ev < MAX_VOLUMES) { // the scatter weight is the albedo
-          if (albedo.x > 0.f)
-            atomicAdd(&g.svol[4 * ev + 1], delta.x * rem.x / albedo.x);
-          if (albedo.y > 0.f)
-            atomicAdd(&g.svol[4 * ev + 2], delta.y * rem.y / albedo.y);
-          if (albedo.z > 0.f)
-            atomicAdd(&g.svol[4 * ev + 3], delta.z * rem.z / albedo.z);
-        }
-      }
-      if (t_sc >= 0.f) {
-        const V3 p = ro + rd * t_sc;
-        primary = false;
-        if (depth >= max_depth || emission_only)
-          break;
-        const V3 tpa = tp * albedo;
-        const float phase = 0.25f * INV_PI;
-        const DirectSample ds = sample_direct<true>(sc, p, rng);
-        if (ds.valid) {
-          const float w_mis = ds.mis ? power_heuristic(ds.pdf, phase) : 1.f;
-          V3 c = clamp_contrib(tpa * ds.radiance * (phase * w_mis / ds.pdf), int(depth), rc.clamp_direct,
-              rc.clamp_indirect);
-          const float stmax = ds.dist < 1e29f ? ds.dist * (1.f - 1e-4f) : 1e30f;
-          if (trace_capped<true>(sc, p, ds.wi, 0.f, stmax, status).prim == 0xffffffffu) {
-            Rng rs = path_rng(pixel, sample_index, 0x10000u + it);
-            float dlt[MAX_VOLUMES] = {0.f, 0.f, 0.f, 0.f};
-            c = c * vol_transmittance_d(sc, p, ds.wi, 0.f, stmax, rs, dlt);
-            if (finite3(c)) {
-              collect(c);
-              if (ADJ)
-                add_vol(g, dlt, nvol, dot(delta, c));
-            }
-          }
-        }
-        V3 tp_next = tpa;
-        if (depth >= 2) {
-          const float max_tp = fmaxf(tpa.x, fmaxf(tpa.y, tpa.z));
-          const float survive = fminf(fmaxf(max_tp, 0.05f), 0.95f);
-          if (rng.next() >= survive)
-            break;
-          tp_next = tpa * (1.f / survive);
-        }
-        if (count_bounce(kinds, 24u, rc.max_volume))
-          kinds |= EMISSION_ONLY;
-        tp = tp_next;
-        prev_pdf = phase;
-        prev_valid = false;
-        depth += 1;
-        ro = p;
-        rd = uniform_sphere(rng);
-        tmin = 0.f;
-        tmax = 1e30f;
-        continue;
-      }
-    }
-    if (!is_hit) { // miss: background / environment (pathtracer.cpp:860-899)
-      V3 Lm{0.f, 0.f, 0.f};
-      if (primary) {
-        if (sc.has_env && sc.env_visible)
-          Lm = env_eval(sc, rd);
-        else if (rc.bg_image) {
-          const uint32_t x = pixel % rc.w, y = pixel / rc.w;
-          const float4 bg = bg_image(rc, (float(x) + 0.5f) / float(rc.w), (float(y) + 0.5f) / float(rc.h));
-          Lm = V3{bg.x, bg.y, bg.z} * bg.w;
-        } else
-          Lm = rc3(rc.bg) * rc.bg[3];
-      } else {
-        Lm = rc3(rc.ambient);
-        if (sc.has_env) {
-          float w_mis = 1.f;
-          if (prev_pdf > 0.f)
-            w_mis = power_heuristic(prev_pdf, env_pdf(sc, rd) / float(sc.strategy_count));
-          const V3 le = env_eval(sc, rd);
-          Lm = Lm + le * w_mis;
-          mis_prev(tp * le * w_mis, w_mis);
-        }
-      }
-      V3 c = tp * Lm;
-      if (!primary || (sc.has_env && sc.env_visible))
-        c = clamp_contrib(c, int(depth) - 1, rc.clamp_direct, rc.clamp_indirect);
-      collect(c);
-      break;
-    }
-    const HitAttr ha = hit_attributes(sc, ro, rd, hit);
-    const V3 p = ha.p;
-    const V3 wo = -rd;
-    V3 hit_sn = ha.sn;
-    if (!(dot(hit_sn, hit_sn) > 0.25f))
-      hit_sn = ha.n;
-    else if (dot(hit_sn, ha.n) < 0.f)
-      hit_sn = hit_sn * -1.f;
-    Query q;
-    q.prim = hit.prim;
-    q.vidx = ha.vidx;
-    q.b1 = hit.u;
-    q.b2 = hit.v;
-    q.p = p;
-    q.sn = hit_sn;
-    float alpha_val = 1.f;
-    const DevMaterial &dm = sc.materials[ha.material_id];
-    const Mat mat = resolve_material<true>(sc, dm, q, alpha_val);
-    const bool hidden = (mat.flags & MF_HIDDEN) != 0 && primary;
-    if (hidden || (alpha_val < 1.f && rng.next() >= alpha_val)) {
-      const float nd = pdist + hit.t;
-      tmin = eps;
-      tmax = 1e30f;
-      if (primary) {
-        float tn, tf;
-        clip_range(rc, rd, tn, tf);
-        if (tf < 1e30f) {
-          tmax = tf - nd;
-          if (tmax < eps) {
-            tmin = 1.f;
-            tmax = 0.f;
-          }
-        }
-      }
-      pdist = nd;
-      ro = p;
-      prev_pdf = -1.f;
-      prev_valid = false;
-      continue;
-    }
-    V3 n = ha.n, sn = hit_sn;
-    const bool front = dot(n, wo) >= 0.f;
-    if (!(mat.transmission > 0.f) && !front) {
-      n = n * -1.f;
-      sn = sn * -1.f;
-    }
-    if (dm.src_kind[SRC_NORMAL] != 0)
-      sn = apply_normal_map(sc, dm.src_kind[SRC_NORMAL], dm.src_index[SRC_NORMAL], q, sn);
-    primary = false;
-    if (may_emit(dm) && emits_on_side(mat.flags, front)) {
-      float w_mis = 1.f;
-      if (prev_pdf > 0.f && sc.emissive_count > 0) {
-        const float pdf_area = __ldg(sc.prim_light_pdf + hit.prim);
-        const float cos_light = fabsf(dot(ha.n, wo));
-        if (pdf_area > 0.f && cos_light > 0.f)
-          w_mis = power_heuristic(prev_pdf, pdf_area * hit.t * hit.t / cos_light / float(sc.strategy_count));
-      }
-      const V3 e = clamp_contrib(tp * mat_emission(mat) * w_mis, int(depth) - 1, rc.clamp_direct, rc.clamp_indirect);
-      collect(e);
-      mis_prev(e, w_mis);
-    }
-    if ((mat.flags & MF_EMITTER_ONLY) != 0 || depth >= max_depth || emission_only)
-      break;
-    MatD md;
-    Taps taps;
-    if (ADJ) {
-      md = make_matd(mat);
-      taps = base_color_taps(sc, dm, q);
-    }
-    { // next event estimation
-      const DirectSample ds = sample_direct<true>(sc, p, rng);
-      if (ds.valid) {
-        const V3 f = bsdf_eval(mat, wo, ds.wi, n, sn);
-        if (f.x > 0.f || f.y > 0.f || f.z > 0.f) {
-          float w_mis = 1.f;
-          if (ds.mis)
-            w_mis = power_heuristic(ds.pdf, bsdf_pdf(mat, wo, ds.wi, n, sn));
-          V3 c = clamp_contrib(tp * f * ds.radiance * (w_mis / ds.pdf), int(depth), rc.clamp_direct,
-              rc.clamp_indirect);
-          const V3 so = p + n * eps;
-          V3 sd;
-          float stmax;
-          if (ds.dist < 1e29f) {
-            const V3 to_light = p + ds.wi * ds.dist - so;
-            const float sdist = length(to_light);
-            sd = sdist > 0.f ? to_light * (1.f / sdist) : ds.wi;
-            stmax = sdist * (1.f - 1e-3f);
-          } else {
-            sd = ds.wi;
-            stmax = 1e30f;
-          }
-          if (trace_capped<true>(sc, so, sd, 0.f, stmax, status).prim == 0xffffffffu) {
-            float dlt[MAX_VOLUMES] = {0.f, 0.f, 0.f, 0.f};
-            if (nvol > 0) {
-              Rng rs = path_rng(pixel, sample_index, 0x10000u + it);
-              c = c * vol_transmittance_d(sc, so, sd, 0.f, stmax, rs, dlt);
-            }
-            if (finite3(c)) {
-              collect(c);
-              if (ADJ) {
-                float gp[NP];
-#pragma unroll
-                for (int q = 0; q < NP; ++q)
-                  gp[q] = 0.f;
-                add_dlog3(bsdf_eval_d(md, wo, ds.wi, n, sn), delta * c, gp);
-                if (ds.mis && w_mis < 1.f) { // d log w_nee = -2 (1 - w_nee) d log pu
-                  D pu, pt;
-                  pdf_pair_d(md, wo, ds.wi, n, sn, pu, pt);
-                  add_dlog(pu, -2.f * (1.f - w_mis) * dot(delta, c), gp);
-                }
-                scatter_grads(g, dm, ha.material_id, taps, gp);
-                add_vol(g, dlt, nvol, dot(delta, c));
-              }
-            }
-          }
-        }
-      }
-    }
-    const BSample bs = bsdf_sample(mat, wo, n, sn, rng);
-    if (bs.pdf <= 0.f || (bs.f.x <= 0.f && bs.f.y <= 0.f && bs.f.z <= 0.f))
-      break;
-    if (ADJ) { // everything still to come passes through this vertex's weight
-      const V3 k = delta * rem;
-      const float K = k.x + k.y + k.z;
-      float gp[NP];
-#pragma unroll
-      for (int q = 0; q < NP; ++q)
-        gp[q] = 0.f;
-      prev_valid = false;
-      if (bs.lobe == LOBE_DIFFUSE || bs.lobe == LOBE_GLOSSY || bs.lobe == LOBE_COAT) {
-        // weight f / pu of a direction drawn from pt
-        D pu, pt;
-        pdf_pair_d(md, wo, bs.wi, n, sn, pu, pt);
-        add_dlog3(bsdf_eval_d(md, wo, bs.wi, n, sn), k, gp);
-        add_dlog(pt, K, gp);
-        add_dlog(pu, -K, gp);
-        if (pu.v > 0.f) {
-          prev_valid = true;
-#pragma unroll
-          for (int q = 0; q < NP; ++q)
-            gprev[q] = pu.d[q] / pu.v;
-          prev_mat = ha.material_id;
-          prev_dm = &dm;
-          prev_taps = taps;
-        }
-      } else {
-        add_dlog3(delta_weight_d(md, bs.lobe, wo, n, sn), k, gp);
-        if (bs.noh > 0.f) // the microfacet normal's density D(h) cos (ggx_half)
-          add_dlog(D_ggx_d(bs.noh, dmax(md.rough, 0.001f)), K, gp);
-      }
-      scatter_grads(g, dm, ha.material_id, taps, gp);
-    }
-    V3 tpn = tp * (bs.f * (1.f / bs.pdf));
-    if (depth >= 2) {
-      const float max_tp = fmaxf(tpn.x, fmaxf(tpn.y, tpn.z));
-      const float survive = fminf(fmaxf(max_tp, 0.05f), 0.95f);
-      if (rng.next() >= survive)
-        break;
-      tpn = tpn * (1.f / survive);
-    }
-    if (rc.tp_clamp > 0.f) {
-      const float mx = fmaxf(tpn.x, fmaxf(tpn.y, tpn.z));
-      if (mx > rc.tp_clamp)
-        tpn = tpn * (rc.tp_clamp / mx);
-    }
-    if (!finite3(tpn))
-      break;
-    tp = tpn;
-    prev_pdf = bs.spec ? -1.f : bs.pdf;
-    depth += 1;
-    const V3 wi = normalize(bs.wi);
-    const float side = dot(wi, ha.n) < 0.f ? -1.f : 1.f;
-    const bool through = (dot(wi, ha.n) < 0.f) != (dot(wo, ha.n) < 0.f);
-    const bool exceeded = through ? count_bounce(kinds, 16u, rc.max_transmission)
-                                  : (bs.diff ? count_bounce(kinds, 0u, rc.max_diffuse)
-                                             : count_bounce(kinds, 8u, rc.max_glossy));
-    if (exceeded)
-      kinds |= EMISSION_ONLY;
-    ro = p + ha.n * (side * eps);
-    rd = wi;
-    tmin = 0.f;
-    tmax = 1e30f;
-  }
-  return collected;
-}
-
-__global__ void __launch_bounds__(128) k_adjoint(const RenderConst *__restrict__ rcp, DevScene sc, AdjointArgs a)
-{
-  __shared__ float smat[MAX_SMEM_MATERIALS * NP];
-  __shared__ float svol[MAX_VOLUMES * 4];
   const bool shared_mat = sc.material_count <= uint32_t(MAX_SMEM_MATERIALS);
   for (uint32_t i = threadIdx.x; i < MAX_SMEM_MATERIALS * NP; i += blockDim.x)
     smat[i] = 0.f;
@@ -975,59 +635,563 @@ __global__ void __launch_bounds__(128) k_adjoint(const RenderConst *__restrict__
 #pragma unroll
   for (int k = 0; k < NP; ++k)
     g.cache[k] = 0.f;
+  return g;
+}
+__device__ __forceinline__ void end_grads(Grads &g, const DevScene &sc, const AdjointArgs &a)
+{
+  flush_mat(g);
+  __syncthreads();
+  if (g.smat)
+    for (uint32_t i = threadIdx.x; i < sc.material_count * NP; i += blockDim.x)
+      if (g.smat[i] != 0.f)
+        atomicAdd(&a.mat_grads[i], g.smat[i]);
+  for (uint32_t i = threadIdx.x; i < MAX_VOLUMES * 4 && i < sc.volume_count * 4; i += blockDim.x)
+    if (g.svol[i] != 0.f)
+      atomicAdd(&a.vol_grads[i], g.svol[i]);
+}
+
+__device__ __forceinline__ void put_vtx(const VtxSoA &v, uint32_t i, const Query &q, uint32_t mat)
+{
+  v.q[i] = make_uint4(q.prim, __float_as_uint(q.b1), __float_as_uint(q.b2), mat | ADJ_VTX_VALID);
+  v.p[i] = f4(q.p, 0.f);
+  v.sn[i] = f4(q.sn, 0.f);
+}
+// The material and base-colour taps of a stored vertex; false: none stored.
+__device__ bool get_vtx(const DevScene &sc, const VtxSoA &v, uint32_t i, uint32_t &mat, Taps &taps)
+{
+  const uint4 q4 = v.q[i];
+  if (!(q4.w & ADJ_VTX_VALID))
+    return false;
+  mat = q4.w & ~ADJ_VTX_VALID;
+  Query q;
+  q.prim = q4.x;
+  q.vidx = __ldg(sc.prim_vidx + q4.x);
+  q.b1 = __uint_as_float(q4.y);
+  q.b2 = __uint_as_float(q4.z);
+  q.p = v3(v.p[i]);
+  q.sn = v3(v.sn[i]);
+  taps = base_color_taps(sc, sc.materials[mat], q);
+  return true;
+}
+
+// d log w / d theta of the power-heuristic weight w that the previous
+// surface sample's pdf pu entered (BSDF side): 2 (1 - w) d log pu, applied
+// to the emission e that the weight multiplied, at the previous vertex.
+__device__ void mis_prev(Grads &g, const DevScene &sc, const AdjPathSoA &in, uint32_t i, V3 delta, V3 e, float w)
+{
+  if (!(w < 1.f))
+    return;
+  const float K = dot(delta, e) * 2.f * (1.f - w);
+  if (K == 0.f)
+    return;
+  uint32_t mat;
+  Taps taps;
+  if (!get_vtx(sc, in.v, i, mat, taps))
+    return;
+  const float4 a = in.g0[i], b = in.g1[i];
+  const float gp[NP] = {K * a.x, K * a.y, K * a.z, K * a.w, K * b.x, K * b.y, K * b.z, K * b.w};
+  scatter_grads(g, sc.materials[mat], mat, taps, gp);
+}
+
+// What one replayed path hands on: its continuation and its shadow ray.
+struct AdjNext {
+  float4 o, d, tp;
+  uint4 info;
+  float pdist;
+  float4 rem, g0, g1;
+  bool has_vtx;
+  Query vq;
+  uint32_t vmat;
+};
+struct AdjShadow {
+  float4 a, b, c, g0, g1;
+  bool has_vtx;
+};
+
+// One bounce of one replayed path: shade_path (shade_kernels.cu) with the
+// derivative bookkeeping of the path-replay adjoint.  Contributions known now
+// (emission, environment) are collected here; the NEE contribution waits for
+// its shadow ray (k_adj_resolve), so the BSDF sample's gradient is taken with
+// the remainder before NEE and the shadow ray carries the correction.
+__device__ __forceinline__ void adj_shade_path(const RenderConst &rc, const DevScene &sc, const AdjPathSoA &in,
+    uint32_t i, float4 hit, int it, const AdjointArgs &a, Grads &g, bool &cont, AdjNext &nx, bool &has_sh,
+    AdjShadow &sh)
+{
+  cont = false;
+  has_sh = false;
+  const float4 ro4 = in.p.ray_o[i], rd4 = in.p.ray_d[i], tp4 = in.p.tp[i];
+  const uint4 info = in.p.info[i];
+  const float pdist = in.p.pdist[i];
+  const uint32_t slot = info.x, sample_index = info.y;
+  const uint32_t pixel = slot % rc.npix;
+  uint32_t kinds = info.z;
+  const uint32_t depth = info.w & 0xffffu;
+  bool primary = (info.w >> 16) & 1u;
+  const bool prev_valid = (info.w & ADJ_PREV_VALID) != 0u;
+  const bool emission_only = (kinds & EMISSION_ONLY) != 0u;
+  const V3 ray_org = v3(ro4), ray_dir = v3(rd4);
+  V3 tp = v3(tp4);
+  const float prev_pdf = tp4.w;
+  const uint32_t max_depth = rc.max_depth;
+  const float eps = sc.eps;
+  const uint32_t nvol = sc.volume_count;
+  const uint32_t prim = __float_as_uint(hit.y);
+  const bool is_hit = prim != 0xffffffffu;
+  V3 rem = it == 0 ? v3(a.primal[slot]) : v3(in.rem[i]);
+  const float4 dI = a.d_image[pixel];
+  const V3 delta{dI.x * a.inv_spp, dI.y * a.inv_spp, dI.z * a.inv_spp};
+  float4 col = a.collected[slot];
+  auto collect = [&](V3 c) {
+    rem = rem - c;
+    col.x = col.x + c.x;
+    col.y = col.y + c.y;
+    col.z = col.z + c.z;
+  };
+  auto done = [&]() { a.collected[slot] = col; };
+  Rng rng = path_rng(pixel, sample_index, 1u + uint32_t(it));
+
+  if (nvol > 0) { // volume segment (pathtracer.cpp:789-858)
+    V3 albedo{0.f, 0.f, 0.f};
+    float dlog[MAX_VOLUMES] = {0.f, 0.f, 0.f, 0.f};
+    int ev = -1;
+    const float t_end = is_hit ? hit.x : rd4.w;
+    const float t_sc = vol_scatter_d(sc, ray_org, ray_dir, ro4.w, t_end, rng, albedo, dlog, ev);
+    add_vol(g, dlog, nvol, dot(delta, rem)); // the segment scales everything collected from here on
+    if (t_sc >= 0.f && ev >= 0 && ev < MAX_VOLUMES) { // the scatter weight is the albedo
+      if (albedo.x > 0.f)
+        atomicAdd(&g.svol[4 * ev + 1], delta.x * rem.x / albedo.x);
+      if (albedo.y > 0.f)
+        atomicAdd(&g.svol[4 * ev + 2], delta.y * rem.y / albedo.y);
+      if (albedo.z > 0.f)
+        atomicAdd(&g.svol[4 * ev + 3], delta.z * rem.z / albedo.z);
+    }
+    if (t_sc >= 0.f) {
+      const V3 p = ray_org + ray_dir * t_sc;
+      primary = false;
+      if (depth >= max_depth || emission_only) {
+        done();
+        return;
+      }
+      const V3 tpa = tp * albedo;
+      const float phase = 0.25f * INV_PI;
+      const DirectSample ds = sample_direct<true>(sc, p, rng);
+      if (ds.valid) {
+        const float w_mis = ds.mis ? power_heuristic(ds.pdf, phase) : 1.f;
+        const V3 c = clamp_contrib(tpa * ds.radiance * (phase * w_mis / ds.pdf), int(depth), rc.clamp_direct,
+            rc.clamp_indirect);
+        const float stmax = ds.dist < 1e29f ? ds.dist * (1.f - 1e-4f) : 1e30f;
+        has_sh = true;
+        sh.a = f4(p, stmax);
+        sh.b = f4(ds.wi, c.x);
+        sh.c = make_float4(c.y, c.z, __uint_as_float(slot), __uint_as_float(sample_index));
+        sh.g0 = make_float4(0.f, 0.f, 0.f, 0.f);
+        sh.g1 = sh.g0;
+        sh.has_vtx = false;
+      }
+      V3 tp_next = tpa;
+      if (depth >= 2) {
+        const float max_tp = fmaxf(tpa.x, fmaxf(tpa.y, tpa.z));
+        const float survive = fminf(fmaxf(max_tp, 0.05f), 0.95f);
+        if (rng.next() >= survive) {
+          done();
+          return;
+        }
+        tp_next = tpa * (1.f / survive);
+      }
+      if (count_bounce(kinds, 24u, rc.max_volume))
+        kinds |= EMISSION_ONLY;
+      const V3 nd = uniform_sphere(rng);
+      cont = true;
+      nx.o = f4(p, 0.f);
+      nx.d = f4(nd, 1e30f);
+      nx.tp = f4(tp_next, phase);
+      nx.info = make_uint4(slot, sample_index, kinds, depth + 1u);
+      nx.pdist = pdist;
+      nx.rem = f4(rem, 0.f);
+      nx.has_vtx = false;
+      done();
+      return;
+    }
+  }
+
+  if (!is_hit) { // miss (pathtracer.cpp:860-899)
+    V3 Lm{0.f, 0.f, 0.f};
+    if (primary) {
+      if (sc.has_env && sc.env_visible)
+        Lm = env_eval(sc, ray_dir);
+      else if (rc.bg_image) {
+        const uint32_t x = pixel % rc.w, y = pixel / rc.w;
+        const float4 bg = bg_image(rc, (float(x) + 0.5f) / float(rc.w), (float(y) + 0.5f) / float(rc.h));
+        Lm = V3{bg.x, bg.y, bg.z} * bg.w;
+      } else
+        Lm = rc3(rc.bg) * rc.bg[3];
+    } else {
+      Lm = rc3(rc.ambient);
+      if (sc.has_env) {
+        float w_mis = 1.f;
+        if (prev_pdf > 0.f)
+          w_mis = power_heuristic(prev_pdf, env_pdf(sc, ray_dir) / float(sc.strategy_count));
+        const V3 le = env_eval(sc, ray_dir);
+        Lm = Lm + le * w_mis;
+        if (prev_valid)
+          mis_prev(g, sc, in, i, delta, tp * le * w_mis, w_mis);
+      }
+    }
+    V3 c = tp * Lm;
+    if (!primary || (sc.has_env && sc.env_visible))
+      c = clamp_contrib(c, int(depth) - 1, rc.clamp_direct, rc.clamp_indirect);
+    collect(c);
+    done();
+    return;
+  }
+
+  const RayHit rh{hit.x, prim, hit.z, hit.w};
+  const HitAttr ha = hit_attributes(sc, ray_org, ray_dir, rh);
+  const V3 p = ha.p;
+  const V3 wo = -ray_dir;
+  V3 hit_sn = ha.sn;
+  if (!(dot(hit_sn, hit_sn) > 0.25f))
+    hit_sn = ha.n;
+  else if (dot(hit_sn, ha.n) < 0.f)
+    hit_sn = hit_sn * -1.f;
+  Query q;
+  q.prim = prim;
+  q.vidx = ha.vidx;
+  q.b1 = rh.u;
+  q.b2 = rh.v;
+  q.p = p;
+  q.sn = hit_sn;
+  float alpha_val = 1.f;
+  const DevMaterial &dm = sc.materials[ha.material_id];
+  const Mat mat = resolve_material<true>(sc, dm, q, alpha_val);
+  const bool hidden = (mat.flags & MF_HIDDEN) != 0 && primary;
+  if (hidden || (alpha_val < 1.f && rng.next() >= alpha_val)) { // stochastic transparency
+    float tmin = eps, tmax = 1e30f;
+    const float nd = pdist + rh.t;
+    if (primary) {
+      float tn, tf;
+      clip_range(rc, ray_dir, tn, tf);
+      if (tf < 1e30f) {
+        tmax = tf - nd;
+        if (tmax < eps) {
+          tmin = 1.f;
+          tmax = 0.f;
+        }
+      }
+    }
+    cont = true;
+    nx.o = f4(p, tmin);
+    nx.d = f4(ray_dir, tmax);
+    nx.tp = f4(tp, -1.f);
+    nx.info = make_uint4(slot, sample_index, kinds, depth | (primary ? 1u << 16 : 0u));
+    nx.pdist = nd;
+    nx.rem = f4(rem, 0.f);
+    nx.has_vtx = false;
+    done();
+    return;
+  }
+  V3 n = ha.n, sn = hit_sn;
+  const bool front = dot(n, wo) >= 0.f;
+  if (!(mat.transmission > 0.f) && !front) {
+    n = n * -1.f;
+    sn = sn * -1.f;
+  }
+  if (dm.src_kind[SRC_NORMAL] != 0)
+    sn = apply_normal_map(sc, dm.src_kind[SRC_NORMAL], dm.src_index[SRC_NORMAL], q, sn);
+  primary = false;
+  if (may_emit(dm) && emits_on_side(mat.flags, front)) {
+    float w_mis = 1.f;
+    if (prev_pdf > 0.f && sc.emissive_count > 0) {
+      const float pdf_area = __ldg(sc.prim_light_pdf + prim);
+      const float cos_light = fabsf(dot(ha.n, wo));
+      if (pdf_area > 0.f && cos_light > 0.f)
+        w_mis = power_heuristic(prev_pdf, pdf_area * rh.t * rh.t / cos_light / float(sc.strategy_count));
+    }
+    const V3 e = clamp_contrib(tp * mat_emission(mat) * w_mis, int(depth) - 1, rc.clamp_direct, rc.clamp_indirect);
+    collect(e);
+    if (prev_valid)
+      mis_prev(g, sc, in, i, delta, e, w_mis);
+  }
+  if ((mat.flags & MF_EMITTER_ONLY) != 0 || depth >= max_depth || emission_only) {
+    done();
+    return;
+  }
+  const MatD md = make_matd(mat);
+  const Taps taps = base_color_taps(sc, dm, q);
+  float gnee[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k)
+    gnee[k] = 0.f;
+  V3 cnee{0.f, 0.f, 0.f};
+  { // next event estimation: the shadow ray and its gradient per unit transmittance
+    const DirectSample ds = sample_direct<true>(sc, p, rng);
+    if (ds.valid) {
+      const V3 f = bsdf_eval(mat, wo, ds.wi, n, sn);
+      if (f.x > 0.f || f.y > 0.f || f.z > 0.f) {
+        float w_mis = 1.f;
+        if (ds.mis)
+          w_mis = power_heuristic(ds.pdf, bsdf_pdf(mat, wo, ds.wi, n, sn));
+        const V3 c = clamp_contrib(tp * f * ds.radiance * (w_mis / ds.pdf), int(depth), rc.clamp_direct,
+            rc.clamp_indirect);
+        const V3 so = p + n * eps;
+        V3 sd;
+        float stmax;
+        if (ds.dist < 1e29f) {
+          const V3 to_light = p + ds.wi * ds.dist - so;
+          const float sdist = length(to_light);
+          sd = sdist > 0.f ? to_light * (1.f / sdist) : ds.wi;
+          stmax = sdist * (1.f - 1e-3f);
+        } else {
+          sd = ds.wi;
+          stmax = 1e30f;
+        }
+        has_sh = true;
+        sh.a = f4(so, stmax);
+        sh.b = f4(sd, c.x);
+        sh.c = make_float4(c.y, c.z, __uint_as_float(slot), __uint_as_float(sample_index));
+        sh.has_vtx = true;
+        cnee = c;
+        add_dlog3(bsdf_eval_d(md, wo, ds.wi, n, sn), delta * c, gnee);
+        if (ds.mis && w_mis < 1.f) { // d log w_nee = -2 (1 - w_nee) d log pu
+          D pu, pt;
+          pdf_pair_d(md, wo, ds.wi, n, sn, pu, pt);
+          add_dlog(pu, -2.f * (1.f - w_mis) * dot(delta, c), gnee);
+        }
+      }
+    }
+  }
+  const BSample bs = bsdf_sample(mat, wo, n, sn, rng);
+  const bool sampled = !(bs.pdf <= 0.f || (bs.f.x <= 0.f && bs.f.y <= 0.f && bs.f.z <= 0.f));
+  float grem[NP], gc[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    grem[k] = 0.f;
+    gc[k] = 0.f;
+  }
+  bool prev_next = false;
+  float gpu[NP];
+  if (sampled) { // everything still to come passes through this sample's weight
+    const V3 krem = delta * rem, kc = delta * cnee;
+    const float Krem = krem.x + krem.y + krem.z, Kc = kc.x + kc.y + kc.z;
+    if (bs.lobe == LOBE_DIFFUSE || bs.lobe == LOBE_GLOSSY || bs.lobe == LOBE_COAT) {
+      D pu, pt; // weight f / pu of a direction drawn from pt
+      pdf_pair_d(md, wo, bs.wi, n, sn, pu, pt);
+      const D3 fd = bsdf_eval_d(md, wo, bs.wi, n, sn);
+      add_dlog3(fd, krem, grem);
+      add_dlog(pt, Krem, grem);
+      add_dlog(pu, -Krem, grem);
+      add_dlog3(fd, kc, gc);
+      add_dlog(pt, Kc, gc);
+      add_dlog(pu, -Kc, gc);
+      if (pu.v > 0.f) {
+        prev_next = true;
+#pragma unroll
+        for (int k = 0; k < NP; ++k)
+          gpu[k] = pu.d[k] / pu.v;
+      }
+    } else {
+      const D3 wd = delta_weight_d(md, bs.lobe, wo, n, sn);
+      add_dlog3(wd, krem, grem);
+      add_dlog3(wd, kc, gc);
+      if (bs.noh > 0.f) { // the microfacet normal's density D(h) cos (ggx_half)
+        const D dh = D_ggx_d(bs.noh, dmax(md.rough, 0.001f));
+        add_dlog(dh, Krem, grem);
+        add_dlog(dh, Kc, gc);
+      }
+    }
+    scatter_grads(g, dm, ha.material_id, taps, grem);
+  }
+  if (has_sh) { // per unit transmittance: the NEE gradient minus the part the sample's term took
+    sh.g0 = make_float4(gnee[0] - gc[0], gnee[1] - gc[1], gnee[2] - gc[2], gnee[3] - gc[3]);
+    sh.g1 = make_float4(gnee[4] - gc[4], gnee[5] - gc[5], gnee[6] - gc[6], gnee[7] - gc[7]);
+  }
+  nx.vq = q;
+  nx.vmat = ha.material_id;
+  done();
+  if (!sampled)
+    return;
+  V3 tpn = tp * (bs.f * (1.f / bs.pdf));
+  if (depth >= 2) {
+    const float max_tp = fmaxf(tpn.x, fmaxf(tpn.y, tpn.z));
+    const float survive = fminf(fmaxf(max_tp, 0.05f), 0.95f);
+    if (rng.next() >= survive)
+      return;
+    tpn = tpn * (1.f / survive);
+  }
+  if (rc.tp_clamp > 0.f) {
+    const float mx = fmaxf(tpn.x, fmaxf(tpn.y, tpn.z));
+    if (mx > rc.tp_clamp)
+      tpn = tpn * (rc.tp_clamp / mx);
+  }
+  if (!finite3(tpn))
+    return;
+  const V3 wi = normalize(bs.wi);
+  const float side = dot(wi, ha.n) < 0.f ? -1.f : 1.f;
+  const bool through = (dot(wi, ha.n) < 0.f) != (dot(wo, ha.n) < 0.f);
+  const bool exceeded = through ? count_bounce(kinds, 16u, rc.max_transmission)
+                                : (bs.diff ? count_bounce(kinds, 0u, rc.max_diffuse)
+                                           : count_bounce(kinds, 8u, rc.max_glossy));
+  if (exceeded)
+    kinds |= EMISSION_ONLY;
+  cont = true;
+  nx.o = f4(p + ha.n * (side * eps), 0.f);
+  nx.d = f4(wi, 1e30f);
+  nx.tp = f4(tpn, bs.spec ? -1.f : bs.pdf);
+  nx.info = make_uint4(slot, sample_index, kinds, (depth + 1u) | (prev_next && !bs.spec ? ADJ_PREV_VALID : 0u));
+  nx.pdist = pdist;
+  nx.rem = f4(rem, 0.f);
+  nx.has_vtx = prev_next && !bs.spec;
+  if (nx.has_vtx) {
+    nx.g0 = make_float4(gpu[0], gpu[1], gpu[2], gpu[3]);
+    nx.g1 = make_float4(gpu[4], gpu[5], gpu[6], gpu[7]);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_adj_shade(const RenderConst *__restrict__ rcp, DevScene sc, AdjPathSoA in,
+    AdjPathSoA out, const float4 *__restrict__ hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a)
+{
+  __shared__ float smat[MAX_SMEM_MATERIALS * NP];
+  __shared__ float svol[MAX_VOLUMES * 4];
+  Grads g = begin_grads(smat, svol, sc, a);
   const RenderConst &rc = *rcp;
-  const uint64_t total = uint64_t(a.npix) * a.spp;
-  unsigned long long longest = 0;
-  for (uint64_t item = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; item < total;
-       item += uint64_t(gridDim.x) * blockDim.x) {
-    if (*reinterpret_cast<volatile unsigned long long *>(a.status) != 0ull)
+  const uint32_t n = wc.count[it];
+  uint32_t *fetch = wc.fetch + 4 * it + 1;
+  for (;;) {
+    const uint32_t base = warp_fetch(fetch);
+    if (base >= n)
       break;
-    const long long t0 = clock64();
-    const uint32_t pixel = uint32_t(item % a.npix);
-    const uint32_t s = uint32_t(item / a.npix);
-    const uint32_t sample_index = a.sample_offset + s;
-    const float4 p4 = a.primal[item];
-    const V3 L{p4.x, p4.y, p4.z};
+    const uint32_t j = base + lane_id();
+    bool cont = false, has_sh = false;
+    AdjNext nx;
+    AdjShadow sr;
+    if (j < n)
+      adj_shade_path(rc, sc, in, j, hits[j], it, a, g, cont, nx, has_sh, sr);
+    const uint32_t o = warp_append(wc.count + it + 1, cont);
+    if (cont) {
+      out.p.ray_o[o] = nx.o;
+      out.p.ray_d[o] = nx.d;
+      out.p.tp[o] = nx.tp;
+      out.p.info[o] = nx.info;
+      out.p.pdist[o] = nx.pdist;
+      out.rem[o] = nx.rem;
+      if (nx.has_vtx) {
+        out.g0[o] = nx.g0;
+        out.g1[o] = nx.g1;
+        put_vtx(out.v, o, nx.vq, nx.vmat);
+      }
+    }
+    const uint32_t so = warp_append(wc.scount + it, has_sh);
+    if (has_sh) {
+      sh.s.a[so] = sr.a;
+      sh.s.b[so] = sr.b;
+      sh.s.c[so] = sr.c;
+      sh.next[so] = cont ? o : ADJ_NO_NEXT;
+      sh.g0[so] = sr.g0;
+      sh.g1[so] = sr.g1;
+      if (sr.has_vtx)
+        put_vtx(sh.v, so, nx.vq, nx.vmat);
+      else
+        sh.v.q[so] = make_uint4(0u, 0u, 0u, 0u);
+    }
+  }
+  end_grads(g, sc, a);
+}
+
+// The shadow rays of one bounce after k_shadow (deferred mode): for each
+// unoccluded one the transmittance (with its derivative), the contribution
+// collected, the continued path's remainder reduced, the vertex's gradient.
+__global__ void __launch_bounds__(128) k_adj_resolve(const RenderConst *__restrict__ rcp, DevScene sc,
+    AdjShadowSoA sh, AdjPathSoA next, WaveCounters wc, int it, AdjointArgs a)
+{
+  __shared__ float smat[MAX_SMEM_MATERIALS * NP];
+  __shared__ float svol[MAX_VOLUMES * 4];
+  Grads g = begin_grads(smat, svol, sc, a);
+  const uint32_t n = wc.scount[it];
+  const uint32_t npix = rcp->npix;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 s4 = sh.s.a[i];
+    if (!(s4.w >= 0.f))
+      continue;
+    const float4 b4 = sh.s.b[i], c4 = sh.s.c[i];
+    const uint32_t slot = __float_as_uint(c4.z), sample_index = __float_as_uint(c4.w);
+    const uint32_t pixel = slot % npix;
+    float T = 1.f;
+    float dlt[MAX_VOLUMES] = {0.f, 0.f, 0.f, 0.f};
+    if (sc.volume_count > 0) {
+      Rng rs = path_rng(pixel, sample_index, 0x10000u + uint32_t(it));
+      T = vol_transmittance_d(sc, v3(s4), v3(b4), 0.f, s4.w, rs, dlt);
+    }
+    const V3 c = V3{b4.w, c4.x, c4.y} * T;
+    if (!finite3(c))
+      continue;
+    float4 col = a.collected[slot];
+    col.x = col.x + c.x;
+    col.y = col.y + c.y;
+    col.z = col.z + c.z;
+    a.collected[slot] = col;
+    const uint32_t nx = sh.next[i];
+    if (nx != ADJ_NO_NEXT) {
+      float4 r = next.rem[nx];
+      r.x = r.x - c.x;
+      r.y = r.y - c.y;
+      r.z = r.z - c.z;
+      next.rem[nx] = r;
+    }
+    const float4 dI = a.d_image[pixel];
+    const V3 delta{dI.x * a.inv_spp, dI.y * a.inv_spp, dI.z * a.inv_spp};
+    add_vol(g, dlt, sc.volume_count, dot(delta, c));
+    uint32_t mat;
+    Taps taps;
+    if (get_vtx(sc, sh.v, i, mat, taps)) {
+      const float4 u = sh.g0[i], w = sh.g1[i];
+      const float gp[NP] = {T * u.x, T * u.y, T * u.z, T * u.w, T * w.x, T * w.y, T * w.z, T * w.w};
+      scatter_grads(g, sc.materials[mat], mat, taps, gp);
+    }
+  }
+  end_grads(g, sc, a);
+}
+
+// The replay collected what the forward pass did (same path), and the image
+// of the pass's samples.
+__global__ void __launch_bounds__(256) k_adj_finish(uint32_t slots, AdjointArgs a)
+{
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
+    const float4 L = a.primal[i], C = a.collected[i];
+    const float tol = 1e-4f * fmaxf(fabsf(L.x) + fabsf(L.y) + fabsf(L.z), 1e-2f);
+    if (!(fabsf(C.x - L.x) + fabsf(C.y - L.y) + fabsf(C.z - L.z) <= tol))
+      atomicAdd(a.mismatches, 1ull);
     if (a.radiance) {
+      const uint32_t pixel = i % a.npix;
       atomicAdd(a.radiance + 3 * pixel, L.x);
       atomicAdd(a.radiance + 3 * pixel + 1, L.y);
       atomicAdd(a.radiance + 3 * pixel + 2, L.z);
     }
-    const float4 dI = a.d_image[pixel];
-    const V3 delta{dI.x * a.inv_spp, dI.y * a.inv_spp, dI.z * a.inv_spp};
-    if (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) {
-      const V3 Lr = replay<true>(rc, sc, pixel, sample_index, L, delta, g, a.status, t0, a.cycle_budget);
-      // the replay must walk the primal path: same radiance up to rounding
-      const float tol = 1e-4f * fmaxf(fabsf(L.x) + fabsf(L.y) + fabsf(L.z), 1e-2f);
-      if (!(fabsf(Lr.x - L.x) + fabsf(Lr.y - L.y) + fabsf(Lr.z - L.z) <= tol))
-        atomicAdd(a.status + 2, 1ull);
-    }
-    const unsigned long long dt = static_cast<unsigned long long>(clock64() - t0);
-    longest = dt > longest ? dt : longest;
   }
-  flush_mat(g);
-  atomicMax(a.status + 1, longest);
-  __syncthreads();
-  if (shared_mat)
-    for (uint32_t i = threadIdx.x; i < sc.material_count * NP; i += blockDim.x)
-      if (smat[i] != 0.f)
-        atomicAdd(&a.mat_grads[i], smat[i]);
-  for (uint32_t i = threadIdx.x; i < MAX_VOLUMES * 4 && i < sc.volume_count * 4; i += blockDim.x)
-    if (svol[i] != 0.f)
-      atomicAdd(&a.vol_grads[i], svol[i]);
 }
 
 } // namespace
 
-void launch_adjoint(cudaStream_t s, int blocks, const RenderConst *rc, DevScene sc, AdjointArgs a)
+void launch_adj_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, AdjPathSoA in,
+    AdjPathSoA out, const float4 *hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a)
 {
-  k_adjoint<<<blocks, 128, 0, s>>>(rc, sc, a);
+  k_adj_shade<<<c.blocks_shade, 128, 0, s>>>(rc, sc, in, out, hits, sh, wc, it, a);
 }
 
-int adjoint_max_active_blocks(int threads)
+void launch_adj_resolve(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, AdjShadowSoA sh,
+    AdjPathSoA next, WaveCounters wc, int it, AdjointArgs a)
+{
+  k_adj_resolve<<<c.blocks_shade, 128, 0, s>>>(rc, sc, sh, next, wc, it, a);
+}
+
+void launch_adj_finish(cudaStream_t s, int blocks, uint32_t slots, AdjointArgs a)
+{
+  k_adj_finish<<<blocks, 256, 0, s>>>(slots, a);
+}
+
+int adj_shade_max_active_blocks(int threads)
 {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adjoint, threads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adj_shade, threads, 0) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }

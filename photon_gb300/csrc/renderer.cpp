@@ -111,7 +111,7 @@ struct phc_renderer {
   // job tags of the shadow queue
   Buf b_jobs, b_entries, b_wave_entry, b_wave_items, sh_job;
   // adjoint: constants, background, loss gradient, gradients, radiance
-  Buf adj_rc, adj_bg, adj_dimg, adj_rad, adj_mat, adj_vol, adj_tex, adj_status;
+  Buf adj_rc, adj_bg, adj_dimg, adj_rad, adj_mat, adj_vol, adj_tex, adj_status, adj_pool;
   phc_render_stats last{};
   cudaEvent_t ev0{nullptr}, ev1{nullptr};
 
@@ -852,6 +852,49 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
 }
 
 // ---------------------------------------------------------------- adjoint
+// The adjoint's per-slot state beside the wavefront buffers: two path queues'
+// extra fields (remainder, previous sample's pdf derivative and vertex), the
+// shadow queue's extra fields and the collected radiance, carved from one
+// allocation.
+struct AdjQueues {
+  AdjPathSoA path[2];
+  AdjShadowSoA shadow;
+  float4 *collected;
+};
+AdjQueues adj_queues(phc_renderer *r, size_t slots)
+{
+  const size_t f4 = slots * 16;
+  const size_t per_path = 6 * f4, per_shadow = 5 * f4 + slots * 4 + 256;
+  ck(r->adj_pool.ensure(2 * per_path + per_shadow + f4 + 1024), "alloc adjoint queues");
+  char *p = r->adj_pool.as<char>();
+  auto take = [&](size_t bytes) {
+    char *q = p;
+    p += (bytes + 255) & ~size_t(255);
+    return q;
+  };
+  AdjQueues a;
+  for (int b = 0; b < 2; ++b) {
+    AdjPathSoA &s = a.path[b];
+    s.p = path_soa(r, b);
+    s.rem = reinterpret_cast<float4 *>(take(f4));
+    s.g0 = reinterpret_cast<float4 *>(take(f4));
+    s.g1 = reinterpret_cast<float4 *>(take(f4));
+    s.v.q = reinterpret_cast<uint4 *>(take(f4));
+    s.v.p = reinterpret_cast<float4 *>(take(f4));
+    s.v.sn = reinterpret_cast<float4 *>(take(f4));
+  }
+  AdjShadowSoA &h = a.shadow;
+  h.s = ShadowSoA{r->sh_a.as<float4>(), r->sh_b.as<float4>(), r->sh_c.as<float4>(), nullptr};
+  h.next = reinterpret_cast<uint32_t *>(take(slots * 4));
+  h.g0 = reinterpret_cast<float4 *>(take(f4));
+  h.g1 = reinterpret_cast<float4 *>(take(f4));
+  h.v.q = reinterpret_cast<uint4 *>(take(f4));
+  h.v.p = reinterpret_cast<float4 *>(take(f4));
+  h.v.sn = reinterpret_cast<float4 *>(take(f4));
+  a.collected = reinterpret_cast<float4 *>(take(f4));
+  return a;
+}
+
 void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st, uint32_t sample_offset,
     const float *d_color, phc_adjoint_grads &g)
 {
@@ -868,7 +911,7 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
   const RenderConst base = render_const(cam, st, r->adj_bg, s);
   const uint32_t npix = base.npix, spp = base.spp;
   const int max_iter = int(base.max_iter);
-  // pass 1 runs the wavefront over chunks of `chunk` samples, one sample per
+  // both passes run over chunks of `chunk` samples, one sample per
   // accumulator slot (slot = sample-in-chunk * npix + pixel)
   const Tuning &tu = tuning();
   const uint64_t per_chunk = std::max<uint64_t>(uint64_t(tu.wave_paths), npix);
@@ -877,6 +920,7 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
   ensure_slots(r, slots);
   ensure_paths(r, slots);
   ensure_wave_buffers(r, max_iter);
+  const AdjQueues q = adj_queues(r, slots);
   const size_t nmat = size_t(sc.material_count) * ADJ_MATERIAL_PARAMS;
   const size_t nvol = size_t(std::min<uint32_t>(sc.volume_count, ADJ_MAX_VOLUMES)) * ADJ_VOLUME_PARAMS;
   const size_t ntex = g.texels ? size_t(r->scene.texel_count) : 0;
@@ -898,7 +942,20 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
     ck(cudaMemsetAsync(r->adj_tex.p, 0, ntex * 16, s), "clear adjoint");
   const WaveCounters wc = wave_counters(r, max_iter);
   const LaunchCfg cfg = launch_cfg(r, slots);
-  const int blocks = r->sm_count * adjoint_max_active_blocks(128);
+  LaunchCfg acfg = cfg;
+  acfg.blocks_shade = r->sm_count * adj_shade_max_active_blocks(128);
+  const RenderConst *drc = r->adj_rc.as<RenderConst>();
+  AdjointArgs a{};
+  a.primal = r->acc.as<float4>();
+  a.d_image = r->adj_dimg.as<float4>();
+  a.collected = q.collected;
+  a.radiance = g.color ? r->adj_rad.as<float>() : nullptr;
+  a.mat_grads = r->adj_mat.as<float>();
+  a.vol_grads = r->adj_vol.as<float>();
+  a.texel_grads = ntex ? r->adj_tex.as<float4>() : nullptr;
+  a.mismatches = r->adj_status.as<unsigned long long>();
+  a.npix = npix;
+  a.inv_spp = 1.f / float(spp);
   for (uint32_t s0 = 0; s0 < spp; s0 += chunk) {
     const uint32_t cnt = std::min(chunk, spp - s0);
     RenderConst rc = base;
@@ -907,26 +964,27 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
     rc.adaptive = 0;
     rc.sample_offset = sample_offset + s0;
     ck(cudaMemcpyAsync(r->adj_rc.p, &rc, sizeof(rc), cudaMemcpyHostToDevice, s), "upload constants");
+    // pass 1: the forward wavefront, one sample per slot
     ck(cudaMemsetAsync(r->acc.p, 0, size_t(cnt) * npix * 16, s), "reset accumulators");
     ck(cudaMemsetAsync(r->nsamp.p, 0, size_t(cnt) * npix * 4, s), "reset accumulators");
     ck(cudaMemsetAsync(r->aov_a.p, 0, size_t(cnt) * npix * 16, s), "reset accumulators");
     ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
-    record_wave(r, s, cfg, r->adj_rc.as<RenderConst>(), npix, max_iter, 0, false);
-    AdjointArgs a{};
-    a.primal = r->acc.as<float4>();
-    a.d_image = r->adj_dimg.as<float4>();
-    a.radiance = g.color ? r->adj_rad.as<float>() : nullptr;
-    a.mat_grads = r->adj_mat.as<float>();
-    a.vol_grads = r->adj_vol.as<float>();
-    a.texel_grads = ntex ? r->adj_tex.as<float4>() : nullptr;
-    a.status = r->adj_status.as<unsigned long long>();
-    a.cycle_budget = 1ull << 31; // about 1 s at the SM clock, per pixel sample
-    a.npix = npix;
-    a.spp = cnt;
-    a.sample_offset = sample_offset + s0;
-    a.inv_spp = 1.f / float(spp);
-    launch_adjoint(s, blocks, r->adj_rc.as<RenderConst>(), sc, a);
-    ck(cudaGetLastError(), "adjoint kernel");
+    record_wave(r, s, cfg, drc, npix, max_iter, 0, false);
+    // pass 2: the replay, bounce by bounce
+    ck(cudaMemsetAsync(wc.count, 0, per_wave_counter_bytes(max_iter), s), "reset counters");
+    ck(cudaMemsetAsync(wc.wave, 0, 4, s), "reset wave");
+    ck(cudaMemsetAsync(q.collected, 0, size_t(cnt) * npix * 16, s), "reset adjoint");
+    launch_raygen(cfg, s, drc, sc, q.path[0].p, accum(r), wc);
+    for (int it = 0; it < max_iter; ++it) {
+      const AdjPathSoA &in = q.path[it & 1], &out = q.path[(it + 1) & 1];
+      float4 *hits = r->hits.as<float4>();
+      launch_trace(cfg, s, sc, in.p, hits, wc, it, nullptr, tu.trace_refill, HitQueues{nullptr, nullptr});
+      launch_adj_shade(acfg, s, drc, sc, in, out, hits, q.shadow, wc, it, a);
+      launch_shadow_deferred(cfg, s, sc, q.shadow.s, wc, it, tu.trace_refill);
+      launch_adj_resolve(acfg, s, drc, sc, q.shadow, out, wc, it, a);
+    }
+    launch_adj_finish(s, r->sm_count * 8, uint32_t(size_t(cnt) * npix), a);
+    ck(cudaGetLastError(), "adjoint kernels");
   }
   ck(cudaEventRecord(r->ev1, s), "event");
   ck(cudaMemcpyAsync(g.materials, r->adj_mat.p, nmat * 4, cudaMemcpyDeviceToHost, s), "read gradients");
@@ -934,9 +992,9 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
     ck(cudaMemcpyAsync(g.volumes, r->adj_vol.p, nvol * 4, cudaMemcpyDeviceToHost, s), "read gradients");
   if (ntex)
     ck(cudaMemcpyAsync(g.texels, r->adj_tex.p, ntex * 16, cudaMemcpyDeviceToHost, s), "read gradients");
-  unsigned long long status[3] = {0, 0, 0};
+  unsigned long long mism = 0;
   uint32_t err_word = 0;
-  ck(cudaMemcpyAsync(status, r->adj_status.p, 24, cudaMemcpyDeviceToHost, s), "read status");
+  ck(cudaMemcpyAsync(&mism, r->adj_status.p, 8, cudaMemcpyDeviceToHost, s), "read status");
   ck(cudaMemcpyAsync(&err_word, wc.error, 4, cudaMemcpyDeviceToHost, s), "read error word");
   std::vector<float> rad;
   if (g.color) {
@@ -948,12 +1006,7 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
   float ms = 0.f;
   cudaEventElapsedTime(&ms, r->ev0, r->ev1);
   g.adjoint_ms = ms;
-  g.longest_sample_cycles = status[1];
-  g.replay_mismatches = status[2];
-  if (status[0] != 0)
-    throw ApiError(PHC_ERR_LIMIT, status[0] >= 0x10000ull
-            ? "adjoint: a ray exceeded the traversal step limit"
-            : "adjoint: a pixel sample exceeded its time budget at bounce " + std::to_string(status[0] - 1));
+  g.replay_mismatches = mism;
   if (g.color)
     for (size_t p = 0; p < npix; ++p) {
       for (int c = 0; c < 3; ++c)

@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(128) k_trace(DevScene sc, BatchTable bt, PathS
 // Any-hit traversal of the shadow queue, then the NEE contribution of the
 // unoccluded rays times the ratio-tracking transmittance of the volumes
 // (stream dimension 0x10000 + iteration), added to the path's pixel slot.
-template <bool COUNT, bool BATCH>
+template <bool COUNT, bool BATCH, bool DEFER = false>
 __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ rcp, DevScene sc, BatchTable bt,
     ShadowSoA sh, Accum acc_param, WaveCounters wc, int it, uint64_t *stats, uint32_t refill)
 {
@@ -335,7 +335,8 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
       // volume; otherwise leave the ray (tmax >= 0) to k_shadow_volume, so
       // that no lane runs a tracking loop inside this warp-voting loop.
       // Occluded or done: tmax < 0.
-      const bool vol = (BATCH ? bt.jobs[job].sc.volume_count : sc.volume_count) > 0;
+      // DEFER: every unoccluded ray is left to a later kernel (the adjoint's).
+      const bool vol = DEFER || (BATCH ? bt.jobs[job].sc.volume_count : sc.volume_count) > 0;
       const bool open = s.best.prim == 0xffffffffu;
       if (open && !vol) {
         const Accum &acc = BATCH ? bt.jobs[job].acc : acc_param;
@@ -540,6 +541,13 @@ void launch_trace_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathS
     k_trace<false, true, true><<<c.blocks_trace, 128, 0, s>>>(none, bt, in, hits, wc, it, nullptr, r, hq);
   else
     k_trace<false, false, true><<<c.blocks_trace, 128, 0, s>>>(none, bt, in, hits, wc, it, nullptr, r, hq);
+}
+
+void launch_shadow_deferred(const LaunchCfg &c, cudaStream_t s, DevScene sc, ShadowSoA sh, WaveCounters wc, int it,
+    int refill)
+{
+  const uint32_t r = uint32_t(refill < 1 ? 1 : (refill > 32 ? 32 : refill));
+  k_shadow<false, false, true><<<c.blocks_trace, 128, 0, s>>>(nullptr, sc, BatchTable{}, sh, Accum{}, wc, it, nullptr, r);
 }
 
 void launch_shadow_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, ShadowSoA sh, WaveCounters wc, int it,

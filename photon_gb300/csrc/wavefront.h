@@ -162,6 +162,9 @@ void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, Dev
     const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, ShadeVariant v, HitQueues hq);
 void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh, Accum acc,
     WaveCounters wc, int it, uint64_t *stats, int refill);
+// Occlusion only: unoccluded rays keep tmax >= 0, occluded ones get tmax < 0.
+void launch_shadow_deferred(const LaunchCfg &c, cudaStream_t s, DevScene sc, ShadowSoA sh, WaveCounters wc, int it,
+    int refill);
 void launch_wave_end(cudaStream_t s, const RenderConst *rc, Accum acc, WaveCounters wc, uint32_t npix, int adaptive,
     int max_iter, uint64_t *ray_totals);
 void launch_resolve(cudaStream_t s, Accum acc, Frame fr, uint32_t npix, uint32_t lanes, float weight, int first);

@@ -120,7 +120,6 @@ class Renderer:
         self._check(self.lib.phc_adjoint(self.h, C.addressof(camera), C.addressof(settings),
                                          int(sample_offset), d.ctypes.data, C.byref(g)))
         out = {"materials": g_mat, "volumes": g_vol, "adjoint_ms": float(g.adjoint_ms),
-               "longest_sample_cycles": int(g.longest_sample_cycles),
                "replay_mismatches": int(g.replay_mismatches)}
         if g_tex is not None:
             out["texels"] = g_tex
