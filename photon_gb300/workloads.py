@@ -12,9 +12,10 @@ and value ranges of the five workloads the project is measured on:
                     1024x512 fp32 sun+sky environment map and 4 emissive
                     triangles; 1024^2, 128 spp, depth 8.
   instanced_2m      ~2M triangles (instances flattened, as the reference
-                    does), 12 RGBA8 2048^2 value-noise textures, emissive
-                    meshes and a 256^3 fBm density grid; 1920^2, 256 spp,
-                    depth 12, adaptive sampling.
+                    does), 12 RGBA8 2048^2 value-noise textures (base colour,
+                    roughness, normal maps), emissive meshes and a 256^3 fBm
+                    density grid (sigma_t up to 8); 1920^2, 256 spp, depth 12,
+                    adaptive sampling.
   batched_jobs      64 independent small renders of uneven size.
   differentiable    50K triangles, 8 textured materials, homogeneous medium.
 
@@ -314,25 +315,34 @@ def batched_jobs(seed=0, n=64, min_tris=1_000, max_tris=200_000, min_res=128, ma
 # ------------------------------------------------------------ differentiable
 
 
+def _lerp_matrix(n, res):
+    """(n, res + 1) linear-interpolation weights of n cell-centred samples of
+    a lattice with res cells (two non-zeros per row)."""
+    x = (np.arange(n) + 0.5) * (res / n)
+    i = np.minimum(np.floor(x).astype(np.int64), res - 1)
+    f = (x - i).astype(np.float32)
+    w = np.zeros((n, res + 1), np.float32)
+    w[np.arange(n), i] = 1.0 - f
+    w[np.arange(n), i + 1] += f
+    return w
+
+
 def value_noise(rng, size=512, octaves=(4, 8, 16, 32, 64), channels=4):
     """(size, size, channels) float32 value noise in [0, 1]: random lattices
     of the given resolutions, bilinearly upsampled (wrapping), summed with
     weights halving per octave."""
-    out = np.zeros((size, size, channels), np.float64)
+    out = np.zeros((size, size, channels), np.float32)
     total = 0.0
     for k, res in enumerate(octaves):
-        lat = rng.uniform(0, 1, (res + 1, res + 1, channels))
+        lat = rng.uniform(0, 1, (res + 1, res + 1, channels)).astype(np.float32)
         lat[res, :] = lat[0, :]
         lat[:, res] = lat[:, 0]
-        x = (np.arange(size) + 0.5) * (res / size)
-        i = np.floor(x).astype(np.int64)
-        f = (x - i)[:, None]
-        rows = lat[i] * (1 - f)[..., None] + lat[i + 1] * f[..., None]
-        img = rows[:, i] * (1 - f.T)[..., None] + rows[:, i + 1] * f.T[..., None]
-        w = 0.5 ** k
-        out += w * img
-        total += w
-    return (out / total).astype(np.float32)
+        w = _lerp_matrix(size, res)
+        rows = np.tensordot(w, lat, axes=(1, 0))                     # (size, res + 1, ch)
+        img = np.tensordot(rows, w, axes=(1, 1)).transpose(0, 2, 1)  # (size, size, ch)
+        out += np.float32(0.5 ** k) * img
+        total += 0.5 ** k
+    return out / np.float32(total)
 
 
 DIFF_MATERIALS = 8
@@ -436,6 +446,130 @@ def differentiable(seed=0, res=256, spp=64, depth=6, texture=DIFF_TEXTURE, targe
     sc.env_pixels = sun_sky_env(256, 128, sun_radiance=(0.0, 0.0, 0.0))
     cam = camera((0.0, 7.0, 17.0), (0.0, 0.8, 0.0), fovy_deg=45.0)
     st = settings(res, res, spp, depth, adaptive_sampling=0, throughput_clamp=0.0)
+    return sc, cam, st
+
+
+# ------------------------------------------------------------- instanced 2M
+
+
+def fbm_volume(rng, n=256, octaves=(8, 16, 32, 64), gain=0.5):
+    """(n, n, n) float32 fBm noise in [0, 1], indexed [z, y, x] (x fastest
+    when flattened): random lattices trilinearly upsampled, summed with
+    weights falling by `gain` per octave."""
+    out = np.zeros((n, n, n), np.float32)
+    total = 0.0
+    for k, res in enumerate(octaves):
+        lat = rng.uniform(0, 1, (res + 1, res + 1, res + 1)).astype(np.float32)
+        w = _lerp_matrix(n, res)
+        a = np.tensordot(w, lat, axes=(1, 0))                        # (n, r, r)
+        a = np.tensordot(a, w, axes=(2, 1))                          # (n, r, n)
+        a = np.tensordot(a, w, axes=(1, 1)).transpose(0, 2, 1)       # (n, n, n)
+        out += np.float32(gain ** k) * a
+        total += gain ** k
+    return out / np.float32(total)
+
+
+def _rot(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def instanced_2m(seed=0, res=1920, spp=256, depth=12, tex_res=2048, grid=256, n_instances=400, adaptive=1):
+    """~2M triangles: two base meshes (displaced icosphere, torus) instanced
+    n_instances times with random rotations, scales and positions and
+    flattened into one mesh (as the reference flattens instances); 4 textured
+    materials, each with an RGBA8 value-noise base-colour, roughness and
+    normal map (12 textures of tex_res^2, stored as the 8-bit values / 255 in
+    fp32); 6 emissive instances; a grid^3 fp32 fBm density volume whose
+    transfer function ramps opacity 0 -> 1 (density scale 8: sigma_t up to 8)
+    over part of the scene; a dim sky.  1920^2, 256 spp, depth 12, adaptive
+    sampling on."""
+    rng = np.random.default_rng(seed)
+    sv, sf = _icosphere(4)
+    sv = _displace(sv.copy(), sv.copy(), rng, 0.08)
+    s_uv = np.stack([np.arctan2(sv[:, 2], sv[:, 0]) / (2 * np.pi) + 0.5,
+                     np.arccos(np.clip(sv[:, 1] / np.linalg.norm(sv, axis=1), -1, 1)) / np.pi], -1)
+    nu, nv = 72, 36
+    tv, tn, tf = _torus(nu, nv, 1.0, 0.35)
+    uu, ww = np.meshgrid(np.arange(nu) / nu, np.arange(nv) / nv, indexing="ij")
+    t_uv = np.stack([uu.reshape(-1) * 3.0, ww.reshape(-1)], -1)
+    bases = [(sv, sf, s_uv, _vertex_normals(sv, sf)), (tv, tf, t_uv, _vertex_normals(tv, tf))]
+    mb = _MeshBuilder()
+    uvs = []
+    G = 30.0
+    gv, gf = _quad((-G, 0, -G), (-G, 0, G), (G, 0, G), (G, 0, -G))
+    mb.add(gv, gf, 0, n=np.tile([0, 1, 0], (4, 1)))
+    uvs.append(np.stack([gv[:, 0] / 4.0, gv[:, 2] / 4.0], -1))
+    for k in range(n_instances):
+        v, f, uv, vn = bases[k % 2]
+        R = _rot(rng)
+        scale = rng.uniform(0.4, 1.2)
+        pos = np.array([rng.uniform(-22, 22), 0.0, rng.uniform(-22, 22)])
+        vw = (v @ R.T) * scale
+        pos[1] = -vw[:, 1].min() + 0.01
+        vw = vw + pos
+        emissive = k < 6
+        mat = 4 if emissive else int(rng.integers(0, 4))
+        mb.add(vw.astype(np.float32), f, mat, n=(vn @ R.T).astype(np.float32))  # uniform scale: rotate normals
+        uvs.append(uv)
+    sc = mb.build(name="instanced_2m")
+    attr = np.zeros((sc.positions.shape[0], 4), np.float32)
+    attr[:, :2] = np.concatenate(uvs)
+    attr[:, 3] = 1.0
+    sc.attributes = [attr, None, None, None, None]
+    trng = np.random.default_rng(seed + 11)
+    mats, samplers = [], []
+
+    def sampler(tex):
+        s = _abi.sampler_default()
+        s.type = 1
+        s.in_attribute = 0
+        s.linear = 1
+        s.wrap[:] = (1, 1, 0)
+        s.size[:] = (tex_res, tex_res, 1)
+        q = np.round(np.clip(tex, 0, 1) * 255.0) / 255.0  # RGBA8 values
+        samplers.append((s, q.astype(np.float32).reshape(-1, 4)))
+        return len(samplers) - 1
+
+    for i in range(4):
+        tint = trng.uniform(0.2, 0.9, 3)
+        base = value_noise(trng, tex_res, octaves=(4, 16, 64))
+        base[..., :3] = base[..., :3] * 0.5 + 0.5 * tint
+        base[..., 3] = 1.0
+        rough = value_noise(trng, tex_res, octaves=(8, 32))
+        rough[..., :3] = rough[..., :1] * 0.8 + 0.1
+        nrm = value_noise(trng, tex_res, octaves=(16, 64))
+        nrm[..., 0:2] = 0.5 + (nrm[..., 0:2] - 0.5) * 0.6
+        nrm[..., 2] = 0.9
+        m = _abi.material_default()
+        m.base_color_src.kind, m.base_color_src.index = 2, sampler(base)
+        m.roughness_src.kind, m.roughness_src.index = 2, sampler(rough)
+        m.normal_src.kind, m.normal_src.index = 2, sampler(nrm)
+        m.metallic = float(trng.uniform(0.0, 0.6))
+        m.specular = 0.5
+        m.clearcoat = float(trng.uniform(0.0, 0.5))
+        mats.append(m)
+    mats.append(emitter((12.0, 10.0, 8.0), both_sides=True))
+    sc.materials = mats
+    sc.samplers = samplers
+    vrng = np.random.default_rng(seed + 23)
+    dens = fbm_volume(vrng, grid)
+    vol = _abi.volume_default()
+    vol.dims[:] = (grid, grid, grid)
+    vol.origin[:] = (-18.0, 0.0, -16.0)
+    vol.spacing[:] = (20.0 / (grid - 1), 7.0 / (grid - 1), 16.0 / (grid - 1))
+    vol.value_range[:] = (0.55, 0.8)
+    vol.density_scale = 8.0
+    tf = np.array([[0.9, 0.9, 0.95, 0.0], [0.85, 0.8, 0.75, 0.5], [0.8, 0.7, 0.6, 1.0]], np.float32)
+    sc.volumes = [(vol, dens.reshape(-1), tf)]
+    sc.env_pixels = sun_sky_env(256, 128, sun_radiance=(0.0, 0.0, 0.0)) * np.float32(0.3)
+    cam = camera((0.0, 14.0, 40.0), (0.0, 1.0, 0.0), fovy_deg=50.0)
+    st = settings(res, res, spp, depth, adaptive_sampling=adaptive, throughput_clamp=0.0)
+    st.max_volume_bounces = 6
     return sc, cam, st
 
 
