@@ -394,12 +394,19 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
     const float *tmax, uint32_t n, float *hits4, void *stream);
 
 /* ------------------------------------------------------------ scheduling */
-/* Launch parameters picked by the autotuner (no reference counterpart; the
-   reference has no tunables on this path).  Keys: "wave_paths" (paths in
-   flight per wave), "trace_blocks_per_sm", "shade_blocks_per_sm",
-   "use_graph" (0/1), "count_traversal" (0/1), "max_leaf" (1..3, BVH8 leaf
-   size, read at the next scene upload).  Returns PHC_ERR_INVALID for an
-   unknown key or out-of-range value; get returns -1 for an unknown key. */
+/* Launch parameters picked by the autotuner (photon_gb300/autotune.py; no
+   reference counterpart, the reference has no tunables on this path).  Keys:
+   "wave_paths" (paths in flight per wave: the queue capacity),
+   "trace_blocks_per_sm", "shade_blocks_per_sm" (persistent grid sizes),
+   "trace_refill" (a traversal warp takes new rays once this many lanes are
+   idle), "split_shade" (0/1: hits and misses shaded by separate kernels),
+   "shade_lean" (0/1: lean shading kernels for scenes without volumes /
+   sources / lights), "sort_threshold" (sort the hit queue by material when it
+   holds at least this many hits; 0: never), "max_leaf" (1..3, BVH8 leaf size,
+   read at the next scene upload), "batch_wave_paths", "use_graph" (0/1),
+   "count_traversal" (0/1), "time_kernels" (0/1).  Returns PHC_ERR_INVALID
+   for an unknown key or out-of-range value; get returns -1 for an unknown
+   key.  Settings are process-wide and read at the start of each call. */
 int phc_tuning_set(const char *key, int64_t value);
 int64_t phc_tuning_get(const char *key);
 

@@ -92,7 +92,8 @@ struct phc_renderer {
 
   // wavefront buffers
   size_t cap_paths{0};
-  Buf st_o[2], st_d[2], st_tp[2], st_info[2], st_dist[2], hits, sh_a, sh_b, sh_c, hitq, missq;
+  Buf st_o[2], st_d[2], st_tp[2], st_info[2], st_dist[2], hits, sh_a, sh_b, sh_c, hitq, missq, hitq_sorted;
+  Buf sort_bins; // per bounce iteration: material-sort counts and starts
   size_t cap_slots{0};
   Buf acc, acc_sq, acc_start, nsamp, aov_n, aov_a;
   Buf counters; // count, scount, fetch, wave, error
@@ -239,6 +240,7 @@ void ensure_paths(phc_renderer *r, size_t n)
   ck(r->hits.ensure(n * 16), "alloc hits");
   ck(r->hitq.ensure(n * 4), "alloc hit queue");
   ck(r->missq.ensure(n * 4), "alloc miss queue");
+  ck(r->hitq_sorted.ensure(n * 4), "alloc sorted hit queue");
   ck(r->sh_a.ensure(n * 16), "alloc shadow queue");
   ck(r->sh_b.ensure(n * 16), "alloc shadow queue");
   ck(r->sh_c.ensure(n * 16), "alloc shadow queue");
@@ -262,11 +264,13 @@ void ensure_slots(phc_renderer *r, size_t n)
 // Counters, statistics and constants buffers of the wave kernels.
 void ensure_wave_buffers(phc_renderer *r, int max_iter)
 {
-  const void *before[3] = {r->counters.p, r->stats_buf.p, r->rc_buf.p};
+  const void *before[4] = {r->counters.p, r->stats_buf.p, r->rc_buf.p, r->sort_bins.p};
   ck(r->counters.ensure(wave_counter_alloc_bytes(max_iter)), "alloc counters");
   ck(r->stats_buf.ensure(8 * sizeof(uint64_t)), "alloc stats");
   ck(r->rc_buf.ensure(sizeof(RenderConst)), "alloc constants");
-  if (before[0] != r->counters.p || before[1] != r->stats_buf.p || before[2] != r->rc_buf.p)
+  ck(r->sort_bins.ensure(size_t(max_iter) * 2 * MAT_SORT_BINS * 4), "alloc sort bins");
+  if (before[0] != r->counters.p || before[1] != r->stats_buf.p || before[2] != r->rc_buf.p ||
+      before[3] != r->sort_bins.p)
     r->buf_gen++;
 }
 
@@ -361,7 +365,14 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
   const Tuning &tu = tuning();
   const bool full = (sc.features & (SCENE_VOLUMES | SCENE_SOURCES | SCENE_LIGHTS)) != 0 || !tu.shade_lean;
   const bool split = (sc.features & SCENE_VOLUMES) == 0 && tu.split_shade;
-  const HitQueues hq = split ? HitQueues{r->hitq.as<uint32_t>(), r->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
+  HitQueues hq = split ? HitQueues{r->hitq.as<uint32_t>(), r->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
+  const bool sort = split && tu.sort_threshold > 0;
+  const size_t bin_words = size_t(2) * MAT_SORT_BINS;
+  if (sort) { // sort_bins sized by ensure_wave_buffers (no allocation while a graph is captured)
+    hq.sorted = r->hitq_sorted.as<uint32_t>();
+    hq.sort_threshold = uint32_t(tu.sort_threshold);
+    ck(cudaMemsetAsync(r->sort_bins.p, 0, size_t(max_iter) * bin_words * 4, s), "reset sort bins");
+  }
   uint64_t launches = 2;
   if (tm)
     tm->begin_wave();
@@ -370,6 +381,12 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
     const PathSoA in = path_soa(r, it & 1), out = path_soa(r, (it + 1) & 1);
     float4 *hits = r->hits.as<float4>();
     timed(1, [&] { launch_trace(cfg, s, sc, in, hits, wc, it, counting ? stats + 3 : nullptr, tu.trace_refill, hq); });
+    if (sort) {
+      timed(2, [&] {
+        launch_material_sort(cfg, s, sc, hits, hq, wc, it, r->sort_bins.as<uint32_t>() + size_t(it) * bin_words);
+      });
+      launches += 3;
+    }
     if (split) {
       timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 1}, hq); });
       timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 2}, hq); });
@@ -564,7 +581,9 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
   const uint64_t key[6] = {uint64_t(npix) | (uint64_t(lanes) << 32),
       uint64_t(max_iter) | (uint64_t(rc.adaptive) << 32), r->scene_generation,
       uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32),
-      uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16), r->buf_gen};
+      uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16) |
+          (uint64_t(tu.sort_threshold) << 24),
+      r->buf_gen};
   uint64_t launches = 0;
   KernelTimer timer;
   if (tu.time_kernels) {
@@ -584,6 +603,7 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
         cudaStreamEndCapture(s, &g);
         if (g)
           cudaGraphDestroy(g);
+        cudaGetLastError(); // the failed capture's error is reported once, not left for later calls
         throw;
       }
       ck(cudaStreamEndCapture(s, &g), "end capture");
@@ -707,13 +727,23 @@ void record_batch_wave(phc_renderer *lead, cudaStream_t s, const LaunchCfg &cfg,
       lead->sh_job.as<uint32_t>()};
   const bool full = (features & (SCENE_VOLUMES | SCENE_SOURCES | SCENE_LIGHTS)) != 0 || !tu.shade_lean;
   const bool split = (features & SCENE_VOLUMES) == 0 && tu.split_shade;
-  const HitQueues hq =
+  HitQueues hq =
       split ? HitQueues{lead->hitq.as<uint32_t>(), lead->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
+  const bool sort = split && tu.sort_threshold > 0;
+  const size_t bin_words = size_t(2) * MAT_SORT_BINS;
+  if (sort) { // sort_bins sized by ensure_wave_buffers
+    hq.sorted = lead->hitq_sorted.as<uint32_t>();
+    hq.sort_threshold = uint32_t(tu.sort_threshold);
+    ck(cudaMemsetAsync(lead->sort_bins.p, 0, size_t(max_iter) * bin_words * 4, s), "reset sort bins");
+  }
   float4 *hits = lead->hits.as<float4>();
   launch_raygen_batch(cfg, s, bt, path_soa(lead, 0), wc);
   for (int it = 0; it < max_iter; ++it) {
     const PathSoA in = path_soa(lead, it & 1), out = path_soa(lead, (it + 1) & 1);
     launch_trace_batch(cfg, s, bt, in, hits, wc, it, tu.trace_refill, hq);
+    if (sort)
+      launch_material_sort_batch(cfg, s, bt, in.info, hits, hq, wc, it,
+          lead->sort_bins.as<uint32_t>() + size_t(it) * bin_words);
     if (split) {
       launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 1}, hq);
       launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 2}, hq);
@@ -798,6 +828,7 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
       cudaStreamEndCapture(s, &g);
       if (g)
         cudaGraphDestroy(g);
+      cudaGetLastError();
       throw;
     }
     ck(cudaStreamEndCapture(s, &g), "end capture");

@@ -313,7 +313,8 @@ __global__ void __launch_bounds__(128) k_shade(const RenderConst *__restrict__ r
     ShadowRec sr;
     uint32_t job_bits = 0;
     if (j < n) {
-      const uint32_t i = PART == 0 ? j : (PART == 1 ? hq.hitq[j] : hq.missq[j]);
+      const bool sorted = PART == 1 && hq.sort_threshold != 0u && n >= hq.sort_threshold;
+      const uint32_t i = PART == 0 ? j : (PART == 1 ? (sorted ? hq.sorted[j] : hq.hitq[j]) : hq.missq[j]);
       const uint4 info = in.info[i];
       if (BATCH) {
         job_bits = info.w & ~((1u << BATCH_JOB_SHIFT) - 1u);

@@ -36,6 +36,7 @@ const Key *keys(size_t &n)
       {"split_shade", "PHC_TUNE_SPLIT_SHADE", 0, 1, nullptr, &g_tuning.split_shade},
       {"shade_lean", "PHC_TUNE_SHADE_LEAN", 0, 1, nullptr, &g_tuning.shade_lean},
       {"batch_wave_paths", "PHC_TUNE_BATCH_WAVE_PATHS", 1024, int64_t(1) << 30, &g_tuning.batch_wave_paths, nullptr},
+      {"sort_threshold", "PHC_TUNE_SORT_THRESHOLD", 0, int64_t(1) << 30, &g_tuning.sort_threshold, nullptr},
   };
   n = sizeof(k) / sizeof(k[0]);
   return k;

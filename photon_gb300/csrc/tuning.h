@@ -1,6 +1,7 @@
 // Launch and scheduling parameters of the renderer, set by the autotuner
 // (photon_gb300/autotune.py) through phc_tuning_set or the PHC_TUNE_<KEY>
-// environment variables, read once per render call.
+// environment variables, read once per render call.  The defaults are the
+// autotuner's choice on the 500K-triangle workload (1024^2, 128 spp) on GB300.
 #pragma once
 
 #include <cstdint>
@@ -8,17 +9,18 @@
 namespace phc {
 
 struct Tuning {
-  int64_t wave_paths{1 << 21};       // paths in flight per wave (lanes = wave_paths / pixels)
-  int trace_blocks_per_sm{16};       // persistent grid of the traversal kernels (128 threads)
-  int shade_blocks_per_sm{8};        // persistent grid of the shading kernel (128 threads)
+  int64_t wave_paths{1 << 25};       // paths in flight per wave (lanes = wave_paths / pixels)
+  int trace_blocks_per_sm{32};       // persistent grid of the traversal kernels (128 threads; capped by occupancy)
+  int shade_blocks_per_sm{16};       // persistent grid of the shading kernel (128 threads; capped by occupancy)
   int use_graph{1};                  // replay each wave as a CUDA graph
   int count_traversal{0};            // node-visit / triangle-test counters (roofline runs)
-  int max_leaf{3};                   // triangles per BVH8 leaf child (1..3), read at scene build
+  int max_leaf{1};                   // triangles per BVH8 leaf child (1..3), read at scene build
   int time_kernels{0};               // CUDA events around every launch (no graph), per-kind times
   int trace_refill{8};               // closest-hit warps refill once this many lanes idle (32: never)
   int split_shade{1};                // misses and hits shaded by separate kernels (no-volume scenes)
   int shade_lean{1};                 // lean shading kernels for scenes without volumes/sources/lights
-  int64_t batch_wave_paths{1 << 22}; // paths per wave of a batched render
+  int64_t batch_wave_paths{1 << 25}; // paths per wave of a batched render
+  int64_t sort_threshold{1 << 18};   // sort the hit queue by material when it holds this many hits (0: never)
 };
 
 Tuning &tuning();

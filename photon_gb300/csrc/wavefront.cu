@@ -265,6 +265,88 @@ __global__ void __launch_bounds__(128) k_trace(DevScene sc, BatchTable bt, PathS
   }
 }
 
+// ------------------------------------------------------- material sort
+// Counting sort of the hit queue by material, so that the hit-shading kernel
+// sees runs of one material (coherent parameter branches, shared texture
+// rows).  Histogram in shared memory, one-block exclusive scan, scatter with
+// warp-aggregated atomics (lanes with the same bin take consecutive slots
+// from one atomic).  Order within a bin is not preserved; every path's result
+// is independent of the order it is shaded in.
+// Bin of a queued hit: its material (batched renders: job and material).
+template <bool BATCH>
+__device__ __forceinline__ uint32_t hit_bin(const DevScene &sc, const BatchTable &bt, const uint4 *info,
+    const float4 *hits, uint32_t qi)
+{
+  const uint32_t prim = __float_as_uint(hits[qi].y);
+  if (BATCH) {
+    const uint32_t job = info[qi].w >> BATCH_JOB_SHIFT;
+    return (job * 1031u + __ldg(&bt.jobs[job].sc.prim_vidx[prim].w)) % MAT_SORT_BINS;
+  }
+  return __ldg(&sc.prim_vidx[prim].w) % MAT_SORT_BINS;
+}
+
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_mat_hist(DevScene sc, BatchTable bt, const uint4 *__restrict__ info,
+    const float4 *__restrict__ hits, HitQueues hq, WaveCounters wc, int it, uint32_t *bins)
+{
+  __shared__ uint32_t h[MAT_SORT_BINS];
+  const uint32_t n = wc.hcount[it];
+  if (n < hq.sort_threshold)
+    return;
+  for (uint32_t b = threadIdx.x; b < MAT_SORT_BINS; b += blockDim.x)
+    h[b] = 0u;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(&h[hit_bin<BATCH>(sc, bt, info, hits, hq.hitq[i])], 1u);
+  __syncthreads();
+  for (uint32_t b = threadIdx.x; b < MAT_SORT_BINS; b += blockDim.x)
+    if (h[b])
+      atomicAdd(&bins[b], h[b]);
+}
+
+// One block of MAT_SORT_BINS threads: bins[0..) counts -> bins[MAT_SORT_BINS..) starts.
+__global__ void __launch_bounds__(MAT_SORT_BINS) k_mat_scan(HitQueues hq, WaveCounters wc, int it, uint32_t *bins)
+{
+  __shared__ uint32_t t[MAT_SORT_BINS];
+  if (wc.hcount[it] < hq.sort_threshold)
+    return;
+  const uint32_t b = threadIdx.x;
+  t[b] = bins[b];
+  __syncthreads();
+  for (uint32_t off = 1; off < MAT_SORT_BINS; off <<= 1) { // Hillis-Steele inclusive scan
+    const uint32_t v = b >= off ? t[b - off] : 0u;
+    __syncthreads();
+    t[b] += v;
+    __syncthreads();
+  }
+  bins[MAT_SORT_BINS + b] = t[b] - bins[b];
+}
+
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_mat_scatter(DevScene sc, BatchTable bt, const uint4 *__restrict__ info,
+    const float4 *__restrict__ hits, HitQueues hq, WaveCounters wc, int it, uint32_t *bins)
+{
+  const uint32_t n = wc.hcount[it];
+  if (n < hq.sort_threshold)
+    return;
+  uint32_t *start = bins + MAT_SORT_BINS;
+  for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + lane_id();
+    const bool live = i < n;
+    const uint32_t q = live ? hq.hitq[i] : 0u;
+    const uint32_t bin = live ? hit_bin<BATCH>(sc, bt, info, hits, q) : 0xffffffffu;
+    __syncwarp();
+    const uint32_t grp = __match_any_sync(WARP_FULL, bin);
+    const uint32_t leader = uint32_t(__ffs(int(grp)) - 1);
+    uint32_t pos = 0;
+    if (live && lane_id() == leader)
+      pos = atomicAdd(&start[bin], uint32_t(__popc(grp)));
+    pos = __shfl_sync(WARP_FULL, pos, int(leader));
+    if (live)
+      hq.sorted[pos + uint32_t(__popc(grp & ((1u << lane_id()) - 1u)))] = q;
+  }
+}
+
 // ----------------------------------------------------------------- shadow
 // Any-hit traversal of the shadow queue, then the NEE contribution of the
 // unoccluded rays times the ratio-tracking transmittance of the volumes
@@ -541,6 +623,25 @@ void launch_trace_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathS
     k_trace<false, true, true><<<c.blocks_trace, 128, 0, s>>>(none, bt, in, hits, wc, it, nullptr, r, hq);
   else
     k_trace<false, false, true><<<c.blocks_trace, 128, 0, s>>>(none, bt, in, hits, wc, it, nullptr, r, hq);
+}
+
+void launch_material_sort(const LaunchCfg &c, cudaStream_t s, DevScene sc, const float4 *hits, HitQueues hq,
+    WaveCounters wc, int it, uint32_t *bins)
+{
+  const int blocks = c.blocks_raygen > 0 ? c.blocks_raygen : 1;
+  const BatchTable none{};
+  k_mat_hist<false><<<blocks, 256, 0, s>>>(sc, none, nullptr, hits, hq, wc, it, bins);
+  k_mat_scan<<<1, MAT_SORT_BINS, 0, s>>>(hq, wc, it, bins);
+  k_mat_scatter<false><<<blocks, 256, 0, s>>>(sc, none, nullptr, hits, hq, wc, it, bins);
+}
+
+void launch_material_sort_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, const uint4 *info,
+    const float4 *hits, HitQueues hq, WaveCounters wc, int it, uint32_t *bins)
+{
+  const int blocks = c.blocks_raygen > 0 ? c.blocks_raygen : 1;
+  k_mat_hist<true><<<blocks, 256, 0, s>>>(DevScene{}, bt, info, hits, hq, wc, it, bins);
+  k_mat_scan<<<1, MAT_SORT_BINS, 0, s>>>(hq, wc, it, bins);
+  k_mat_scatter<true><<<blocks, 256, 0, s>>>(DevScene{}, bt, info, hits, hq, wc, it, bins);
 }
 
 void launch_shadow_deferred(const LaunchCfg &c, cudaStream_t s, DevScene sc, ShadowSoA sh, WaveCounters wc, int it,

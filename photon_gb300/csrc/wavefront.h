@@ -92,10 +92,16 @@ inline size_t wave_counter_alloc_bytes(int max_iter) { return (wave_counter_word
 
 // Indices (into the iteration's path queue) of the paths whose closest-hit
 // query hit / missed, when the shading of misses and hits is split.
+// sorted / sort_threshold: when the iteration has at least sort_threshold
+// hits (0: never), the hit queue is also sorted by material into `sorted`
+// (launch_material_sort) and the hit-shading kernel reads that order.
 struct HitQueues {
   uint32_t *hitq;
   uint32_t *missq;
+  uint32_t *sorted = nullptr;
+  uint32_t sort_threshold = 0;
 };
+constexpr uint32_t MAT_SORT_BINS = 1024; // materials map to bin = id % MAT_SORT_BINS
 
 // Shading kernel variants: FULL compiles volumes, material sources and
 // analytic lights; PART 0 shades every path, 1 the hit queue, 2 the misses.
@@ -162,6 +168,13 @@ void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, Dev
     const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, ShadeVariant v, HitQueues hq);
 void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh, Accum acc,
     WaveCounters wc, int it, uint64_t *stats, int refill);
+// Counting sort of iteration it's hit queue by material (when hcount[it] >=
+// hq.sort_threshold): bins = 2 * MAT_SORT_BINS words of scratch.
+void launch_material_sort(const LaunchCfg &c, cudaStream_t s, DevScene sc, const float4 *hits, HitQueues hq,
+    WaveCounters wc, int it, uint32_t *bins);
+// Batched renders: bins by (job, material); info = the iteration's path info.
+void launch_material_sort_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, const uint4 *info,
+    const float4 *hits, HitQueues hq, WaveCounters wc, int it, uint32_t *bins);
 // Occlusion only: unoccluded rays keep tmax >= 0, occluded ones get tmax < 0.
 void launch_shadow_deferred(const LaunchCfg &c, cudaStream_t s, DevScene sc, ShadowSoA sh, WaveCounters wc, int it,
     int refill);

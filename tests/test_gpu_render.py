@@ -134,3 +134,24 @@ def test_empty_scene_renders_background(photon):
     c = r.read("color")
     assert np.allclose(c[..., :3], [0.25, 0.5, 0.75])
     assert np.all(np.isinf(r.read("depth")))
+
+
+def test_material_sorted_shading_keeps_images(photon):
+    """Shading the hit queue in material order changes no pixel."""
+    from photon_gb300 import tuning_get, tuning_set, workloads
+    sc, cam, st = workloads.procedural_500k()
+    st.width = st.height = 128
+    st.pixel_samples = 8
+    old = tuning_get("sort_threshold")
+    try:
+        imgs = []
+        for thr in (0, 1):
+            tuning_set("sort_threshold", thr)
+            r = photon.Renderer()
+            r.set_scene(sc)
+            r.render(cam, st, True)
+            imgs.append(r.read("color").copy())
+            r.close()
+        assert np.array_equal(imgs[0].view(np.uint32), imgs[1].view(np.uint32))
+    finally:
+        tuning_set("sort_threshold", old)
