@@ -322,28 +322,49 @@ __global__ void __launch_bounds__(MAT_SORT_BINS) k_mat_scan(HitQueues hq, WaveCo
   bins[MAT_SORT_BINS + b] = t[b] - bins[b];
 }
 
+// Scatter in chunks of 256 x MAT_SCATTER_PER_THREAD queue entries per block:
+// ranks within the chunk from shared-memory counters (warp-aggregated), then
+// one global atomic per (chunk, bin) reserves the chunk's run in that bin.
+constexpr uint32_t MAT_SCATTER_PER_THREAD = 8;
 template <bool BATCH>
 __global__ void __launch_bounds__(256) k_mat_scatter(DevScene sc, BatchTable bt, const uint4 *__restrict__ info,
     const float4 *__restrict__ hits, HitQueues hq, WaveCounters wc, int it, uint32_t *bins)
 {
+  __shared__ uint32_t cnt[MAT_SORT_BINS];
   const uint32_t n = wc.hcount[it];
   if (n < hq.sort_threshold)
     return;
   uint32_t *start = bins + MAT_SORT_BINS;
-  for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += gridDim.x * blockDim.x) {
-    const uint32_t i = base + lane_id();
-    const bool live = i < n;
-    const uint32_t q = live ? hq.hitq[i] : 0u;
-    const uint32_t bin = live ? hit_bin<BATCH>(sc, bt, info, hits, q) : 0xffffffffu;
-    __syncwarp();
-    const uint32_t grp = __match_any_sync(WARP_FULL, bin);
-    const uint32_t leader = uint32_t(__ffs(int(grp)) - 1);
-    uint32_t pos = 0;
-    if (live && lane_id() == leader)
-      pos = atomicAdd(&start[bin], uint32_t(__popc(grp)));
-    pos = __shfl_sync(WARP_FULL, pos, int(leader));
-    if (live)
-      hq.sorted[pos + uint32_t(__popc(grp & ((1u << lane_id()) - 1u)))] = q;
+  const uint32_t chunk = blockDim.x * MAT_SCATTER_PER_THREAD;
+  for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
+    for (uint32_t b = threadIdx.x; b < MAT_SORT_BINS; b += blockDim.x)
+      cnt[b] = 0u;
+    __syncthreads();
+    uint32_t q[MAT_SCATTER_PER_THREAD], bin[MAT_SCATTER_PER_THREAD], rank[MAT_SCATTER_PER_THREAD];
+#pragma unroll
+    for (uint32_t k = 0; k < MAT_SCATTER_PER_THREAD; ++k) {
+      const uint32_t i = c0 + k * blockDim.x + threadIdx.x;
+      const bool live = i < n;
+      q[k] = live ? hq.hitq[i] : 0u;
+      bin[k] = live ? hit_bin<BATCH>(sc, bt, info, hits, q[k]) : 0xffffffffu;
+      const uint32_t grp = __match_any_sync(WARP_FULL, bin[k]);
+      const uint32_t leader = uint32_t(__ffs(int(grp)) - 1);
+      uint32_t r = 0;
+      if (live && lane_id() == leader)
+        r = atomicAdd(&cnt[bin[k]], uint32_t(__popc(grp)));
+      r = __shfl_sync(WARP_FULL, r, int(leader));
+      rank[k] = r + uint32_t(__popc(grp & ((1u << lane_id()) - 1u)));
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < MAT_SORT_BINS; b += blockDim.x)
+      if (cnt[b])
+        cnt[b] = atomicAdd(&start[b], cnt[b]); // the chunk's run in bin b
+    __syncthreads();
+#pragma unroll
+    for (uint32_t k = 0; k < MAT_SCATTER_PER_THREAD; ++k)
+      if (bin[k] != 0xffffffffu)
+        hq.sorted[cnt[bin[k]] + rank[k]] = q[k];
+    __syncthreads();
   }
 }
 
