@@ -148,6 +148,32 @@ def trace(which, positions, indices, orgs, dirs, tmin, tmax, any_hit=False, norm
     return occ if any_hit else hits
 
 
+def adjoint_fp64(renderer, cam, settings, d_color, params, directions=(), sample_offset=0, h=1e-4):
+    """FP64 CPU adjoint (adjoint_fp64.inc) on a CpuRenderer("oracle") with a
+    scene: gradients of sum(d_color * I) for params [(kind, index, comp)]
+    (kind 0 material, 1 volume, 2 texels along directions[index])."""
+    if renderer.which != "oracle":
+        raise ValueError("the FP64 adjoint lives in the restatement oracle")
+    lib = renderer.lib
+    fn = lib.orc_adjoint_fp64
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+    d = np.ascontiguousarray(d_color, np.float32)
+    n = len(params)
+    kind = np.array([p[0] for p in params], np.int32)
+    index = np.array([p[1] for p in params], np.int32)
+    comp = np.array([p[2] for p in params], np.int32)
+    dirs = [np.ascontiguousarray(x, np.float32) for x in directions]
+    ptrs = (C.c_void_p * max(1, len(dirs)))(*[x.ctypes.data for x in dirs])
+    out = np.zeros(n, np.float64)
+    rc = fn(renderer.h, C.addressof(cam), C.addressof(settings), int(sample_offset), d.ctypes.data, n,
+            kind.ctypes.data, index.ctypes.data, comp.ctypes.data, C.addressof(ptrs), float(h), out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("orc_adjoint_fp64: " + renderer._fn("last_error")(renderer.h).decode())
+    return out
+
+
 def bsdf_probe(which, material, n_geo, n_shade, wo, wi, seeds):
     """Disney BSDF eval/pdf/sample at n cases (see ref_harness.cpp)."""
     prefix = "ref_" if which == "ref" else "orc_"

@@ -2628,3 +2628,6 @@ int orc_bsdf_probe(const phc_material *pm, const float *n_geo, const float *n_sh
 }
 
 } // extern "C"
+
+// FP64 CPU adjoint (test infrastructure): see the file's own header.
+#include "adjoint_fp64.inc"

@@ -29,6 +29,10 @@ int orc_bsdf_probe(const phc_material *m, const float *n_geo, const float *n_sha
    parity: renders sample index `sample_index` alone (spp 1, no adaptive). */
 int orc_render_sample(void *h, const phc_camera *cam, const phc_settings *settings, uint32_t sample_index,
     float *rgb_out);
+/* FP64 CPU adjoint of the image loss sum(d_color * I) (oracle/adjoint_fp64.inc). */
+int orc_adjoint_fp64(void *h, const phc_camera *camera, const phc_settings *settings, uint32_t sample_offset,
+    const float *d_color, uint32_t n_params, const int32_t *kind, const int32_t *index, const int32_t *comp,
+    const float *const *directions, double h_step, double *grad);
 
 #ifdef __cplusplus
 }

@@ -184,6 +184,43 @@ def test_fd_texel_directions(photon):
     assert np.all(np.abs(adj - fd) <= FD_REL_TOL * np.abs(fd) + 1e-6), (adj, fd)
 
 
+def test_gpu_adjoint_matches_fp64_cpu_adjoint(photon, oracle_lib):
+    """The GPU adjoint against the FP64 CPU adjoint (oracle/adjoint_fp64.inc:
+    the same paths replayed by the oracle, derivatives by central differences
+    in double of each weight's forward formula) on the same pixel samples:
+    every scalar material parameter, the medium's density and albedo, and the
+    texels along three random directions."""
+    sc, cam, st = _diff_small(res=16, spp=16)
+    wt = _weights(st.height, st.width)
+    g = _adjoint(photon, sc, cam, st, wt)
+    ref = oracle_lib.CpuRenderer("oracle")
+    ref.set_scene(sc)
+    params, gpu = [], []
+    for m in range(len(sc.materials)):
+        for k in range(3, 8):
+            params.append((0, m, k))
+            gpu.append(g["materials"][m, k])
+    for k in range(4):
+        params.append((1, 0, k))
+        gpu.append(g["volumes"][0, k])
+    rng = np.random.default_rng(3)
+    ntex = g["texels"].shape[0]
+    dirs = []
+    for d in range(3):
+        v = np.zeros((ntex, 4), np.float32)
+        v[:, :3] = rng.uniform(-1, 1, (ntex, 3))
+        dirs.append(v)
+        params.append((2, d, 0))
+        gpu.append(float(np.sum(g["texels"].astype(np.float64) * v)))
+    cpu = oracle_lib.adjoint_fp64(ref, cam, st, wt, params, dirs)
+    gpu = np.array(gpu, np.float64)
+    err = np.linalg.norm(gpu - cpu) / np.linalg.norm(cpu)
+    print("gpu", np.array2string(gpu, precision=4), "\nfp64", np.array2string(cpu, precision=4), "\nrel", err)
+    assert err <= 2e-3, err
+    scale = np.abs(cpu).max()
+    assert np.all(np.abs(gpu - cpu) <= 1e-2 * np.abs(cpu) + 1e-3 * scale), np.abs(gpu - cpu) / scale
+
+
 def test_adjoint_api_errors(photon):
     sc, cam, st = _diff_small(res=16, spp=2)
     r = photon.Renderer()
