@@ -1047,7 +1047,12 @@ __device__ __forceinline__ void adj_shade_path(const RenderConst &rc, const DevS
   }
 }
 
-__global__ void __launch_bounds__(128) k_adj_shade(const RenderConst *__restrict__ rcp, DevScene sc, AdjPathSoA in,
+// Minimum resident 128-thread blocks per SM for the replay shading kernel
+// (caps its registers; see k_shade).
+#ifndef PHC_ADJ_MIN_BLOCKS
+#define PHC_ADJ_MIN_BLOCKS 8
+#endif
+__global__ void __launch_bounds__(128, PHC_ADJ_MIN_BLOCKS) k_adj_shade(const RenderConst *__restrict__ rcp, DevScene sc, AdjPathSoA in,
     AdjPathSoA out, const float4 *__restrict__ hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a)
 {
   __shared__ float smat[MAX_SMEM_MATERIALS * NP];

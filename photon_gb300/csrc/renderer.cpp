@@ -553,6 +553,7 @@ LaunchCfg launch_cfg(phc_renderer *r, size_t raygen_items)
   cfg.threads = 128;
   cfg.blocks_trace = r->sm_count * std::max(1, std::min(tu.trace_blocks_per_sm, max_active_blocks(0, 128)));
   cfg.blocks_shade = r->sm_count * std::max(1, std::min(tu.shade_blocks_per_sm, max_active_blocks(1, 128)));
+  cfg.blocks_shade_lean = r->sm_count * std::max(1, std::min(tu.shade_blocks_per_sm, max_active_blocks(4, 128)));
   cfg.blocks_raygen = int(std::max<size_t>(1, std::min<size_t>((raygen_items + 255) / 256, size_t(r->sm_count) * 8)));
   return cfg;
 }

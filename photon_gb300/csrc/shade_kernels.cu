@@ -296,8 +296,18 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
 
 // BATCH: the path's job (PathSoA::info.w bits 17..) selects scene, constants
 // and accumulators, and travels with the continued path and its shadow ray.
+// Minimum resident 128-thread blocks per SM that the register allocation
+// must allow, per variant.  Shading is latency-bound (scattered path-state,
+// material and texture loads); a capped register count with some spilling
+// keeps more warps resident and hides more of that latency.
+#ifndef PHC_SHADE_MIN_BLOCKS_LEAN
+#define PHC_SHADE_MIN_BLOCKS_LEAN 12
+#endif
+#ifndef PHC_SHADE_MIN_BLOCKS_FULL
+#define PHC_SHADE_MIN_BLOCKS_FULL 16
+#endif
 template <bool FULL, int PART, bool BATCH>
-__global__ void __launch_bounds__(128) k_shade(const RenderConst *__restrict__ rcp, DevScene sc, BatchTable bt,
+__global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SHADE_MIN_BLOCKS_LEAN) k_shade(const RenderConst *__restrict__ rcp, DevScene sc, BatchTable bt,
     PathSoA in, PathSoA out, const float4 *__restrict__ hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it,
     HitQueues hq)
 {
@@ -352,7 +362,7 @@ __global__ void __launch_bounds__(128) k_shade(const RenderConst *__restrict__ r
 void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in, PathSoA out,
     const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, ShadeVariant v, HitQueues hq)
 {
-  const int b = c.blocks_shade;
+  const int b = v.full ? c.blocks_shade : c.blocks_shade_lean;
   const BatchTable none{};
   if (v.full) {
     if (v.part == 0)
@@ -374,7 +384,7 @@ void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, Dev
 void launch_shade_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA in, PathSoA out,
     const float4 *hits, ShadowSoA sh, WaveCounters wc, int it, ShadeVariant v, HitQueues hq)
 {
-  const int b = c.blocks_shade;
+  const int b = v.full ? c.blocks_shade : c.blocks_shade_lean;
   const DevScene sc{};
   const Accum acc{};
   if (v.full) {
@@ -394,10 +404,13 @@ void launch_shade_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathS
   }
 }
 
-int shade_max_active_blocks(int threads)
+int shade_max_active_blocks(int threads, bool full)
 {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade<true, 0, false>, threads, 0);
+  if (full)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade<true, 0, false>, threads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade<false, 1, false>, threads, 0);
   return n;
 }
 

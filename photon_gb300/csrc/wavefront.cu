@@ -698,14 +698,15 @@ void launch_read(cudaStream_t s, Frame fr, uint32_t npix, float inv_samples, int
   k_read<<<(npix + 255) / 256, 256, 0, s>>>(fr, npix, inv_samples, channel, out);
 }
 
-int shade_max_active_blocks(int threads);
+int shade_max_active_blocks(int threads, bool full);
 
 int max_active_blocks(int which, int threads)
 {
   int n = 0;
   switch (which) {
   case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace<false, true, false>, threads, 0); break;
-  case 1: n = shade_max_active_blocks(threads); break;
+  case 1: n = shade_max_active_blocks(threads, true); break;
+  case 4: n = shade_max_active_blocks(threads, false); break;
   case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<false, false>, threads, 0); break;
   default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raygen, threads, 0); break;
   }

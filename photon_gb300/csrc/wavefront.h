@@ -119,6 +119,7 @@ struct Frame {
 
 struct LaunchCfg {
   int blocks_trace, blocks_shade, blocks_raygen;
+  int blocks_shade_lean; // grid of the lean shading variant (its own occupancy)
   int threads;
 };
 
