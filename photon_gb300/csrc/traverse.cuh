@@ -94,6 +94,51 @@ PHC_HD float byte_f(uint32_t w, int j)
 #endif
 }
 
+#ifdef __CUDA_ARCH__
+// Paired fp32 arithmetic (sm_100+ .f32x2 forms): each element is rounded
+// exactly as the scalar instruction would round it, so the box tests below
+// make the same decisions as the host restatement with half the issue slots.
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi)
+{
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void upk2(unsigned long long v, float &lo, float &hi)
+{
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b)
+{
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+// 2^23 + byte j of w, as float bits (one byte permute)
+__device__ __forceinline__ float byte_f23(uint32_t w, int j)
+{
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + uint32_t(j)));
+}
+#endif
+
 // Intersects the 8 child boxes of one node; returns the k-ordered hit mask of
 // internal children (bit k = slot k ^ oct) and the triangle mask.
 PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V3 idir, uint32_t oct, float tmin,
@@ -123,6 +168,37 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
   const uint32_t fz0 = nzl ? w4.z : w3.x, fz1 = nzl ? w4.w : w3.y;
   hits = 0u;
   tri_hits = 0u;
+#ifdef __CUDA_ARCH__
+  // (near, far) of one axis as a pair: q = (2^23 + byte) - 2^23 exactly, then
+  // t = fma(q, a, b) per element.
+  const unsigned long long m23 = pk2(-8388608.f, -8388608.f);
+  const unsigned long long ax2 = pk2(ax, ax), ay2 = pk2(ay, ay), az2 = pk2(az, az);
+  const unsigned long long bx2 = pk2(bx, bx), by2 = pk2(by, by), bz2 = pk2(bz, bz);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const uint32_t m4 = h ? w1.w : w1.z;
+    const uint32_t nxw = h ? nx1 : nx0, fxw = h ? fx1 : fx0;
+    const uint32_t nyw = h ? ny1 : ny0, fyw = h ? fy1 : fy0;
+    const uint32_t nzw = h ? nz1 : nz0, fzw = h ? fz1 : fz0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t mb = (m4 >> (8 * j)) & 0xffu;
+      float tnx, tfx, tny, tfy, tnz, tfz;
+      upk2(fma2(add2(pk2(byte_f23(nxw, j), byte_f23(fxw, j)), m23), ax2, bx2), tnx, tfx);
+      upk2(fma2(add2(pk2(byte_f23(nyw, j), byte_f23(fyw, j)), m23), ay2, by2), tny, tfy);
+      upk2(fma2(add2(pk2(byte_f23(nzw, j), byte_f23(fzw, j)), m23), az2, bz2), tnz, tfz);
+      const float t0 = fmaxf(max3f(tnx, tny, tnz), tmin);
+      const float t1 = fminf(min3f(tfx, tfy, tfz), tmax);
+      if (mb != 0u && t0 <= t1 * 1.0000004f) {
+        const int s = 4 * h + j;
+        if (mb & 0x80u)
+          hits |= 1u << (uint32_t(s) ^ oct);
+        else
+          tri_hits |= ((1u << (mb >> 5)) - 1u) << (mb & 31u);
+      }
+    }
+  }
+#else
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const uint32_t m4 = h ? w1.w : w1.z;
@@ -149,6 +225,7 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
       }
     }
   }
+#endif
 }
 
 // Resumable traversal state of one ray: the current node group (child base,

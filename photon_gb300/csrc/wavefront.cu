@@ -186,8 +186,11 @@ __device__ __forceinline__ void record_cap(const WaveCounters &wc, uint32_t code
 // whole warp of finished lanes.  Each loop trip is one traversal step (one
 // node and the triangles of its hit leaves) of every busy lane.  With SPLIT
 // the finished queue positions also go to the hit or the miss index queue.
+#ifndef PHC_TRACE_MIN_BLOCKS
+#define PHC_TRACE_MIN_BLOCKS 8 // 64 registers: 8 resident 128-thread blocks per SM
+#endif
 template <bool COUNT, bool SPLIT, bool BATCH>
-__global__ void __launch_bounds__(128) k_trace(DevScene sc, BatchTable bt, PathSoA in, float4 *__restrict__ hits,
+__global__ void __launch_bounds__(128, PHC_TRACE_MIN_BLOCKS) k_trace(DevScene sc, BatchTable bt, PathSoA in, float4 *__restrict__ hits,
     WaveCounters wc, int it, uint64_t *stats, uint32_t refill, HitQueues hq)
 {
   const uint32_t n = wc.count[it];
