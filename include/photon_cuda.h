@@ -146,7 +146,56 @@ typedef struct phc_volume {
   int32_t linear;
 } phc_volume;
 
-/* Mirrors bridge::SceneData (RenderBridge.h:112-126). */
+/* Material at the path tracer's own level: the fields of
+   photon::pt::Material (include/photon/pt/material.h:35-82) that scenes built
+   without the bridge set, used as given (no bridge conversion: roughness is
+   not squared, specular is not halved, flags are taken as they are).  The
+   pbrt reader (pbrt_to_photon.cpp:98-170) produces these. */
+typedef struct phc_pt_material {
+  float base_color[3];
+  float metallic;
+  float roughness; /* as pt::Material::roughness */
+  float ior;
+  float transmission;
+  float specular; /* as pt::Material::specular (0.5 = Fresnel of ior) */
+  float clearcoat;
+  float clearcoat_roughness;
+  float sheen;
+  float alpha;
+  float emission[3];
+  float emission_strength;
+  int32_t flags;          /* pt MATERIAL_FLAG_* bits (material.h:28-32) */
+  int32_t base_color_tex; /* texture of the list below, or -1 */
+  int32_t alpha_tex;      /* texture of the list below (red channel), or -1 */
+} phc_pt_material;
+
+/* Texture of pt::TextureAtlas (include/photon/pt/texture.h:11-65): RGB,
+   row 0 = the top row of the image (v = 1), sampled bilinearly with repeat
+   wrapping. */
+typedef struct phc_texture {
+  uint32_t width;
+  uint32_t height;
+  const float *rgb; /* width*height*3 */
+} phc_texture;
+
+/* Scene data that only a scene built at the path tracer's level carries
+   (photon::pt::Scene, include/photon/pt/scene.h:40-70, as the pbrt reader
+   fills it).  With it the renderer takes `materials` instead of
+   phc_scene_desc::materials (same count, material_count) and ignores
+   phc_scene_desc::samplers and attributes. */
+typedef struct phc_pt_scene {
+  const phc_pt_material *materials; /* phc_scene_desc::material_count of them */
+  const float *texcoords;           /* uv per vertex, or NULL (uv = 0)        */
+  const phc_texture *textures;
+  uint32_t texture_count;
+  int32_t env_map_to_world_given;   /* 1: env_map_to_world is the map-to-world
+                                       rotation; 0: the transpose of
+                                       phc_environment::world_to_map */
+  float env_map_to_world[9];        /* row-major 3x3 */
+} phc_pt_scene;
+
+/* Mirrors bridge::SceneData (RenderBridge.h:112-126).  `pt` (may be NULL)
+   adds the path-tracer-level data of phc_pt_scene. */
 typedef struct phc_scene_desc {
   const float *positions; /* xyz per vertex */
   uint64_t vertex_count;
@@ -165,6 +214,7 @@ typedef struct phc_scene_desc {
   phc_environment environment;
   const phc_volume *volumes;
   uint32_t volume_count;
+  const phc_pt_scene *pt;
 } phc_scene_desc;
 
 /* Mirrors bridge::CameraData (RenderBridge.h:128-144). */

@@ -186,3 +186,93 @@ def bsdf_probe(which, material, n_geo, n_shade, wo, wi, seeds):
     getattr(lib, prefix + "bsdf_probe")(C.addressof(material), *[a.ctypes.data for a in arrs], s.ctypes.data, n,
                                         out.ctypes.data, out2.ctypes.data)
     return out, out2
+
+
+class RefPbrt:
+    """The reference's own pbrt path (parse_pbrt_file + convert_pbrt_scene +
+    PathTracer::render) from oracle/_ref/libphoton_ref.so.  Exists only where
+    the reference checkout was present at build time."""
+
+    COUNTS = ("triangles", "materials", "emissive", "textures", "lights", "width", "height", "spp",
+              "max_depth", "meshes", "named_materials", "object_defs", "object_instances", "has_env")
+
+    def __init__(self, path, use_instancing=False, width=0, height=0, spp=0, max_depth=0):
+        from photon_gb300 import _abi
+        self._abi = _abi
+        lib = _load(REF_LIB, "ref_")
+        vp = C.c_void_p
+        lib.ref_pbrt_load.restype = vp
+        lib.ref_pbrt_load.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        lib.ref_pbrt_free.argtypes = [vp]
+        for n in ("counts", "mesh", "materials", "emissive", "camera", "env", "render"):
+            getattr(lib, "ref_pbrt_" + n).restype = C.c_int
+        lib.ref_pbrt_counts.argtypes = [vp, vp]
+        lib.ref_pbrt_mesh.argtypes = [vp, vp, vp, vp, vp, vp]
+        lib.ref_pbrt_materials.argtypes = [vp, vp]
+        lib.ref_pbrt_emissive.argtypes = [vp, vp, vp]
+        lib.ref_pbrt_camera.argtypes = [vp, vp]
+        lib.ref_pbrt_env.argtypes = [vp, vp, vp, vp, vp]
+        lib.ref_pbrt_texture.argtypes = [vp, C.c_uint32, vp, vp]
+        lib.ref_pbrt_render.argtypes = [vp, C.c_int, C.c_int, vp]
+        self.lib = lib
+        self.h = lib.ref_pbrt_load(str(path).encode(), int(use_instancing), width, height, spp, max_depth)
+        c = np.zeros(len(self.COUNTS), np.uint64)
+        lib.ref_pbrt_counts(self.h, c.ctypes.data)
+        self.counts = dict(zip(self.COUNTS, (int(x) for x in c)))
+
+    def arrays(self) -> dict:
+        n = self.counts
+        nt = n["triangles"]
+        pos = np.zeros((3 * nt, 3), np.float32)
+        nrm = np.zeros((3 * nt, 3), np.float32)
+        uv = np.zeros((3 * nt, 2), np.float32)
+        mids = np.zeros(nt, np.uint32)
+        idx = np.zeros(3 * nt, np.uint32)
+        if nt:
+            self.lib.ref_pbrt_mesh(self.h, pos.ctypes.data, nrm.ctypes.data, uv.ctypes.data, mids.ctypes.data,
+                                   idx.ctypes.data)
+        mats = (self._abi.PtMaterial * max(n["materials"], 1))()
+        self.lib.ref_pbrt_materials(self.h, C.addressof(mats))
+        eids = np.zeros(n["emissive"], np.uint32)
+        eareas = np.zeros(n["emissive"], np.float32)
+        if n["emissive"]:
+            self.lib.ref_pbrt_emissive(self.h, eids.ctypes.data, eareas.ctypes.data)
+        cam = np.zeros(23, np.float32)
+        self.lib.ref_pbrt_camera(self.h, cam.ctypes.data)
+        wh = np.zeros(2, np.uint32)
+        w2t = np.zeros(9, np.float32)
+        t2w = np.zeros(9, np.float32)
+        self.lib.ref_pbrt_env(self.h, wh.ctypes.data, None, w2t.ctypes.data, t2w.ctypes.data)
+        env = None
+        if wh[0]:
+            px = np.zeros((int(wh[1]), int(wh[0]), 3), np.float32)
+            self.lib.ref_pbrt_env(self.h, wh.ctypes.data, px.ctypes.data, w2t.ctypes.data, t2w.ctypes.data)
+            env = {"pixels": px, "world_to_map": w2t.reshape(3, 3), "map_to_world": t2w.reshape(3, 3)}
+        tex = []
+        for i in range(n["textures"]):
+            twh = np.zeros(2, np.uint32)
+            self.lib.ref_pbrt_texture(self.h, i, twh.ctypes.data, None)
+            px = np.zeros((int(twh[1]), int(twh[0]), 3), np.float32)
+            self.lib.ref_pbrt_texture(self.h, i, twh.ctypes.data, px.ctypes.data)
+            tex.append(px)
+        return {"positions": pos, "normals": nrm, "texcoords": uv, "material_ids": mids,
+                "indices": idx.reshape(-1, 3), "materials": [mats[i] for i in range(n["materials"])],
+                "emissive_ids": eids, "emissive_areas": eareas, "camera": cam, "env": env, "textures": tex}
+
+    def render(self, adaptive=False, bottom_up=True) -> np.ndarray:
+        """(h, w, 3) radiance; row 0 = the bottom row when bottom_up."""
+        w, h = self.counts["width"], self.counts["height"]
+        out = np.zeros((h, w, 3), np.float32)
+        self.lib.ref_pbrt_render(self.h, int(adaptive), int(bottom_up), out.ctypes.data)
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.ref_pbrt_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -216,6 +216,7 @@ struct Mat { // material.h:35-82 (the fields the bridge fills)
   i32 flags{0};
   i32 base_color_alpha{0};
   i32 roughness_src_squared{0};
+  i32 base_color_tex{-1}, alpha_tex{-1};
 };
 inline V3 mat_emission(const Mat &m) { return m.emission * m.emission_strength; }
 inline bool may_emit(const Mat &m) // material.h:97-103 (no emission textures here)
@@ -269,6 +270,29 @@ Mat convert_material(const phc_material &in)
     m.flags |= F_EMIT_BOTH;
   else if (in.emission_side == 1)
     m.flags |= F_EMIT_BACK;
+  return m;
+}
+
+// A pt::Material given at the path tracer's level (pbrt_to_photon.cpp:98-170):
+// taken as it is, the other fields keep the Material{} defaults.
+Mat pt_material(const phc_pt_material &in, u32 texture_count)
+{
+  Mat m;
+  m.base_color = {in.base_color[0], in.base_color[1], in.base_color[2]};
+  m.metallic = in.metallic;
+  m.roughness = in.roughness;
+  m.ior = in.ior;
+  m.transmission = in.transmission;
+  m.specular = in.specular;
+  m.clearcoat = in.clearcoat;
+  m.clearcoat_roughness = in.clearcoat_roughness;
+  m.sheen = in.sheen;
+  m.alpha = in.alpha;
+  m.emission = {in.emission[0], in.emission[1], in.emission[2]};
+  m.emission_strength = in.emission_strength;
+  m.flags = in.flags & (F_EMITTER_ONLY | F_HIDDEN | F_EMIT_BOTH | F_REFRACTIVE | F_EMIT_BACK);
+  m.base_color_tex = texture_count ? (in.base_color_tex < 0 ? -1 : in.base_color_tex) : -1;
+  m.alpha_tex = texture_count ? (in.alpha_tex < 0 ? -1 : in.alpha_tex) : -1;
   return m;
 }
 
@@ -1382,6 +1406,10 @@ struct Scene {
   i32 attr_offset[5]{-1, -1, -1, -1, -1};
   std::vector<SInfo> samplers;
   std::vector<V4> texels;
+  // pt::TextureAtlas (texture.h:19-23): texel offset, width, height per texture
+  std::vector<u32> atlas_off, atlas_w, atlas_h;
+  std::vector<V3> atlas_px;
+  std::vector<V2> uv;   // mesh.texcoords, empty: none
   std::vector<Light> lights;
   bool has_env{false}, env_visible{true};
   Env env;
@@ -1528,10 +1556,55 @@ V3 apply_normal_map(const Scene &sc, const Src &src, const Query &q, const V3 &s
   return dot(n, n) > 0.f ? normalize(n) : sn;
 }
 inline f32 clamp01(f32 x) { return x < 0.f ? 0.f : (x > 1.f ? 1.f : x); }
+// TextureAtlas::sample, texture.h:25-64
+V3 atlas_sample(const Scene &sc, i32 tex_id, f32 u, f32 v)
+{
+  if (tex_id < 0 || u32(tex_id) >= sc.atlas_w.size())
+    return {1.f, 1.f, 1.f};
+  const u32 w = sc.atlas_w[u32(tex_id)], h = sc.atlas_h[u32(tex_id)];
+  if (w == 0 || h == 0)
+    return {1.f, 1.f, 1.f};
+  u = u - std::floor(u);
+  v = 1.f - (v - std::floor(v));
+  const f32 fx = u * f32(w) - 0.5f, fy = v * f32(h) - 0.5f;
+  const i32 ix = i32(std::floor(fx)), iy = i32(std::floor(fy));
+  const f32 tx = fx - std::floor(fx), ty = fy - std::floor(fy);
+  auto wrap = [](i32 i, u32 sz) -> u32 {
+    const i32 n = i32(sz);
+    return u32(((i % n) + n) % n);
+  };
+  const u32 x0 = wrap(ix, w), x1 = wrap(ix + 1, w), y0 = wrap(iy, h), y1 = wrap(iy + 1, h);
+  const u32 base = sc.atlas_off[u32(tex_id)];
+  const V3 c00 = sc.atlas_px[base + y0 * w + x0], c10 = sc.atlas_px[base + y0 * w + x1];
+  const V3 c01 = sc.atlas_px[base + y1 * w + x0], c11 = sc.atlas_px[base + y1 * w + x1];
+  const V3 top = c00 * (1.f - tx) + c10 * tx;
+  const V3 bot = c01 * (1.f - tx) + c11 * tx;
+  return top * (1.f - ty) + bot * ty;
+}
+
+// the hit's uv (mesh_intersector.h:146-163)
+V2 hit_uv(const Scene &sc, const Query &q)
+{
+  if (sc.uv.empty())
+    return {0.f, 0.f};
+  const u32 i0 = sc.mesh.idx[3 * q.prim], i1 = sc.mesh.idx[3 * q.prim + 1], i2 = sc.mesh.idx[3 * q.prim + 2];
+  const f32 w0 = 1.f - q.b1 - q.b2, w1 = q.b1, w2 = q.b2;
+  const V2 a = sc.uv[i0], b = sc.uv[i1], c = sc.uv[i2];
+  return {a.x * w0 + b.x * w1 + c.x * w2, a.y * w0 + b.y * w1 + c.y * w2};
+}
+
 Mat resolve_material(const Scene &sc, const Query &q, f32 &alpha)
 {
   Mat m = sc.mats[q.material_id];
   alpha = m.alpha;
+  const bool has_textures = !sc.atlas_w.empty(); // pathtracer.cpp:190-199
+  if (has_textures && (m.alpha_tex >= 0 || m.base_color_tex >= 0)) {
+    const V2 uv = hit_uv(sc, q);
+    if (m.alpha_tex >= 0)
+      alpha = atlas_sample(sc, m.alpha_tex, uv.x, uv.y).x;
+    if (m.base_color_tex >= 0)
+      m.base_color = atlas_sample(sc, m.base_color_tex, uv.x, uv.y);
+  }
   if (m.base_color_src.kind != K_CONST) {
     const V4 c = eval_source(sc, m.base_color_src, q);
     m.base_color = {std::fmax(c.x, 0.f), std::fmax(c.y, 0.f), std::fmax(c.z, 0.f)};
@@ -2079,9 +2152,10 @@ void build_scene(Scene &s, const phc_scene_desc &in)
     for (size_t i = 0; i < vc; ++i)
       s.mesh.nrm[i] = v3(&in.normals[3 * i]);
   }
+  const phc_pt_scene *pt = in.pt;
   size_t total = 0;
   for (int slot = 0; slot < 5; ++slot)
-    if (!empty && in.attributes[slot]) {
+    if (!pt && !empty && in.attributes[slot]) {
       s.attr_offset[slot] = int(total);
       total += vc;
     }
@@ -2093,13 +2167,31 @@ void build_scene(Scene &s, const phc_scene_desc &in)
     for (size_t i = 0; i < vc; ++i)
       s.attr_values[size_t(s.attr_offset[slot]) + i] = V4{src[4 * i], src[4 * i + 1], src[4 * i + 2], src[4 * i + 3]};
   }
-  for (u32 i = 0; i < in.material_count; ++i)
-    s.mats.push_back(convert_material(in.materials[i]));
+  if (pt) { // a scene at the path tracer's level: materials, atlas and uv as given
+    for (u32 i = 0; i < in.material_count; ++i)
+      s.mats.push_back(pt_material(pt->materials[i], pt->texture_count));
+    if (!empty && pt->texcoords)
+      for (size_t i = 0; i < vc; ++i)
+        s.uv.push_back(V2{pt->texcoords[2 * i], pt->texcoords[2 * i + 1]});
+    u32 off = 0;
+    for (u32 i = 0; i < pt->texture_count; ++i) {
+      const phc_texture &t = pt->textures[i];
+      s.atlas_off.push_back(off);
+      s.atlas_w.push_back(t.width);
+      s.atlas_h.push_back(t.height);
+      for (size_t k = 0; k < size_t(t.width) * t.height; ++k)
+        s.atlas_px.push_back(V3{t.rgb[3 * k], t.rgb[3 * k + 1], t.rgb[3 * k + 2]});
+      off += t.width * t.height;
+    }
+  } else {
+    for (u32 i = 0; i < in.material_count; ++i)
+      s.mats.push_back(convert_material(in.materials[i]));
+  }
   if (s.mats.empty())
     s.mats.push_back(Mat{});
   // samplers (RenderBridge.cpp:527-571)
   size_t offset = 0;
-  for (u32 i = 0; i < in.sampler_count; ++i) {
+  for (u32 i = 0; !pt && i < in.sampler_count; ++i) {
     const phc_sampler &sd = in.samplers[i];
     SInfo si;
     si.type = sd.type == 0 ? 0 : (sd.type == 2 ? 2 : (sd.type == 3 ? 3 : 1));
@@ -2151,6 +2243,8 @@ void build_scene(Scene &s, const phc_scene_desc &in)
         s.env.w2t[r * 3 + c] = env.world_to_map[r * 3 + c];
         s.env.t2w[c * 3 + r] = env.world_to_map[r * 3 + c];
       }
+    if (pt && pt->env_map_to_world_given) // pbrt_to_photon.cpp:455-466
+      std::memcpy(s.env.t2w, pt->env_map_to_world, sizeof(s.env.t2w));
     s.env.build_cdf();
     s.has_env = true;
     s.env_visible = env.visible != 0;

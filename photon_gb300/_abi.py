@@ -77,6 +77,28 @@ class Volume(C.Structure):
     ]
 
 
+class PtMaterial(C.Structure):
+    _fields_ = [
+        ("base_color", f3), ("metallic", C.c_float), ("roughness", C.c_float), ("ior", C.c_float),
+        ("transmission", C.c_float), ("specular", C.c_float), ("clearcoat", C.c_float),
+        ("clearcoat_roughness", C.c_float), ("sheen", C.c_float), ("alpha", C.c_float),
+        ("emission", f3), ("emission_strength", C.c_float), ("flags", C.c_int32),
+        ("base_color_tex", C.c_int32), ("alpha_tex", C.c_int32),
+    ]
+
+
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgb", C.POINTER(C.c_float))]
+
+
+class PtScene(C.Structure):
+    _fields_ = [
+        ("materials", C.POINTER(PtMaterial)), ("texcoords", C.POINTER(C.c_float)),
+        ("textures", C.POINTER(Texture)), ("texture_count", C.c_uint32),
+        ("env_map_to_world_given", C.c_int32), ("env_map_to_world", f9),
+    ]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [
         ("positions", C.POINTER(C.c_float)), ("vertex_count", C.c_uint64),
@@ -89,6 +111,7 @@ class SceneDesc(C.Structure):
         ("lights", C.POINTER(Light)), ("light_count", C.c_uint32),
         ("environment", Environment),
         ("volumes", C.POINTER(Volume)), ("volume_count", C.c_uint32),
+        ("pt", C.POINTER(PtScene)),
     ]
 
 

@@ -79,6 +79,10 @@ struct ApiError : std::runtime_error {
 
 } // namespace
 
+// The per-thread message of phc_global_error, for the other translation
+// units of the C-ABI (the pbrt reader).
+void phc::set_global_error(const std::string &msg) { g_error = msg; }
+
 struct phc_renderer {
   int device{0};
   int sm_count{0};
@@ -88,6 +92,7 @@ struct phc_renderer {
 
   DeviceScene scene;
   bool has_scene{false};
+  bool atlas_textures{false}; // a material reads a pt-level atlas texture
   uint64_t scene_generation{0};
 
   // wavefront buffers
@@ -935,6 +940,8 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
     throw ApiError(PHC_ERR_INVALID, "the adjoint takes every sample: adaptive sampling must be off");
   if (!g.materials)
     throw ApiError(PHC_ERR_INVALID, "null material gradient buffer");
+  if (r->atlas_textures)
+    throw ApiError(PHC_ERR_INVALID, "the adjoint does not differentiate atlas (pt-level) textures");
   const DevScene &sc = r->scene.dev;
   if (g.volumes && sc.volume_count > uint32_t(PHC_ADJ_MAX_VOLUMES))
     throw ApiError(PHC_ERR_LIMIT, "volume gradients for more than PHC_ADJ_MAX_VOLUMES volumes");
@@ -1214,6 +1221,9 @@ int phc_set_scene(phc_renderer *r, const phc_scene_desc *desc)
     const std::string err = r->scene.upload(hs, r->stream);
     if (!err.empty())
       throw ApiError(err.find("out of memory") != std::string::npos ? PHC_ERR_OOM : PHC_ERR_CUDA, err);
+    r->atlas_textures = false;
+    for (const DevMaterial &m : hs.materials)
+      r->atlas_textures = r->atlas_textures || m.base_tex >= 0 || m.alpha_tex >= 0;
     r->has_scene = true;
     r->scene_generation++;
   });

@@ -48,6 +48,8 @@ DevMaterial convert_material(const phc_material &in)
     m.src_index[k] = src[k]->index;
   }
   m.base_color_alpha = in.base_color_alpha ? 1 : 0;
+  m.base_tex = -1;
+  m.alpha_tex = -1;
   if (m.src_kind[SRC_ALPHA] != 0)
     m.alpha = 1.f;
   m.alpha_mode = in.alpha_mode == 0 ? 0 : (in.alpha_mode == 2 ? 2 : 1);
@@ -84,6 +86,34 @@ DevMaterial default_material()
   m.alpha_mode = 0;
   m.alpha_cutoff = 0.5f;
   m.flags = 0;
+  m.base_tex = -1;
+  m.alpha_tex = -1;
+  return m;
+}
+
+// A material of a scene built at the path tracer's level (the pbrt reader,
+// pbrt_to_photon.cpp:98-170): pt::Material as given, with its defaults for
+// the fields such scenes leave alone (material.h:35-82).
+DevMaterial pt_material(const phc_pt_material &in, uint32_t texture_count)
+{
+  DevMaterial m = default_material();
+  std::memcpy(m.base_color, in.base_color, sizeof(m.base_color));
+  m.metallic = in.metallic;
+  m.roughness = in.roughness;
+  m.ior = in.ior;
+  m.transmission = in.transmission;
+  m.specular = in.specular;
+  m.clearcoat = in.clearcoat;
+  m.clearcoat_roughness = in.clearcoat_roughness;
+  m.sheen = in.sheen;
+  m.alpha = in.alpha;
+  std::memcpy(m.emission, in.emission, sizeof(m.emission));
+  m.emission_strength = in.emission_strength;
+  m.flags = in.flags & (MF_EMITTER_ONLY | MF_HIDDEN | MF_EMIT_BOTH | MF_REFRACTIVE | MF_EMIT_BACK);
+  // TextureAtlas::sample returns white for an id past the list; with no
+  // textures at all the ids are not looked at (pathtracer.cpp:190-199)
+  m.base_tex = texture_count ? (in.base_color_tex < 0 ? -1 : in.base_color_tex) : -1;
+  m.alpha_tex = texture_count ? (in.alpha_tex < 0 ? -1 : in.alpha_tex) : -1;
   return m;
 }
 
@@ -326,24 +356,68 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     s.prim_vidx[4 * t + 3] = s.material_ids[t];
   }
   build_prim_records(pos3.data(), s.indices.data(), tc, s.prim_geo);
-  // attributes (RenderBridge.cpp:489-511)
-  size_t total = 0;
-  for (int slot = 0; slot < 5; ++slot)
-    if (!empty && in.attributes[slot]) {
-      s.attr_offset[slot] = int32_t(total);
-      total += vc;
+  const phc_pt_scene *pt = in.pt;
+  if (pt) {
+    if (in.material_count && !pt->materials)
+      throw std::invalid_argument("scene: pt materials pointer is null");
+    if (pt->texture_count && !pt->textures)
+      throw std::invalid_argument("scene: pt textures pointer is null");
+    // texture coordinates (mesh.texcoords) ride in attribute slot 0 as (u, v,
+    // 0, 1): its barycentric interpolation is the hit's uv
+    // (mesh_intersector.h:146-163)
+    if (!empty && pt->texcoords) {
+      s.attr_offset[0] = 0;
+      s.attr_values.resize(vc * 4);
+      for (size_t i = 0; i < vc; ++i) {
+        s.attr_values[4 * i] = pt->texcoords[2 * i];
+        s.attr_values[4 * i + 1] = pt->texcoords[2 * i + 1];
+        s.attr_values[4 * i + 2] = 0.f;
+        s.attr_values[4 * i + 3] = 1.f;
+      }
     }
-  s.attr_values.resize(total * 4);
-  for (int slot = 0; slot < 5; ++slot)
-    if (s.attr_offset[slot] >= 0)
-      std::memcpy(&s.attr_values[size_t(s.attr_offset[slot]) * 4], in.attributes[slot], vc * 16);
-  for (uint32_t i = 0; i < in.material_count; ++i)
-    s.materials.push_back(convert_material(in.materials[i]));
+    for (uint32_t i = 0; i < in.material_count; ++i)
+      s.materials.push_back(pt_material(pt->materials[i], pt->texture_count));
+  } else {
+    // attributes (RenderBridge.cpp:489-511)
+    size_t total = 0;
+    for (int slot = 0; slot < 5; ++slot)
+      if (!empty && in.attributes[slot]) {
+        s.attr_offset[slot] = int32_t(total);
+        total += vc;
+      }
+    s.attr_values.resize(total * 4);
+    for (int slot = 0; slot < 5; ++slot)
+      if (s.attr_offset[slot] >= 0)
+        std::memcpy(&s.attr_values[size_t(s.attr_offset[slot]) * 4], in.attributes[slot], vc * 16);
+    for (uint32_t i = 0; i < in.material_count; ++i)
+      s.materials.push_back(convert_material(in.materials[i]));
+  }
   if (s.materials.empty())
     s.materials.push_back(default_material());
-  // samplers (RenderBridge.cpp:527-571)
+  // samplers (RenderBridge.cpp:527-571); a pt scene has atlas textures
+  // (texture.h:11-65) in their place, RGB widened to float4
   size_t offset = 0;
-  for (uint32_t i = 0; i < in.sampler_count; ++i) {
+  for (uint32_t i = 0; pt && i < pt->texture_count; ++i) {
+    const phc_texture &td = pt->textures[i];
+    DevSampler si{};
+    si.type = 4;
+    si.size[0] = td.width;
+    si.size[1] = td.height;
+    si.size[2] = 1;
+    si.offset = uint32_t(offset);
+    const size_t n = size_t(td.width) * td.height;
+    if (n && !td.rgb)
+      throw std::invalid_argument("scene: texture pixels pointer is null");
+    for (size_t k = 0; k < n; ++k) {
+      s.texels.push_back(td.rgb[3 * k]);
+      s.texels.push_back(td.rgb[3 * k + 1]);
+      s.texels.push_back(td.rgb[3 * k + 2]);
+      s.texels.push_back(1.f);
+    }
+    offset += n;
+    s.samplers.push_back(si);
+  }
+  for (uint32_t i = 0; !pt && i < in.sampler_count; ++i) {
     const phc_sampler &sd = in.samplers[i];
     DevSampler si{};
     si.type = sd.type == 0 ? 0 : (sd.type == 2 ? 2 : (sd.type == 3 ? 3 : 1));
@@ -398,6 +472,8 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
         s.env_w2t[r * 3 + c] = env.world_to_map[r * 3 + c];
         s.env_t2w[c * 3 + r] = env.world_to_map[r * 3 + c];
       }
+    if (pt && pt->env_map_to_world_given) // pbrt_to_photon.cpp:455-466
+      std::memcpy(s.env_t2w, pt->env_map_to_world, sizeof(s.env_t2w));
     build_env_cdf(s);
     s.has_env = true;
     s.env_visible = env.visible != 0;
@@ -542,10 +618,13 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
     d.features |= SCENE_VOLUMES;
   if (!h.lights.empty())
     d.features |= SCENE_LIGHTS;
-  for (const DevMaterial &m : h.materials)
+  for (const DevMaterial &m : h.materials) {
     for (int k = 0; k < 7; ++k)
       if (m.src_kind[k] != 0)
         d.features |= SCENE_SOURCES;
+    if (m.base_tex >= 0 || m.alpha_tex >= 0)
+      d.features |= SCENE_SOURCES;
+  }
   node_bytes = uint64_t(h.bvh.nodes.size()) * 4;
   tri_bytes = uint64_t(h.bvh.tris.size()) * 4;
   bvh_depth = h.bvh.max_depth;

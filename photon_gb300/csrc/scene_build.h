@@ -13,6 +13,9 @@
 
 namespace phc {
 
+// Sets the message phc_global_error returns on this thread.
+void set_global_error(const std::string &msg);
+
 // Scene tables in host memory, exactly the content the reference's bridge
 // builds (RenderBridge.cpp:441-826) plus the light tables of
 // PathTracer::build_light_tables (pathtracer.cpp:411-503).

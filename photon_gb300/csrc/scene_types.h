@@ -44,7 +44,9 @@ struct DevMaterial {
   int32_t flags;
   int32_t thin;
   int32_t base_color_alpha;
-  int32_t pad_[3];
+  int32_t base_tex;  // atlas texture of the base colour (pt::Material::base_color_tex), -1: none
+  int32_t alpha_tex; // atlas texture of alpha (pt::Material::alpha_tex), -1: none
+  int32_t pad_;
 };
 
 enum : int32_t { SRC_BASE = 0, SRC_ALPHA = 1, SRC_METAL = 2, SRC_ROUGH = 3, SRC_EMIT = 4, SRC_TRANS = 5, SRC_NORMAL = 6 };
@@ -57,7 +59,7 @@ enum : int32_t {
 };
 
 struct DevSampler { // include/photon/pt/sampler.h:49-63
-  int32_t type; // 0 1D, 1 2D, 2 3D, 3 transform
+  int32_t type; // 0 1D, 1 2D, 2 3D, 3 transform, 4 atlas texture (pt::TextureAtlas entry)
   int32_t in_attribute;
   uint32_t linear;
   int32_t wrap[3];

@@ -516,9 +516,36 @@ static __device__ __noinline__ V3 apply_normal_map(const DevScene &sc, int32_t k
   const V3 n = normalize(t) * nm.x + normalize(b) * nm.y + sn * nm.z;
   return dot(n, n) > 0.f ? normalize(n) : sn;
 }
-// resolve_material, pathtracer.cpp:188-247 (seam materials: no atlas textures)
-// SRC = false: the scene has no attribute / sampler sources, the constants
-// are the parameters (the source branches are not compiled).
+// TextureAtlas::sample (include/photon/pt/texture.h:25-64): bilinear with
+// repeat wrapping, v = 1 at row 0; white for an id that is not a texture.
+__device__ __forceinline__ V3 atlas_sample(const DevScene &sc, int32_t tex, float u, float v)
+{
+  if (tex < 0 || uint32_t(tex) >= sc.sampler_count)
+    return V3{1.f, 1.f, 1.f};
+  const DevSampler &si = sc.samplers[uint32_t(tex)];
+  const uint32_t w = si.size[0], h = si.size[1];
+  if (si.type != 4 || w == 0u || h == 0u)
+    return V3{1.f, 1.f, 1.f};
+  u = u - floorf(u);
+  v = 1.f - (v - floorf(v));
+  const float fx = u * float(w) - 0.5f, fy = v * float(h) - 0.5f;
+  const int32_t ix = int32_t(floorf(fx)), iy = int32_t(floorf(fy));
+  const float tx = fx - floorf(fx), ty = fy - floorf(fy);
+  const int32_t sw = int32_t(w), sh = int32_t(h);
+  const uint32_t x0 = uint32_t(((ix % sw) + sw) % sw), x1 = uint32_t((((ix + 1) % sw) + sw) % sw);
+  const uint32_t y0 = uint32_t(((iy % sh) + sh) % sh), y1 = uint32_t((((iy + 1) % sh) + sh) % sh);
+  const float4 *px = sc.texels + si.offset;
+  const float4 c00 = __ldg(px + y0 * w + x0), c10 = __ldg(px + y0 * w + x1);
+  const float4 c01 = __ldg(px + y1 * w + x0), c11 = __ldg(px + y1 * w + x1);
+  const V3 top = v3(c00) * (1.f - tx) + v3(c10) * tx;
+  const V3 bot = v3(c01) * (1.f - tx) + v3(c11) * tx;
+  return top * (1.f - ty) + bot * ty;
+}
+
+// resolve_material, pathtracer.cpp:188-247.  Atlas textures (pt-level
+// scenes) read the hit's uv from attribute slot 0.
+// SRC = false: the scene has no attribute / sampler / atlas sources, the
+// constants are the parameters (the source branches are not compiled).
 template <bool SRC>
 static __device__ __noinline__ Mat resolve_material(const DevScene &sc, const DevMaterial &dm, const Query &q, float &alpha)
 {
@@ -537,6 +564,13 @@ static __device__ __noinline__ Mat resolve_material(const DevScene &sc, const De
   m.flags = dm.flags;
   m.thin = dm.thin;
   alpha = dm.alpha;
+  if (SRC && (dm.alpha_tex >= 0 || dm.base_tex >= 0)) {
+    const float4 uv = fetch_attribute(sc, 0, q);
+    if (dm.alpha_tex >= 0)
+      alpha = atlas_sample(sc, dm.alpha_tex, uv.x, uv.y).x;
+    if (dm.base_tex >= 0)
+      m.base_color = atlas_sample(sc, dm.base_tex, uv.x, uv.y);
+  }
   if (SRC && dm.src_kind[SRC_BASE] != 0) {
     const float4 c = eval_source(sc, dm.src_kind[SRC_BASE], dm.src_index[SRC_BASE], q);
     m.base_color = V3{fmaxf(c.x, 0.f), fmaxf(c.y, 0.f), fmaxf(c.z, 0.f)};

@@ -189,7 +189,7 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
       upk2(fma2(add2(pk2(byte_f23(nzw, j), byte_f23(fzw, j)), m23), az2, bz2), tnz, tfz);
       const float t0 = fmaxf(max3f(tnx, tny, tnz), tmin);
       const float t1 = fminf(min3f(tfx, tfy, tfz), tmax);
-      if (mb != 0u && t0 <= t1 * 1.0000004f) {
+      if (t0 <= t1 * 1.0000004f) { // an empty slot (mb 0) adds nothing
         const int s = 4 * h + j;
         if (mb & 0x80u)
           hits |= 1u << (uint32_t(s) ^ oct);
@@ -216,7 +216,7 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
       const float tfz = fmaf(byte_f(fzw, j), az, bz);
       const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
       const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
-      if (mb != 0u && t0 <= t1 * 1.0000004f) {
+      if (t0 <= t1 * 1.0000004f) { // an empty slot (mb 0) adds nothing
         const int s = 4 * h + j;
         if (mb & 0x80u)
           hits |= 1u << (uint32_t(s) ^ oct);

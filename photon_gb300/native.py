@@ -1,4 +1,5 @@
-"""Loads libphoton_cuda.so and declares the C-ABI of include/photon_cuda.h.
+"""Loads libphoton_cuda.so and declares the C-ABI of include/photon_cuda.h and
+include/photon_pbrt.h.
 
 The product path has no fallback: when the library is missing or fails to
 load, every entry point raises.
@@ -13,7 +14,7 @@ from . import _abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libphoton_cuda.so")
 
-# name -> (restype, argtypes); every symbol include/photon_cuda.h declares.
+# name -> (restype, argtypes); every symbol the headers in include/ declare.
 vp = C.c_void_p
 SIGNATURES = {
     "phc_material_default": (None, [vp]),
@@ -51,6 +52,13 @@ SIGNATURES = {
     "phc_trace_closest_compact_static": (C.c_int, [vp, vp, vp, vp, vp, C.c_uint32, vp, vp]),
     "phc_tuning_set": (C.c_int, [C.c_char_p, C.c_int64]),
     "phc_tuning_get": (C.c_int64, [C.c_char_p]),
+    # include/photon_pbrt.h
+    "phc_pbrt_load": (C.c_int, [C.c_char_p, vp, C.POINTER(vp)]),
+    "phc_pbrt_free": (None, [vp]),
+    "phc_pbrt_scene_desc": (C.c_int, [vp, C.POINTER(vp)]),
+    "phc_pbrt_camera": (C.c_int, [vp, vp]),
+    "phc_pbrt_settings": (C.c_int, [vp, vp]),
+    "phc_pbrt_info_get": (C.c_int, [vp, vp]),
 }
 
 _lib = None

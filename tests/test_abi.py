@@ -12,12 +12,15 @@ from photon_gb300 import _abi
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "photon_cuda.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("photon_cuda.h", "photon_pbrt.h")]
 
 
 def header_functions():
-    text = open(HEADER).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(phc_[a-z0-9_]+)\s*\(", text)))
+    names = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names |= set(re.findall(r"\b(phc_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
 
 
 def test_library_exports_every_header_function(photon):
@@ -39,6 +42,7 @@ STRUCTS = {
     "phc_light": _abi.Light, "phc_environment": _abi.Environment, "phc_volume": _abi.Volume,
     "phc_scene_desc": _abi.SceneDesc, "phc_camera": _abi.Camera, "phc_settings": _abi.Settings,
     "phc_render_stats": _abi.RenderStats, "phc_hit_result": _abi.HitResult, "phc_job": _abi.Job,
+    "phc_pt_material": _abi.PtMaterial, "phc_texture": _abi.Texture, "phc_pt_scene": _abi.PtScene,
 }
 
 
