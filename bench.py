@@ -17,7 +17,10 @@ Our arm prints one JSON line with
   roofline   the dominant kernel's algorithmic bytes / its event-timed
              duration against the measured HBM copy bandwidth;
   cpu_baseline  the CPU oracle (a restatement of the reference's algorithm)
-             on the host cores, on a bounded sample of the same workload.
+             on the host cores, on a bounded sample of the same workload;
+  batched_vs_plain, adjoint, instancing  the batched mode against one call
+             at a time, the path-replay adjoint against the forward pass, and
+             the two-level BVH against flattened placements (each skippable).
 --impl reference times that CPU implementation as the main line.
 Under torchrun (N > 1) every rank renders its own replica (the path is
 replicated, not sharded) and rank 0 prints the line.
@@ -297,6 +300,45 @@ def adjoint_vs_forward(p, reps=3):
             "grad_volume": g["volumes"][0].tolist()}
 
 
+def instancing_vs_flat(p, reps=3):
+    """Instanced geometry (four objects of 12-1280 triangles placed by random
+    rotations, non-uniform scales and translations over a lit ground plane,
+    1024^2, 16 spp, depth 6): the two-level BVH8 against the same placements
+    flattened into world-space triangles (the reference's single-level
+    handling), 2,000 placements; and the two-level form at 20,000 placements,
+    where flattening would hold 18M triangles.  Device time per render,
+    Msamples/s, device memory of the scene and upload time."""
+    import torch
+
+    from photon_gb300 import workloads
+    out = {}
+    for name, n, flat in (("flat_2k", 2000, True), ("instanced_2k", 2000, False), ("instanced_20k", 20000, False)):
+        sc, cam, st = workloads.instanced_objects(n_instances=n, res=1024, spp=16, flatten=flat)
+        r = p.Renderer()
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        t = time.perf_counter()
+        r.set_scene(sc)
+        upload = time.perf_counter() - t
+        scene_mb = (free0 - torch.cuda.mem_get_info()[0]) / 2 ** 20
+        r.render(cam, st, True)
+        ms = []
+        for _ in range(reps):
+            r.render(cam, st, True)
+            ms.append(r.stats()["render_ms"])
+        m = sorted(ms)[len(ms) // 2]
+        placed = sc.triangle_count if flat else sc.triangle_count + sum(
+            len(sc.pt.objects[o]["indices"]) for o, _ in sc.pt.instances)
+        out[name] = {"placements": n, "placed_triangles": int(placed), "render_ms": m,
+                     "msamples_per_s": st.width * st.height * st.pixel_samples / (m / 1e3) / 1e6,
+                     "scene_device_mb": scene_mb, "upload_s": upload,
+                     "image_mean": float(r.read("color")[..., :3].mean())}
+        r.close()
+    out["instanced_over_flat_time"] = out["instanced_2k"]["render_ms"] / out["flat_2k"]["render_ms"]
+    out["flat_over_instanced_memory"] = out["flat_2k"]["scene_device_mb"] / max(out["instanced_2k"]["scene_device_mb"], 1e-3)
+    return out
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -448,6 +490,10 @@ def run_ours(args, world, rank, local):
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_vs_forward(p)
         _log("adjoint/forward done")
+    instancing = None
+    if rank == 0 and not args.no_instancing:
+        instancing = instancing_vs_flat(p)
+        _log("instancing/flat done")
 
     if rank == 0:
         h2d = C.sizeof(cam) + C.sizeof(st)
@@ -468,6 +514,7 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "batched_vs_plain": batched,
             "adjoint": adjoint,
+            "instancing": instancing,
             "clocks": clk.summary(),
             "gpu_launches": launches,
         }
@@ -484,6 +531,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched/plain measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
+    ap.add_argument("--no-instancing", action="store_true", help="skip the instanced/flattened measurement")
     args = ap.parse_args()
     world, rank, local = dist_setup(args.gpus if args.impl == "ours" else 0)
     if args.impl == "reference":

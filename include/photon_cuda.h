@@ -178,6 +178,23 @@ typedef struct phc_texture {
   const float *rgb; /* width*height*3 */
 } phc_texture;
 
+/* One object of instanced geometry (include/photon/pt/scene.h:22-28,
+   ObjectMesh): a triangle mesh in its own space with one material. */
+typedef struct phc_object {
+  const float *positions;  /* xyz per vertex */
+  uint64_t vertex_count;
+  const uint32_t *indices; /* three per triangle */
+  uint64_t triangle_count;
+  const float *normals;    /* xyz per vertex, or NULL */
+  uint32_t material_id;
+} phc_object;
+
+/* One placement of an object (scene.h:30-33, Instance). */
+typedef struct phc_instance {
+  uint32_t object_id;
+  float transform[16]; /* object to world, column-major (pbrt order) */
+} phc_instance;
+
 /* Scene data that only a scene built at the path tracer's level carries
    (photon::pt::Scene, include/photon/pt/scene.h:40-70, as the pbrt reader
    fills it).  With it the renderer takes `materials` instead of
@@ -192,6 +209,17 @@ typedef struct phc_pt_scene {
                                        rotation; 0: the transpose of
                                        phc_environment::world_to_map */
   float env_map_to_world[9];        /* row-major 3x3 */
+  /* Instanced geometry (scene.h:35-39, InstancedGeometry), traced as a
+     two-level BVH beside the scene's own triangles instead of being
+     flattened into them.  Hits on instances report, as the reference's
+     instanced back-end does (backend/optix/photon_optix.cu:68-99, 161-187),
+     the object's material, object-space normals carried to world space by
+     the inverse transpose of the instance transform, and the barycentrics
+     as texture coordinates; instances are not light sources. */
+  const phc_object *objects;
+  uint32_t object_count;
+  const phc_instance *instances;
+  uint32_t instance_count;
 } phc_pt_scene;
 
 /* Mirrors bridge::SceneData (RenderBridge.h:112-126).  `pt` (may be NULL)

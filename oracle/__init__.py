@@ -259,6 +259,32 @@ class RefPbrt:
                 "indices": idx.reshape(-1, 3), "materials": [mats[i] for i in range(n["materials"])],
                 "emissive_ids": eids, "emissive_areas": eareas, "camera": cam, "env": env, "textures": tex}
 
+    def instanced(self) -> dict:
+        """ConvertedScene::instanced_geometry: objects (positions, indices,
+        normals, material id) and instances (object id, column-major 4x4)."""
+        lib, vp = self.lib, C.c_void_p
+        lib.ref_pbrt_ig_counts.argtypes = [vp, vp]
+        lib.ref_pbrt_ig_object.argtypes = [vp, C.c_uint32, vp, vp, vp, vp]
+        lib.ref_pbrt_ig_instance.argtypes = [vp, C.c_uint32, vp, vp]
+        c = np.zeros(2, np.uint64)
+        lib.ref_pbrt_ig_counts(self.h, c.ctypes.data)
+        objs = []
+        for i in range(int(c[0])):
+            sz = np.zeros(4, np.uint64)
+            lib.ref_pbrt_ig_object(self.h, i, sz.ctypes.data, None, None, None)
+            pos = np.zeros(int(sz[0]), np.float32)
+            idx = np.zeros(int(sz[1]), np.int32)
+            nrm = np.zeros(int(sz[2]), np.float32)
+            lib.ref_pbrt_ig_object(self.h, i, sz.ctypes.data, pos.ctypes.data, idx.ctypes.data, nrm.ctypes.data)
+            objs.append({"positions": pos, "indices": idx, "normals": nrm, "material_id": int(sz[3])})
+        insts = []
+        for i in range(int(c[1])):
+            oid = np.zeros(1, np.uint32)
+            xf = np.zeros(16, np.float32)
+            lib.ref_pbrt_ig_instance(self.h, i, oid.ctypes.data, xf.ctypes.data)
+            insts.append((int(oid[0]), xf))
+        return {"objects": objs, "instances": insts}
+
     def render(self, adaptive=False, bottom_up=True) -> np.ndarray:
         """(h, w, 3) radiance; row 0 = the bottom row when bottom_up."""
         w, h = self.counts["width"], self.counts["height"]

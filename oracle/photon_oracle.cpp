@@ -1201,11 +1201,13 @@ struct Mesh {
   Bvh bvh;
 };
 
+constexpr u32 NO_INST = 0xffffffffu;
 struct Hit {
   bool hit{false};
   f32 t{0.f};
   u32 prim{0};
   f32 u{0.f}, v{0.f};
+  u32 inst{NO_INST}; // instance of an instanced hit
 };
 
 // mesh_intersector.h:30-45
@@ -1318,6 +1320,39 @@ HitAttr hit_attributes(const Mesh &m, const V3 &o, const V3 &d, const Hit &h)
   return a;
 }
 
+// Instanced geometry (scene.h:18-39) as the reference's instanced back-end
+// traces it (optix_backend.cpp:502-590, photon_optix.cu:68-99 and 161-187):
+// the ray is carried into the object's space by the instance's
+// world-to-object rows, the object's own BVH is intersected there (t keeps
+// its meaning: the direction is not renormalised), and the hit's normals go
+// back through the inverse transpose of the instance transform.
+struct Obj {
+  Mesh mesh;
+  u32 material{0};
+};
+struct Inst {
+  u32 obj{0};
+  f32 w2o[12]; // rows of the world-to-object 3x4 matrix
+  Aabb box;    // world bounds (padded)
+};
+inline V3 xf_point(const f32 *m, const V3 &p)
+{
+  return {m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3], m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+      m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]};
+}
+inline V3 xf_dir(const f32 *m, const V3 &d)
+{
+  return {m[0] * d.x + m[1] * d.y + m[2] * d.z, m[4] * d.x + m[5] * d.y + m[6] * d.z,
+      m[8] * d.x + m[9] * d.y + m[10] * d.z};
+}
+// n' = M^T n for the world-to-object rows M: the inverse transpose of the
+// object-to-world transform
+inline V3 xf_normal(const f32 *m, const V3 &n)
+{
+  return {m[0] * n.x + m[4] * n.y + m[8] * n.z, m[1] * n.x + m[5] * n.y + m[9] * n.z,
+      m[2] * n.x + m[6] * n.y + m[10] * n.z};
+}
+
 // ----------------------------------------------------------------- camera
 struct Cam { // camera.h:11-160
   V3 origin, lower_left, horizontal, vertical, u, v, w;
@@ -1418,7 +1453,47 @@ struct Scene {
   std::vector<f32> emissive_cdf, prim_light_pdf;
   u32 strategy_count{0};
   f32 eps{1e-3f};
+  std::vector<Obj> objs; // instanced geometry
+  std::vector<Inst> insts;
 };
+
+// Closest (or any) hit over the scene's triangles and every instance.
+Hit intersect_scene(const Scene &sc, const V3 &o, const V3 &d, f32 tmin, f32 tmax, bool any_hit)
+{
+  Hit best = intersect(sc.mesh, o, d, tmin, tmax, any_hit);
+  if (sc.insts.empty() || (any_hit && best.hit))
+    return best;
+  auto inv1 = [](f32 x) { return 1.f / (std::fabs(x) > 1e-20f ? x : (x < 0.f ? -1e-20f : 1e-20f)); };
+  const V3 inv{inv1(d.x), inv1(d.y), inv1(d.z)};
+  for (u32 i = 0; i < u32(sc.insts.size()); ++i) {
+    const Inst &in = sc.insts[i];
+    if (entry_distance(in.box, o, inv, tmin, best.t) < 0.f)
+      continue;
+    Hit h = intersect(sc.objs[in.obj].mesh, xf_point(in.w2o, o), xf_dir(in.w2o, d), tmin, best.t, any_hit);
+    if (!h.hit)
+      continue;
+    h.inst = i;
+    best = h;
+    if (any_hit)
+      return best;
+  }
+  return best;
+}
+
+// Hit attributes; an instanced hit's in object space, its normals carried to
+// world space and normalised (photon_optix.cu:68-99, 183-186).
+HitAttr hit_attributes_scene(const Scene &sc, const V3 &o, const V3 &d, const Hit &h)
+{
+  if (h.inst == NO_INST)
+    return hit_attributes(sc.mesh, o, d, h);
+  const Inst &in = sc.insts[h.inst];
+  const Obj &ob = sc.objs[in.obj];
+  HitAttr a = hit_attributes(ob.mesh, o, d, h);
+  a.n = normalize(xf_normal(in.w2o, a.n));
+  a.sn = normalize(xf_normal(in.w2o, a.sn));
+  a.material_id = ob.material;
+  return a;
+}
 
 struct Params {
   u32 w, h, spp, max_depth, sample_offset;
@@ -1441,6 +1516,7 @@ struct Query {
   u32 prim{0}, material_id{0};
   f32 b1{0.f}, b2{0.f};
   V3 p, sn;
+  u32 inst{NO_INST};
 };
 V4 fetch_attribute(const Scene &sc, i32 slot, const Query &q)
 {
@@ -1448,7 +1524,7 @@ V4 fetch_attribute(const Scene &sc, i32 slot, const Query &q)
     return {q.p, 1.f};
   if (slot == 6)
     return {q.sn, 1.f};
-  if (!(slot >= 0 && slot < 5 && sc.attr_offset[slot] >= 0))
+  if (!(slot >= 0 && slot < 5 && sc.attr_offset[slot] >= 0) || q.inst != NO_INST) // instances carry none
     return {0.f, 0.f, 0.f, 1.f};
   const u32 base = u32(sc.attr_offset[slot]);
   const V4 a0 = sc.attr_values[base + sc.mesh.idx[q.prim * 3 + 0]];
@@ -1599,7 +1675,7 @@ Mat resolve_material(const Scene &sc, const Query &q, f32 &alpha)
   alpha = m.alpha;
   const bool has_textures = !sc.atlas_w.empty(); // pathtracer.cpp:190-199
   if (has_textures && (m.alpha_tex >= 0 || m.base_color_tex >= 0)) {
-    const V2 uv = hit_uv(sc, q);
+    const V2 uv = q.inst != NO_INST ? V2{q.b1, q.b2} : hit_uv(sc, q); // an instance's uv: its barycentrics
     if (m.alpha_tex >= 0)
       alpha = atlas_sample(sc, m.alpha_tex, uv.x, uv.y).x;
     if (m.base_color_tex >= 0)
@@ -1836,7 +1912,7 @@ void render_pixel_sample(const Scene &sc, const Cam &cam, const Params &pr, u32 
 
     for (u32 it = 0; it < max_iterations && active; ++it) {
       // trace_closest (kokkos_backend.cpp:21-61)
-      const Hit hr = intersect(sc.mesh, ro, rd, tmin, tmax, false);
+      const Hit hr = intersect_scene(sc, ro, rd, tmin, tmax, false);
       V3 nee_contrib;
       bool nee_active = false;
       V3 sh_o, sh_d;
@@ -1935,7 +2011,7 @@ void render_pixel_sample(const Scene &sc, const Cam &cam, const Params &pr, u32 
           active = false;
           return;
         }
-        const HitAttr ha = hit_attributes(sc.mesh, ro, rd, hr);
+        const HitAttr ha = hit_attributes_scene(sc, ro, rd, hr);
         const V3 p = ha.p;
         const V3 wo = -rd;
         V3 hit_sn = ha.sn;
@@ -1945,6 +2021,7 @@ void render_pixel_sample(const Scene &sc, const Cam &cam, const Params &pr, u32 
           hit_sn = hit_sn * -1.f;
         Query q;
         q.prim = hr.prim;
+        q.inst = hr.inst;
         q.material_id = ha.material_id;
         q.b1 = hr.u;
         q.b2 = hr.v;
@@ -1995,7 +2072,7 @@ void render_pixel_sample(const Scene &sc, const Cam &cam, const Params &pr, u32 
         if (may_emit(mat) && emits_on_side(mat, front)) {
           f32 w_mis = 1.f;
           if (prev_pdf > 0.f && !sc.emissive_cdf.empty()) {
-            const f32 pdf_area = sc.prim_light_pdf[hr.prim];
+            const f32 pdf_area = hr.inst == NO_INST ? sc.prim_light_pdf[hr.prim] : 0.f; // instances are no lights
             const f32 cos_light = std::fabs(dot(ha.n, wo));
             if (pdf_area > 0.f && cos_light > 0.f) {
               const f32 light_pdf = pdf_area * hr.t * hr.t / cos_light / f32(sc.strategy_count);
@@ -2078,7 +2155,7 @@ void render_pixel_sample(const Scene &sc, const Cam &cam, const Params &pr, u32 
 
       // ---- trace_occluded + pt_nee_accum_pack (pathtracer.cpp:1092-1123)
       if (nee_active) {
-        const Hit occ = intersect(sc.mesh, sh_o, sh_d, sh_tmin, sh_tmax, true);
+        const Hit occ = intersect_scene(sc, sh_o, sh_d, sh_tmin, sh_tmax, true);
         if (!occ.hit) {
           V3 contrib = nee_contrib;
           if (has_volumes) {
@@ -2248,6 +2325,72 @@ void build_scene(Scene &s, const phc_scene_desc &in)
     s.env.build_cdf();
     s.has_env = true;
     s.env_visible = env.visible != 0;
+  }
+  // instanced geometry: objects in their own space, each with its BVH; per
+  // placement the world-to-object rows (inverted in double, then rounded)
+  // and padded world bounds
+  if (pt && pt->instance_count && pt->object_count) {
+    const u32 nm = u32(s.mats.size());
+    for (u32 o = 0; o < pt->object_count; ++o) {
+      const phc_object &ob = pt->objects[o];
+      Obj obj;
+      if (ob.triangle_count && ob.vertex_count) {
+        for (size_t v = 0; v < ob.vertex_count; ++v) {
+          obj.mesh.pos.push_back(v3(&ob.positions[3 * v]));
+          if (ob.normals)
+            obj.mesh.nrm.push_back(v3(&ob.normals[3 * v]));
+        }
+        obj.mesh.idx.assign(ob.indices, ob.indices + 3 * ob.triangle_count);
+        obj.mesh.bvh.build(obj.mesh.pos, obj.mesh.idx);
+      }
+      obj.material = ob.material_id < nm ? ob.material_id : 0u;
+      s.objs.push_back(std::move(obj));
+    }
+    for (u32 i = 0; i < pt->instance_count; ++i) {
+      const phc_instance &in = pt->instances[i];
+      if (in.object_id >= pt->object_count || s.objs[in.object_id].mesh.idx.empty())
+        continue;
+      double m[3][4];
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c)
+          m[r][c] = double(in.transform[c * 4 + r]);
+      const double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+          m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) + m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+      if (!(std::fabs(det) > 1e-30) || !std::isfinite(det))
+        continue;
+      const double id = 1.0 / det;
+      double inv[3][3];
+      inv[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]) * id;
+      inv[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+      inv[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+      inv[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) * id;
+      inv[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+      inv[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
+      inv[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]) * id;
+      inv[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
+      inv[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
+      Inst it;
+      it.obj = in.object_id;
+      for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c)
+          it.w2o[r * 4 + c] = f32(inv[r][c]);
+        it.w2o[r * 4 + 3] = f32(-(inv[r][0] * m[0][3] + inv[r][1] * m[1][3] + inv[r][2] * m[2][3]));
+      }
+      const Mesh &om = s.objs[in.object_id].mesh;
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, ext = 0.0;
+      for (const V3 &p : om.pos)
+        for (int r = 0; r < 3; ++r) {
+          const double w = m[r][0] * p.x + m[r][1] * p.y + m[r][2] * p.z + m[r][3];
+          lo[r] = std::min(lo[r], w);
+          hi[r] = std::max(hi[r], w);
+        }
+      for (int r = 0; r < 3; ++r)
+        ext = std::max(ext, std::max(std::fabs(lo[r]), std::fabs(hi[r])));
+      const double pad = 1e-5 * ext + 1e-30;
+      it.box.lo = V3{f32(lo[0] - pad), f32(lo[1] - pad), f32(lo[2] - pad)};
+      it.box.hi = V3{f32(hi[0] + pad), f32(hi[1] + pad), f32(hi[2] + pad)};
+      s.insts.push_back(it);
+    }
   }
   // volumes with macro-cell majorants (RenderBridge.cpp:622-778)
   size_t value_offset = 0, tf_offset = 0;

@@ -194,6 +194,47 @@ int ref_pbrt_texture(void *hv, uint32_t i, uint32_t *wh, float *rgb)
   return 0;
 }
 
+// Instanced geometry of the conversion (ConvertedScene::instanced_geometry):
+// counts of objects and instances.
+int ref_pbrt_ig_counts(void *hv, uint64_t *out)
+{
+  const auto &ig = static_cast<RefPbrt *>(hv)->conv.instanced_geometry;
+  out[0] = ig.objects.size();
+  out[1] = ig.instances.size();
+  return 0;
+}
+
+// Object i: sizes (position floats, indices, normal floats, material id),
+// then the arrays when the pointers are not null.
+int ref_pbrt_ig_object(void *hv, uint32_t i, uint64_t *sizes, float *pos, int32_t *idx, float *nrm)
+{
+  const auto &ig = static_cast<RefPbrt *>(hv)->conv.instanced_geometry;
+  if (i >= ig.objects.size())
+    return -1;
+  const auto &o = ig.objects[i];
+  sizes[0] = o.positions.size();
+  sizes[1] = o.indices.size();
+  sizes[2] = o.normals.size();
+  sizes[3] = o.material_id;
+  if (pos)
+    std::memcpy(pos, o.positions.data(), o.positions.size() * sizeof(float));
+  if (idx)
+    std::memcpy(idx, o.indices.data(), o.indices.size() * sizeof(int32_t));
+  if (nrm)
+    std::memcpy(nrm, o.normals.data(), o.normals.size() * sizeof(float));
+  return 0;
+}
+
+int ref_pbrt_ig_instance(void *hv, uint32_t i, uint32_t *object_id, float *xf16)
+{
+  const auto &ig = static_cast<RefPbrt *>(hv)->conv.instanced_geometry;
+  if (i >= ig.instances.size())
+    return -1;
+  *object_id = ig.instances[i].object_id;
+  std::memcpy(xf16, ig.instances[i].transform, 16 * sizeof(float));
+  return 0;
+}
+
 // Renders the converted scene; rgb gets width*height*3 floats, row 0 first.
 int ref_pbrt_render(void *hv, int adaptive, int bottom_up, float *rgb)
 {

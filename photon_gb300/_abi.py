@@ -91,11 +91,25 @@ class Texture(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgb", C.POINTER(C.c_float))]
 
 
+class Object(C.Structure):
+    _fields_ = [
+        ("positions", C.POINTER(C.c_float)), ("vertex_count", C.c_uint64),
+        ("indices", C.POINTER(C.c_uint32)), ("triangle_count", C.c_uint64),
+        ("normals", C.POINTER(C.c_float)), ("material_id", C.c_uint32),
+    ]
+
+
+class Instance(C.Structure):
+    _fields_ = [("object_id", C.c_uint32), ("transform", C.c_float * 16)]
+
+
 class PtScene(C.Structure):
     _fields_ = [
         ("materials", C.POINTER(PtMaterial)), ("texcoords", C.POINTER(C.c_float)),
         ("textures", C.POINTER(Texture)), ("texture_count", C.c_uint32),
         ("env_map_to_world_given", C.c_int32), ("env_map_to_world", f9),
+        ("objects", C.POINTER(Object)), ("object_count", C.c_uint32),
+        ("instances", C.POINTER(Instance)), ("instance_count", C.c_uint32),
     ]
 
 

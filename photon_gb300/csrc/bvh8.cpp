@@ -236,6 +236,11 @@ struct Collapse {
 
   void emit_tri(uint32_t prim)
   {
+    if (!pos) { // box primitives: the leaf lists primitive ids
+      out.leaf_prims.push_back(prim);
+      out.tri_count++;
+      return;
+    }
     const float *v0 = &pos[3 * size_t(idx[3 * size_t(prim) + 0])];
     const float *v1 = &pos[3 * size_t(idx[3 * size_t(prim) + 1])];
     const float *v2 = &pos[3 * size_t(idx[3 * size_t(prim) + 2])];
@@ -376,6 +381,31 @@ struct Collapse {
 
 } // namespace
 
+namespace {
+
+// SAH BVH2 over the references, collapsed into `out`; triangle records when
+// positions is set, leaf primitive ids otherwise.
+void build_from_refs(Builder2 &b, const float *positions, const uint32_t *indices, Bvh8Host &out)
+{
+  const uint32_t n = uint32_t(b.refs.size());
+  b.nodes.resize(size_t(n) * 2 + 2);
+  b.next = 1;
+#pragma omp parallel
+#pragma omp single
+  b.build(0, 0, n, 0);
+  b.nodes.resize(b.next.load());
+
+  Collapse c{b.nodes, b.refs, positions, indices, out};
+  c.root_area = std::max(b.nodes[0].b.area(), 1e-30);
+  if (positions)
+    out.tris.reserve(size_t(n) * 12);
+  const uint32_t root = c.alloc_nodes(1);
+  c.fill(root, 0, 1);
+  out.sah_cost = c.sah;
+}
+
+} // namespace
+
 void build_bvh8(const float *positions, uint64_t vertex_count, const uint32_t *indices, uint64_t triangle_count,
     Bvh8Host &out, int max_leaf)
 {
@@ -399,19 +429,29 @@ void build_bvh8(const float *positions, uint64_t vertex_count, const uint32_t *i
       r.c[a] = 0.5f * (r.b.lo[a] + r.b.hi[a]);
     r.id = uint32_t(i);
   }
-  b.nodes.resize(size_t(n) * 2 + 2);
-  b.next = 1;
-#pragma omp parallel
-#pragma omp single
-  b.build(0, 0, n, 0);
-  b.nodes.resize(b.next.load());
+  build_from_refs(b, positions, indices, out);
+}
 
-  Collapse c{b.nodes, b.refs, positions, indices, out};
-  c.root_area = std::max(b.nodes[0].b.area(), 1e-30);
-  out.tris.reserve(size_t(n) * 12);
-  const uint32_t root = c.alloc_nodes(1);
-  c.fill(root, 0, 1);
-  out.sah_cost = c.sah;
+void build_bvh8_boxes(const float *boxes, uint64_t count, Bvh8Host &out, int max_leaf)
+{
+  out = Bvh8Host{};
+  if (count == 0)
+    throw std::runtime_error("build_bvh8_boxes: no boxes");
+  if (count > 0x7fffffffull)
+    throw std::runtime_error("build_bvh8_boxes: too many boxes");
+  Builder2 b;
+  b.max_leaf = std::min(std::max(max_leaf, 1), 3);
+  b.refs.resize(size_t(count));
+  for (size_t i = 0; i < count; ++i) {
+    Ref &r = b.refs[i];
+    r.b = Box{};
+    r.b.grow(&boxes[6 * i]);
+    r.b.grow(&boxes[6 * i + 3]);
+    for (int a = 0; a < 3; ++a)
+      r.c[a] = 0.5f * (r.b.lo[a] + r.b.hi[a]);
+    r.id = uint32_t(i);
+  }
+  build_from_refs(b, nullptr, nullptr, out);
 }
 
 void build_prim_records(const float *positions, const uint32_t *indices, uint64_t triangle_count,

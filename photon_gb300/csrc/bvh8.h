@@ -31,6 +31,7 @@ namespace phc {
 struct Bvh8Host {
   std::vector<uint32_t> nodes; // 20 u32 per node
   std::vector<float> tris;     // 12 floats per triangle record, leaf order
+  std::vector<uint32_t> leaf_prims; // box builds: primitive id per leaf entry, leaf order
   uint32_t node_count{0};
   uint32_t tri_count{0};
   uint32_t max_depth{0};
@@ -42,6 +43,11 @@ struct Bvh8Host {
 // reference).  max_leaf is the largest triangle count of one leaf child (1..3).
 void build_bvh8(const float *positions, uint64_t vertex_count, const uint32_t *indices, uint64_t triangle_count,
     Bvh8Host &out, int max_leaf = 3);
+
+// Builds the BVH8 over axis-aligned boxes (lo xyz, hi xyz per primitive):
+// the top level over instances.  Leaf children address `leaf_prims` (the
+// box ids in leaf order) where a triangle build addresses its records.
+void build_bvh8_boxes(const float *boxes, uint64_t count, Bvh8Host &out, int max_leaf = 1);
 
 // Per-primitive triangle records (v0, e1, e2 as in the leaf records) in
 // primitive order, for shading.

@@ -101,7 +101,11 @@ struct Parsed {
   std::map<std::string, NamedMaterial> materials;
   std::vector<Mesh> meshes;
   std::map<std::string, std::vector<Mesh>> objects;
-  uint64_t instances{0};
+  struct Placement {
+    std::string object;
+    float xf[16];
+  };
+  std::vector<Placement> instances; // every ObjectInstance of a defined object
   std::string env_file;
   float env_xf[16];
   float env_scale{1.f};
@@ -865,7 +869,10 @@ Parsed parse(const std::string &path, bool use_instancing)
       const auto it = sc.objects.find(name);
       if (it == sc.objects.end())
         continue;
-      ++sc.instances;
+      Parsed::Placement pl;
+      pl.object = name;
+      std::memcpy(pl.xf, st.xf, sizeof(st.xf));
+      sc.instances.push_back(pl);
       if (use_instancing || total_tris >= kMaxTotalTriangles)
         continue;
       uint64_t &count = inst_count[name];
@@ -1037,6 +1044,14 @@ struct phc_pbrt_scene {
   std::vector<std::vector<float>> texture_pixels;
   std::vector<phc_texture> textures;
   std::vector<float> env_pixels;
+  // instanced geometry (use_instancing): merged objects and placements
+  struct ObjectData {
+    std::vector<float> positions, normals;
+    std::vector<uint32_t> indices;
+  };
+  std::vector<ObjectData> object_data;
+  std::vector<phc_object> objects;
+  std::vector<phc_instance> instances;
   phc_pt_scene pt{};
   phc_scene_desc desc{};
   phc_camera camera{};
@@ -1046,7 +1061,7 @@ struct phc_pbrt_scene {
 
 namespace {
 
-void convert(const Parsed &ps, const std::string &base, phc_pbrt_scene &out)
+void convert(const Parsed &ps, const std::string &base, bool use_instancing, phc_pbrt_scene &out)
 {
   // textures: every imagemap with a file name is loaded; the atlas holds the
   // loaded ones in name order (pbrt_to_photon.cpp:62-90)
@@ -1250,6 +1265,64 @@ void convert(const Parsed &ps, const std::string &base, phc_pbrt_scene &out)
       out.pt.env_map_to_world_given = 1;
     }
   }
+  // instanced geometry (pbrt_to_photon.cpp:470-503): each object's
+  // sub-meshes merged in object space (their own transforms unused), normals
+  // only when every sub-mesh has them, the last sub-mesh's material; one
+  // placement per ObjectInstance.  Only with use_instancing: otherwise the
+  // instances are flattened into the mesh above, as the reference's
+  // single-level back-end renders them.
+  if (use_instancing && !ps.objects.empty() && !ps.instances.empty()) {
+    std::map<std::string, uint32_t> obj_id;
+    for (const auto &kv : ps.objects) {
+      obj_id[kv.first] = uint32_t(out.object_data.size());
+      phc_pbrt_scene::ObjectData od;
+      uint32_t mid = 0, voff = 0;
+      size_t nsum = 0, psum = 0;
+      for (const Mesh &m : kv.second) {
+        const auto it = mat_id.find(m.material);
+        mid = it != mat_id.end() ? it->second : 0u;
+        od.positions.insert(od.positions.end(), m.P.begin(), m.P.end());
+        for (int v : m.indices) {
+          if (v < 0 || size_t(v) >= m.P.size() / 3)
+            throw std::out_of_range("pbrt: vertex index out of range in an object");
+          od.indices.push_back(uint32_t(v) + voff);
+        }
+        if (m.N.size() >= m.P.size())
+          od.normals.insert(od.normals.end(), m.N.begin(), m.N.begin() + std::ptrdiff_t(m.P.size()));
+        nsum += m.N.size() >= m.P.size() ? m.P.size() : 0;
+        psum += m.P.size();
+        voff += uint32_t(m.P.size() / 3);
+      }
+      if (nsum < psum)
+        od.normals.clear();
+      out.object_data.push_back(std::move(od));
+      phc_object ob{};
+      ob.material_id = mid;
+      out.objects.push_back(ob);
+    }
+    for (size_t o = 0; o < out.objects.size(); ++o) {
+      const auto &od = out.object_data[o];
+      phc_object &ob = out.objects[o];
+      ob.positions = od.positions.data();
+      ob.vertex_count = od.positions.size() / 3;
+      ob.indices = od.indices.data();
+      ob.triangle_count = od.indices.size() / 3;
+      ob.normals = od.normals.empty() ? nullptr : od.normals.data();
+    }
+    for (const auto &pl : ps.instances) {
+      const auto it = obj_id.find(pl.object);
+      if (it == obj_id.end())
+        continue;
+      phc_instance in{};
+      in.object_id = it->second;
+      std::memcpy(in.transform, pl.xf, sizeof(in.transform));
+      out.instances.push_back(in);
+    }
+    out.pt.objects = out.objects.data();
+    out.pt.object_count = uint32_t(out.objects.size());
+    out.pt.instances = out.instances.data();
+    out.pt.instance_count = uint32_t(out.instances.size());
+  }
   d.pt = &out.pt;
 
   // camera: LookAt, else the inverse of the camera transform
@@ -1301,7 +1374,7 @@ void convert(const Parsed &ps, const std::string &base, phc_pbrt_scene &out)
   in.textures = ps.textures.size();
   in.loaded_textures = out.textures.size();
   in.object_defs = ps.objects.size();
-  in.object_instances = ps.instances;
+  in.object_instances = ps.instances.size();
   in.triangles = d.triangle_count;
   in.emissive_triangles = emissive;
   in.width = s.width;
@@ -1347,7 +1420,7 @@ int phc_pbrt_load(const char *path, const phc_pbrt_options *options, phc_pbrt_sc
         ps.max_depth = options->max_depth;
     }
     auto sc = std::make_unique<phc_pbrt_scene>();
-    convert(ps, dir_of(path), *sc);
+    convert(ps, dir_of(path), instancing, *sc);
     *out = sc.release();
     return PHC_OK;
   } catch (const std::bad_alloc &) {

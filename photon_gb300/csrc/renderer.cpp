@@ -98,6 +98,7 @@ struct phc_renderer {
   // wavefront buffers
   size_t cap_paths{0};
   Buf st_o[2], st_d[2], st_tp[2], st_info[2], st_dist[2], hits, sh_a, sh_b, sh_c, hitq, missq, hitq_sorted;
+  Buf hit_inst; // instance slot per hit (scenes with instances)
   Buf sort_bins; // per bounce iteration: material-sort counts and starts
   size_t cap_slots{0};
   Buf acc, acc_sq, acc_start, nsamp, aov_n, aov_a;
@@ -246,6 +247,7 @@ void ensure_paths(phc_renderer *r, size_t n)
   ck(r->hitq.ensure(n * 4), "alloc hit queue");
   ck(r->missq.ensure(n * 4), "alloc miss queue");
   ck(r->hitq_sorted.ensure(n * 4), "alloc sorted hit queue");
+  ck(r->hit_inst.ensure(n * 4), "alloc hit instances");
   ck(r->sh_a.ensure(n * 16), "alloc shadow queue");
   ck(r->sh_b.ensure(n * 16), "alloc shadow queue");
   ck(r->sh_c.ensure(n * 16), "alloc shadow queue");
@@ -371,6 +373,7 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
   const bool full = (sc.features & (SCENE_VOLUMES | SCENE_SOURCES | SCENE_LIGHTS)) != 0 || !tu.shade_lean;
   const bool split = (sc.features & SCENE_VOLUMES) == 0 && tu.split_shade;
   HitQueues hq = split ? HitQueues{r->hitq.as<uint32_t>(), r->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
+  hq.inst = r->hit_inst.as<uint32_t>();
   const bool sort = split && tu.sort_threshold > 0;
   const size_t bin_words = size_t(2) * MAT_SORT_BINS;
   if (sort) { // sort_bins sized by ensure_wave_buffers (no allocation while a graph is captured)
@@ -790,10 +793,11 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
     throw ApiError(PHC_ERR_LIMIT, "more than 32768 jobs in one batch");
   check_device(lead);
   cudaStream_t s = lead->stream;
-  // adaptive sampling needs the samples of a pixel in order: such jobs run
-  // through their own render path first
+  // adaptive sampling needs the samples of a pixel in order, and the batched
+  // kernels trace single-level scenes: such jobs run through their own
+  // render path first
   for (uint32_t i = 0; i < n; ++i) {
-    if (jobs[i].settings->adaptive_sampling) {
+    if (jobs[i].settings->adaptive_sampling || (jobs[i].renderer->has_scene && jobs[i].renderer->scene.dev.inst_count)) {
       render_impl(jobs[i].renderer, *jobs[i].camera, *jobs[i].settings, jobs[i].reset != 0);
       continue;
     }
@@ -942,6 +946,8 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
     throw ApiError(PHC_ERR_INVALID, "null material gradient buffer");
   if (r->atlas_textures)
     throw ApiError(PHC_ERR_INVALID, "the adjoint does not differentiate atlas (pt-level) textures");
+  if (r->scene.dev.inst_count)
+    throw ApiError(PHC_ERR_INVALID, "the adjoint does not trace instanced geometry");
   const DevScene &sc = r->scene.dev;
   if (g.volumes && sc.volume_count > uint32_t(PHC_ADJ_MAX_VOLUMES))
     throw ApiError(PHC_ERR_LIMIT, "volume gradients for more than PHC_ADJ_MAX_VOLUMES volumes");

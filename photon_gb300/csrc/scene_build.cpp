@@ -297,6 +297,228 @@ void build_volumes(const phc_scene_desc &in, HostScene &s)
 
 } // namespace
 
+// Appends bottom level `b` (node and triangle indices rebased, triangle
+// records' primitive ids offset by prim_base) to the combined arrays.
+uint32_t append_blas(Bvh8Host &all, const Bvh8Host &b, uint32_t prim_base)
+{
+  const uint32_t node_off = all.node_count, tri_off = all.tri_count;
+  const size_t n0 = all.nodes.size();
+  all.nodes.insert(all.nodes.end(), b.nodes.begin(), b.nodes.end());
+  for (size_t k = n0; k < all.nodes.size(); k += 20) {
+    all.nodes[k + 4] += node_off; // child base (read only where imask has bits)
+    all.nodes[k + 5] += tri_off;  // triangle base
+  }
+  const size_t t0 = all.tris.size();
+  all.tris.insert(all.tris.end(), b.tris.begin(), b.tris.end());
+  for (size_t k = t0; k < all.tris.size(); k += 12) {
+    uint32_t id;
+    std::memcpy(&id, &all.tris[k + 3], 4);
+    id += prim_base;
+    std::memcpy(&all.tris[k + 3], &id, 4);
+  }
+  all.node_count += b.node_count;
+  all.tri_count += b.tri_count;
+  all.max_depth = std::max(all.max_depth, b.max_depth);
+  return node_off;
+}
+
+// Two-level BVH of a pt scene with instanced geometry (scene.h:18-39): the
+// objects' triangles are appended to the vertex and primitive arrays in
+// object space, each object gets its own bottom level, and the top level
+// holds one leaf per instance plus one for the scene's own triangles (an
+// identity placement), the layout of the reference's instanced back-end
+// (optix_backend.cpp:502-590) on this renderer's BVH8.
+void build_instancing(const phc_pt_scene &pt, bool has_scene_tris, const float lo[3], const float hi[3],
+    HostScene &s, int max_leaf)
+{
+  const uint32_t n_obj = pt.object_count;
+  if (!pt.objects)
+    throw std::invalid_argument("scene: objects pointer is null");
+  if (!pt.instances)
+    throw std::invalid_argument("scene: instances pointer is null");
+  const uint32_t material_count = uint32_t(s.materials.size());
+  const size_t vc0 = s.positions4.size() / 4;
+  bool any_normals = s.scene_normals;
+  for (uint32_t o = 0; o < n_obj; ++o)
+    any_normals = any_normals || (pt.objects[o].normals && pt.objects[o].triangle_count);
+  if (any_normals && s.normals4.empty())
+    s.normals4.assign(vc0 * 4, 0.f);
+
+  // bottom levels: the scene's triangles, then every object with triangles
+  Bvh8Host all;
+  all.node_count = 0;
+  Bvh8Host scene_blas = std::move(s.bvh);
+  std::vector<uint32_t> obj_root(n_obj, 0u), obj_flags(n_obj, 0u);
+  std::vector<char> obj_ok(n_obj, 0);
+  std::vector<uint64_t> obj_tris(n_obj, 0u);
+  std::vector<Bvh8Host> blas(n_obj);
+  std::vector<uint32_t> obj_prim_base(n_obj, 0u);
+  for (uint32_t o = 0; o < n_obj; ++o) {
+    const phc_object &ob = pt.objects[o];
+    if (ob.triangle_count == 0 || ob.vertex_count == 0)
+      continue;
+    if (!ob.positions || !ob.indices)
+      throw std::invalid_argument("scene: object positions/indices pointer is null");
+    if (ob.triangle_count > 0x3fffffffull || ob.vertex_count > 0xffffffffull)
+      throw std::length_error("scene: object too large");
+    for (size_t i = 0; i < ob.triangle_count * 3; ++i)
+      if (ob.indices[i] >= ob.vertex_count)
+        throw std::out_of_range("scene: object vertex index out of range");
+    const uint32_t prim_base = uint32_t(s.prim_vidx.size() / 4);
+    const uint32_t vbase = uint32_t(s.positions4.size() / 4);
+    if (uint64_t(prim_base) + ob.triangle_count > 0x3fffffffull)
+      throw std::length_error("scene: too many primitives");
+    for (size_t v = 0; v < ob.vertex_count; ++v) {
+      for (int a = 0; a < 3; ++a)
+        s.positions4.push_back(ob.positions[3 * v + a]);
+      s.positions4.push_back(0.f);
+      if (any_normals) {
+        for (int a = 0; a < 3; ++a)
+          s.normals4.push_back(ob.normals ? ob.normals[3 * v + a] : 0.f);
+        s.normals4.push_back(0.f);
+      }
+    }
+    const uint32_t mat = ob.material_id < material_count ? ob.material_id : 0u;
+    for (size_t t = 0; t < ob.triangle_count; ++t) {
+      s.prim_vidx.push_back(vbase + ob.indices[3 * t]);
+      s.prim_vidx.push_back(vbase + ob.indices[3 * t + 1]);
+      s.prim_vidx.push_back(vbase + ob.indices[3 * t + 2]);
+      s.prim_vidx.push_back(mat);
+    }
+    std::vector<float> geo;
+    build_prim_records(ob.positions, ob.indices, ob.triangle_count, geo);
+    for (size_t t = 0; t < ob.triangle_count; ++t) { // record ids are global primitive ids
+      const uint32_t id = prim_base + uint32_t(t);
+      std::memcpy(&geo[12 * t + 3], &id, 4);
+    }
+    s.prim_geo.insert(s.prim_geo.end(), geo.begin(), geo.end());
+    build_bvh8(ob.positions, ob.vertex_count, ob.indices, ob.triangle_count, blas[o], max_leaf);
+    obj_flags[o] = ob.normals ? INST_NORMALS : 0u;
+    obj_ok[o] = 1;
+    obj_tris[o] = ob.triangle_count;
+    obj_prim_base[o] = prim_base;
+  }
+
+  // top-level entries: the scene's triangles (identity), then the instances
+  struct Entry {
+    uint32_t object; // n_obj: the scene's triangles
+    double w2o[12];
+    float box[6];
+  };
+  std::vector<Entry> ent;
+  if (has_scene_tris) {
+    Entry e{};
+    e.object = n_obj;
+    e.w2o[0] = e.w2o[5] = e.w2o[10] = 1.0;
+    for (int a = 0; a < 3; ++a) {
+      e.box[a] = lo[a];
+      e.box[3 + a] = hi[a];
+    }
+    ent.push_back(e);
+  }
+  for (uint32_t i = 0; i < pt.instance_count; ++i) {
+    const phc_instance &in = pt.instances[i];
+    if (in.object_id >= n_obj || !obj_ok[in.object_id])
+      continue; // as the reference's back-end skips them (optix_backend.cpp:511-513)
+    // object-to-world rows from the column-major transform
+    double m[3][4];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 4; ++c)
+        m[r][c] = double(in.transform[c * 4 + r]);
+    const double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+        m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) + m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    if (!(std::fabs(det) > 1e-30) || !std::isfinite(det))
+      continue; // a singular placement has no world-to-object map
+    Entry e{};
+    e.object = in.object_id;
+    const double id = 1.0 / det;
+    double inv[3][3];
+    inv[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]) * id;
+    inv[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+    inv[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+    inv[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) * id;
+    inv[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+    inv[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
+    inv[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]) * id;
+    inv[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
+    inv[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
+    for (int r = 0; r < 3; ++r) {
+      for (int c = 0; c < 3; ++c)
+        e.w2o[r * 4 + c] = inv[r][c];
+      e.w2o[r * 4 + 3] = -(inv[r][0] * m[0][3] + inv[r][1] * m[1][3] + inv[r][2] * m[2][3]);
+    }
+    // world box of the placed vertices (tight, unlike the transformed object
+    // box), padded so float rounding of the transform never shrinks it below
+    // the placed geometry
+    const phc_object &obd = pt.objects[in.object_id];
+    double wl[3] = {1e300, 1e300, 1e300}, wh[3] = {-1e300, -1e300, -1e300};
+    for (size_t v = 0; v < obd.vertex_count; ++v) {
+      const float *p = &obd.positions[3 * v];
+      for (int r = 0; r < 3; ++r) {
+        const double w = m[r][0] * p[0] + m[r][1] * p[1] + m[r][2] * p[2] + m[r][3];
+        wl[r] = std::min(wl[r], w);
+        wh[r] = std::max(wh[r], w);
+      }
+    }
+    double ext = 0.0;
+    for (int r = 0; r < 3; ++r)
+      ext = std::max(ext, std::max(std::fabs(wl[r]), std::fabs(wh[r])));
+    const double pad = 1e-5 * ext + 1e-30;
+    for (int r = 0; r < 3; ++r) {
+      e.box[r] = float(wl[r] - pad);
+      e.box[3 + r] = float(wh[r] + pad);
+    }
+    ent.push_back(e);
+    s.instanced_triangles += obj_tris[in.object_id];
+  }
+  if (ent.empty())
+    return; // nothing placed: the scene stays single-level
+  std::vector<float> boxes(ent.size() * 6);
+  for (size_t i = 0; i < ent.size(); ++i)
+    std::memcpy(&boxes[6 * i], ent[i].box, sizeof(ent[i].box));
+  Bvh8Host tlas;
+  build_bvh8_boxes(boxes.data(), boxes.size() / 6, tlas, 1);
+
+  // combined arrays: top level at node 0, then the bottom levels
+  all = Bvh8Host{};
+  all.nodes = tlas.nodes;
+  all.node_count = tlas.node_count;
+  all.max_depth = 0;
+  uint32_t scene_root = 0;
+  if (has_scene_tris)
+    scene_root = append_blas(all, scene_blas, 0u);
+  for (uint32_t o = 0; o < n_obj; ++o)
+    if (obj_ok[o])
+      obj_root[o] = append_blas(all, blas[o], obj_prim_base[o]);
+  const uint32_t blas_depth = all.max_depth;
+  all.max_depth = tlas.max_depth + blas_depth + 1;
+  all.sah_cost = tlas.sah_cost;
+
+  // instance records in top-level leaf order
+  s.inst_count = uint32_t(tlas.leaf_prims.size());
+  s.inst_w2o.assign(size_t(s.inst_count) * 12, 0.f);
+  s.inst_info.assign(size_t(s.inst_count) * 4, 0u);
+  for (uint32_t j = 0; j < s.inst_count; ++j) {
+    const Entry &e = ent[tlas.leaf_prims[j]];
+    for (int k = 0; k < 12; ++k)
+      s.inst_w2o[12 * size_t(j) + k] = float(e.w2o[k]);
+    uint32_t *info = &s.inst_info[4 * size_t(j)];
+    if (e.object == n_obj) {
+      info[0] = scene_root;
+      info[1] = n_obj;
+      info[2] = INST_IDENTITY | (s.scene_normals ? INST_NORMALS : 0u);
+    } else {
+      info[0] = obj_root[e.object];
+      info[1] = e.object;
+      info[2] = obj_flags[e.object];
+    }
+  }
+  s.bvh = std::move(all);
+  // primitives of objects have no light pdf (instances do not emit light)
+  if (!s.prim_light_pdf.empty())
+    s.prim_light_pdf.resize(s.prim_vidx.size() / 4, 0.f);
+}
+
 void build_host_scene(const phc_scene_desc &in, HostScene &s)
 {
   s = HostScene{};
@@ -537,6 +759,9 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
   }
   s.strategy_count = uint32_t(s.lights.size()) + (s.emissive_cdf.empty() ? 0u : 1u) + (s.has_env ? 1u : 0u);
   build_bvh8(pos3.data(), vc, s.indices.data(), tc, s.bvh, tuning().max_leaf);
+  s.scene_normals = !empty && in.normals;
+  if (pt && pt->instance_count && pt->object_count)
+    build_instancing(*pt, !empty, lo, hi, s, tuning().max_leaf);
 }
 
 // ------------------------------------------------------------------ upload
@@ -613,7 +838,11 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   d.vol_majorants = put(h.vol_majorants, s, err);
   d.strategy_count = h.strategy_count;
   d.eps = h.eps;
-  d.features = 0u;
+  d.inst_w2o = reinterpret_cast<const float4 *>(put(h.inst_w2o, s, err));
+  d.inst_info = reinterpret_cast<const uint4 *>(put(h.inst_info, s, err));
+  d.inst_count = h.inst_count;
+  d.scene_normals = h.scene_normals ? 1 : 0;
+  d.features = h.inst_count ? SCENE_INSTANCES : 0u;
   if (!h.volumes.empty())
     d.features |= SCENE_VOLUMES;
   if (!h.lights.empty())

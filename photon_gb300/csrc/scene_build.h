@@ -43,6 +43,13 @@ struct HostScene {
   uint32_t strategy_count{0};
   float eps{1e-3f};
   Bvh8Host bvh;
+  // instancing: one record per top-level leaf slot (3 float4 world-to-object
+  // rows; uint4 bottom-level root, object id, INST_* flags, 0)
+  std::vector<float> inst_w2o;
+  std::vector<uint32_t> inst_info;
+  uint32_t inst_count{0};
+  bool scene_normals{false};
+  uint64_t instanced_triangles{0}; // triangles the instances place (not stored)
 };
 
 void build_host_scene(const phc_scene_desc &in, HostScene &out);

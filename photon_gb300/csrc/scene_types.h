@@ -136,12 +136,27 @@ struct DevScene {
   uint32_t strategy_count;
   float eps;
   uint32_t features; // SCENE_* bits: which shading features the scene uses
+  // two-level BVH (SCENE_INSTANCES): `nodes` holds the top level (root at
+  // node 0, leaves address instance slots) followed by every bottom level;
+  // per top-level leaf slot the world-to-object rows and
+  // (bottom-level root, object id, INST_* flags, 0)
+  const float4 *inst_w2o; // 3 per instance
+  const uint4 *inst_info;
+  uint32_t inst_count;
+  int32_t scene_normals; // the scene's own triangles carry vertex normals
+};
+
+enum : uint32_t {
+  INST_IDENTITY = 1u, // the scene's own triangles: world space, no transform
+  INST_NORMALS = 2u,  // the object has vertex normals
+  INST_NONE = 0xffffffffu
 };
 
 enum : uint32_t {
   SCENE_VOLUMES = 1u,  // transfer-function volumes (delta / ratio tracking)
   SCENE_SOURCES = 2u,  // material parameters from attributes or samplers, normal maps
-  SCENE_LIGHTS = 4u    // analytic point / directional / spot lights
+  SCENE_LIGHTS = 4u,   // analytic point / directional / spot lights
+  SCENE_INSTANCES = 8u // instanced geometry: two-level traversal
 };
 
 } // namespace phc

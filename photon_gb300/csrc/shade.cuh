@@ -393,6 +393,7 @@ struct Query {
   uint4 vidx;
   float b1, b2;
   V3 p, sn;
+  uint32_t inst = INST_NONE; // instance slot of an instanced hit
 };
 __device__ __forceinline__ float4 fetch_attribute(const DevScene &sc, int32_t slot, const Query &q)
 {
@@ -400,7 +401,7 @@ __device__ __forceinline__ float4 fetch_attribute(const DevScene &sc, int32_t sl
     return f4(q.p, 1.f);
   if (slot == 6)
     return f4(q.sn, 1.f);
-  if (!(slot >= 0 && slot < 5 && sc.attr_offset[slot] >= 0))
+  if (!(slot >= 0 && slot < 5 && sc.attr_offset[slot] >= 0) || q.inst != INST_NONE) // instances carry no attributes
     return make_float4(0.f, 0.f, 0.f, 1.f);
   const uint32_t base = uint32_t(sc.attr_offset[slot]);
   const float4 a0 = __ldg(sc.attr_values + base + q.vidx.x);
@@ -565,7 +566,8 @@ static __device__ __noinline__ Mat resolve_material(const DevScene &sc, const De
   m.thin = dm.thin;
   alpha = dm.alpha;
   if (SRC && (dm.alpha_tex >= 0 || dm.base_tex >= 0)) {
-    const float4 uv = fetch_attribute(sc, 0, q);
+    // an instance's uv is its barycentrics (photon_optix.cu:88-90)
+    const float4 uv = q.inst != INST_NONE ? make_float4(q.b1, q.b2, 0.f, 1.f) : fetch_attribute(sc, 0, q);
     if (dm.alpha_tex >= 0)
       alpha = atlas_sample(sc, dm.alpha_tex, uv.x, uv.y).x;
     if (dm.base_tex >= 0)

@@ -28,7 +28,7 @@ struct ShadowRec {
 template <bool FULL, int PART>
 __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene &sc, const float4 ro4,
     const float4 rd4, const float4 tp4, const uint4 info, const float pdist, const float4 hit, const Accum &acc,
-    int it, bool &cont, NextPath &next, bool &has_shadow, ShadowRec &sh)
+    int it, bool &cont, NextPath &next, bool &has_shadow, ShadowRec &sh, uint32_t inst = INST_NONE)
 {
   cont = false;
   has_shadow = false;
@@ -154,7 +154,7 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
 
   // surface hit
   const RayHit rh{hit.x, prim, hit.z, hit.w};
-  const HitAttr ha = hit_attributes(sc, ray_org, ray_dir, rh);
+  const HitAttr ha = hit_attributes(sc, ray_org, ray_dir, rh, inst);
   const V3 p = ha.p;
   const V3 wo = -ray_dir;
   V3 hit_sn = ha.sn;
@@ -169,6 +169,7 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
   q.b2 = rh.v;
   q.p = p;
   q.sn = hit_sn;
+  q.inst = inst;
   float alpha_val = 1.f;
   const DevMaterial &dm = sc.materials[ha.material_id];
   const Mat mat = resolve_material<FULL>(sc, dm, q, alpha_val);
@@ -332,8 +333,9 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
         shade_path<FULL, PART>(J.rc, J.sc, in.ray_o[i], in.ray_d[i], in.tp[i], info, in.pdist[i], hits[i], J.acc,
             it, cont, np, has_sh, sr);
       } else {
+        const uint32_t inst = (PART != 2 && sc.inst_count) ? hq.inst[i] : INST_NONE;
         shade_path<FULL, PART>(*rcp, sc, in.ray_o[i], in.ray_d[i], in.tp[i], info, in.pdist[i], hits[i], acc, it,
-            cont, np, has_sh, sr);
+            cont, np, has_sh, sr, inst);
       }
     }
     if (PART != 2) { // misses never continue nor cast shadow rays

@@ -303,6 +303,158 @@ PHC_HD bool trav_step(const uint4 *__restrict__ nodes, const float4 *__restrict_
   return s.g_hits != 0u || s.sp != 0;
 }
 
+// ------------------------------------------------------- two levels
+// Traversal of a scene with instances (SCENE_INSTANCES): the top level's
+// leaves are instance slots.  Reaching them queues the slots; each is
+// entered in turn by carrying the ray into the object's space (origin and
+// direction through the world-to-object rows, the direction not
+// renormalised so that t keeps its meaning) and traversing the object's
+// bottom level from its root.  A marker entry on the stack brings the world
+// ray back when the bottom level is done.  The short stack holds the top
+// level's groups, one queued-slot entry and the marker, then the bottom
+// level's groups: the scene build keeps their sum below the stack size.
+constexpr uint32_t STACK_SLOTS = 0x80000000u; // entry: queued instance slots (x base, mask)
+constexpr uint32_t STACK_RETURN = 0x40000000u; // entry: back to the world ray
+
+struct TravState2 : TravState {
+  V3 wo, wd, widir; // the world ray
+  uint32_t woct;
+  uint32_t inst;      // current instance slot, INST_NONE on the top level
+  uint32_t inst_hit;  // what a hit in it records: the slot, or INST_NONE for
+                      // the scene's own triangles (an identity placement)
+  uint32_t best_inst; // instance slot of the closest hit so far
+  uint32_t pend_base, pend_mask;
+};
+
+PHC_HD void trav_init2(TravState2 &s, V3 o, V3 d, float tmin, float tmax)
+{
+  trav_init(s, o, d, tmin, tmax);
+  s.wo = s.o;
+  s.wd = s.d;
+  s.widir = s.idir;
+  s.woct = s.oct;
+  s.inst = INST_NONE;
+  s.inst_hit = INST_NONE;
+  s.best_inst = INST_NONE;
+  s.pend_base = 0u;
+  s.pend_mask = 0u;
+}
+
+// p' = M p (rows r0..r2 of a 3x4 matrix); d' = M d without the translation
+PHC_HD V3 xf_point3(float4 r0, float4 r1, float4 r2, V3 p)
+{
+  return V3{r0.x * p.x + r0.y * p.y + r0.z * p.z + r0.w, r1.x * p.x + r1.y * p.y + r1.z * p.z + r1.w,
+      r2.x * p.x + r2.y * p.y + r2.z * p.z + r2.w};
+}
+PHC_HD V3 xf_dir3(float4 r0, float4 r1, float4 r2, V3 d)
+{
+  return V3{r0.x * d.x + r0.y * d.y + r0.z * d.z, r1.x * d.x + r1.y * d.y + r1.z * d.z,
+      r2.x * d.x + r2.y * d.y + r2.z * d.z};
+}
+
+PHC_HD void stack_push(uint2 *stack, int &sp, uint32_t x, uint32_t y)
+{
+  if (sp < PHC_STACK_SIZE) {
+    stack[sp].x = x;
+    stack[sp].y = y;
+    ++sp;
+  }
+}
+
+template <bool ANY, bool COUNT>
+PHC_HD bool trav_step2(const uint4 *__restrict__ nodes, const float4 *__restrict__ tris,
+    const float4 *__restrict__ inst_w2o, const uint4 *__restrict__ inst_info, TravState2 &s, uint2 *stack,
+    TravCounters *ctr)
+{
+  // bookkeeping (entering an instance, popping queued slots or the return
+  // marker) runs in the same step as the next node visit, so that every
+  // step of a busy lane visits one node
+  for (int guard = 0; guard < 4 * PHC_STACK_SIZE + 8; ++guard) {
+    if (s.pend_mask != 0u) { // enter the next queued instance
+      if (s.g_hits != 0u)
+        stack_push(stack, s.sp, s.g_base, s.g_hits | (s.g_imask << 8));
+      const uint32_t k = ffs32(s.pend_mask) - 1u;
+      s.pend_mask &= s.pend_mask - 1u;
+      if (s.pend_mask != 0u)
+        stack_push(stack, s.sp, s.pend_base, STACK_SLOTS | s.pend_mask);
+      stack_push(stack, s.sp, 0u, STACK_RETURN);
+      const uint32_t j = s.pend_base + k;
+      s.pend_mask = 0u;
+      const uint4 info = ldg4(inst_info + j);
+      s.inst = j;
+      s.inst_hit = (info.z & INST_IDENTITY) ? INST_NONE : j;
+      if (!(info.z & INST_IDENTITY)) {
+        const float4 r0 = ldg4(inst_w2o + 3 * size_t(j)), r1 = ldg4(inst_w2o + 3 * size_t(j) + 1);
+        const float4 r2 = ldg4(inst_w2o + 3 * size_t(j) + 2);
+        s.o = xf_point3(r0, r1, r2, s.wo);
+        s.d = xf_dir3(r0, r1, r2, s.wd);
+        s.idir = V3{safe_inv(s.d.x), safe_inv(s.d.y), safe_inv(s.d.z)};
+        s.oct = (s.d.x < 0.f ? 4u : 0u) | (s.d.y < 0.f ? 2u : 0u) | (s.d.z < 0.f ? 1u : 0u);
+      }
+      s.g_base = info.x; // the bottom level's root as a one-child group
+      s.g_hits = 1u << s.oct;
+      s.g_imask = 1u;
+      break;
+    }
+    if (s.g_hits != 0u)
+      break;
+    if (s.sp == 0)
+      return false;
+    const uint2 e = stack[--s.sp];
+    if (e.y & STACK_SLOTS) {
+      s.pend_base = e.x;
+      s.pend_mask = e.y & ~STACK_SLOTS;
+    } else if (e.y == STACK_RETURN) {
+      s.o = s.wo;
+      s.d = s.wd;
+      s.idir = s.widir;
+      s.oct = s.woct;
+      s.inst = INST_NONE;
+    } else {
+      s.g_base = e.x;
+      s.g_hits = e.y & 0xffu;
+      s.g_imask = e.y >> 8;
+    }
+  }
+  if (s.g_hits == 0u) // not reached: every trip above pops an entry or enters an instance
+    return false;
+  const uint32_t k = ffs32(s.g_hits) - 1u;
+  s.g_hits &= s.g_hits - 1u;
+  const uint32_t slot = k ^ s.oct;
+  const uint32_t ni = s.g_base + popc32(s.g_imask & ((1u << slot) - 1u));
+  if (s.g_hits != 0u)
+    stack_push(stack, s.sp, s.g_base, s.g_hits | (s.g_imask << 8));
+  uint32_t tri_base, tri_hits;
+  intersect_node(nodes, ni, s.o, s.idir, s.oct, s.tmin, s.best.t, s.g_base, s.g_hits, s.g_imask, tri_base,
+      tri_hits);
+  if (COUNT)
+    ctr->nodes++;
+  if (s.inst == INST_NONE) { // top level: the leaves are instance slots
+    s.pend_base = tri_base;
+    s.pend_mask = tri_hits;
+    return s.pend_mask != 0u || s.g_hits != 0u || s.sp != 0;
+  }
+  while (tri_hits) {
+    const uint32_t b = ffs32(tri_hits) - 1u;
+    tri_hits &= tri_hits - 1u;
+    const float4 *r = tris + 3 * size_t(tri_base + b);
+    const float4 r0 = ldg4(r), r1 = ldg4(r + 1), r2 = ldg4(r + 2);
+    if (COUNT)
+      ctr->tris++;
+    float t, u, v;
+    if (tri_test(s.o, s.d, r0, r1, r2, s.tmin, s.best.t, t, u, v)) {
+      s.best.t = t;
+      s.best.prim = f2u(r0.w);
+      s.best.u = u;
+      s.best.v = v;
+      s.best_inst = s.inst_hit;
+      if (ANY)
+        return false;
+    }
+  }
+  return s.g_hits != 0u || s.sp != 0;
+}
+
 // Full traversal of one ray.  ANY: stop at the first hit (occlusion).
 template <bool ANY, bool COUNT>
 PHC_HD RayHit trace_ray(const DevScene &sc, V3 o, V3 d, float tmin, float tmax, TravCounters *ctr)
@@ -324,7 +476,13 @@ struct HitAttr {
   uint32_t material_id;
   uint4 vidx;
 };
-PHC_HD HitAttr hit_attributes(const DevScene &sc, V3 o, V3 d, const RayHit &h)
+//
+// A hit on an instance (inst = its slot, not INST_NONE) is computed in the
+// object's space and carried to world space as the reference's instanced
+// back-end does (backend/optix/photon_optix.cu:68-99, 183-186): both normals
+// through the inverse transpose of the instance transform (the transpose of
+// the world-to-object rows), normalised.
+PHC_HD HitAttr hit_attributes(const DevScene &sc, V3 o, V3 d, const RayHit &h, uint32_t inst = INST_NONE)
 {
   HitAttr a;
   const float4 *g = sc.prim_geo + 3 * size_t(h.prim);
@@ -338,13 +496,25 @@ PHC_HD HitAttr hit_attributes(const DevScene &sc, V3 o, V3 d, const RayHit &h)
   const V3 nn = normalize(cross(e1, e2));
   a.n = nn;
   a.sn = nn;
-  if (sc.normals) {
+  uint32_t flags = sc.scene_normals ? INST_NORMALS : 0u;
+  if (inst != INST_NONE)
+    flags = ldg4(sc.inst_info + inst).z;
+  if (flags & INST_NORMALS) {
     const float w0 = 1.f - h.u - h.v, w1 = h.u, w2 = h.v;
     const V3 n0 = v3(ldg4(sc.normals + a.vidx.x)), n1 = v3(ldg4(sc.normals + a.vidx.y));
     const V3 n2 = v3(ldg4(sc.normals + a.vidx.z));
     a.sn = normalize(n0 * w0 + n1 * w1 + n2 * w2);
     if (dot(a.sn, nn) < 0.f)
       a.sn = a.sn * -1.f;
+  }
+  if (inst != INST_NONE && !(flags & INST_IDENTITY)) {
+    const float4 r0 = ldg4(sc.inst_w2o + 3 * size_t(inst)), r1 = ldg4(sc.inst_w2o + 3 * size_t(inst) + 1);
+    const float4 r2 = ldg4(sc.inst_w2o + 3 * size_t(inst) + 2);
+    const V3 n = a.n, sn = a.sn;
+    a.n = normalize(V3{r0.x * n.x + r1.x * n.y + r2.x * n.z, r0.y * n.x + r1.y * n.y + r2.y * n.z,
+        r0.z * n.x + r1.z * n.y + r2.z * n.z});
+    a.sn = normalize(V3{r0.x * sn.x + r1.x * sn.y + r2.x * sn.z, r0.y * sn.x + r1.y * sn.y + r2.y * sn.z,
+        r0.z * sn.x + r1.z * sn.y + r2.z * sn.z});
   }
   a.material_id = a.vidx.w;
   return a;

@@ -17,6 +17,8 @@
 // counter until the queue length (also in device memory) is reached.
 #include "wave_common.cuh"
 
+#include <type_traits>
+
 namespace phc {
 namespace {
 
@@ -189,8 +191,13 @@ __device__ __forceinline__ void record_cap(const WaveCounters &wc, uint32_t code
 #ifndef PHC_TRACE_MIN_BLOCKS
 #define PHC_TRACE_MIN_BLOCKS 8 // 64 registers: 8 resident 128-thread blocks per SM
 #endif
-template <bool COUNT, bool SPLIT, bool BATCH>
-__global__ void __launch_bounds__(128, PHC_TRACE_MIN_BLOCKS) k_trace(DevScene sc, BatchTable bt, PathSoA in, float4 *__restrict__ hits,
+#ifndef PHC_TRACE_MIN_BLOCKS_INST
+#define PHC_TRACE_MIN_BLOCKS_INST 8 // the two-level variant (more state: the world ray)
+#endif
+// INST: the scene has instances (two-level traversal, trav_step2); the hit's
+// instance slot goes to hq.inst.
+template <bool COUNT, bool SPLIT, bool BATCH, bool INST = false>
+__global__ void __launch_bounds__(128, INST ? PHC_TRACE_MIN_BLOCKS_INST : PHC_TRACE_MIN_BLOCKS) k_trace(DevScene sc, BatchTable bt, PathSoA in, float4 *__restrict__ hits,
     WaveCounters wc, int it, uint64_t *stats, uint32_t refill, HitQueues hq)
 {
   const uint32_t n = wc.count[it];
@@ -198,7 +205,7 @@ __global__ void __launch_bounds__(128, PHC_TRACE_MIN_BLOCKS) k_trace(DevScene sc
   const uint32_t lane = lane_id();
   const uint32_t lt_mask = (1u << lane) - 1u;
   TravCounters ctr{0u, 0u};
-  TravState s;
+  std::conditional_t<INST, TravState2, TravState> s;
   uint2 stack[PHC_STACK_SIZE];
   bool busy = false, exhausted = false;
   uint32_t idx = 0, steps = 0, rays = 0, fetch_trips = 0, step_trips = 0, max_steps = 0, max_idx = 0;
@@ -228,7 +235,10 @@ __global__ void __launch_bounds__(128, PHC_TRACE_MIN_BLOCKS) k_trace(DevScene sc
             nodes = job.sc.nodes;
             tris = job.sc.tris;
           }
-          trav_init(s, v3(o), v3(d), o.w, d.w);
+          if constexpr (INST)
+            trav_init2(s, v3(o), v3(d), o.w, d.w);
+          else
+            trav_init(s, v3(o), v3(d), o.w, d.w);
           steps = 0;
           ++rays;
           busy = true;
@@ -243,7 +253,10 @@ __global__ void __launch_bounds__(128, PHC_TRACE_MIN_BLOCKS) k_trace(DevScene sc
     bool done = false;
     ++step_trips;
     if (busy) {
-      done = !trav_step<false, COUNT>(nodes, tris, s, stack, &ctr);
+      if constexpr (INST)
+        done = !trav_step2<false, COUNT>(nodes, tris, sc.inst_w2o, sc.inst_info, s, stack, &ctr);
+      else
+        done = !trav_step<false, COUNT>(nodes, tris, s, stack, &ctr);
       ++steps;
       if (steps > max_steps) {
         max_steps = steps;
@@ -259,6 +272,8 @@ __global__ void __launch_bounds__(128, PHC_TRACE_MIN_BLOCKS) k_trace(DevScene sc
     }
     if (done) {
       hits[idx] = make_float4(s.best.t, __uint_as_float(s.best.prim), s.best.u, s.best.v);
+      if constexpr (INST)
+        hq.inst[idx] = s.best_inst;
       busy = false;
     }
   }
@@ -375,7 +390,7 @@ __global__ void __launch_bounds__(256) k_mat_scatter(DevScene sc, BatchTable bt,
 // Any-hit traversal of the shadow queue, then the NEE contribution of the
 // unoccluded rays times the ratio-tracking transmittance of the volumes
 // (stream dimension 0x10000 + iteration), added to the path's pixel slot.
-template <bool COUNT, bool BATCH, bool DEFER = false>
+template <bool COUNT, bool BATCH, bool DEFER = false, bool INST = false>
 __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ rcp, DevScene sc, BatchTable bt,
     ShadowSoA sh, Accum acc_param, WaveCounters wc, int it, uint64_t *stats, uint32_t refill)
 {
@@ -384,7 +399,7 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
   const uint32_t lane = lane_id();
   const uint32_t lt_mask = (1u << lane) - 1u;
   TravCounters ctr{0u, 0u};
-  TravState s;
+  std::conditional_t<INST, TravState2, TravState> s;
   uint2 stack[PHC_STACK_SIZE];
   bool busy = false, exhausted = false;
   uint32_t idx = 0, job = 0, steps = 0, rays = 0, fetch_trips = 0, step_trips = 0, max_steps = 0, max_idx = 0;
@@ -415,7 +430,10 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
             nodes = bt.jobs[job].sc.nodes;
             tris = bt.jobs[job].sc.tris;
           }
-          trav_init(s, v3(a), v3(b), 0.f, a.w);
+          if constexpr (INST)
+            trav_init2(s, v3(a), v3(b), 0.f, a.w);
+          else
+            trav_init(s, v3(a), v3(b), 0.f, a.w);
           steps = 0;
           ++rays;
           busy = true;
@@ -435,7 +453,14 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
         max_idx = idx;
       }
     }
-    if (busy && !trav_step<true, COUNT>(nodes, tris, s, stack, &ctr)) {
+    bool more = true;
+    if (busy) {
+      if constexpr (INST)
+        more = trav_step2<true, COUNT>(nodes, tris, sc.inst_w2o, sc.inst_info, s, stack, &ctr);
+      else
+        more = trav_step<true, COUNT>(nodes, tris, s, stack, &ctr);
+    }
+    if (busy && !more) {
       busy = false;
       // Unoccluded: add the contribution here when the ray's scene has no
       // volume; otherwise leave the ray (tmax >= 0) to k_shadow_volume, so
@@ -607,6 +632,20 @@ void launch_trace(const LaunchCfg &c, cudaStream_t s, DevScene sc, PathSoA in, f
   const uint32_t r = uint32_t(refill < 1 ? 1 : (refill > 32 ? 32 : refill));
   const bool split = hq.hitq != nullptr;
   const BatchTable none{};
+  if (sc.inst_count > 0) { // two-level traversal
+    if (stats) {
+      if (split)
+        k_trace<true, true, false, true><<<c.blocks_trace, 128, 0, s>>>(sc, none, in, hits, wc, it, stats, r, hq);
+      else
+        k_trace<true, false, false, true><<<c.blocks_trace, 128, 0, s>>>(sc, none, in, hits, wc, it, stats, r, hq);
+    } else {
+      if (split)
+        k_trace<false, true, false, true><<<c.blocks_trace, 128, 0, s>>>(sc, none, in, hits, wc, it, nullptr, r, hq);
+      else
+        k_trace<false, false, false, true><<<c.blocks_trace, 128, 0, s>>>(sc, none, in, hits, wc, it, nullptr, r, hq);
+    }
+    return;
+  }
   if (stats) {
     if (split)
       k_trace<true, true, false><<<c.blocks_trace, 128, 0, s>>>(sc, none, in, hits, wc, it, stats, r, hq);
@@ -625,7 +664,12 @@ void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, De
 {
   const uint32_t r = uint32_t(refill < 1 ? 1 : (refill > 32 ? 32 : refill));
   const BatchTable none{};
-  if (stats)
+  if (sc.inst_count > 0) {
+    if (stats)
+      k_shadow<true, false, false, true><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, stats, r);
+    else
+      k_shadow<false, false, false, true><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, nullptr, r);
+  } else if (stats)
     k_shadow<true, false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, stats, r);
   else
     k_shadow<false, false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, nullptr, r);

@@ -100,6 +100,7 @@ struct HitQueues {
   uint32_t *missq;
   uint32_t *sorted = nullptr;
   uint32_t sort_threshold = 0;
+  uint32_t *inst = nullptr; // per path: instance slot of its hit (scenes with instances)
 };
 constexpr uint32_t MAT_SORT_BINS = 1024; // materials map to bin = id % MAT_SORT_BINS
 

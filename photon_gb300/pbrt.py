@@ -95,6 +95,17 @@ class PbrtScene:
         for i in range(pt.texture_count):
             t = pt.textures[i]
             out["textures"].append(arr(t.rgb, t.width * t.height * 3, np.float32).reshape(t.height, t.width, 3))
+        out["objects"], out["instances"] = [], []
+        for i in range(pt.object_count):
+            ob = pt.objects[i]
+            out["objects"].append({
+                "positions": arr(ob.positions, ob.vertex_count * 3, np.float32),
+                "indices": arr(ob.indices, ob.triangle_count * 3, np.uint32),
+                "normals": arr(ob.normals, ob.vertex_count * 3, np.float32),
+                "material_id": int(ob.material_id)})
+        for i in range(pt.instance_count):
+            ins = pt.instances[i]
+            out["instances"].append((int(ins.object_id), np.array(ins.transform[:], np.float32)))
         e = d.environment
         if e.present:
             out["env"] = {

@@ -38,6 +38,70 @@ def _f32(a, shape_last=None):
 
 
 @dataclass
+class PtData:
+    """The path-tracer-level part of a scene (phc_pt_scene): pt::Material
+    records, per-vertex texture coordinates, atlas textures, the environment's
+    map-to-world rotation and instanced geometry (objects in their own space,
+    placed by column-major object-to-world transforms)."""
+    materials: list = field(default_factory=list)   # _abi.PtMaterial
+    texcoords: np.ndarray | None = None             # (V, 2) float32
+    textures: list = field(default_factory=list)    # (h, w, 3) float32, row 0 = top
+    env_map_to_world: tuple | None = None           # 9 floats, row-major
+    objects: list = field(default_factory=list)     # dict(positions, indices, normals=None, material_id=0)
+    instances: list = field(default_factory=list)   # (object_id, 16 floats column-major)
+
+    def desc(self, keep):
+        p = _abi.PtScene()
+        if self.materials:
+            arr = (_abi.PtMaterial * len(self.materials))(*self.materials)
+            keep.append(arr)
+            p.materials = C.cast(arr, C.POINTER(_abi.PtMaterial))
+        if self.texcoords is not None:
+            t = np.ascontiguousarray(self.texcoords, dtype=np.float32).reshape(-1, 2)
+            keep.append(t)
+            p.texcoords = _fptr(t)
+        if self.textures:
+            recs = []
+            for img in self.textures:
+                a = np.ascontiguousarray(img, dtype=np.float32)
+                keep.append(a)
+                recs.append(_abi.Texture(a.shape[1], a.shape[0], _fptr(a)))
+            arr = (_abi.Texture * len(recs))(*recs)
+            keep.append(arr)
+            p.textures = C.cast(arr, C.POINTER(_abi.Texture))
+            p.texture_count = len(recs)
+        if self.env_map_to_world is not None:
+            p.env_map_to_world_given = 1
+            p.env_map_to_world[:] = list(self.env_map_to_world)
+        if self.objects:
+            recs = []
+            for ob in self.objects:
+                pos = _f32(ob["positions"], 3)
+                idx = np.ascontiguousarray(ob["indices"], dtype=np.uint32).reshape(-1, 3)
+                nrm = _f32(ob.get("normals"), 3)
+                keep += [pos, idx, nrm]
+                recs.append(_abi.Object(_fptr(pos), pos.shape[0], _uptr(idx), idx.shape[0], _fptr(nrm),
+                                        int(ob.get("material_id", 0))))
+            arr = (_abi.Object * len(recs))(*recs)
+            keep.append(arr)
+            p.objects = C.cast(arr, C.POINTER(_abi.Object))
+            p.object_count = len(recs)
+        if self.instances:
+            recs = []
+            for oid, xf in self.instances:
+                r = _abi.Instance()
+                r.object_id = int(oid)
+                r.transform[:] = [float(x) for x in np.asarray(xf, np.float32).ravel()]
+                recs.append(r)
+            arr = (_abi.Instance * len(recs))(*recs)
+            keep.append(arr)
+            p.instances = C.cast(arr, C.POINTER(_abi.Instance))
+            p.instance_count = len(recs)
+        keep.append(p)
+        return p
+
+
+@dataclass
 class SceneData:
     positions: np.ndarray                      # (V, 3) float32
     indices: np.ndarray                        # (T, 3) uint32
@@ -52,6 +116,7 @@ class SceneData:
     env_world_to_map: tuple = (1, 0, 0, 0, 1, 0, 0, 0, 1)
     volumes: list = field(default_factory=list)     # (_abi.Volume, values f32, transfer (K,4) f32)
     name: str = "scene"
+    pt: PtData | None = None                   # path-tracer-level part (phc_pt_scene)
 
     def __post_init__(self):
         self.positions = _f32(self.positions, 3)
@@ -131,6 +196,10 @@ class SceneData:
             keep.append(arr)
             d.volumes = C.cast(arr, C.POINTER(_abi.Volume))
             d.volume_count = len(recs)
+        if self.pt is not None:
+            p = self.pt.desc(keep)
+            d.pt = C.pointer(p)
+            d.material_count = len(self.pt.materials)
         return d, keep
 
 

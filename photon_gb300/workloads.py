@@ -790,3 +790,97 @@ def feature_scene(kind: str, seed=0, res=48):
 
 
 FEATURES = ("basic", "glass", "env", "lights", "volume", "textures", "alpha", "limits", "camera", "ortho")
+
+
+# ------------------------------------------------------- instanced objects
+
+def _pt_material(base=(0.8, 0.8, 0.8), roughness=0.5, metallic=0.0, transmission=0.0, ior=1.5, clearcoat=0.0,
+                 emission=(0.0, 0.0, 0.0), strength=0.0, base_tex=-1, flags=0):
+    """pt::Material record (material.h:35-82 defaults) for PtData scenes."""
+    m = _abi.PtMaterial()
+    m.base_color[:] = base
+    m.metallic, m.roughness, m.ior, m.transmission = metallic, roughness, ior, transmission
+    m.specular, m.clearcoat, m.clearcoat_roughness, m.sheen, m.alpha = 0.5, clearcoat, 0.03, 0.0, 1.0
+    m.emission[:] = emission
+    m.emission_strength = strength
+    m.flags, m.base_color_tex, m.alpha_tex = flags, base_tex, -1
+    return m
+
+
+def _random_placement(rng, extent, scale_range):
+    """Column-major object-to-world matrix: random rotation, non-uniform
+    scale, translation on the ground area."""
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    S = np.diag(rng.uniform(*scale_range, 3))
+    M = np.eye(4)
+    M[:3, :3] = R @ S
+    M[:3, 3] = (rng.uniform(-extent, extent), rng.uniform(0.3, 1.2), rng.uniform(-extent, extent))
+    return M.T.ravel().astype(np.float32)  # column-major
+
+
+def instanced_objects(seed=0, n_instances=60, res=128, spp=4, depth=6, flatten=False, sphere_subdiv=3):
+    """A ground plane and an area light (the scene's own triangles) with
+    `n_instances` placements of four objects (a smooth icosphere, a torus, a
+    box without normals, a displaced sphere) under random rotations,
+    non-uniform scales and translations; path-tracer-level materials.
+    flatten=True returns the same geometry with every placement transformed
+    into the scene's triangles (float64 transform, then float32), the
+    reference's single-level handling of instances."""
+    from .scene import PtData
+    rng = np.random.default_rng(seed)
+    objs = []
+    v, f = _icosphere(sphere_subdiv)
+    objs.append(dict(positions=0.3 * v, indices=f, normals=v, material_id=1))
+    v, n, f = _torus(32, 16, 0.3, 0.1)
+    objs.append(dict(positions=v, indices=f, normals=n, material_id=2))
+    bv, bi = _box((0.0, -0.2, 0.0), (0.4, 0.4, 0.4), 0.0)
+    objs.append(dict(positions=bv, indices=bi, normals=None, material_id=3))
+    v, f = _icosphere(sphere_subdiv)
+    vn = v.copy()
+    v = 0.25 * v * (1.0 + 0.15 * np.sin(7 * v[:, :1]) * np.cos(5 * v[:, 2:3]))
+    objs.append(dict(positions=v, indices=f, normals=_vertex_normals(v, f), material_id=4))
+    insts = [(int(rng.integers(0, len(objs))), _random_placement(rng, 2.5, (0.6, 1.6)))
+             for _ in range(n_instances)]
+    mats = [_pt_material((0.7, 0.7, 0.7), roughness=1.0),
+            _pt_material((0.7, 0.15, 0.1), roughness=0.6),
+            _pt_material((1.0, 0.78, 0.34), roughness=0.25, metallic=1.0),
+            _pt_material((1.0, 1.0, 1.0), roughness=0.05, transmission=1.0, ior=1.45, flags=8),
+            _pt_material((0.2, 0.4, 0.7), roughness=0.4, clearcoat=1.0),
+            _pt_material((0.0, 0.0, 0.0), roughness=1.0, emission=(12.0, 11.0, 9.0), strength=1.0)]
+    pos = [np.array([(-4, 0, -4), (4, 0, -4), (4, 0, 4), (-4, 0, 4)], np.float64),
+           np.array([(-0.6, 3.0, -0.6), (0.6, 3.0, -0.6), (0.6, 3.0, 0.6), (-0.6, 3.0, 0.6)], np.float64)]
+    idx = [np.array([[0, 2, 1], [0, 3, 2]]), np.array([[0, 1, 2], [0, 2, 3]])]
+    mid = [np.zeros(2, np.uint32), np.full(2, 5, np.uint32)]
+    nrm = [np.tile([0.0, 1.0, 0.0], (4, 1)), np.tile([0.0, -1.0, 0.0], (4, 1))]
+    pt = PtData(materials=mats)
+    if flatten:
+        for oid, xf in insts:
+            ob = objs[oid]
+            M = np.asarray(xf, np.float64).reshape(4, 4).T
+            p = np.asarray(ob["positions"], np.float64)
+            pw = p @ M[:3, :3].T + M[:3, 3]
+            pos.append(pw)
+            idx.append(np.asarray(ob["indices"]))
+            mid.append(np.full(len(ob["indices"]), ob["material_id"], np.uint32))
+            if ob["normals"] is not None:
+                nw = np.asarray(ob["normals"], np.float64) @ np.linalg.inv(M[:3, :3])
+                nw /= np.maximum(np.linalg.norm(nw, axis=1, keepdims=True), 1e-30)
+            else:  # no normals: zero vectors, for which shading uses the geometric normal
+                nw = np.zeros_like(pw)
+            nrm.append(nw)
+    else:
+        pt.objects = objs
+        pt.instances = insts
+    off = np.cumsum([0] + [len(p) for p in pos[:-1]])
+    sc = SceneData(positions=np.concatenate(pos).astype(np.float32),
+                   indices=np.concatenate([i + o for i, o in zip(idx, off)]).astype(np.uint32),
+                   material_ids=np.concatenate(mid), normals=np.concatenate(nrm).astype(np.float32),
+                   name="instanced_objects" + ("_flat" if flatten else ""), pt=pt)
+    cam = camera((0.0, 2.6, 6.5), (0.0, 0.6, 0.0), fovy_deg=45.0)
+    st = settings(res, res, spp, depth, adaptive_sampling=0)
+    return sc, cam, st

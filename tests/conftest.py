@@ -49,3 +49,25 @@ def photon():
     import photon_gb300
     photon_gb300.load()
     return photon_gb300
+
+
+@pytest.fixture(scope="session")
+def host_traverse_lib(tmp_path_factory):
+    """tests/native/host_traverse.cpp with the host BVH8 builder and the
+    renderer's host scene build, compiled with the host compiler: the device
+    traversal code (traverse.cuh) run on the CPU."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    cuda = "/usr/local/cuda"
+    if not os.path.isdir(os.path.join(cuda, "include")) or not shutil.which("g++"):
+        pytest.skip("needs g++ and the CUDA headers")
+    csrc = os.path.join(ROOT, "photon_gb300", "csrc")
+    out = tmp_path_factory.mktemp("ht") / "libhost_traverse.so"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+                    "-I", os.path.join(cuda, "include"), "-I", csrc,
+                    os.path.join(ROOT, "tests", "native", "host_traverse.cpp"),
+                    os.path.join(csrc, "bvh8.cpp"), os.path.join(csrc, "scene_build.cpp"),
+                    os.path.join(csrc, "tuning.cpp"), "-L", os.path.join(cuda, "lib64"), "-lcudart",
+                    "-o", str(out)], check=True)
+    return C.CDLL(str(out))

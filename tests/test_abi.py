@@ -43,6 +43,7 @@ STRUCTS = {
     "phc_scene_desc": _abi.SceneDesc, "phc_camera": _abi.Camera, "phc_settings": _abi.Settings,
     "phc_render_stats": _abi.RenderStats, "phc_hit_result": _abi.HitResult, "phc_job": _abi.Job,
     "phc_pt_material": _abi.PtMaterial, "phc_texture": _abi.Texture, "phc_pt_scene": _abi.PtScene,
+    "phc_object": _abi.Object, "phc_instance": _abi.Instance,
 }
 
 
