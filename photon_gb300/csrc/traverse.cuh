@@ -305,17 +305,16 @@ PHC_HD bool trav_step(const uint4 *__restrict__ nodes, const float4 *__restrict_
 
 // ------------------------------------------------------- two levels
 // Traversal of a scene with instances (SCENE_INSTANCES): the top level's
-// leaves are instance slots.  Reaching them queues the slots; each is
-// entered in turn by carrying the ray into the object's space (origin and
-// direction through the world-to-object rows, the direction not
-// renormalised so that t keeps its meaning) and traversing the object's
-// bottom level from its root.  A marker entry on the stack brings the world
-// ray back when the bottom level is done.  The short stack holds the top
-// level's groups, one queued-slot entry and the marker, then the bottom
-// level's groups: the scene build keeps their sum below the stack size.
-constexpr uint32_t STACK_SLOTS = 0x80000000u; // entry: queued instance slots (x base, mask)
-constexpr uint32_t STACK_RETURN = 0x40000000u; // entry: back to the world ray
-
+// leaves are instance slots.  A top-level node visit that reaches leaves
+// queues their slots (in registers); each queued slot is entered in turn by
+// carrying the ray into the object's space (origin and direction through
+// the world-to-object rows, the direction not renormalised so that t keeps
+// its meaning) and traversing the object's bottom level from its root.  The
+// stack depth at entry marks where the bottom level's entries end: when the
+// bottom level has no group left above it, the world ray comes back and the
+// next queued slot (or the top level's stack) continues.  The stack holds
+// the top level's groups below the bottom level's; the scene build keeps the
+// two depths' sum below its size.
 struct TravState2 : TravState {
   V3 wo, wd, widir; // the world ray
   uint32_t woct;
@@ -323,7 +322,8 @@ struct TravState2 : TravState {
   uint32_t inst_hit;  // what a hit in it records: the slot, or INST_NONE for
                       // the scene's own triangles (an identity placement)
   uint32_t best_inst; // instance slot of the closest hit so far
-  uint32_t pend_base, pend_mask;
+  uint32_t pend_base, pend_mask; // queued instance slots of a top-level node
+  int blas_sp;        // stack depth where the current bottom level began
 };
 
 PHC_HD void trav_init2(TravState2 &s, V3 o, V3 d, float tmin, float tmax)
@@ -338,6 +338,7 @@ PHC_HD void trav_init2(TravState2 &s, V3 o, V3 d, float tmin, float tmax)
   s.best_inst = INST_NONE;
   s.pend_base = 0u;
   s.pend_mask = 0u;
+  s.blas_sp = 0;
 }
 
 // p' = M p (rows r0..r2 of a 3x4 matrix); d' = M d without the translation
@@ -366,20 +367,37 @@ PHC_HD bool trav_step2(const uint4 *__restrict__ nodes, const float4 *__restrict
     const float4 *__restrict__ inst_w2o, const uint4 *__restrict__ inst_info, TravState2 &s, uint2 *stack,
     TravCounters *ctr)
 {
-  // bookkeeping (entering an instance, popping queued slots or the return
-  // marker) runs in the same step as the next node visit, so that every
-  // step of a busy lane visits one node
-  for (int guard = 0; guard < 4 * PHC_STACK_SIZE + 8; ++guard) {
-    if (s.pend_mask != 0u) { // enter the next queued instance
+  // bookkeeping (popping a group, leaving a bottom level, entering a queued
+  // instance) runs in the same step as the next node visit, so that every
+  // step of a busy lane visits one node.  The loop has no return: all its
+  // exits meet before the node visit, where the warp's lanes reconverge.
+  bool alive = true;
+  for (int guard = 0; guard < 2 * PHC_STACK_SIZE + 66; ++guard) {
+    if (s.inst != INST_NONE) { // in a bottom level
       if (s.g_hits != 0u)
+        break;
+      if (s.sp > s.blas_sp) {
+        const uint2 e = stack[--s.sp];
+        s.g_base = e.x;
+        s.g_hits = e.y & 0xffu;
+        s.g_imask = e.y >> 8;
+        continue;
+      }
+      s.o = s.wo; // the bottom level is done: back to the world ray
+      s.d = s.wd;
+      s.idir = s.widir;
+      s.oct = s.woct;
+      s.inst = INST_NONE;
+      continue;
+    }
+    if (s.pend_mask != 0u) { // enter the next queued instance
+      if (s.g_hits != 0u) {
         stack_push(stack, s.sp, s.g_base, s.g_hits | (s.g_imask << 8));
+        s.g_hits = 0u;
+      }
       const uint32_t k = ffs32(s.pend_mask) - 1u;
       s.pend_mask &= s.pend_mask - 1u;
-      if (s.pend_mask != 0u)
-        stack_push(stack, s.sp, s.pend_base, STACK_SLOTS | s.pend_mask);
-      stack_push(stack, s.sp, 0u, STACK_RETURN);
       const uint32_t j = s.pend_base + k;
-      s.pend_mask = 0u;
       const uint4 info = ldg4(inst_info + j);
       s.inst = j;
       s.inst_hit = (info.z & INST_IDENTITY) ? INST_NONE : j;
@@ -391,6 +409,7 @@ PHC_HD bool trav_step2(const uint4 *__restrict__ nodes, const float4 *__restrict
         s.idir = V3{safe_inv(s.d.x), safe_inv(s.d.y), safe_inv(s.d.z)};
         s.oct = (s.d.x < 0.f ? 4u : 0u) | (s.d.y < 0.f ? 2u : 0u) | (s.d.z < 0.f ? 1u : 0u);
       }
+      s.blas_sp = s.sp;
       s.g_base = info.x; // the bottom level's root as a one-child group
       s.g_hits = 1u << s.oct;
       s.g_imask = 1u;
@@ -398,25 +417,16 @@ PHC_HD bool trav_step2(const uint4 *__restrict__ nodes, const float4 *__restrict
     }
     if (s.g_hits != 0u)
       break;
-    if (s.sp == 0)
-      return false;
-    const uint2 e = stack[--s.sp];
-    if (e.y & STACK_SLOTS) {
-      s.pend_base = e.x;
-      s.pend_mask = e.y & ~STACK_SLOTS;
-    } else if (e.y == STACK_RETURN) {
-      s.o = s.wo;
-      s.d = s.wd;
-      s.idir = s.widir;
-      s.oct = s.woct;
-      s.inst = INST_NONE;
-    } else {
-      s.g_base = e.x;
-      s.g_hits = e.y & 0xffu;
-      s.g_imask = e.y >> 8;
+    if (s.sp == 0) {
+      alive = false;
+      break;
     }
+    const uint2 e = stack[--s.sp];
+    s.g_base = e.x;
+    s.g_hits = e.y & 0xffu;
+    s.g_imask = e.y >> 8;
   }
-  if (s.g_hits == 0u) // not reached: every trip above pops an entry or enters an instance
+  if (!alive || s.g_hits == 0u) // (g_hits 0 with alive: not reached, the loop always ends on a group)
     return false;
   const uint32_t k = ffs32(s.g_hits) - 1u;
   s.g_hits &= s.g_hits - 1u;
@@ -452,7 +462,7 @@ PHC_HD bool trav_step2(const uint4 *__restrict__ nodes, const float4 *__restrict
         return false;
     }
   }
-  return s.g_hits != 0u || s.sp != 0;
+  return s.g_hits != 0u || s.sp != 0 || s.pend_mask != 0u;
 }
 
 // Full traversal of one ray.  ANY: stop at the first hit (occlusion).
