@@ -429,6 +429,17 @@ typedef struct phc_hit_result {
    optional normals xyz and material ids). */
 int phc_accel_create(phc_accel **out, const float *positions, uint64_t vertex_count, const uint32_t *indices,
     uint64_t triangle_count, const float *normals, const uint32_t *material_ids);
+/* RayBackend::build_accel_instanced (ray_backend.h:47-49), as the reference's
+   instanced back-end builds it (optix_backend.cpp:659-722): the mesh above
+   (may be empty) plus objects placed by instances, traced as a two-level
+   BVH8 without flattening.  Hit records of such an accel report, as that
+   back-end does: the barycentrics as uv, prim_id within its object, inst_id
+   = the object's index (object_count for the mesh's own triangles), the
+   object's material id, normals carried to world space by the inverse
+   transpose.  With no objects or instances it is phc_accel_create. */
+int phc_accel_create_instanced(phc_accel **out, const float *positions, uint64_t vertex_count,
+    const uint32_t *indices, uint64_t triangle_count, const float *normals, const uint32_t *material_ids,
+    const phc_object *objects, uint32_t object_count, const phc_instance *instances, uint32_t instance_count);
 void phc_accel_destroy(phc_accel *a);
 /* RayBackend::trace_closest (kokkos_backend.cpp:21-61) on device pointers:
    origins/directions are xyz float triples (RayBatch, ray_backend.h:31-37),

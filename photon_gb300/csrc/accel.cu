@@ -42,8 +42,12 @@ int fail(int code, const std::string &m)
 
 constexpr uint32_t FULL = 0xffffffffu;
 
-// One ray per thread; persistent warps take 32-ray batches.
-template <int MODE, bool COUNT> // 0 full hit record, 1 compact, 2 occluded
+// One ray per thread; persistent warps take 32-ray batches.  INST: the
+// accel holds instances (two-level traversal); full hit records then follow
+// the reference's instanced back-end (photon_optix.cu:68-99, 161-187): the
+// barycentrics as uv, the primitive's index within its object, the object's
+// index as inst_id (the object count for the accel's own triangles).
+template <int MODE, bool COUNT, bool INST = false> // MODE 0 full hit record, 1 compact, 2 occluded
 __global__ void __launch_bounds__(128) k_level_a(DevScene sc, const float *__restrict__ orgs,
     const float *__restrict__ dirs, const float *__restrict__ tmins, const float *__restrict__ tmaxs, uint32_t n,
     void *out, uint32_t *fetch, unsigned long long *stats)
@@ -62,12 +66,15 @@ __global__ void __launch_bounds__(128) k_level_a(DevScene sc, const float *__res
     const V3 o{orgs[3 * i], orgs[3 * i + 1], orgs[3 * i + 2]};
     const V3 d{dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
     const float t0 = tmins[i], t1 = tmaxs[i];
+    uint32_t inst = INST_NONE;
     if (MODE == 2) {
-      const RayHit h = trace_ray<true, COUNT>(sc, o, d, t0, t1, &ctr);
+      const RayHit h = INST ? trace_ray2<true, COUNT>(sc, o, d, t0, t1, &ctr, inst)
+                            : trace_ray<true, COUNT>(sc, o, d, t0, t1, &ctr);
       static_cast<uint32_t *>(out)[i] = h.prim != 0xffffffffu ? 1u : 0u;
       continue;
     }
-    const RayHit h = trace_ray<false, COUNT>(sc, o, d, t0, t1, &ctr);
+    const RayHit h = INST ? trace_ray2<false, COUNT>(sc, o, d, t0, t1, &ctr, inst)
+                          : trace_ray<false, COUNT>(sc, o, d, t0, t1, &ctr);
     if (MODE == 1) {
       reinterpret_cast<float4 *>(out)[i] = make_float4(h.t, __uint_as_float(h.prim), h.u, h.v);
       continue;
@@ -79,7 +86,7 @@ __global__ void __launch_bounds__(128) k_level_a(DevScene sc, const float *__res
       rec[k] = 0.f;
     uint32_t *urec = reinterpret_cast<uint32_t *>(rec);
     if (h.prim != 0xffffffffu) {
-      const HitAttr a = hit_attributes(sc, o, d, h);
+      const HitAttr a = hit_attributes(sc, o, d, h, inst);
       rec[0] = h.t;
       rec[1] = a.p.x;
       rec[2] = a.p.y;
@@ -95,6 +102,17 @@ __global__ void __launch_bounds__(128) k_level_a(DevScene sc, const float *__res
       urec[17] = h.prim;
       urec[20] = a.material_id;
       urec[21] = 1u; // hit = 1, has_interpolated_color = 0
+      if (INST) {
+        rec[10] = h.u; // no texture coordinates: uv = barycentrics
+        rec[11] = h.v;
+        if (inst != INST_NONE) {
+          const uint4 info = __ldg(sc.inst_info + inst);
+          urec[17] = h.prim - info.w;
+          urec[19] = info.y;
+        } else {
+          urec[19] = sc.scene_object_id;
+        }
+      }
     }
     float *dst = static_cast<float *>(out) + size_t(i) * 22;
     for (int k = 0; k < 22; ++k)
@@ -123,8 +141,13 @@ int launch(phc_accel *a, const float *o, const float *d, const float *t0, const 
   const int blocks = a->sm_count * 16;
   const bool count = std::getenv("PHC_TUNE_COUNT_TRAVERSAL") && std::atoi(std::getenv("PHC_TUNE_COUNT_TRAVERSAL"));
   auto *st = reinterpret_cast<unsigned long long *>(a->counters);
-  if (count)
+  const bool inst = a->scene.dev.inst_count > 0;
+  if (count && inst)
+    k_level_a<MODE, true, true><<<blocks, 128, 0, s>>>(a->scene.dev, o, d, t0, t1, n, out, fetch, st);
+  else if (count)
     k_level_a<MODE, true><<<blocks, 128, 0, s>>>(a->scene.dev, o, d, t0, t1, n, out, fetch, st);
+  else if (inst)
+    k_level_a<MODE, false, true><<<blocks, 128, 0, s>>>(a->scene.dev, o, d, t0, t1, n, out, fetch, st);
   else
     k_level_a<MODE, false><<<blocks, 128, 0, s>>>(a->scene.dev, o, d, t0, t1, n, out, fetch, st);
   cudaError_t e = cudaGetLastError();
@@ -148,12 +171,25 @@ extern "C" {
 int phc_accel_create(phc_accel **out, const float *positions, uint64_t vertex_count, const uint32_t *indices,
     uint64_t triangle_count, const float *normals, const uint32_t *material_ids)
 {
+  return phc_accel_create_instanced(out, positions, vertex_count, indices, triangle_count, normals, material_ids,
+      nullptr, 0u, nullptr, 0u);
+}
+
+int phc_accel_create_instanced(phc_accel **out, const float *positions, uint64_t vertex_count,
+    const uint32_t *indices, uint64_t triangle_count, const float *normals, const uint32_t *material_ids,
+    const phc_object *objects, uint32_t object_count, const phc_instance *instances, uint32_t instance_count)
+{
   static_assert(sizeof(phc_hit_result) == 88, "HitResult layout");
   if (!out)
     return fail(PHC_ERR_INVALID, "null output pointer");
   *out = nullptr;
-  if (!positions || !indices || vertex_count == 0 || triangle_count == 0)
+  const bool instanced = object_count > 0 && instance_count > 0;
+  if (instanced && (!objects || !instances))
+    return fail(PHC_ERR_INVALID, "null objects or instances");
+  if (!instanced && (!positions || !indices || vertex_count == 0 || triangle_count == 0))
     return fail(PHC_ERR_INVALID, "empty mesh");
+  if ((vertex_count || triangle_count) && (!positions || !indices))
+    return fail(PHC_ERR_INVALID, "null positions or indices");
   phc_accel *a = nullptr;
   try {
     a = new phc_accel();
@@ -174,12 +210,24 @@ int phc_accel_create(phc_accel **out, const float *positions, uint64_t vertex_co
     d.normals = normals;
     d.material_ids = material_ids;
     d.material_id_count = material_ids ? triangle_count : 0;
+    phc_pt_scene pt{};
+    if (instanced) { // RayBackend::build_accel_instanced (optix_backend.cpp:659-722)
+      pt.objects = objects;
+      pt.object_count = object_count;
+      pt.instances = instances;
+      pt.instance_count = instance_count;
+      d.pt = &pt;
+    }
     HostScene hs;
     build_host_scene(d, hs);
-    // Level A keeps the caller's material ids as given (no material table).
-    if (material_ids)
+    // Level A keeps the caller's material ids as given (no material table);
+    // an object's triangles carry its material id (optix_backend.cpp:694-695)
+    if (material_ids && triangle_count)
       for (uint64_t t = 0; t < triangle_count; ++t)
         hs.prim_vidx[4 * t + 3] = material_ids[t];
+    for (size_t o = 0; o < hs.obj_prim_base.size(); ++o)
+      for (uint32_t t = 0; t < hs.obj_prim_count[o]; ++t)
+        hs.prim_vidx[4 * (size_t(hs.obj_prim_base[o]) + t) + 3] = objects[o].material_id;
     if (hs.bvh.max_depth >= 64) {
       delete a;
       return fail(PHC_ERR_LIMIT, "BVH deeper than the traversal stack (64 levels)");
@@ -307,8 +355,12 @@ extern "C" int phc_trace_closest_compact_static(phc_accel *a, const float *origi
   e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess)
     return fail(PHC_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
-  k_level_a<1, false><<<a->sm_count * 16, 128, 0, s>>>(a->scene.dev, origins, directions, tmin, tmax, n, hits4,
-      scratch, nullptr);
+  if (a->scene.dev.inst_count)
+    k_level_a<1, false, true><<<a->sm_count * 16, 128, 0, s>>>(a->scene.dev, origins, directions, tmin, tmax, n,
+        hits4, scratch, nullptr);
+  else
+    k_level_a<1, false><<<a->sm_count * 16, 128, 0, s>>>(a->scene.dev, origins, directions, tmin, tmax, n, hits4,
+        scratch, nullptr);
   e = cudaGetLastError();
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(s);

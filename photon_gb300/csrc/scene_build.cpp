@@ -507,13 +507,19 @@ void build_instancing(const phc_pt_scene &pt, bool has_scene_tris, const float l
       info[0] = scene_root;
       info[1] = n_obj;
       info[2] = INST_IDENTITY | (s.scene_normals ? INST_NORMALS : 0u);
+      info[3] = 0u;
     } else {
       info[0] = obj_root[e.object];
       info[1] = e.object;
       info[2] = obj_flags[e.object];
+      info[3] = obj_prim_base[e.object]; // local primitive id = global - base
     }
   }
   s.bvh = std::move(all);
+  s.obj_prim_base = obj_prim_base;
+  s.obj_prim_count.assign(n_obj, 0u);
+  for (uint32_t o = 0; o < n_obj; ++o)
+    s.obj_prim_count[o] = uint32_t(obj_tris[o]);
   // primitives of objects have no light pdf (instances do not emit light)
   if (!s.prim_light_pdf.empty())
     s.prim_light_pdf.resize(s.prim_vidx.size() / 4, 0.f);
@@ -841,6 +847,7 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   d.inst_w2o = reinterpret_cast<const float4 *>(put(h.inst_w2o, s, err));
   d.inst_info = reinterpret_cast<const uint4 *>(put(h.inst_info, s, err));
   d.inst_count = h.inst_count;
+  d.scene_object_id = uint32_t(h.obj_prim_base.size());
   d.scene_normals = h.scene_normals ? 1 : 0;
   d.features = h.inst_count ? SCENE_INSTANCES : 0u;
   if (!h.volumes.empty())

@@ -50,6 +50,7 @@ struct HostScene {
   uint32_t inst_count{0};
   bool scene_normals{false};
   uint64_t instanced_triangles{0}; // triangles the instances place (not stored)
+  std::vector<uint32_t> obj_prim_base, obj_prim_count; // per object: its primitives
 };
 
 void build_host_scene(const phc_scene_desc &in, HostScene &out);

@@ -143,6 +143,7 @@ struct DevScene {
   const float4 *inst_w2o; // 3 per instance
   const uint4 *inst_info;
   uint32_t inst_count;
+  uint32_t scene_object_id; // instance id a ray back-end reports for the scene's own triangles
   int32_t scene_normals; // the scene's own triangles carry vertex normals
 };
 

@@ -478,6 +478,21 @@ PHC_HD RayHit trace_ray(const DevScene &sc, V3 o, V3 d, float tmin, float tmax, 
   return s.best;
 }
 
+// Full two-level traversal of one ray; `inst` gets the hit's instance slot
+// (INST_NONE: the scene's own triangles, or a miss).
+template <bool ANY, bool COUNT>
+PHC_HD RayHit trace_ray2(const DevScene &sc, V3 o, V3 d, float tmin, float tmax, TravCounters *ctr, uint32_t &inst)
+{
+  TravState2 s;
+  trav_init2(s, o, d, tmin, tmax);
+  uint2 stack[PHC_STACK_SIZE];
+  if (s.g_hits != 0u)
+    while (trav_step2<ANY, COUNT>(sc.nodes, sc.tris, sc.inst_w2o, sc.inst_info, s, stack, ctr)) {
+    }
+  inst = s.best_inst;
+  return s.best;
+}
+
 // Attributes of a hit as intersect_mesh_bvh computes them after the
 // traversal (mesh_intersector.h:129-178): position, geometric normal,
 // interpolated shading normal, material id.

@@ -42,6 +42,8 @@ SIGNATURES = {
     "phc_adjoint": (C.c_int, [vp, vp, vp, C.c_uint32, vp, vp]),
     "phc_adjoint_sizes": (C.c_int, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "phc_accel_create": (C.c_int, [C.POINTER(vp), vp, C.c_uint64, vp, C.c_uint64, vp, vp]),
+    "phc_accel_create_instanced": (C.c_int, [C.POINTER(vp), vp, C.c_uint64, vp, C.c_uint64, vp, vp, vp, C.c_uint32,
+                                             vp, C.c_uint32]),
     "phc_accel_destroy": (None, [vp]),
     "phc_trace_closest": (C.c_int, [vp, vp, vp, vp, vp, C.c_uint32, vp, vp]),
     "phc_trace_closest_compact": (C.c_int, [vp, vp, vp, vp, vp, C.c_uint32, vp, vp]),

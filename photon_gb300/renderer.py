@@ -175,16 +175,30 @@ def tuning_get(key: str) -> int:
 class Accel:
     """Level A: the ray back-end over caller device pointers (torch tensors)."""
 
-    def __init__(self, positions, indices, normals=None, material_ids=None):
+    def __init__(self, positions, indices, normals=None, material_ids=None, objects=None, instances=None):
+        """objects / instances: instanced geometry (RayBackend::build_accel_instanced),
+        as in scene.PtData: dicts of positions, indices, normals, material_id, and
+        (object_id, column-major 4x4 object-to-world) pairs."""
         self.lib = load()
-        pos = np.ascontiguousarray(positions, np.float32)
-        idx = np.ascontiguousarray(indices, np.uint32)
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+        idx = np.ascontiguousarray(indices, np.uint32).reshape(-1)
         nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
         mid = None if material_ids is None else np.ascontiguousarray(material_ids, np.uint32)
         h = C.c_void_p()
-        rc = self.lib.phc_accel_create(C.byref(h), pos.ctypes.data, pos.size // 3, idx.ctypes.data, idx.size // 3,
-                                       None if nrm is None else nrm.ctypes.data,
-                                       None if mid is None else mid.ctypes.data)
+        if objects and instances:
+            from .scene import PtData
+            keep = []
+            pt = PtData(objects=list(objects), instances=list(instances)).desc(keep)
+            self._keep = keep
+            rc = self.lib.phc_accel_create_instanced(
+                C.byref(h), pos.ctypes.data if pos.size else None, pos.size // 3,
+                idx.ctypes.data if idx.size else None, idx.size // 3, None if nrm is None else nrm.ctypes.data,
+                None if mid is None else mid.ctypes.data, C.cast(pt.objects, C.c_void_p), pt.object_count,
+                C.cast(pt.instances, C.c_void_p), pt.instance_count)
+        else:
+            rc = self.lib.phc_accel_create(C.byref(h), pos.ctypes.data, pos.size // 3, idx.ctypes.data, idx.size // 3,
+                                           None if nrm is None else nrm.ctypes.data,
+                                           None if mid is None else mid.ctypes.data)
         if rc != 0:
             raise PhotonError(rc, self.lib.phc_accel_error().decode())
         self.h = h
