@@ -492,7 +492,9 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
    "shade_lean" (0/1: lean shading kernels for scenes without volumes /
    sources / lights), "sort_threshold" (sort the hit queue by material when it
    holds at least this many hits; 0: never), "max_leaf" (1..3, BVH8 leaf size,
-   read at the next scene upload), "batch_wave_paths", "use_graph" (0/1),
+   read at the next scene upload), "gpu_bvh" (0/1: build the BVH8 of
+   single-level scenes on the GPU, leaves of one triangle, read at the next
+   scene upload), "batch_wave_paths", "use_graph" (0/1),
    "count_traversal" (0/1), "time_kernels" (0/1).  Returns PHC_ERR_INVALID
    for an unknown key or out-of-range value; get returns -1 for an unknown
    key.  Settings are process-wide and read at the start of each call. */

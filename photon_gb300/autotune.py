@@ -4,7 +4,8 @@ Coordinate descent on one workload: each key in turn takes every candidate
 value of SPACE with the other keys fixed, and keeps the value with the lowest
 median device time of a render call (phc_render's render_ms, after a warm-up
 call).  Passes repeat until a pass changes nothing or `passes` is reached.
-"max_leaf" changes the BVH8 and is applied by re-uploading the scene.
+"max_leaf" and "gpu_bvh" change the BVH8 and are applied by re-uploading the
+scene.
 
 The reference has no tunables on this path; the keys are this renderer's:
 queue capacity (wave_paths), persistent grid sizes of the traversal and
@@ -30,8 +31,9 @@ SPACE = {
     "shade_lean": [0, 1],
     "sort_threshold": [0, 1 << 12, 1 << 14, 1 << 16, 1 << 18, 1 << 20],
     "max_leaf": [1, 2, 3],
+    "gpu_bvh": [0, 1],
 }
-SCENE_KEYS = {"max_leaf"}  # read at scene upload
+SCENE_KEYS = {"max_leaf", "gpu_bvh"}  # read at scene upload
 
 
 class RenderTimer:

@@ -237,6 +237,10 @@ int phc_accel_create_instanced(phc_accel **out, const float *positions, uint64_t
       delete a;
       return fail(PHC_ERR_CUDA, err);
     }
+    if (a->scene.bvh_depth >= 64) {
+      delete a;
+      return fail(PHC_ERR_LIMIT, "BVH deeper than the traversal stack (64 levels)");
+    }
   } catch (const std::bad_alloc &) {
     delete a;
     return fail(PHC_ERR_OOM, "host allocation failed");

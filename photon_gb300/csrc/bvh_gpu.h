@@ -1,0 +1,22 @@
+// GPU construction of the BVH8 (bvh_gpu.cu): Morton sort, parallel
+// locally-ordered clustering, collapse into the quantised 8-wide nodes of
+// bvh8.h with leaves of one triangle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace phc {
+
+struct GpuBvh8 {
+  void *nodes{nullptr}; // node_cap x 80 bytes (cudaMalloc; the caller frees)
+  void *tris{nullptr};  // tri_count x 48 bytes (cudaMalloc; the caller frees)
+  uint32_t node_count{0}, node_cap{0}, tri_count{0}, max_depth{0};
+};
+
+// positions: float4 per vertex; prim_vidx: (i0, i1, i2, material) per
+// triangle, both on the device.  Blocks on `s` until the build is done.
+GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t triangle_count, cudaStream_t s);
+
+} // namespace phc

@@ -1227,6 +1227,10 @@ int phc_set_scene(phc_renderer *r, const phc_scene_desc *desc)
     const std::string err = r->scene.upload(hs, r->stream);
     if (!err.empty())
       throw ApiError(err.find("out of memory") != std::string::npos ? PHC_ERR_OOM : PHC_ERR_CUDA, err);
+    if (r->scene.bvh_depth >= 64) { // a GPU-built BVH8 is checked here
+      r->scene.release();
+      throw ApiError(PHC_ERR_LIMIT, "BVH deeper than the traversal stack (64 levels)");
+    }
     r->atlas_textures = false;
     for (const DevMaterial &m : hs.materials)
       r->atlas_textures = r->atlas_textures || m.base_tex >= 0 || m.alpha_tex >= 0;

@@ -5,6 +5,7 @@
 // arithmetic (this file is compiled with -ffp-contract=off) so the device sees
 // identical CDFs, majorants and light densities, then uploaded to HBM.
 #include "scene_build.h"
+#include "bvh_gpu.h"
 #include "tuning.h"
 
 #include <algorithm>
@@ -764,9 +765,14 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     s.eps = std::min(std::max(e, 1e-6f), 1e-2f);
   }
   s.strategy_count = uint32_t(s.lights.size()) + (s.emissive_cdf.empty() ? 0u : 1u) + (s.has_env ? 1u : 0u);
-  build_bvh8(pos3.data(), vc, s.indices.data(), tc, s.bvh, tuning().max_leaf);
   s.scene_normals = !empty && in.normals;
-  if (pt && pt->instance_count && pt->object_count)
+  const bool instanced = pt && pt->instance_count && pt->object_count;
+  if (tuning().gpu_bvh && !instanced && !empty) {
+    s.bvh_on_gpu = true; // single-level scenes: the upload builds the BVH8 on the GPU
+    return;
+  }
+  build_bvh8(pos3.data(), vc, s.indices.data(), tc, s.bvh, tuning().max_leaf);
+  if (instanced)
     build_instancing(*pt, !empty, lo, hi, s, tuning().max_leaf);
 }
 
@@ -868,6 +874,23 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   if (!err.empty()) {
     release();
     return err;
+  }
+  if (h.bvh_on_gpu) {
+    try {
+      const GpuBvh8 g = build_bvh8_gpu(d.positions, d.prim_vidx, uint32_t(h.prim_vidx.size() / 4), s);
+      allocations.push_back(g.nodes);
+      allocations.push_back(g.tris);
+      bytes += size_t(g.node_cap) * 80 + size_t(g.tri_count) * 48;
+      d.nodes = static_cast<const uint4 *>(g.nodes);
+      d.tris = static_cast<const float4 *>(g.tris);
+      d.node_count = g.node_count;
+      node_bytes = uint64_t(g.node_count) * 80;
+      tri_bytes = uint64_t(g.tri_count) * 48;
+      bvh_depth = g.max_depth;
+    } catch (const std::exception &ex) {
+      release();
+      return ex.what();
+    }
   }
   const cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {

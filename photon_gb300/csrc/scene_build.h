@@ -51,6 +51,7 @@ struct HostScene {
   bool scene_normals{false};
   uint64_t instanced_triangles{0}; // triangles the instances place (not stored)
   std::vector<uint32_t> obj_prim_base, obj_prim_count; // per object: its primitives
+  bool bvh_on_gpu{false}; // `bvh` left empty: DeviceScene::upload builds it on the GPU
 };
 
 void build_host_scene(const phc_scene_desc &in, HostScene &out);

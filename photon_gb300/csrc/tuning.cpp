@@ -37,6 +37,7 @@ const Key *keys(size_t &n)
       {"shade_lean", "PHC_TUNE_SHADE_LEAN", 0, 1, nullptr, &g_tuning.shade_lean},
       {"batch_wave_paths", "PHC_TUNE_BATCH_WAVE_PATHS", 1024, int64_t(1) << 30, &g_tuning.batch_wave_paths, nullptr},
       {"sort_threshold", "PHC_TUNE_SORT_THRESHOLD", 0, int64_t(1) << 30, &g_tuning.sort_threshold, nullptr},
+      {"gpu_bvh", "PHC_TUNE_GPU_BVH", 0, 1, nullptr, &g_tuning.gpu_bvh},
   };
   n = sizeof(k) / sizeof(k[0]);
   return k;

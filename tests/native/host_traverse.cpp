@@ -48,6 +48,18 @@ extern "C" int ht_trace(const float *pos, uint64_t nv, const uint32_t *idx, uint
 // scene's own triangles or a miss), world hit position and world normals
 // as the shading kernels compute them (hit_attributes).
 #include "scene_build.h"
+#include "bvh_gpu.h"
+
+#include <stdexcept>
+
+namespace phc {
+// The harness never uploads a scene, so the GPU builder (bvh_gpu.cu, compiled
+// by nvcc) is not linked in; scene_build.cpp's upload refers to it.
+GpuBvh8 build_bvh8_gpu(const float4 *, const uint4 *, uint32_t, cudaStream_t)
+{
+  throw std::runtime_error("the host harness builds no BVH on the GPU");
+}
+} // namespace phc
 
 extern "C" int ht_trace_instanced(const phc_scene_desc *desc, const float *orgs, const float *dirs,
     const float *tmin, const float *tmax, uint32_t n, int any_hit, float *out4, uint32_t *obj, float *geo9,
