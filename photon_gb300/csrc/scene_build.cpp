@@ -289,7 +289,8 @@ void build_volumes(const phc_scene_desc &in, HostScene &s)
           const size_t cell = (size_t(mz) * v.macro_dims[1] + my) * v.macro_dims[0] + mx;
           s.vol_majorants[base + cell] = bound * vd.density_scale * 1.01f;
         }
-    s.vol_values.insert(s.vol_values.end(), vals, vals + nvals);
+    if (nvals)
+      s.vol_value_spans.push_back({vals, nvals}); // copied to the device from the caller's array
     value_offset += nvals;
     tf_offset += table;
     s.volumes.push_back(v);
@@ -637,11 +638,13 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     const size_t n = size_t(td.width) * td.height;
     if (n && !td.rgb)
       throw std::invalid_argument("scene: texture pixels pointer is null");
+    const size_t at = s.texels.size();
+    s.texels.resize(at + 4 * n);
     for (size_t k = 0; k < n; ++k) {
-      s.texels.push_back(td.rgb[3 * k]);
-      s.texels.push_back(td.rgb[3 * k + 1]);
-      s.texels.push_back(td.rgb[3 * k + 2]);
-      s.texels.push_back(1.f);
+      s.texels[at + 4 * k] = td.rgb[3 * k];
+      s.texels[at + 4 * k + 1] = td.rgb[3 * k + 1];
+      s.texels[at + 4 * k + 2] = td.rgb[3 * k + 2];
+      s.texels[at + 4 * k + 3] = 1.f;
     }
     offset += n;
     s.samplers.push_back(si);
@@ -664,7 +667,8 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     const size_t n = sd.texels ? size_t(sd.texel_count) : 0;
     if (si.type != 3 && n < size_t(si.size[0]) * si.size[1] * si.size[2])
       si.type = 3; // incomplete image: a transform keeps lookups in bounds
-    s.texels.insert(s.texels.end(), sd.texels, sd.texels + 4 * n);
+    if (n)
+      s.texel_spans.push_back({sd.texels, 4 * n});
     offset += n;
     s.samplers.push_back(si);
   }
@@ -808,6 +812,39 @@ template <class T> T *DeviceScene::put(const std::vector<T> &v, cudaStream_t s, 
   return static_cast<T *>(p);
 }
 
+// An owned host array followed by spans of the caller's arrays, in one
+// device array (texels: the atlas, then every sampler's texels; volume
+// values: every volume's field), in the offsets build_host_scene assigned.
+float *DeviceScene::put_spans(const std::vector<float> &owned, const std::vector<HostScene::Span> &spans,
+    cudaStream_t s, std::string &err)
+{
+  size_t total = owned.size();
+  for (const HostScene::Span &sp : spans)
+    total += sp.floats;
+  if (total == 0 || !err.empty())
+    return nullptr;
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, total * sizeof(float));
+  if (e != cudaSuccess) {
+    err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  allocations.push_back(p);
+  bytes += total * sizeof(float);
+  float *dst = static_cast<float *>(p);
+  if (!owned.empty())
+    e = cudaMemcpyAsync(dst, owned.data(), owned.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+  size_t at = owned.size();
+  for (const HostScene::Span &sp : spans) {
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dst + at, sp.p, sp.floats * sizeof(float), cudaMemcpyHostToDevice, s);
+    at += sp.floats;
+  }
+  if (e != cudaSuccess)
+    err = std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e);
+  return dst;
+}
+
 std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
 {
   release();
@@ -827,7 +864,7 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   std::memcpy(d.attr_offset, h.attr_offset, sizeof(d.attr_offset));
   d.samplers = put(h.samplers, s, err);
   d.sampler_count = uint32_t(h.samplers.size());
-  d.texels = reinterpret_cast<const float4 *>(put(h.texels, s, err));
+  d.texels = reinterpret_cast<const float4 *>(put_spans(h.texels, h.texel_spans, s, err));
   d.lights = put(h.lights, s, err);
   d.light_count = uint32_t(h.lights.size());
   d.emissive_ids = put(h.emissive_ids, s, err);
@@ -845,7 +882,7 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   d.env_visible = h.env_visible ? 1 : 0;
   d.volumes = put(h.volumes, s, err);
   d.volume_count = uint32_t(h.volumes.size());
-  d.vol_values = put(h.vol_values, s, err);
+  d.vol_values = put_spans(h.vol_values, h.vol_value_spans, s, err);
   d.vol_tf = reinterpret_cast<const float4 *>(put(h.vol_tf, s, err));
   d.vol_majorants = put(h.vol_majorants, s, err);
   d.strategy_count = h.strategy_count;
@@ -871,6 +908,8 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   tri_bytes = uint64_t(h.bvh.tris.size()) * 4;
   bvh_depth = h.bvh.max_depth;
   texel_count = uint64_t(h.texels.size() / 4);
+  for (const HostScene::Span &sp : h.texel_spans)
+    texel_count += sp.floats / 4;
   if (!err.empty()) {
     release();
     return err;

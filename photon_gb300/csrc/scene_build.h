@@ -30,7 +30,16 @@ struct HostScene {
   std::vector<float> attr_values;     // float4
   int32_t attr_offset[5]{-1, -1, -1, -1, -1};
   std::vector<DevSampler> samplers;
-  std::vector<float> texels;          // float4
+  std::vector<float> texels;          // float4 (atlas textures, converted from RGB)
+  // sampler texels, read from the caller's arrays (valid for the set-scene
+  // call that builds and uploads this scene) and copied straight to the
+  // device after `texels`
+  struct Span {
+    const float *p;
+    size_t floats;
+  };
+  std::vector<Span> texel_spans;
+  std::vector<Span> vol_value_spans; // volume fields, likewise
   std::vector<DevLight> lights;
   std::vector<uint32_t> emissive_ids;
   std::vector<float> emissive_cdf, prim_light_pdf;
@@ -71,6 +80,8 @@ struct DeviceScene {
 
 private:
   template <class T> T *put(const std::vector<T> &v, cudaStream_t s, std::string &err);
+  float *put_spans(const std::vector<float> &owned, const std::vector<HostScene::Span> &spans, cudaStream_t s,
+      std::string &err);
 };
 
 } // namespace phc
