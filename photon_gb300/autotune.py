@@ -26,7 +26,7 @@ SPACE = {
     "trace_blocks_per_sm": [4, 8, 12, 16, 24, 32],
     "shade_blocks_per_sm": [2, 4, 6, 8, 12, 16],
     "trace_refill": [1, 4, 8, 12, 16, 32],
-    "wave_paths": [1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25],
+    "wave_paths": [1 << 20, 1 << 22, 1 << 24, 1 << 25, 1 << 26, 1 << 27],
     "split_shade": [0, 1],
     "shade_lean": [0, 1],
     "sort_threshold": [0, 1 << 12, 1 << 14, 1 << 16, 1 << 18, 1 << 20],

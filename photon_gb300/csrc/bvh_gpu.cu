@@ -37,7 +37,10 @@
 namespace phc {
 namespace {
 
-constexpr int RADIUS = 16;   // PLOC search radius (clusters on each side)
+#ifndef PHC_PLOC_RADIUS
+#define PHC_PLOC_RADIUS 16
+#endif
+constexpr int RADIUS = PHC_PLOC_RADIUS; // PLOC search radius (clusters on each side)
 constexpr int SORT_BLOCK = 256;
 constexpr int TILE = 256;    // clusters per block of the neighbour search
 

@@ -11,7 +11,8 @@
 namespace phc {
 
 struct Tuning {
-  int64_t wave_paths{1 << 25};       // paths in flight per wave (lanes = wave_paths / pixels)
+  int64_t wave_paths{1 << 27};       // paths in flight per wave (lanes = wave_paths / pixels); 2^27 holds a
+                                     // 1024^2 x 128-spp frame in one wave (~36 GB of path state)
   int trace_blocks_per_sm{32};       // persistent grid of the traversal kernels (128 threads; capped by occupancy)
   int shade_blocks_per_sm{16};       // persistent grid of the shading kernel (128 threads; capped by occupancy)
   int use_graph{1};                  // replay each wave as a CUDA graph
