@@ -40,8 +40,6 @@ void set_global_error(const std::string &msg);
 namespace {
 
 // ----------------------------------------------------------------- model
-using M16 = float[16];
-
 void identity16(float *m)
 {
   for (int i = 0; i < 16; ++i)
@@ -629,7 +627,6 @@ Parsed parse(const std::string &path, bool use_instancing)
   std::vector<GState> stack;
   GState st;
   identity16(st.xf);
-  bool in_world = false;
   std::string object;
   std::map<std::string, uint64_t> inst_count;
   uint64_t total_tris = 0;
@@ -742,7 +739,6 @@ Parsed parse(const std::string &path, bool use_instancing)
     } else if (d == "Identity") {
       identity16(st.xf);
     } else if (d == "WorldBegin") {
-      in_world = true;
       identity16(st.xf);
     } else if (d == "AttributeBegin") {
       stack.push_back(st);
@@ -898,7 +894,6 @@ Parsed parse(const std::string &path, bool use_instancing)
       skip_params(lx);
     }
   }
-  (void)in_world;
   return sc;
 }
 
