@@ -76,6 +76,16 @@ __global__ void __launch_bounds__(256) k_raygen(const RenderConst *__restrict__ 
   const RenderConst &rc = *rcp;
   const uint32_t wave = *wc.wave;
   const uint32_t total = rc.npix * rc.lanes;
+  // Without adaptive sampling the live slots are a prefix of the slot order
+  // (lane-major: the lanes below spp - wave * lanes), so the queue is the slot
+  // order itself: position = slot, no atomic per warp.
+  const bool dense = !rc.adaptive;
+  if (dense) {
+    const uint32_t first = wave * rc.lanes;
+    const uint32_t live_lanes = first < rc.spp ? min(rc.lanes, rc.spp - first) : 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+      wc.count[0] = live_lanes * rc.npix;
+  }
   for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < total;
        base += gridDim.x * blockDim.x) {
     const uint32_t i = base + lane_id();
@@ -112,7 +122,7 @@ __global__ void __launch_bounds__(256) k_raygen(const RenderConst *__restrict__ 
         }
       }
     }
-    const uint32_t o = warp_append(wc.count, live);
+    const uint32_t o = dense ? i : warp_append(wc.count, live);
     if (live) {
       out.ray_o[o] = f4(ro, tmin);
       out.ray_d[o] = f4(rd, tmax);
