@@ -1,0 +1,510 @@
+// Photon's Kokkos BVH ray back-end as it executes on a GPU under Kokkos-CUDA,
+// restated so that the reference's own Level-A algorithm can be timed beside
+// this library's BVH8 back-end on the same GB300, on the same rays.
+//
+// This is a comparator, not part of the library: nothing in photon_gb300/
+// includes or links it.  It follows, step for step:
+//   * Bvh::build_cpu / build_node (src/photon/pt/bvh/bvh.cpp:20-125): binary
+//     BVH, split at the median centroid (std::nth_element) of the largest
+//     centroid-box axis, leaves of at most 4 triangles, 44-byte AoS nodes
+//     (include/photon/pt/bvh/bvh.h:11-19), a prim_ids indirection;
+//   * intersect_mesh_bvh (include/photon/pt/geom/mesh_intersector.h:57-181):
+//     one thread per ray, a 64-entry stack in local memory, whole-node
+//     copies, both child boxes tested before the push (nearer child first),
+//     any-hit early exit, then the hit attributes from the indexed mesh;
+//   * aabb_entry_distance (mesh_intersector.h:30-45), safe_inverse_direction
+//     (:47-53), intersect_triangle (triangle_intersect.h:18-52);
+//   * KokkosBackend::trace_closest / trace_occluded
+//     (src/photon/pt/backend/kokkos_backend.cpp:21-86): a parallel_for over
+//     the WorkOrder permutation of the ray indices (work_order.h:19-70),
+//     88-byte HitResult records (ray_backend.h:15-29) of which a miss writes
+//     only `hit`, u32 occlusion flags.
+// Device code is compiled with nvcc's defaults (multiply-add contraction on),
+// as the reference's CMake compiles its Kokkos-CUDA sources
+// (src/CMakeLists.txt:78-86).  The same per-ray function also runs on the
+// host (kbp_trace_host), which is how its traversal is checked against the
+// CPU oracle.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#define KBP_HD __host__ __device__ __forceinline__
+
+namespace kbp {
+
+struct F3 {
+  float x, y, z;
+};
+KBP_HD F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+KBP_HD F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+KBP_HD F3 operator*(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+KBP_HD float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+KBP_HD F3 cross(F3 a, F3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+KBP_HD F3 normalize(F3 v)
+{
+  const float len = sqrtf(dot(v, v));
+  return len > 0.f ? v * (1.f / len) : F3{0.f, 0.f, 0.f};
+}
+
+struct Box {
+  F3 lo{+1e30f, +1e30f, +1e30f}, hi{-1e30f, -1e30f, -1e30f};
+  void extend(F3 p)
+  {
+    lo.x = lo.x < p.x ? lo.x : p.x;
+    lo.y = lo.y < p.y ? lo.y : p.y;
+    lo.z = lo.z < p.z ? lo.z : p.z;
+    hi.x = hi.x > p.x ? hi.x : p.x;
+    hi.y = hi.y > p.y ? hi.y : p.y;
+    hi.z = hi.z > p.z ? hi.z : p.z;
+  }
+  void extend(const Box &b)
+  {
+    extend(b.lo);
+    extend(b.hi);
+  }
+};
+
+struct Node {
+  Box b;
+  uint32_t left, right, begin, count, is_leaf;
+};
+static_assert(sizeof(Node) == 44, "the reference's BvhNode is 44 bytes");
+
+struct Hit88 {
+  float t;
+  F3 position, normal, shading_normal;
+  float uv[2], bary[2];
+  F3 color;
+  uint32_t prim_id, geom_id, inst_id, material_id;
+  uint8_t hit, has_color, pad[2];
+};
+static_assert(sizeof(Hit88) == 88, "HitResult is 88 bytes");
+
+struct Mesh {
+  const F3 *pos;
+  const uint32_t *idx;
+  const F3 *nrm;       // may be null
+  const uint32_t *mat; // may be null
+  const Node *nodes;
+  const uint32_t *prim_ids;
+  uint32_t node_count;
+};
+
+// ---------------------------------------------------------------- build
+struct PrimRef {
+  uint32_t id;
+  Box b;
+  F3 c;
+};
+
+static uint32_t build_node(std::vector<Node> &nodes, std::vector<PrimRef> &prims, std::vector<uint32_t> &ids,
+    uint32_t begin, uint32_t end)
+{
+  const uint32_t id = uint32_t(nodes.size());
+  nodes.push_back(Node{});
+  Box b, cb;
+  for (uint32_t i = begin; i < end; ++i) {
+    b.extend(prims[i].b);
+    cb.extend(prims[i].c);
+  }
+  nodes[id].b = b;
+  nodes[id].count = end - begin;
+  if (end - begin <= 4) {
+    nodes[id].begin = uint32_t(ids.size());
+    for (uint32_t i = begin; i < end; ++i)
+      ids.push_back(prims[i].id);
+    nodes[id].is_leaf = 1;
+    return id;
+  }
+  nodes[id].begin = begin;
+  const F3 diag = cb.hi - cb.lo;
+  int axis = diag.y > diag.x ? 1 : 0;
+  if (diag.z > (axis == 0 ? diag.x : diag.y))
+    axis = 2;
+  const uint32_t mid = begin + (end - begin) / 2;
+  std::nth_element(prims.begin() + begin, prims.begin() + mid, prims.begin() + end,
+      [axis](const PrimRef &a, const PrimRef &c) {
+        return (axis == 0 ? a.c.x : (axis == 1 ? a.c.y : a.c.z)) < (axis == 0 ? c.c.x : (axis == 1 ? c.c.y : c.c.z));
+      });
+  const uint32_t l = build_node(nodes, prims, ids, begin, mid);
+  const uint32_t r = build_node(nodes, prims, ids, mid, end);
+  nodes[id].left = l;
+  nodes[id].right = r;
+  nodes[id].is_leaf = 0;
+  return id;
+}
+
+static void build(const F3 *pos, const uint32_t *idx, uint32_t ntris, std::vector<Node> &nodes,
+    std::vector<uint32_t> &ids)
+{
+  std::vector<PrimRef> prims(ntris);
+  for (uint32_t i = 0; i < ntris; ++i) {
+    const F3 v0 = pos[idx[3 * i]], v1 = pos[idx[3 * i + 1]], v2 = pos[idx[3 * i + 2]];
+    prims[i].id = i;
+    prims[i].b = Box{};
+    prims[i].b.extend(v0);
+    prims[i].b.extend(v1);
+    prims[i].b.extend(v2);
+    prims[i].c = (v0 + v1 + v2) * (1.f / 3.f);
+  }
+  nodes.clear();
+  ids.clear();
+  ids.reserve(ntris);
+  nodes.reserve(size_t(ntris) * 2);
+  if (ntris)
+    build_node(nodes, prims, ids, 0, ntris);
+}
+
+// ------------------------------------------------------------ traversal
+KBP_HD float entry_distance(const Box &b, F3 o, F3 inv, float tmin, float tmax)
+{
+  const float tx0 = (b.lo.x - o.x) * inv.x, tx1 = (b.hi.x - o.x) * inv.x;
+  const float ty0 = (b.lo.y - o.y) * inv.y, ty1 = (b.hi.y - o.y) * inv.y;
+  const float tz0 = (b.lo.z - o.z) * inv.z, tz1 = (b.hi.z - o.z) * inv.z;
+  const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+  const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+  return tn <= tf ? tn : -1.f;
+}
+
+KBP_HD float inv1(float x) { return 1.f / (fabsf(x) > 1e-20f ? x : (x < 0.f ? -1e-20f : 1e-20f)); }
+
+KBP_HD bool tri_test(F3 o, F3 d, F3 v0, F3 v1, F3 v2, float tmin, float tmax, float &t, float &u, float &v)
+{
+  const F3 e1 = v1 - v0, e2 = v2 - v0;
+  const F3 p = cross(d, e2);
+  const float det = dot(e1, p);
+  if (fabsf(det) < 1e-30f)
+    return false;
+  const float inv_det = 1.f / det;
+  const F3 tv = o - v0;
+  u = dot(tv, p) * inv_det;
+  if (u < 0.f || u > 1.f)
+    return false;
+  const F3 q = cross(tv, e1);
+  v = dot(d, q) * inv_det;
+  if (v < 0.f || (u + v) > 1.f)
+    return false;
+  t = dot(e2, q) * inv_det;
+  if (t < tmin || t > tmax)
+    return false;
+  return true;
+}
+
+// intersect_mesh_bvh; returns whether the ray hit, fills `h` for closest hits
+__host__ __device__ bool trace_one(const Mesh &m, F3 o, F3 d, float tmin, float tmax, bool any_hit, Hit88 *h)
+{
+  if (!(tmax > tmin) || m.node_count == 0)
+    return false;
+  const F3 inv{inv1(d.x), inv1(d.y), inv1(d.z)};
+  float best_t = tmax, bu = 0.f, bv = 0.f;
+  uint32_t best_prim = 0;
+  bool hit = false;
+  uint32_t stack[64];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp > 0) {
+    const Node node = m.nodes[stack[--sp]];
+    if (entry_distance(node.b, o, inv, tmin, best_t) < 0.f)
+      continue;
+    if (node.is_leaf) {
+      for (uint32_t i = 0; i < node.count; ++i) {
+        const uint32_t pid = m.prim_ids[node.begin + i];
+        const F3 v0 = m.pos[m.idx[3 * pid]], v1 = m.pos[m.idx[3 * pid + 1]], v2 = m.pos[m.idx[3 * pid + 2]];
+        float t, u, v;
+        if (!tri_test(o, d, v0, v1, v2, tmin, best_t, t, u, v))
+          continue;
+        best_t = t;
+        best_prim = pid;
+        hit = true;
+        bu = u;
+        bv = v;
+        if (any_hit)
+          return true;
+      }
+    } else if (sp + 2 <= 64) {
+      const float dl = entry_distance(m.nodes[node.left].b, o, inv, tmin, best_t);
+      const float dr = entry_distance(m.nodes[node.right].b, o, inv, tmin, best_t);
+      if (dl >= 0.f && dr >= 0.f) {
+        if (dl < dr) {
+          stack[sp++] = node.right;
+          stack[sp++] = node.left;
+        } else {
+          stack[sp++] = node.left;
+          stack[sp++] = node.right;
+        }
+      } else if (dl >= 0.f) {
+        stack[sp++] = node.left;
+      } else if (dr >= 0.f) {
+        stack[sp++] = node.right;
+      }
+    }
+  }
+  if (!hit || any_hit)
+    return hit;
+  const uint32_t i0 = m.idx[3 * best_prim], i1 = m.idx[3 * best_prim + 1], i2 = m.idx[3 * best_prim + 2];
+  const F3 v0 = m.pos[i0], v1 = m.pos[i1], v2 = m.pos[i2];
+  h->t = best_t;
+  h->position = o + d * best_t;
+  const F3 nn = normalize(cross(v1 - v0, v2 - v0));
+  h->normal = nn;
+  h->shading_normal = nn;
+  h->uv[0] = h->uv[1] = 0.f;
+  h->bary[0] = bu;
+  h->bary[1] = bv;
+  h->geom_id = 0;
+  h->material_id = 0;
+  const float w0 = 1.f - bu - bv, w1 = bu, w2 = bv;
+  if (m.nrm) {
+    F3 sn = normalize(m.nrm[i0] * w0 + m.nrm[i1] * w1 + m.nrm[i2] * w2);
+    if (dot(sn, nn) < 0.f)
+      sn = sn * -1.f;
+    h->shading_normal = sn;
+  }
+  if (m.mat)
+    h->material_id = m.mat[best_prim];
+  h->prim_id = best_prim;
+  h->color = F3{0.f, 0.f, 0.f};
+  h->has_color = 0;
+  return true;
+}
+
+// The record write of trace_closest (kokkos_backend.cpp:41-55): a miss
+// writes only `hit`, a hit every field but inst_id.
+KBP_HD void store_hit(Hit88 &out, const Hit88 &h, bool hit)
+{
+  out.hit = hit ? 1 : 0;
+  if (hit) {
+    out.t = h.t;
+    out.position = h.position;
+    out.normal = h.normal;
+    out.shading_normal = h.shading_normal;
+    out.uv[0] = h.uv[0];
+    out.uv[1] = h.uv[1];
+    out.bary[0] = h.bary[0];
+    out.bary[1] = h.bary[1];
+    out.prim_id = h.prim_id;
+    out.geom_id = h.geom_id;
+    out.material_id = h.material_id;
+    out.color = h.color;
+    out.has_color = h.has_color;
+  }
+}
+
+// WorkOrder (work_order.h:19-70): blocks of 256 items visited with a stride
+// coprime to the block count, near the golden ratio of it.
+struct WorkOrder {
+  uint32_t count, block, block_count, stride;
+};
+
+static WorkOrder work_order(uint32_t count)
+{
+  WorkOrder w{count, 256u, (count + 255u) / 256u, 1u};
+  if (w.block_count > 2) {
+    uint32_t c = uint32_t(0.6180339887 * double(w.block_count));
+    if (c < 1)
+      c = 1;
+    for (; c < w.block_count; ++c) {
+      uint32_t a = c, b = w.block_count;
+      while (b != 0) {
+        const uint32_t r = a % b;
+        a = b;
+        b = r;
+      }
+      if (a == 1) {
+        w.stride = c;
+        break;
+      }
+    }
+  }
+  return w;
+}
+
+KBP_HD int work_item(const WorkOrder &w, int i)
+{
+  const uint32_t b = uint32_t(i) / w.block, o = uint32_t(i) % w.block;
+  const uint32_t pb = uint32_t((static_cast<unsigned long long>(b) * w.stride) % w.block_count);
+  const uint32_t index = pb * w.block + o;
+  return index < w.count ? int(index) : -1;
+}
+
+__global__ void k_trace_closest(Mesh m, WorkOrder w, const F3 *__restrict__ o, const F3 *__restrict__ d,
+    const float *__restrict__ t0, const float *__restrict__ t1, Hit88 *__restrict__ hits)
+{
+  const int wi = int(blockIdx.x * blockDim.x + threadIdx.x);
+  if (wi >= int(w.block_count * w.block))
+    return;
+  const int i = work_item(w, wi);
+  if (i < 0)
+    return;
+  Hit88 h;
+  const bool hit = trace_one(m, o[i], d[i], t0[i], t1[i], false, &h);
+  store_hit(hits[i], h, hit);
+}
+
+__global__ void k_trace_occluded(Mesh m, WorkOrder w, const F3 *__restrict__ o, const F3 *__restrict__ d,
+    const float *__restrict__ t0, const float *__restrict__ t1, uint32_t *__restrict__ occ)
+{
+  const int wi = int(blockIdx.x * blockDim.x + threadIdx.x);
+  if (wi >= int(w.block_count * w.block))
+    return;
+  const int i = work_item(w, wi);
+  if (i < 0)
+    return;
+  occ[i] = trace_one(m, o[i], d[i], t0[i], t1[i], true, nullptr) ? 1u : 0u;
+}
+
+struct Accel {
+  std::vector<Node> nodes;
+  std::vector<uint32_t> ids;
+  std::vector<F3> pos, nrm;
+  std::vector<uint32_t> idx, mat;
+  void *dev[6]{};
+  Mesh host{}, device{};
+};
+
+} // namespace kbp
+
+using namespace kbp;
+
+static std::string g_err;
+
+static int fail(const std::string &m)
+{
+  g_err = m;
+  return -1;
+}
+
+template <class T>
+static int upload(void *&dst, const std::vector<T> &v)
+{
+  if (v.empty())
+    return 0;
+  if (cudaMalloc(&dst, v.size() * sizeof(T)) != cudaSuccess)
+    return -1;
+  return cudaMemcpy(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess ? 0 : -1;
+}
+
+extern "C" {
+
+const char *kbp_error() { return g_err.c_str(); }
+
+// Builds the binary BVH on the host (Bvh::build_cpu) and, with `device` set,
+// copies mesh and BVH to the current GPU.  Host arrays are copied.
+int kbp_create(void **out, const float *positions, uint64_t vertex_count, const uint32_t *indices,
+    uint64_t triangle_count, const float *normals, const uint32_t *material_ids, int device)
+{
+  if (!out || (triangle_count && (!positions || !indices)))
+    return fail("null argument");
+  for (uint64_t i = 0; i < 3 * triangle_count; ++i)
+    if (indices[i] >= vertex_count)
+      return fail("index out of range");
+  Accel *a = new Accel;
+  a->pos.assign((const F3 *)positions, (const F3 *)positions + vertex_count);
+  a->idx.assign(indices, indices + 3 * triangle_count);
+  if (normals)
+    a->nrm.assign((const F3 *)normals, (const F3 *)normals + vertex_count);
+  if (material_ids)
+    a->mat.assign(material_ids, material_ids + triangle_count);
+  build(a->pos.data(), a->idx.data(), uint32_t(triangle_count), a->nodes, a->ids);
+  a->host = Mesh{a->pos.data(), a->idx.data(), normals ? a->nrm.data() : nullptr,
+      material_ids ? a->mat.data() : nullptr, a->nodes.data(), a->ids.data(), uint32_t(a->nodes.size())};
+  if (device) {
+    if (upload(a->dev[0], a->pos) || upload(a->dev[1], a->idx) || upload(a->dev[2], a->nrm) ||
+        upload(a->dev[3], a->mat) || upload(a->dev[4], a->nodes) || upload(a->dev[5], a->ids)) {
+      for (void *p : a->dev)
+        if (p)
+          cudaFree(p);
+      delete a;
+      return fail("device upload failed");
+    }
+    a->device = Mesh{(const F3 *)a->dev[0], (const uint32_t *)a->dev[1], normals ? (const F3 *)a->dev[2] : nullptr,
+        material_ids ? (const uint32_t *)a->dev[3] : nullptr, (const Node *)a->dev[4], (const uint32_t *)a->dev[5],
+        uint32_t(a->nodes.size())};
+  }
+  *out = a;
+  return 0;
+}
+
+void kbp_destroy(void *h)
+{
+  Accel *a = (Accel *)h;
+  if (!a)
+    return;
+  for (void *p : a->dev)
+    if (p)
+      cudaFree(p);
+  delete a;
+}
+
+// node count, leaf count and tree depth of the built BVH
+void kbp_info(void *h, uint64_t *nodes, uint64_t *depth)
+{
+  Accel *a = (Accel *)h;
+  *nodes = a->nodes.size();
+  uint64_t dmax = 0;
+  std::vector<std::pair<uint32_t, uint32_t>> st;
+  if (!a->nodes.empty())
+    st.push_back({0u, 1u});
+  while (!st.empty()) {
+    auto [n, dd] = st.back();
+    st.pop_back();
+    dmax = std::max<uint64_t>(dmax, dd);
+    if (!a->nodes[n].is_leaf) {
+      st.push_back({a->nodes[n].left, dd + 1});
+      st.push_back({a->nodes[n].right, dd + 1});
+    }
+  }
+  *depth = dmax;
+}
+
+// trace_closest (any_hit 0: 88-byte records into hits) or trace_occluded
+// (any_hit 1: u32 flags into hits) on device pointers, on `stream`.
+// Asynchronous like a kernel launch; the caller synchronises.
+int kbp_trace(void *h, const float *o, const float *d, const float *tmin, const float *tmax, uint32_t n,
+    int any_hit, void *hits, void *stream)
+{
+  Accel *a = (Accel *)h;
+  if (!a || (!a->dev[4] && !a->nodes.empty()))
+    return fail("no device copy");
+  if (n == 0)
+    return 0;
+  const WorkOrder w = work_order(n);
+  const uint32_t items = w.block_count * w.block;
+  const uint32_t blocks = (items + 255u) / 256u;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (any_hit)
+    k_trace_occluded<<<blocks, 256, 0, s>>>(a->device, w, (const F3 *)o, (const F3 *)d, tmin, tmax,
+        (uint32_t *)hits);
+  else
+    k_trace_closest<<<blocks, 256, 0, s>>>(a->device, w, (const F3 *)o, (const F3 *)d, tmin, tmax, (Hit88 *)hits);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : fail(cudaGetErrorString(e));
+}
+
+// The same traversal on the host over host arrays (the check of this
+// restatement against the CPU oracle).
+int kbp_trace_host(void *h, const float *o, const float *d, const float *tmin, const float *tmax, uint32_t n,
+    int any_hit, void *hits)
+{
+  Accel *a = (Accel *)h;
+  if (!a)
+    return fail("null accel");
+  for (uint32_t i = 0; i < n; ++i) {
+    const F3 oi{o[3 * i], o[3 * i + 1], o[3 * i + 2]}, di{d[3 * i], d[3 * i + 1], d[3 * i + 2]};
+    if (any_hit) {
+      ((uint32_t *)hits)[i] = trace_one(a->host, oi, di, tmin[i], tmax[i], true, nullptr) ? 1u : 0u;
+    } else {
+      Hit88 hh;
+      const bool hit = trace_one(a->host, oi, di, tmin[i], tmax[i], false, &hh);
+      store_hit(((Hit88 *)hits)[i], hh, hit);
+    }
+  }
+  return 0;
+}
+
+} // extern "C"

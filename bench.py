@@ -15,12 +15,18 @@ Our arm prints one JSON line with
              step renders from host-side camera/settings and reads the colour
              channel back into pinned host memory;
   roofline   the dominant kernel's algorithmic bytes / its event-timed
-             duration against the measured HBM copy bandwidth;
+             duration against the measured HBM copy bandwidth, and against
+             the read bandwidth of an L2-resident buffer measured in the same
+             run (roofline.l2, baseline/l2_probe.cu);
   cpu_baseline  the CPU oracle (a restatement of the reference's algorithm)
              on the host cores, on a bounded sample of the same workload;
-  batched_vs_plain, adjoint, instancing  the batched mode against one call
-             at a time, the path-replay adjoint against the forward pass, and
-             the two-level BVH against flattened placements (each skippable).
+  batched_vs_plain, adjoint, instancing, configs  the batched mode against
+             one call at a time, the path-replay adjoint against the forward
+             pass, the two-level BVH against flattened placements, and the
+             box-room and 2M-triangle instanced configurations (each skippable);
+  kokkos_port  Level A of this library against the reference's Kokkos BVH
+             back-end restated for the GPU (baseline/kokkos_port.cu) on the
+             same rays, and the bound it gives on the reference's frame rate.
 --impl reference times that CPU implementation as the main line.
 Under torchrun (N > 1) every rank renders its own replica (the path is
 replicated, not sharded) and rank 0 prints the line.
@@ -150,6 +156,168 @@ def barrier(world):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
+
+
+def scene_configs(p, reps=1):
+    """The other single-GPU forward configurations, one render each after a
+    warm-up, device time: the box room (about 36 triangles, 512^2, 64 spp,
+    depth 8) and the 2M-triangle instanced scene (12 RGBA8 2048^2 noise
+    textures, 256^3 fBm volume, 1920^2, 256 spp, depth 12, adaptive
+    sampling, so Msamples/s counts the pixel samples actually traced)."""
+    from photon_gb300 import workloads
+    out = {}
+    for name, make in (("box_room_512", workloads.box_room), ("instanced_2m_1920", workloads.instanced_2m)):
+        sc, cam, st = make()
+        _log(f"configs: {name} generated")
+        r = p.Renderer()
+        t = time.perf_counter()
+        r.set_scene(sc)
+        upload = time.perf_counter() - t
+        r.render(cam, st, True)
+        ms, samples = [], []
+        for _ in range(reps):
+            r.render(cam, st, True)
+            s = r.stats()
+            ms.append(s["render_ms"])
+            samples.append(s["pixel_samples"])
+        m = sorted(ms)[len(ms) // 2]
+        k = ms.index(m)
+        out[name] = {"triangles": int(sc.triangle_count), "res": [st.width, st.height],
+                     "spp": st.pixel_samples, "depth": st.max_depth, "adaptive": int(st.adaptive_sampling),
+                     "render_ms": m, "pixel_samples": int(samples[k]),
+                     "msamples_per_s": samples[k] / (m / 1e3) / 1e6, "upload_s": upload}
+        r.close()
+        del sc
+    return out
+
+
+def workload_rays(sc, cam, width, height, seed=1):
+    """Three ray batches of the workload, built with this library's Level A:
+    camera rays (one jittered ray per pixel), diffuse bounce rays (cosine
+    directions about the geometric normal at the camera rays' hits) and
+    shadow rays from the same hits (half toward the sun, half over the upper
+    hemisphere, unbounded).  Device tensors (o, d, tmin, tmax) per batch."""
+    import numpy as np
+    import torch
+    import photon_gb300 as p
+    rng = np.random.default_rng(seed)
+    fwd = np.asarray(cam.direction[:], np.float32)
+    up = np.asarray(cam.up[:], np.float32)
+    right = np.cross(fwd, up)
+    right /= np.linalg.norm(right)
+    tup = np.cross(right, fwd)
+    th = np.tan(0.5 * cam.fovy)
+    aspect = cam.aspect if cam.aspect > 0 else width / height
+    py, px = np.mgrid[0:height, 0:width].astype(np.float32)
+    sx = (2.0 * (px + rng.random(px.shape, np.float32)) / width - 1.0) * th * aspect
+    sy = (2.0 * (py + rng.random(py.shape, np.float32)) / height - 1.0) * th
+    d = fwd[None] + sx.reshape(-1, 1) * right[None] + sy.reshape(-1, 1) * tup[None]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    n = d.shape[0]
+    o = np.broadcast_to(np.asarray(cam.position[:], np.float32), (n, 3)).copy()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+    cam_b = (dev(o), dev(d), dev(np.zeros(n)), dev(np.full(n, 1e30)))
+    acc = p.Accel(sc.positions, sc.indices, sc.normals, sc.material_ids)
+    rec = np.frombuffer(acc.trace_closest(*cam_b).cpu().numpy().tobytes(), p._abi.hit_dtype())
+    acc.close()
+    h = rec["hit"].astype(bool)
+    pos, ng = rec["position"][h], rec["normal"][h]
+    ng = np.where((np.sum(ng * d[h], 1) > 0)[:, None], -ng, ng)
+    m = len(pos)
+    # cosine-weighted directions about ng
+    u1, u2 = rng.random(m, np.float32), rng.random(m, np.float32)
+    r, phi = np.sqrt(u1), 2.0 * np.pi * u2
+    a = np.where(np.abs(ng[:, :1]) > 0.9, np.array([[0, 1, 0]], np.float32), np.array([[1, 0, 0]], np.float32))
+    t1 = np.cross(ng, a)
+    t1 /= np.linalg.norm(t1, axis=1, keepdims=True)
+    t2 = np.cross(ng, t1)
+    bd = (r * np.cos(phi))[:, None] * t1 + (r * np.sin(phi))[:, None] * t2 + np.sqrt(1 - u1)[:, None] * ng
+    bd /= np.linalg.norm(bd, axis=1, keepdims=True)
+    eps = 1e-4 * float(np.abs(sc.positions).max())
+    bo = pos + eps * ng
+    bounce_b = (dev(bo), dev(bd), dev(np.zeros(m)), dev(np.full(m, 1e30)))
+    sun = np.asarray((0.35, 0.55, -0.75), np.float32)
+    sun /= np.linalg.norm(sun)
+    sd = rng.normal(size=(m, 3)).astype(np.float32)
+    sd[:, 1] = np.abs(sd[:, 1])
+    sd /= np.linalg.norm(sd, axis=1, keepdims=True)
+    sd[::2] = sun
+    shadow_b = (dev(bo), dev(sd), dev(np.zeros(m)), dev(np.full(m, 1e30)))
+    return {"camera": cam_b, "bounce": bounce_b, "shadow": shadow_b}
+
+
+def kokkos_port_vs_ours(p, sc, cam, st, frame, reps=3):
+    """Level A of both back-ends on the same GPU and rays: this library's
+    BVH8 (phc_trace_closest / phc_trace_occluded, 88-byte HitResult records)
+    against the reference's Kokkos BVH back-end restated for the GPU
+    (baseline/kokkos_port.cu: binary median-split BVH, one thread per ray,
+    64-entry local stack).  Both calls are synchronous; wall time around
+    each call, median of `reps` after a warm-up.  Also a bound on the whole
+    frame: the reference's render needs at least its own traversal time for
+    this frame's closest and shadow rays (at the port's rates) plus this
+    library's time for everything else (camera rays, shading, bookkeeping),
+    so frame samples over that time bounds its Msamples/s from above."""
+    import numpy as np
+    import torch
+    import baseline
+    batches = workload_rays(sc, cam, st.width, st.height)
+    _log("kokkos port: ray batches built")
+    ours = p.Accel(sc.positions, sc.indices, sc.normals, sc.material_ids)
+    t = time.perf_counter()
+    port = baseline.KokkosPortAccel(sc.positions, sc.indices, sc.normals, sc.material_ids)
+    port_build_s = time.perf_counter() - t
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return sorted(ts)[len(ts) // 2]
+
+    out = {"port_bvh": {**port.info(), "build_s": port_build_s}}
+    for name, (o, d, t0, t1) in batches.items():
+        n = int(t0.numel())
+        any_hit = name == "shadow"
+        if any_hit:
+            a = torch.empty(n, dtype=torch.int32, device="cuda")
+            b = torch.empty(n, dtype=torch.int32, device="cuda")
+            t_ours = timed(lambda: ours.trace_occluded(o, d, t0, t1, a))
+            t_port = timed(lambda: port.trace(o, d, t0, t1, b, any_hit=True, stream=stream))
+            agree = float(np.mean((a.cpu().numpy() != 0) == (b.cpu().numpy() != 0)))
+        else:
+            a = torch.empty((n, 88), dtype=torch.uint8, device="cuda")
+            b = torch.zeros((n, 88), dtype=torch.uint8, device="cuda")
+            t_ours = timed(lambda: ours.trace_closest(o, d, t0, t1, a))
+            t_port = timed(lambda: port.trace(o, d, t0, t1, b, stream=stream))
+            ra = np.frombuffer(a.cpu().numpy().tobytes(), p._abi.hit_dtype())
+            rb = np.frombuffer(b.cpu().numpy().tobytes(), p._abi.hit_dtype())
+            same_hit = ra["hit"] == rb["hit"]
+            both = (ra["hit"] != 0) & (rb["hit"] != 0)
+            agree = float((same_hit & (~both | (ra["prim_id"] == rb["prim_id"]))).mean())
+        out[name] = {"rays": n, "ours_mrays_per_s": n / t_ours / 1e6, "port_mrays_per_s": n / t_port / 1e6,
+                     "ours_ms": t_ours * 1e3, "port_ms": t_port * 1e3, "speedup": t_port / t_ours,
+                     "agreement": agree}
+        _log(f"kokkos port: {name} timed")
+    ours.close()
+    port.close()
+    # the frame bound
+    prim = frame["pixel_samples"]
+    sec = max(0, frame["closest_rays"] - prim)
+    t_trav = (prim / (out["camera"]["port_mrays_per_s"] * 1e6) + sec / (out["bounce"]["port_mrays_per_s"] * 1e6)
+              + frame["shadow_rays"] / (out["shadow"]["port_mrays_per_s"] * 1e6))
+    t_rest = (frame["render_ms"] - frame["kernel_ms"]["trace_closest"] - frame["kernel_ms"]["trace_shadow"]) / 1e3
+    ref_bound = prim / (t_trav + t_rest) / 1e6
+    out["frame_bound"] = {"reference_traversal_s": t_trav, "other_work_s": t_rest,
+                          "reference_msamples_per_s_at_most": ref_bound,
+                          "closest_rays": int(frame["closest_rays"]), "shadow_rays": int(frame["shadow_rays"]),
+                          "pixel_samples": int(prim)}
+    return out
 
 
 def workload():
@@ -475,6 +643,10 @@ def run_ours(args, world, rank, local):
         "tris_per_ray": prof["tri_tests"] / max(1, prof["closest_rays"]),
         "launches": kcount["trace_closest"], "kernel_ms_total": kms["trace_closest"],
     }
+    import baseline
+    l2 = baseline.l2_read_gbs()
+    roofline["l2"] = {"peak": l2, "frac": achieved / l2, "unit": "GB/s",
+                      "peak_source": "one-launch read sweeps of a 32 MiB L2-resident buffer, measured in this run"}
 
     _log("e2e and kernel profile done")
     cpu = None
@@ -494,6 +666,18 @@ def run_ours(args, world, rank, local):
     if rank == 0 and not args.no_instancing:
         instancing = instancing_vs_flat(p)
         _log("instancing/flat done")
+    kokkos = None
+    if rank == 0 and not args.no_kokkos_port:
+        frame = {"pixel_samples": samples / args.steps, "closest_rays": closest / args.steps,
+                 "shadow_rays": shadow / args.steps, "render_ms": dev_ms / args.steps, "kernel_ms": kms}
+        kokkos = kokkos_port_vs_ours(p, sc, cam, st, frame)
+        kokkos["frame_bound"]["ours_msamples_per_s"] = value
+        kokkos["frame_bound"]["speedup_at_least"] = value / kokkos["frame_bound"]["reference_msamples_per_s_at_most"]
+        _log("kokkos port comparison done")
+    configs = None
+    if rank == 0 and not args.no_configs:
+        configs = scene_configs(p)
+        _log("other configurations done")
 
     if rank == 0:
         h2d = C.sizeof(cam) + C.sizeof(st)
@@ -515,6 +699,8 @@ def run_ours(args, world, rank, local):
             "batched_vs_plain": batched,
             "adjoint": adjoint,
             "instancing": instancing,
+            "configs": configs,
+            "kokkos_port": kokkos,
             "clocks": clk.summary(),
             "gpu_launches": launches,
         }
@@ -532,6 +718,10 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched/plain measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
     ap.add_argument("--no-instancing", action="store_true", help="skip the instanced/flattened measurement")
+    ap.add_argument("--no-kokkos-port", action="store_true",
+                    help="skip the Level-A comparison with the reference's Kokkos BVH back-end restated for the GPU")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the box-room and 2M-triangle instanced configurations")
     args = ap.parse_args()
     world, rank, local = dist_setup(args.gpus if args.impl == "ours" else 0)
     if args.impl == "reference":
