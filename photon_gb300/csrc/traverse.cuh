@@ -140,7 +140,11 @@ __device__ __forceinline__ float byte_f23(uint32_t w, int j)
 #endif
 
 // Intersects the 8 child boxes of one node; returns the k-ordered hit mask of
-// internal children (bit k = slot k ^ oct) and the triangle mask.
+// internal children (bit k = slot k ^ oct) and the triangle mask.  SLOTS
+// collects the box hits as one slot-order mask first and decodes the leaf
+// meta bytes only for hit leaves (fewer instructions per node when leaf hits
+// are rare, as for closest-hit rays); the masks are the same either way.
+template <bool SLOTS = false>
 PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V3 idir, uint32_t oct, float tmin,
     float tmax, uint32_t &child_base, uint32_t &hits, uint32_t &imask, uint32_t &tri_base, uint32_t &tri_hits)
 {
@@ -168,6 +172,7 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
   const uint32_t fz0 = nzl ? w4.z : w3.x, fz1 = nzl ? w4.w : w3.y;
   hits = 0u;
   tri_hits = 0u;
+  uint32_t slots = 0u; // SLOTS: bit s set when the ray overlaps child box s
 #ifdef __CUDA_ARCH__
   // (near, far) of one axis as a pair: q = (2^23 + byte) - 2^23 exactly, then
   // t = fma(q, a, b) per element.
@@ -189,7 +194,9 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
       upk2(fma2(add2(pk2(byte_f23(nzw, j), byte_f23(fzw, j)), m23), az2, bz2), tnz, tfz);
       const float t0 = fmaxf(max3f(tnx, tny, tnz), tmin);
       const float t1 = fminf(min3f(tfx, tfy, tfz), tmax);
-      if (t0 <= t1 * 1.0000004f) { // an empty slot (mb 0) adds nothing
+      if constexpr (SLOTS) {
+        slots |= (t0 <= t1 * 1.0000004f ? 1u : 0u) << (4 * h + j);
+      } else if (t0 <= t1 * 1.0000004f) { // an empty slot (mb 0) adds nothing
         const int s = 4 * h + j;
         if (mb & 0x80u)
           hits |= 1u << (uint32_t(s) ^ oct);
@@ -216,7 +223,9 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
       const float tfz = fmaf(byte_f(fzw, j), az, bz);
       const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
       const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
-      if (t0 <= t1 * 1.0000004f) { // an empty slot (mb 0) adds nothing
+      if constexpr (SLOTS) {
+        slots |= (t0 <= t1 * 1.0000004f ? 1u : 0u) << (4 * h + j);
+      } else if (t0 <= t1 * 1.0000004f) { // an empty slot (mb 0) adds nothing
         const int s = 4 * h + j;
         if (mb & 0x80u)
           hits |= 1u << (uint32_t(s) ^ oct);
@@ -226,6 +235,27 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
     }
   }
 #endif
+  if constexpr (SLOTS) {
+    // internal children: slot order -> visiting order (bit k = slot k ^ oct),
+    // one swap stage per octant bit
+    uint32_t m = slots & imask;
+    if (oct & 1u)
+      m = ((m << 1) & 0xaau) | ((m >> 1) & 0x55u);
+    if (oct & 2u)
+      m = ((m << 2) & 0xccu) | ((m >> 2) & 0x33u);
+    if (oct & 4u)
+      m = ((m << 4) & 0xf0u) | ((m >> 4) & 0x0fu);
+    hits = m;
+    // leaf children: their triangle ranges from the meta bytes (an empty slot,
+    // meta 0, adds nothing)
+    uint32_t lm = slots & ~imask;
+    while (lm) {
+      const uint32_t sl = ffs32(lm) - 1u;
+      lm &= lm - 1u;
+      const uint32_t mb = ((sl < 4u ? w1.z : w1.w) >> (8u * (sl & 3u))) & 0xffu;
+      tri_hits |= ((1u << (mb >> 5)) - 1u) << (mb & 31u);
+    }
+  }
 }
 
 // Resumable traversal state of one ray: the current node group (child base,
@@ -279,7 +309,7 @@ PHC_HD bool trav_step(const uint4 *__restrict__ nodes, const float4 *__restrict_
     ++s.sp;
   }
   uint32_t tri_base, tri_hits;
-  intersect_node(nodes, ni, s.o, s.idir, s.oct, s.tmin, s.best.t, s.g_base, s.g_hits, s.g_imask, tri_base,
+  intersect_node<!ANY>(nodes, ni, s.o, s.idir, s.oct, s.tmin, s.best.t, s.g_base, s.g_hits, s.g_imask, tri_base,
       tri_hits);
   if (COUNT)
     ctr->nodes++;
@@ -435,7 +465,7 @@ PHC_HD bool trav_step2(const uint4 *__restrict__ nodes, const float4 *__restrict
   if (s.g_hits != 0u)
     stack_push(stack, s.sp, s.g_base, s.g_hits | (s.g_imask << 8));
   uint32_t tri_base, tri_hits;
-  intersect_node(nodes, ni, s.o, s.idir, s.oct, s.tmin, s.best.t, s.g_base, s.g_hits, s.g_imask, tri_base,
+  intersect_node<!ANY>(nodes, ni, s.o, s.idir, s.oct, s.tmin, s.best.t, s.g_base, s.g_hits, s.g_imask, tri_base,
       tri_hits);
   if (COUNT)
     ctr->nodes++;

@@ -221,15 +221,17 @@ __global__ void __launch_bounds__(128, INST ? PHC_TRACE_MIN_BLOCKS_INST : PHC_TR
   uint32_t idx = 0, steps = 0, rays = 0, fetch_trips = 0, step_trips = 0, max_steps = 0, max_idx = 0;
   const uint4 *nodes = sc.nodes;
   const float4 *tris = sc.tris;
+  // The idle mask changes only when lanes finish or fetch, so the warp votes
+  // (refill, queue appends) run only on trips where some lane finished.
+  uint32_t idle = WARP_FULL;
   for (uint32_t trips = 0;; ++trips) {
     if (trips >= WAVE_TRIP_CAP) { // warp-uniform: every lane counts the same trips
       record_cap(wc, (WAVE_ERR_TRACE << 16) | uint32_t(it), n, *fetch, busy, exhausted, idx, in.ray_o[idx],
           in.ray_d[idx], s, steps, rays, fetch_trips, step_trips, max_steps, max_idx, trips);
       break;
     }
-    __syncwarp(); // every lane back from the last trip's divergent work before the votes
-    const uint32_t idle = __ballot_sync(WARP_FULL, !busy);
     if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= refill)) {
+      __syncwarp();
       const uint32_t k = uint32_t(__popc(idle));
       const uint32_t base = warp_fetch(fetch, k);
       ++fetch_trips;
@@ -254,8 +256,9 @@ __global__ void __launch_bounds__(128, INST ? PHC_TRACE_MIN_BLOCKS_INST : PHC_TR
           busy = true;
         }
       }
+      idle = __ballot_sync(WARP_FULL, !busy);
     }
-    if (__ballot_sync(WARP_FULL, busy) == 0u) {
+    if (idle == WARP_FULL) {
       if (exhausted)
         break;
       continue;
@@ -273,12 +276,29 @@ __global__ void __launch_bounds__(128, INST ? PHC_TRACE_MIN_BLOCKS_INST : PHC_TR
         max_idx = idx;
       }
     }
+    __syncwarp(); // every lane back from the step's divergent work before the vote
+    const uint32_t dm = __ballot_sync(WARP_FULL, done);
+    if (dm == 0u)
+      continue;
     if (SPLIT) {
       const bool is_hit = done && s.best.prim != 0xffffffffu;
-      const uint32_t ph = warp_append(wc.hcount + it, is_hit);
-      const uint32_t pm = warp_append(wc.mcount + it, done && !is_hit);
-      if (done)
-        (is_hit ? hq.hitq[ph] : hq.missq[pm]) = idx;
+      const uint32_t hm = __ballot_sync(WARP_FULL, is_hit);
+      const uint32_t mm = dm & ~hm;
+      uint32_t hb = 0, mb = 0;
+      if (lane == 0) {
+        if (hm)
+          hb = atomicAdd(wc.hcount + it, uint32_t(__popc(hm)));
+        if (mm)
+          mb = atomicAdd(wc.mcount + it, uint32_t(__popc(mm)));
+      }
+      hb = __shfl_sync(WARP_FULL, hb, 0);
+      mb = __shfl_sync(WARP_FULL, mb, 0);
+      if (done) {
+        if (is_hit)
+          hq.hitq[hb + uint32_t(__popc(hm & lt_mask))] = idx;
+        else
+          hq.missq[mb + uint32_t(__popc(mm & lt_mask))] = idx;
+      }
     }
     if (done) {
       hits[idx] = make_float4(s.best.t, __uint_as_float(s.best.prim), s.best.u, s.best.v);
@@ -286,6 +306,7 @@ __global__ void __launch_bounds__(128, INST ? PHC_TRACE_MIN_BLOCKS_INST : PHC_TR
         hq.inst[idx] = s.best_inst;
       busy = false;
     }
+    idle |= dm;
   }
   if (COUNT) {
     atomicAdd((unsigned long long *)&stats[0], (unsigned long long)ctr.nodes);
