@@ -171,6 +171,71 @@ void build_env_cdf(HostScene &s)
   }
 }
 
+// Guide tables for the CDF searches of the shading kernels.  The searches
+// themselves are the reference's: the largest row / column i with
+// cdf[i] <= u (environment_map.h:62-104) and the first emissive triangle with
+// cdf[i] > u (pathtracer.cpp:296-306).  Both results are non-decreasing in u
+// when the CDF is, so the result for u lies between the results for the two
+// grid points k / G <= u < (k + 1) / G, which the guide stores; the device
+// bisects only that range.  A CDF that is not non-decreasing (NaN texels)
+// keeps the plain bisection, whose probe order then decides the result.
+static bool non_decreasing(const float *c, uint32_t n)
+{
+  for (uint32_t i = 1; i < n; ++i)
+    if (!(c[i - 1] <= c[i]))
+      return false;
+  return true;
+}
+
+// guide[k] = max{i in [0, n - 1] : cdf[i] <= k / G} (0 when none), guide[G] = n - 1
+static void le_guide(const float *cdf, uint32_t n, uint32_t bits, uint32_t *out)
+{
+  const uint32_t G = 1u << bits;
+  uint32_t i = 0;
+  for (uint32_t k = 0; k < G; ++k) {
+    const float u = float(k) / float(G);
+    while (i + 1 < n && cdf[i + 1] <= u)
+      ++i;
+    out[k] = i;
+  }
+  out[G] = n - 1;
+}
+
+void build_search_guides(HostScene &s)
+{
+  s.emissive_guide.clear();
+  s.env_mguide.clear();
+  s.env_cguide.clear();
+  const uint32_t ne = uint32_t(s.emissive_cdf.size());
+  if (ne > 1 && non_decreasing(s.emissive_cdf.data(), ne)) {
+    // guide[k] = min({i in [0, n - 2] : cdf[i] > k / G} U {n - 1}), guide[G] = n - 1
+    const uint32_t G = 1u << EMISSIVE_GUIDE_BITS;
+    s.emissive_guide.resize(G + 1);
+    uint32_t i = 0;
+    for (uint32_t k = 0; k < G; ++k) {
+      const float u = float(k) / float(G);
+      while (i < ne - 1 && s.emissive_cdf[i] <= u)
+        ++i;
+      s.emissive_guide[k] = i;
+    }
+    s.emissive_guide[G] = ne - 1;
+  }
+  if (s.has_env && s.env_w > 0 && s.env_h > 0) {
+    const uint32_t w = s.env_w, h = s.env_h;
+    bool ok = non_decreasing(s.env_marginal.data(), h + 1);
+    for (uint32_t y = 0; ok && y < h; ++y)
+      ok = non_decreasing(&s.env_conditional[size_t(y) * (w + 1)], w + 1);
+    if (ok) {
+      const uint32_t gm = (1u << ENV_MGUIDE_BITS) + 1, gc = (1u << ENV_CGUIDE_BITS) + 1;
+      s.env_mguide.resize(gm);
+      le_guide(s.env_marginal.data(), h, ENV_MGUIDE_BITS, s.env_mguide.data());
+      s.env_cguide.resize(size_t(h) * gc);
+      for (uint32_t y = 0; y < h; ++y)
+        le_guide(&s.env_conditional[size_t(y) * (w + 1)], w, ENV_CGUIDE_BITS, &s.env_cguide[size_t(y) * gc]);
+    }
+  }
+}
+
 // Volume tables and the macro-cell majorant grid (RenderBridge.cpp:622-778):
 // per macro cell the largest extinction the transfer function reaches over
 // the values the trilinear field can take inside it, with a 1% margin.
@@ -769,6 +834,7 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     s.eps = std::min(std::max(e, 1e-6f), 1e-2f);
   }
   s.strategy_count = uint32_t(s.lights.size()) + (s.emissive_cdf.empty() ? 0u : 1u) + (s.has_env ? 1u : 0u);
+  build_search_guides(s);
   s.scene_normals = !empty && in.normals;
   const bool instanced = pt && pt->instance_count && pt->object_count;
   if (tuning().gpu_bvh && !instanced && !empty) {
@@ -874,6 +940,9 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   d.env_pixels = reinterpret_cast<const float4 *>(put(h.env_pixels4, s, err));
   d.env_marginal = put(h.env_marginal, s, err);
   d.env_conditional = put(h.env_conditional, s, err);
+  d.emissive_guide = h.emissive_guide.empty() ? nullptr : put(h.emissive_guide, s, err);
+  d.env_mguide = h.env_mguide.empty() ? nullptr : put(h.env_mguide, s, err);
+  d.env_cguide = h.env_cguide.empty() ? nullptr : put(h.env_cguide, s, err);
   d.env_w = h.env_w;
   d.env_h = h.env_h;
   std::memcpy(d.env_w2t, h.env_w2t, sizeof(d.env_w2t));

@@ -46,6 +46,8 @@ struct HostScene {
   bool has_env{false}, env_visible{true};
   uint32_t env_w{0}, env_h{0};
   std::vector<float> env_pixels4, env_marginal, env_conditional;
+  // guide tables of the CDF searches (empty: plain bisection on the device)
+  std::vector<uint32_t> emissive_guide, env_mguide, env_cguide;
   float env_w2t[9]{1, 0, 0, 0, 1, 0, 0, 0, 1}, env_t2w[9]{1, 0, 0, 0, 1, 0, 0, 0, 1};
   std::vector<DevVolume> volumes;
   std::vector<float> vol_values, vol_tf, vol_majorants;

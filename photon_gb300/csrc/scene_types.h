@@ -96,6 +96,10 @@ struct DevVolume { // include/photon/pt/tf_volume.h:14-33
   uint32_t macro_dims[3];
 };
 
+constexpr uint32_t EMISSIVE_GUIDE_BITS = 10;
+constexpr uint32_t ENV_MGUIDE_BITS = 10;
+constexpr uint32_t ENV_CGUIDE_BITS = 8;
+
 struct DevScene {
   // geometry
   const uint4 *nodes;
@@ -120,6 +124,15 @@ struct DevScene {
   const float *emissive_cdf;
   const float *prim_light_pdf;
   uint32_t emissive_count;
+  // Guide tables of the three CDF searches (nullptr: plain binary search).
+  // Entry k of a guide is the search's result for u = k / G (G = 2^bits,
+  // exact in float), entry G its largest result; a search for u then only
+  // bisects [guide[k], guide[k + 1]] with k = u * G, which returns the same
+  // index as the bisection of the whole table for every u of the reference's
+  // RNG (multiples of 2^-24 in [0, 1)) when the CDF is non-decreasing.
+  const uint32_t *emissive_guide; // EMISSIVE_GUIDE_BITS: G + 1 entries
+  const uint32_t *env_mguide;     // ENV_MGUIDE_BITS: G + 1 entries (marginal)
+  const uint32_t *env_cguide;     // ENV_CGUIDE_BITS: h x (G + 1) entries (rows)
   // environment (environment_map.h)
   const float4 *env_pixels; // (h, w)
   const float *env_marginal; // h + 1

@@ -14,6 +14,7 @@
 // with __ldg.
 #pragma once
 
+#include "cdf_search.cuh"
 #include "pt_math.cuh"
 #include "scene_types.h"
 #include "traverse.cuh"
@@ -647,26 +648,10 @@ static __device__ __noinline__ V3 env_sample(const DevScene &sc, Rng &rng, float
 {
   const float u1 = rng.next();
   const float u2 = rng.next();
-  uint32_t lo = 0, hi = sc.env_h;
-  while (lo + 1 < hi) {
-    const uint32_t mid = (lo + hi) / 2;
-    if (__ldg(sc.env_marginal + mid) <= u2)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  const uint32_t row = lo;
+  const uint32_t row = cdf_search_le(sc.env_marginal, sc.env_h, sc.env_mguide, ENV_MGUIDE_BITS, u2);
   const float *c = sc.env_conditional + size_t(row) * (sc.env_w + 1);
-  lo = 0;
-  hi = sc.env_w;
-  while (lo + 1 < hi) {
-    const uint32_t mid = (lo + hi) / 2;
-    if (__ldg(c + mid) <= u1)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  const uint32_t col = lo;
+  const uint32_t col = cdf_search_le(c, sc.env_w,
+      sc.env_cguide ? sc.env_cguide + size_t(row) * ((1u << ENV_CGUIDE_BITS) + 1) : nullptr, ENV_CGUIDE_BITS, u1);
   const float row_pdf = __ldg(sc.env_marginal + row + 1) - __ldg(sc.env_marginal + row);
   const float col_pdf = __ldg(c + col + 1) - __ldg(c + col);
   const float u = (float(col) + rng.next()) / float(sc.env_w);
@@ -774,14 +759,7 @@ static __device__ __noinline__ DirectSample sample_direct(const DevScene &sc, V3
   }
   if (sc.emissive_count > 0 && pick == sc.light_count) {
     const float xi = rng.next();
-    uint32_t lo = 0, hi = sc.emissive_count - 1;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi) / 2;
-      if (__ldg(sc.emissive_cdf + mid) <= xi)
-        lo = mid + 1;
-      else
-        hi = mid;
-    }
+    const uint32_t lo = cdf_search_gt(sc.emissive_cdf, sc.emissive_count, sc.emissive_guide, EMISSIVE_GUIDE_BITS, xi);
     const uint32_t prim = __ldg(sc.emissive_ids + lo);
     const float pdf_area = __ldg(sc.prim_light_pdf + prim);
     if (!(pdf_area > 0.f))

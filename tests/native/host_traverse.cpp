@@ -1,11 +1,13 @@
 // Host build of the device BVH8 traversal (photon_gb300/csrc/traverse.cuh)
 // over the host BVH8 builder, for CPU tests of the traversal logic against the
 // oracle before any GPU run.  Test infrastructure only.
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <vector>
 
 #include "bvh8.h"
+#include "cdf_search.cuh"
 #include "traverse.cuh"
 
 using namespace phc;
@@ -118,5 +120,82 @@ extern "C" int ht_trace_instanced(const phc_scene_desc *desc, const float *orgs,
   stats[2] = h.bvh.node_count;
   stats[3] = h.bvh.max_depth;
   stats[4] = h.inst_count;
+  return 0;
+}
+
+// The guided CDF searches of the shading kernels (cdf_search.cuh) against
+// the plain bisection, over the scene's emissive CDF and environment CDFs:
+// every u of `us` and, per CDF, every u at and next to one of its entries
+// (RNG values: multiples of 2^-24 in [0, 1)).  counts: [0] guides present
+// (bit 0 emissive, 1 marginal, 2 rows), [1] emissive, [2] marginal, [3] row
+// searches compared, [4] mismatches.
+extern "C" int ht_guide_check(const phc_scene_desc *desc, const float *us, uint32_t n, uint64_t *counts)
+{
+  HostScene h;
+  build_host_scene(*desc, h);
+  for (int k = 0; k < 5; ++k)
+    counts[k] = 0;
+  counts[0] = (h.emissive_guide.empty() ? 0u : 1u) | (h.env_mguide.empty() ? 0u : 2u) |
+      (h.env_cguide.empty() ? 0u : 4u);
+  const float q = 1.f / 16777216.f;
+  // the RNG values at and next to each entry of a CDF
+  auto near_entries = [&](const float *c, uint32_t m, std::vector<float> &out) {
+    out.clear();
+    for (uint32_t i = 0; i < m; ++i) {
+      if (!(c[i] >= 0.f && c[i] < 1.f))
+        continue;
+      const float b = std::floor(c[i] / q) * q;
+      for (float v : {b - q, b, b + q})
+        if (v >= 0.f && v < 1.f)
+          out.push_back(v);
+    }
+  };
+  std::vector<float> extra;
+  const uint32_t ne = uint32_t(h.emissive_cdf.size());
+  if (ne > 0) {
+    const uint32_t *g = h.emissive_guide.empty() ? nullptr : h.emissive_guide.data();
+    near_entries(h.emissive_cdf.data(), ne, extra);
+    for (int pass = 0; pass < 2; ++pass) {
+      const float *vals = pass ? extra.data() : us;
+      const size_t m = pass ? extra.size() : n;
+      for (size_t i = 0; i < m; ++i) {
+        const uint32_t a = cdf_search_gt(h.emissive_cdf.data(), ne, nullptr, EMISSIVE_GUIDE_BITS, vals[i]);
+        const uint32_t b = cdf_search_gt(h.emissive_cdf.data(), ne, g, EMISSIVE_GUIDE_BITS, vals[i]);
+        counts[1]++;
+        counts[4] += a != b;
+      }
+    }
+  }
+  if (h.has_env) {
+    const uint32_t w = h.env_w, hh = h.env_h;
+    const uint32_t *gm = h.env_mguide.empty() ? nullptr : h.env_mguide.data();
+    near_entries(h.env_marginal.data(), hh + 1, extra);
+    for (int pass = 0; pass < 2; ++pass) {
+      const float *vals = pass ? extra.data() : us;
+      const size_t m = pass ? extra.size() : n;
+      for (size_t i = 0; i < m; ++i) {
+        const uint32_t a = cdf_search_le(h.env_marginal.data(), hh, nullptr, ENV_MGUIDE_BITS, vals[i]);
+        const uint32_t b = cdf_search_le(h.env_marginal.data(), hh, gm, ENV_MGUIDE_BITS, vals[i]);
+        counts[2]++;
+        counts[4] += a != b;
+      }
+    }
+    for (uint32_t row = 0; row < hh; ++row) {
+      const float *c = &h.env_conditional[size_t(row) * (w + 1)];
+      const uint32_t *g = h.env_cguide.empty() ? nullptr
+                                               : &h.env_cguide[size_t(row) * ((1u << ENV_CGUIDE_BITS) + 1)];
+      near_entries(c, w + 1, extra);
+      for (int pass = 0; pass < 2; ++pass) {
+        const float *vals = pass ? extra.data() : us;
+        const size_t m = pass ? extra.size() : std::min<size_t>(n, 4096);
+        for (size_t i = 0; i < m; ++i) {
+          const uint32_t x = cdf_search_le(c, w, nullptr, ENV_CGUIDE_BITS, vals[i]);
+          const uint32_t y = cdf_search_le(c, w, g, ENV_CGUIDE_BITS, vals[i]);
+          counts[3]++;
+          counts[4] += x != y;
+        }
+      }
+    }
+  }
   return 0;
 }
