@@ -46,7 +46,11 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
   const uint32_t prim = __float_as_uint(hit.y);
   const bool is_hit = PART == 1 ? true : (PART == 2 ? false : prim != 0xffffffffu);
   Rng rng = path_rng(pixel, sample_index, 1u + uint32_t(it));
-  float4 a = acc.acc[slot]; // radiance.xyz, alpha
+  // The slot's radiance and alpha, read only on the branches that update them
+  // (a secondary hit on a surface that does not emit toward the ray leaves
+  // them alone): one scattered 16-byte load and four live registers fewer
+  // for most paths.
+  float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
   bool a_dirty = false;
 
   auto write_primary_aov = [&](float depth_v, V3 n, V3 albedo) {
@@ -65,6 +69,7 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
     if (t_sc >= 0.f) {
       const V3 p = ray_org + ray_dir * t_sc;
       if (primary) {
+        a = acc.acc[slot];
         primary = false;
         a.w = a.w + 1.f;
         a_dirty = true;
@@ -115,6 +120,7 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
   }
 
   if (PART != 1 && !is_hit) { // miss (pathtracer.cpp:860-899)
+    a = acc.acc[slot];
     V3 L{0.f, 0.f, 0.f};
     if (primary) {
       if (sc.has_env && sc.env_visible) {
@@ -205,13 +211,16 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
   }
   if (FULL && dm.src_kind[SRC_NORMAL] != 0)
     sn = apply_normal_map(sc, dm.src_kind[SRC_NORMAL], dm.src_index[SRC_NORMAL], q, sn);
+  const bool emits = may_emit(dm) && emits_on_side(mat.flags, front);
+  if (primary || emits)
+    a = acc.acc[slot];
   if (primary) {
     primary = false;
     a.w = a.w + 1.f;
     a_dirty = true;
     write_primary_aov(pdist + rh.t, normalize(sn), mat.base_color);
   }
-  if (may_emit(dm) && emits_on_side(mat.flags, front)) {
+  if (emits) {
     float w_mis = 1.f;
     if (prev_pdf > 0.f && sc.emissive_count > 0) {
       const float pdf_area = __ldg(sc.prim_light_pdf + prim);

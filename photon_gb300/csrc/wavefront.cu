@@ -436,16 +436,17 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
   uint32_t idx = 0, job = 0, steps = 0, rays = 0, fetch_trips = 0, step_trips = 0, max_steps = 0, max_idx = 0;
   const uint4 *nodes = sc.nodes;
   const float4 *tris = sc.tris;
-  // persistent warps with dynamic refill, as in k_trace
+  // persistent warps with dynamic refill, as in k_trace: the idle mask
+  // changes only where lanes finish or fetch
+  uint32_t idle = WARP_FULL;
   for (uint32_t trips = 0;; ++trips) {
     if (trips >= WAVE_TRIP_CAP) {
       record_cap(wc, (WAVE_ERR_SHADOW << 16) | uint32_t(it), n, *fetch, busy, exhausted, idx, sh.a[idx], sh.b[idx],
           s, steps, rays, fetch_trips, step_trips, max_steps, max_idx, trips);
       break;
     }
-    __syncwarp(); // every lane back from the last trip's divergent work before the votes
-    const uint32_t idle = __ballot_sync(WARP_FULL, !busy);
     if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= refill)) {
+      __syncwarp();
       const uint32_t k = uint32_t(__popc(idle));
       const uint32_t base = warp_fetch(fetch, k);
       ++fetch_trips;
@@ -470,22 +471,21 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
           busy = true;
         }
       }
+      idle = __ballot_sync(WARP_FULL, !busy);
     }
-    if (__ballot_sync(WARP_FULL, busy) == 0u) {
+    if (idle == WARP_FULL) {
       if (exhausted)
         break;
       continue;
     }
     ++step_trips;
+    bool more = true;
     if (busy) {
       ++steps;
       if (steps > max_steps) {
         max_steps = steps;
         max_idx = idx;
       }
-    }
-    bool more = true;
-    if (busy) {
       if constexpr (INST)
         more = trav_step2<true, COUNT>(nodes, tris, sc.inst_w2o, sc.inst_info, s, stack, &ctr);
       else
@@ -516,6 +516,8 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
       if (!(open && vol))
         sh.a[idx].w = -1.f;
     }
+    __syncwarp(); // every lane back from the step's divergent work before the vote
+    idle = __ballot_sync(WARP_FULL, !busy);
   }
   if (COUNT) {
     atomicAdd((unsigned long long *)&stats[0], (unsigned long long)ctr.nodes);
