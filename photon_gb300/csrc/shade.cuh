@@ -632,17 +632,33 @@ __device__ __forceinline__ V3 env_eval(const DevScene &sc, V3 dir)
   env_texel(sc, dir, x, y, v);
   return v3(__ldg(sc.env_pixels + size_t(y) * sc.env_w + x));
 }
-__device__ __forceinline__ float env_pdf(const DevScene &sc, V3 dir)
+// The pdf of a texel found by env_texel (EnvironmentMap::pdf,
+// environment_map.h:117-136).
+__device__ __forceinline__ float env_texel_pdf(const DevScene &sc, uint32_t x, uint32_t y, float v)
 {
-  uint32_t x, y;
-  float v;
-  env_texel(sc, dir, x, y, v);
   const float row_pdf = __ldg(sc.env_marginal + y + 1) - __ldg(sc.env_marginal + y);
   const float *c = sc.env_conditional + size_t(y) * (sc.env_w + 1);
   const float col_pdf = __ldg(c + x + 1) - __ldg(c + x);
   const float theta = v * PI;
   const float denom = TWO_PI * PI * fmaxf(sinf(theta), 1e-6f);
   return (row_pdf * col_pdf) * float(sc.env_w) * float(sc.env_h) / denom;
+}
+__device__ __forceinline__ float env_pdf(const DevScene &sc, V3 dir)
+{
+  uint32_t x, y;
+  float v;
+  env_texel(sc, dir, x, y, v);
+  return env_texel_pdf(sc, x, y, v);
+}
+// Radiance and, with want_pdf, pdf of one direction (the direction -> texel
+// mapping is evaluated once for both).
+__device__ __forceinline__ V3 env_eval_pdf(const DevScene &sc, V3 dir, bool want_pdf, float &pdf)
+{
+  uint32_t x, y;
+  float v;
+  env_texel(sc, dir, x, y, v);
+  pdf = want_pdf ? env_texel_pdf(sc, x, y, v) : 0.f;
+  return v3(__ldg(sc.env_pixels + size_t(y) * sc.env_w + x));
 }
 static __device__ __noinline__ V3 env_sample(const DevScene &sc, Rng &rng, float &pdf_out)
 {

@@ -140,12 +140,13 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
     } else {
       L = rc3(rc.ambient);
       if (sc.has_env) {
-        float w_mis = 1.f;
+        float w_mis = 1.f, env_p = 0.f;
+        const V3 le = env_eval_pdf(sc, ray_dir, prev_pdf > 0.f, env_p);
         if (prev_pdf > 0.f) {
-          const float light_pdf = env_pdf(sc, ray_dir) / float(sc.strategy_count);
+          const float light_pdf = env_p / float(sc.strategy_count);
           w_mis = power_heuristic(prev_pdf, light_pdf);
         }
-        L = L + env_eval(sc, ray_dir) * w_mis;
+        L = L + le * w_mis;
       }
     }
     V3 from_miss = tp * L;
