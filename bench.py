@@ -48,6 +48,12 @@ NODE_BYTES = 80   # one BVH8 node
 TRI_BYTES = 48    # one triangle record (v0, e1, e2 as float4)
 RAY_BYTES = 32    # origin+tmin, direction+tmax
 HIT_BYTES = 16    # t, prim, u, v
+# DRAM bytes per closest-hit ray of k_trace, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum = 291.76 + 147.45 MB over the
+# 8,388,608 camera rays of bounce iteration 0 at 8 spp; the node and triangle
+# reads stay in L2, so the traffic is the ray/hit queues and grows with the
+# ray count).  The roofline's `traffic` scales it to the average launch.
+TRACE_DRAM_BYTES_PER_RAY = (291.76e6 + 147.45e6) / 8388608
 
 
 _T0 = time.perf_counter()
@@ -637,7 +643,12 @@ def run_ours(args, world, rank, local):
     roofline = {
         "kernel": "k_trace (BVH8 closest hit)" if dom != "trace_shadow" else "k_shadow (BVH8 any hit)",
         "dominant_kernel_by_time": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "traffic": None,
+        "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+        "traffic": (TRACE_DRAM_BYTES_PER_RAY * prof["closest_rays"] / max(1, kcount["trace_closest"])
+                    if dom != "trace_shadow" else None),
+        "traffic_source": "ncu capture of k_trace (profiles/k_trace_procedural_500k.md): 52.4 DRAM bytes per "
+                          "ray, times the rays of the average launch of this frame",
+        "algorithmic_bytes_per_launch": bytes_alg / max(1, kcount["trace_closest"]),
         "bytes_per_ray": bytes_alg / max(1, prof["closest_rays"] if dom != "trace_shadow" else prof["shadow_rays"]),
         "nodes_per_ray": prof["node_visits"] / max(1, prof["closest_rays"]),
         "tris_per_ray": prof["tri_tests"] / max(1, prof["closest_rays"]),
