@@ -188,10 +188,16 @@ def scene_configs(p, reps=1):
             samples.append(s["pixel_samples"])
         m = sorted(ms)[len(ms) // 2]
         k = ms.index(m)
+        p.tuning_set("time_kernels", 1)  # per-kind device time of one more render
+        r.render(cam, st, True)
+        kinds = r.stats()["kernel_ms"]
+        p.tuning_set("time_kernels", 0)
         out[name] = {"triangles": int(sc.triangle_count), "res": [st.width, st.height],
                      "spp": st.pixel_samples, "depth": st.max_depth, "adaptive": int(st.adaptive_sampling),
                      "render_ms": m, "pixel_samples": int(samples[k]),
-                     "msamples_per_s": samples[k] / (m / 1e3) / 1e6, "upload_s": upload}
+                     "msamples_per_s": samples[k] / (m / 1e3) / 1e6, "upload_s": upload,
+                     "kernel_ms": dict(zip(["raygen", "trace_closest", "shade", "trace_shadow", "wave_end+resolve"],
+                                           kinds))}
         r.close()
         del sc
     return out
