@@ -325,11 +325,48 @@ def kokkos_port_vs_ours(p, sc, cam, st, frame, reps=3):
               + frame["shadow_rays"] / (out["shadow"]["port_mrays_per_s"] * 1e6))
     t_rest = (frame["render_ms"] - frame["kernel_ms"]["trace_closest"] - frame["kernel_ms"]["trace_shadow"]) / 1e3
     ref_bound = prim / (t_trav + t_rest) / 1e6
+    # the reference renders one sample of every pixel per wavefront and pays
+    # the fixed cost of its bounce loop per iteration of every sample
+    iters = int(frame["iterations"])
+    t_iter = reference_iteration_overhead_s()
+    t_loop = st.pixel_samples * iters * t_iter
     out["frame_bound"] = {"reference_traversal_s": t_trav, "other_work_s": t_rest,
                           "reference_msamples_per_s_at_most": ref_bound,
                           "closest_rays": int(frame["closest_rays"]), "shadow_rays": int(frame["shadow_rays"]),
-                          "pixel_samples": int(prim)}
+                          "pixel_samples": int(prim),
+                          "with_bounce_loop": {
+                              "iteration_overhead_us": t_iter * 1e6, "iterations_per_sample": iters,
+                              "samples_per_pixel": int(st.pixel_samples), "loop_s": t_loop,
+                              "reference_msamples_per_s_at_most": prim / (t_trav + t_rest + t_loop) / 1e6}}
     return out
+
+
+def reference_iteration_overhead_s(reps=300):
+    """Fixed cost of one bounce iteration of the reference's render loop on
+    this GPU and host, without its work: PathTracer::render runs per bounce
+    iteration a trace_closest kernel and a fence (kokkos_backend.cpp:21-61),
+    the shading kernel, the shadow-ray set-up kernel, a trace_occluded kernel
+    and a fence (:63-86), and the pt_nee_accum_pack reduction whose active
+    count goes to the host (pathtracer.cpp:1094-1126).  Here: five empty
+    launches, two synchronisations and one 4-byte read-back per iteration,
+    median of `reps`."""
+    import torch
+    x = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ts = []
+    for k in range(reps + 20):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        x.add_(1)
+        torch.cuda.synchronize()
+        x.add_(1)
+        x.add_(1)
+        x.add_(1)
+        torch.cuda.synchronize()
+        x.add_(1)
+        _ = int(x.item())
+        if k >= 20:
+            ts.append(time.perf_counter() - t)
+    return sorted(ts)[len(ts) // 2]
 
 
 def workload():
@@ -686,10 +723,13 @@ def run_ours(args, world, rank, local):
     kokkos = None
     if rank == 0 and not args.no_kokkos_port:
         frame = {"pixel_samples": samples / args.steps, "closest_rays": closest / args.steps,
-                 "shadow_rays": shadow / args.steps, "render_ms": dev_ms / args.steps, "kernel_ms": kms}
+                 "shadow_rays": shadow / args.steps, "render_ms": dev_ms / args.steps, "kernel_ms": kms,
+                 "iterations": kcount["trace_closest"] // max(1, kcount["raygen"])}  # per wave
         kokkos = kokkos_port_vs_ours(p, sc, cam, st, frame)
-        kokkos["frame_bound"]["ours_msamples_per_s"] = value
-        kokkos["frame_bound"]["speedup_at_least"] = value / kokkos["frame_bound"]["reference_msamples_per_s_at_most"]
+        fb = kokkos["frame_bound"]
+        fb["ours_msamples_per_s"] = value
+        fb["speedup_at_least"] = value / fb["reference_msamples_per_s_at_most"]
+        fb["with_bounce_loop"]["speedup_at_least"] = value / fb["with_bounce_loop"]["reference_msamples_per_s_at_most"]
         _log("kokkos port comparison done")
     configs = None
     if rank == 0 and not args.no_configs:
