@@ -98,6 +98,8 @@ struct phc_renderer {
   // wavefront buffers
   size_t cap_paths{0};
   Buf st_o[2], st_d[2], st_tp[2], st_info[2], st_dist[2], hits, sh_a, sh_b, sh_c, hitq, missq, hitq_sorted;
+  Buf vol_scatter, vol_rng; // scenes with volumes: k_vol_scatter results per path
+  size_t cap_vol{0};
   Buf hit_inst; // instance slot per hit (scenes with instances)
   Buf sort_bins; // per bounce iteration: material-sort counts and starts
   size_t cap_slots{0};
@@ -231,10 +233,8 @@ void make_camera(const phc_camera &c, uint32_t w, uint32_t h, RenderConst &rc)
 
 void check_device(phc_renderer *r) { ck(cudaSetDevice(r->device), "cudaSetDevice"); }
 
-void ensure_paths(phc_renderer *r, size_t n)
+void ensure_path_state(phc_renderer *r, size_t n)
 {
-  if (n <= r->cap_paths)
-    return;
   r->buf_gen++;
   for (int b = 0; b < 2; ++b) {
     ck(r->st_o[b].ensure(n * 16), "alloc path state");
@@ -252,6 +252,18 @@ void ensure_paths(phc_renderer *r, size_t n)
   ck(r->sh_b.ensure(n * 16), "alloc shadow queue");
   ck(r->sh_c.ensure(n * 16), "alloc shadow queue");
   r->cap_paths = n;
+}
+
+void ensure_paths(phc_renderer *r, size_t n)
+{
+  if (n > r->cap_paths)
+    ensure_path_state(r, n);
+  if (r->scene.dev.volume_count > 0 && r->cap_vol < r->cap_paths) {
+    r->buf_gen++;
+    ck(r->vol_scatter.ensure(r->cap_paths * 16), "alloc volume scattering");
+    ck(r->vol_rng.ensure(r->cap_paths * 4), "alloc volume scattering");
+    r->cap_vol = r->cap_paths;
+  }
 }
 
 void ensure_slots(phc_renderer *r, size_t n)
@@ -374,6 +386,12 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
   const bool split = (sc.features & SCENE_VOLUMES) == 0 && tu.split_shade;
   HitQueues hq = split ? HitQueues{r->hitq.as<uint32_t>(), r->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
   hq.inst = r->hit_inst.as<uint32_t>();
+  // volume scenes: delta tracking in its own kernel ahead of the shading
+  const bool vol_pre = full && !split && sc.volume_count > 0 && r->cap_vol >= r->cap_paths && r->cap_vol > 0;
+  if (vol_pre) {
+    hq.vscatter = r->vol_scatter.as<float4>();
+    hq.vrng = r->vol_rng.as<uint32_t>();
+  }
   const bool sort = split && tu.sort_threshold > 0;
   const size_t bin_words = size_t(2) * MAT_SORT_BINS;
   if (sort) { // sort_bins sized by ensure_wave_buffers (no allocation while a graph is captured)
@@ -400,6 +418,10 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
       timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 2}, hq); });
       launches += 4;
     } else {
+      if (vol_pre) {
+        timed(2, [&] { launch_vol_scatter(cfg, s, rc, sc, in, hits, wc, it, hq); });
+        launches += 1;
+      }
       timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 0}, hq); });
       launches += 3;
     }

@@ -24,11 +24,18 @@ struct NextPath {
 struct ShadowRec {
   float4 a, b, c;
 };
+// Result of k_vol_scatter for one path: the scattering distance (or -1) and
+// albedo, and the random-number state after the tracking.
+struct VolPre {
+  float4 s;
+  uint32_t rng;
+};
 
 template <bool FULL, int PART>
 __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene &sc, const float4 ro4,
     const float4 rd4, const float4 tp4, const uint4 info, const float pdist, const float4 hit, const Accum &acc,
-    int it, bool &cont, NextPath &next, bool &has_shadow, ShadowRec &sh, uint32_t inst = INST_NONE)
+    int it, bool &cont, NextPath &next, bool &has_shadow, ShadowRec &sh, uint32_t inst = INST_NONE,
+    const VolPre *pre = nullptr)
 {
   cont = false;
   has_shadow = false;
@@ -64,8 +71,15 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
   // Scattering inside a volume in front of the surface (pathtracer.cpp:789-858)
   if (FULL && PART == 0 && sc.volume_count > 0) {
     V3 albedo{0.f, 0.f, 0.f};
-    const float t_end = is_hit ? hit.x : rd4.w;
-    const float t_sc = vol_sample_scatter(sc, ray_org, ray_dir, ro4.w, t_end, rng, albedo);
+    float t_sc;
+    if (pre) { // tracked by k_vol_scatter: continue its random-number stream
+      t_sc = pre->s.x;
+      albedo = V3{pre->s.y, pre->s.z, pre->s.w};
+      rng = Rng(pre->rng);
+    } else {
+      const float t_end = is_hit ? hit.x : rd4.w;
+      t_sc = vol_sample_scatter(sc, ray_org, ray_dir, ro4.w, t_end, rng, albedo);
+    }
     if (t_sc >= 0.f) {
       const V3 p = ray_org + ray_dir * t_sc;
       if (primary) {
@@ -344,8 +358,14 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
             it, cont, np, has_sh, sr);
       } else {
         const uint32_t inst = (PART != 2 && sc.inst_count) ? hq.inst[i] : INST_NONE;
+        VolPre pre;
+        const bool has_pre = FULL && PART == 0 && hq.vscatter != nullptr;
+        if (has_pre) {
+          pre.s = hq.vscatter[i];
+          pre.rng = hq.vrng[i];
+        }
         shade_path<FULL, PART>(*rcp, sc, in.ray_o[i], in.ray_d[i], in.tp[i], info, in.pdist[i], hits[i], acc, it,
-            cont, np, has_sh, sr, inst);
+            cont, np, has_sh, sr, inst, has_pre ? &pre : nullptr);
       }
     }
     if (PART != 2) { // misses never continue nor cast shadow rays
@@ -369,7 +389,35 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
   }
 }
 
+// The volume step of pt_shade (pathtracer.cpp:789-858) for every path of the
+// iteration, ahead of the shading kernel: delta tracking along the path's
+// segment (up to its hit, or its tmax for a miss) with the stream the shading
+// would use (dimension 1 + iteration), whose state after the tracking goes
+// with the result.  Tracking loops differ in length from path to path; in a
+// kernel of their own they no longer hold the lanes of the shading code.
+__global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restrict__ rcp, DevScene sc, PathSoA in,
+    const float4 *__restrict__ hits, WaveCounters wc, int it, HitQueues hq)
+{
+  const uint32_t n = wc.count[it];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint4 info = in.info[i];
+    const float4 ro4 = in.ray_o[i], rd4 = in.ray_d[i], hit = hits[i];
+    Rng rng = path_rng(info.x % rcp->npix, info.y, 1u + uint32_t(it));
+    const bool is_hit = __float_as_uint(hit.y) != 0xffffffffu;
+    V3 albedo{0.f, 0.f, 0.f};
+    const float t_sc = vol_sample_scatter(sc, v3(ro4), v3(rd4), ro4.w, is_hit ? hit.x : rd4.w, rng, albedo);
+    hq.vscatter[i] = make_float4(t_sc, albedo.x, albedo.y, albedo.z);
+    hq.vrng[i] = rng.s;
+  }
+}
+
 } // namespace
+
+void launch_vol_scatter(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,
+    const float4 *hits, WaveCounters wc, int it, HitQueues hq)
+{
+  k_vol_scatter<<<c.blocks_shade, 128, 0, s>>>(rc, sc, in, hits, wc, it, hq);
+}
 
 void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in, PathSoA out,
     const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, ShadeVariant v, HitQueues hq)

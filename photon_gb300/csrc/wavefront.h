@@ -101,6 +101,11 @@ struct HitQueues {
   uint32_t *sorted = nullptr;
   uint32_t sort_threshold = 0;
   uint32_t *inst = nullptr; // per path: instance slot of its hit (scenes with instances)
+  // Scenes with volumes: the scattering event sampled along each path's
+  // segment by k_vol_scatter before shading (t or -1, albedo.xyz) and the
+  // path's random-number state after it, from which shading continues.
+  float4 *vscatter = nullptr;
+  uint32_t *vrng = nullptr;
 };
 constexpr uint32_t MAT_SORT_BINS = 1024; // materials map to bin = id % MAT_SORT_BINS
 
@@ -168,6 +173,10 @@ void launch_trace(const LaunchCfg &c, cudaStream_t s, DevScene sc, PathSoA in, f
     uint64_t *stats, int refill, HitQueues hq);
 void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in, PathSoA out,
     const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, ShadeVariant v, HitQueues hq);
+// Delta tracking of every path of iteration `it` through the scene's volumes
+// (the first step of pt_shade for volume scenes), into hq.vscatter / hq.vrng.
+void launch_vol_scatter(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,
+    const float4 *hits, WaveCounters wc, int it, HitQueues hq);
 void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh, Accum acc,
     WaveCounters wc, int it, uint64_t *stats, int refill);
 // Counting sort of iteration it's hit queue by material (when hcount[it] >=
