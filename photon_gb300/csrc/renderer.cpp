@@ -312,6 +312,7 @@ WaveCounters wave_counters(phc_renderer *r, int max_iter)
   wc.hcount = c + (2 * max_iter + 1);
   wc.mcount = c + (3 * max_iter + 1);
   wc.fetch = c + (4 * max_iter + 1);
+  wc.vfetch = c + (8 * max_iter + 1);
   wc.wave = c + wave_counter_words(max_iter);
   wc.error = c + wave_counter_words(max_iter) + 1;
   wc.dbg = c + wave_counter_words(max_iter) + 4;
@@ -450,6 +451,9 @@ void check_wave_error(uint32_t w, const WaveCounters &wc, cudaStream_t s)
     return std::to_string(x);
   };
   const uint32_t kind = w >> 16;
+  if (kind == WAVE_ERR_VOLUME)
+    throw ApiError(PHC_ERR_DEVICE, "a volume-tracking warp exceeded its loop-trip cap at bounce iteration " +
+        std::to_string(w & 0xffffu));
   throw ApiError(PHC_ERR_DEVICE, std::string("a ") + (kind == WAVE_ERR_TRACE ? "closest-hit" : "shadow") +
           " traversal warp exceeded its loop-trip cap at bounce iteration " + std::to_string(w & 0xffffu) +
           " (queue " + std::to_string(d[0]) + ", fetched " + std::to_string(d[1]) + ", busy " +

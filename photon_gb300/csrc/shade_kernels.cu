@@ -398,16 +398,58 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
 __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restrict__ rcp, DevScene sc, PathSoA in,
     const float4 *__restrict__ hits, WaveCounters wc, int it, HitQueues hq)
 {
+  // persistent warps with refill: a lane whose ray is done takes a new one
+  // once VOL_REFILL lanes of its warp are idle; every step is one density
+  // lookup of every busy lane (vt_step)
   const uint32_t n = wc.count[it];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint4 info = in.info[i];
-    const float4 ro4 = in.ray_o[i], rd4 = in.ray_d[i], hit = hits[i];
-    Rng rng = path_rng(info.x % rcp->npix, info.y, 1u + uint32_t(it));
-    const bool is_hit = __float_as_uint(hit.y) != 0xffffffffu;
-    V3 albedo{0.f, 0.f, 0.f};
-    const float t_sc = vol_sample_scatter(sc, v3(ro4), v3(rd4), ro4.w, is_hit ? hit.x : rd4.w, rng, albedo);
-    hq.vscatter[i] = make_float4(t_sc, albedo.x, albedo.y, albedo.z);
-    hq.vrng[i] = rng.s;
+  uint32_t *fetch = wc.vfetch + 2 * it;
+  const uint32_t lane = lane_id();
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  VolTrack s;
+  Rng rng(1u);
+  bool busy = false, exhausted = false;
+  uint32_t idx = 0, idle = WARP_FULL;
+  for (uint32_t trips = 0;; ++trips) {
+    if (trips >= WAVE_TRIP_CAP) { // warp-uniform
+      if (lane == 0)
+        atomicCAS(wc.error, 0u, (WAVE_ERR_VOLUME << 16) | uint32_t(it));
+      break;
+    }
+    if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= VOL_REFILL)) {
+      __syncwarp();
+      const uint32_t k = uint32_t(__popc(idle));
+      const uint32_t base = warp_fetch(fetch, k);
+      if (base + k >= n)
+        exhausted = true;
+      if (!busy) {
+        const uint32_t my = base + uint32_t(__popc(idle & lt_mask));
+        if (my < n) {
+          idx = my;
+          const uint4 info = in.info[idx];
+          const float4 ro4 = in.ray_o[idx], rd4 = in.ray_d[idx], hit = hits[idx];
+          rng = path_rng(info.x % rcp->npix, info.y, 1u + uint32_t(it));
+          const bool is_hit = __float_as_uint(hit.y) != 0xffffffffu;
+          vt_init(s, v3(ro4), v3(rd4), ro4.w, is_hit ? hit.x : rd4.w);
+          busy = true;
+        }
+      }
+      idle = __ballot_sync(WARP_FULL, !busy);
+    }
+    if (idle == WARP_FULL) {
+      if (exhausted)
+        break;
+      continue;
+    }
+    if (busy) {
+      vt_step<true>(sc, s, rng);
+      if (s.done) {
+        hq.vscatter[idx] = make_float4(s.t_event, s.albedo.x, s.albedo.y, s.albedo.z);
+        hq.vrng[idx] = rng.s;
+        busy = false;
+      }
+    }
+    __syncwarp(); // every lane back from the step's divergent work before the vote
+    idle = __ballot_sync(WARP_FULL, !busy);
   }
 }
 
@@ -416,7 +458,7 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
 void launch_vol_scatter(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,
     const float4 *hits, WaveCounters wc, int it, HitQueues hq)
 {
-  k_vol_scatter<<<c.blocks_shade, 128, 0, s>>>(rc, sc, in, hits, wc, it, hq);
+  k_vol_scatter<<<c.blocks_trace, 128, 0, s>>>(rc, sc, in, hits, wc, it, hq);
 }
 
 void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in, PathSoA out,

@@ -532,26 +532,72 @@ template <bool BATCH>
 __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__restrict__ rcp, DevScene sc,
     BatchTable bt, ShadowSoA sh, Accum acc_param, WaveCounters wc, int it)
 {
+  // the unoccluded shadow rays (tmax >= 0) of the iteration: ratio-tracking
+  // transmittance (stream dimension 0x10000 + iteration) times the NEE
+  // contribution into the path's pixel slot; persistent warps with refill,
+  // one density lookup per busy lane and step, as in k_vol_scatter
   const uint32_t n = wc.scount[it];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float4 a = sh.a[i];
-    if (!(a.w >= 0.f))
-      continue;
-    const uint32_t job = BATCH ? sh.job[i] : 0u;
-    const DevScene &S = BATCH ? bt.jobs[job].sc : sc;
-    const Accum &acc = BATCH ? bt.jobs[job].acc : acc_param;
-    const uint32_t npix = BATCH ? bt.jobs[job].rc.npix : rcp->npix;
-    const float4 b = sh.b[i], c = sh.c[i];
-    const uint32_t slot = __float_as_uint(c.z), sample_index = __float_as_uint(c.w);
-    Rng rs = path_rng(slot % npix, sample_index, 0x10000u + uint32_t(it));
-    const V3 contrib = V3{b.w, c.x, c.y} * vol_transmittance(S, v3(a), v3(b), 0.f, a.w, rs);
-    if (finite3(contrib)) {
-      float4 v = acc.acc[slot];
-      v.x = v.x + contrib.x;
-      v.y = v.y + contrib.y;
-      v.z = v.z + contrib.z;
-      acc.acc[slot] = v;
+  uint32_t *fetch = wc.vfetch + 2 * it + 1;
+  const uint32_t lane = lane_id();
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  VolTrack s;
+  Rng rng(1u);
+  bool busy = false, exhausted = false;
+  uint32_t idx = 0, job = 0, idle = WARP_FULL;
+  for (uint32_t trips = 0;; ++trips) {
+    if (trips >= WAVE_TRIP_CAP) { // warp-uniform
+      if (lane == 0)
+        atomicCAS(wc.error, 0u, (WAVE_ERR_VOLUME << 16) | uint32_t(it));
+      break;
     }
+    if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= VOL_REFILL)) {
+      __syncwarp();
+      const uint32_t k = uint32_t(__popc(idle));
+      const uint32_t base = warp_fetch(fetch, k);
+      if (base + k >= n)
+        exhausted = true;
+      if (!busy) {
+        const uint32_t my = base + uint32_t(__popc(idle & lt_mask));
+        if (my < n) {
+          const float4 a = sh.a[my];
+          if (a.w >= 0.f) { // occluded or already accumulated rays: tmax < 0
+            idx = my;
+            job = BATCH ? sh.job[idx] : 0u;
+            const uint32_t npix = BATCH ? bt.jobs[job].rc.npix : rcp->npix;
+            const float4 b = sh.b[idx], c = sh.c[idx];
+            rng = path_rng(__float_as_uint(c.z) % npix, __float_as_uint(c.w), 0x10000u + uint32_t(it));
+            vt_init(s, v3(a), v3(b), 0.f, a.w);
+            busy = true;
+          }
+        }
+      }
+      idle = __ballot_sync(WARP_FULL, !busy);
+    }
+    if (idle == WARP_FULL) {
+      if (exhausted)
+        break;
+      continue;
+    }
+    if (busy) {
+      const DevScene &S = BATCH ? bt.jobs[job].sc : sc;
+      vt_step<false>(S, s, rng);
+      if (s.done) {
+        busy = false;
+        const Accum &acc = BATCH ? bt.jobs[job].acc : acc_param;
+        const float4 b = sh.b[idx], c = sh.c[idx];
+        const uint32_t slot = __float_as_uint(c.z);
+        const V3 contrib = V3{b.w, c.x, c.y} * s.tr;
+        if (finite3(contrib)) {
+          float4 v = acc.acc[slot];
+          v.x = v.x + contrib.x;
+          v.y = v.y + contrib.y;
+          v.z = v.z + contrib.z;
+          acc.acc[slot] = v;
+        }
+      }
+    }
+    __syncwarp(); // every lane back from the step's divergent work before the vote
+    idle = __ballot_sync(WARP_FULL, !busy);
   }
 }
 
@@ -707,7 +753,7 @@ void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, De
   else
     k_shadow<false, false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, nullptr, r);
   if (sc.volume_count > 0)
-    k_shadow_volume<false><<<c.blocks_shade, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it);
+    k_shadow_volume<false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it);
 }
 
 void launch_raygen_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA out, WaveCounters wc)
@@ -758,7 +804,7 @@ void launch_shadow_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, Shad
   const uint32_t r = uint32_t(refill < 1 ? 1 : (refill > 32 ? 32 : refill));
   k_shadow<false, true><<<c.blocks_trace, 128, 0, s>>>(nullptr, DevScene{}, bt, sh, Accum{}, wc, it, nullptr, r);
   if (volumes)
-    k_shadow_volume<true><<<c.blocks_shade, 128, 0, s>>>(nullptr, DevScene{}, bt, sh, Accum{}, wc, it);
+    k_shadow_volume<true><<<c.blocks_trace, 128, 0, s>>>(nullptr, DevScene{}, bt, sh, Accum{}, wc, it);
 }
 
 void launch_wave_end(cudaStream_t s, const RenderConst *rc, Accum acc, WaveCounters wc, uint32_t npix, int adaptive,

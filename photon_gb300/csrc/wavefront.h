@@ -71,18 +71,21 @@ struct WaveCounters {
   uint32_t *hcount;  // [max_iter] closest-hit results that hit (split queues)
   uint32_t *mcount;  // [max_iter] closest-hit results that missed (split queues)
   uint32_t *fetch;   // [4 * max_iter] work counters: trace, shade (all/hits), shade misses, shadow
+  uint32_t *vfetch;  // [2 * max_iter] work counters: volume scattering, shadow transmittance
   uint32_t *wave;    // current wave index within the render call
   uint32_t *error;   // sticky error word
   uint32_t *dbg;     // [WAVE_DBG_WORDS] record of the first self-check failure
 };
-inline size_t wave_counter_words(int max_iter) { return size_t(9 * max_iter + 1); }
+inline size_t wave_counter_words(int max_iter) { return size_t(10 * max_iter + 1); }
 
 // Self-check of the persistent traversal loops: a warp that makes more than
 // WAVE_TRIP_CAP loop trips (each trip is one traversal step of every busy
 // lane; legitimate work needs a few thousand) stops and records
 // (kernel << 16) | iteration in the error word, first writer wins.
 constexpr uint32_t WAVE_TRIP_CAP = 1u << 24;
-enum : uint32_t { WAVE_ERR_TRACE = 1u, WAVE_ERR_SHADOW = 2u };
+enum : uint32_t { WAVE_ERR_TRACE = 1u, WAVE_ERR_SHADOW = 2u, WAVE_ERR_VOLUME = 3u };
+// A volume-tracking warp takes new rays once this many of its lanes are idle.
+constexpr uint32_t VOL_REFILL = 8u;
 // dbg words: queue length, fetch counter, busy ballot, exhausted, then for
 // the warp's first busy lane: ray index, origin xyz, tmax, direction xyz,
 // stack depth, group base, group hits, group internal mask, steps of the ray.
