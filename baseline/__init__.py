@@ -50,6 +50,8 @@ def load():
         lib.kbp_info.argtypes = [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         lib.kbp_trace.argtypes = [C.c_void_p] + [C.c_void_p] * 4 + [C.c_uint32, C.c_int, C.c_void_p, C.c_void_p]
         lib.kbp_trace_host.argtypes = [C.c_void_p] + [C.c_void_p] * 4 + [C.c_uint32, C.c_int, C.c_void_p]
+        lib.kbp_loop_overhead_us.restype = C.c_double
+        lib.kbp_loop_overhead_us.argtypes = [C.c_int]
         lib.l2_read_gbs.restype = C.c_double
         lib.l2_read_gbs.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p]
         _lib = lib
@@ -132,3 +134,13 @@ def l2_read_gbs(mib: int = 32, reps: int = 64) -> float:
     if best <= 0:
         raise RuntimeError("l2 probe failed")
     return best
+
+
+def loop_overhead_s(reps: int = 300) -> float:
+    """Fixed cost in seconds of one bounce iteration of the reference's render
+    loop on this GPU and host (kokkos_port.cu kbp_loop_overhead_us: five empty
+    launches, two synchronisations, one 4-byte read-back from C++)."""
+    us = load().kbp_loop_overhead_us(int(reps))
+    if us <= 0:
+        raise RuntimeError("loop overhead probe failed")
+    return us * 1e-6

@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -505,6 +506,58 @@ int kbp_trace_host(void *h, const float *o, const float *d, const float *tmin, c
     }
   }
   return 0;
+}
+
+// Fixed cost, in microseconds, of one bounce iteration of the reference's
+// render loop without its work (median of `reps`): PathTracer::render runs
+// per iteration a trace_closest kernel and a fence (kokkos_backend.cpp:21-61),
+// the shading kernel, the shadow-ray set-up kernel, a trace_occluded kernel
+// and a fence (:63-86), and the pt_nee_accum_pack reduction whose active
+// count is read back by the host (pathtracer.cpp:1094-1126).  Here: five
+// empty launches, two stream synchronisations and one 4-byte read-back,
+// issued from C++ (Kokkos adds its own dispatch on top of these).
+__global__ void k_empty(uint32_t *p)
+{
+  if (threadIdx.x == 0 && blockIdx.x == 0 && p[0] == 0xffffffffu)
+    p[1] = 0u;
+}
+
+double kbp_loop_overhead_us(int reps)
+{
+  uint32_t *d = nullptr;
+  if (cudaMalloc(&d, 16) != cudaSuccess)
+    return -1.0;
+  cudaMemset(d, 0, 16);
+  cudaStream_t s;
+  if (cudaStreamCreate(&s) != cudaSuccess) {
+    cudaFree(d);
+    return -1.0;
+  }
+  std::vector<double> ts;
+  uint32_t h = 0;
+  for (int k = 0; k < reps + 20; ++k) {
+    cudaStreamSynchronize(s);
+    const auto t0 = std::chrono::steady_clock::now();
+    k_empty<<<1, 32, 0, s>>>(d);
+    cudaStreamSynchronize(s);
+    k_empty<<<1, 32, 0, s>>>(d);
+    k_empty<<<1, 32, 0, s>>>(d);
+    k_empty<<<1, 32, 0, s>>>(d);
+    cudaStreamSynchronize(s);
+    k_empty<<<1, 32, 0, s>>>(d);
+    cudaMemcpyAsync(&h, d, 4, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const auto t1 = std::chrono::steady_clock::now();
+    if (k >= 20)
+      ts.push_back(std::chrono::duration<double, std::micro>(t1 - t0).count());
+  }
+  const bool ok = cudaGetLastError() == cudaSuccess;
+  cudaStreamDestroy(s);
+  cudaFree(d);
+  if (!ok || ts.empty())
+    return -1.0;
+  std::sort(ts.begin(), ts.end());
+  return ts[ts.size() / 2];
 }
 
 } // extern "C"

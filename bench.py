@@ -268,7 +268,11 @@ def kokkos_port_vs_ours(p, sc, cam, st, frame, reps=3):
     frame: the reference's render needs at least its own traversal time for
     this frame's closest and shadow rays (at the port's rates) plus this
     library's time for everything else (camera rays, shading, bookkeeping),
-    so frame samples over that time bounds its Msamples/s from above."""
+    so frame samples over that time bounds its Msamples/s from above; and a
+    second bound that adds the fixed cost of the reference's bounce loop (one
+    wavefront per sample of every pixel, launches, fences and the host
+    read-back of the active count every iteration), measured from C++ on the
+    same GPU and host (baseline.loop_overhead_s)."""
     import numpy as np
     import torch
     import baseline
@@ -328,7 +332,7 @@ def kokkos_port_vs_ours(p, sc, cam, st, frame, reps=3):
     # the reference renders one sample of every pixel per wavefront and pays
     # the fixed cost of its bounce loop per iteration of every sample
     iters = int(frame["iterations"])
-    t_iter = reference_iteration_overhead_s()
+    t_iter = baseline.loop_overhead_s()
     t_loop = st.pixel_samples * iters * t_iter
     out["frame_bound"] = {"reference_traversal_s": t_trav, "other_work_s": t_rest,
                           "reference_msamples_per_s_at_most": ref_bound,
@@ -339,34 +343,6 @@ def kokkos_port_vs_ours(p, sc, cam, st, frame, reps=3):
                               "samples_per_pixel": int(st.pixel_samples), "loop_s": t_loop,
                               "reference_msamples_per_s_at_most": prim / (t_trav + t_rest + t_loop) / 1e6}}
     return out
-
-
-def reference_iteration_overhead_s(reps=300):
-    """Fixed cost of one bounce iteration of the reference's render loop on
-    this GPU and host, without its work: PathTracer::render runs per bounce
-    iteration a trace_closest kernel and a fence (kokkos_backend.cpp:21-61),
-    the shading kernel, the shadow-ray set-up kernel, a trace_occluded kernel
-    and a fence (:63-86), and the pt_nee_accum_pack reduction whose active
-    count goes to the host (pathtracer.cpp:1094-1126).  Here: five empty
-    launches, two synchronisations and one 4-byte read-back per iteration,
-    median of `reps`."""
-    import torch
-    x = torch.zeros(1, dtype=torch.int32, device="cuda")
-    ts = []
-    for k in range(reps + 20):
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        x.add_(1)
-        torch.cuda.synchronize()
-        x.add_(1)
-        x.add_(1)
-        x.add_(1)
-        torch.cuda.synchronize()
-        x.add_(1)
-        _ = int(x.item())
-        if k >= 20:
-            ts.append(time.perf_counter() - t)
-    return sorted(ts)[len(ts) // 2]
 
 
 def workload():
