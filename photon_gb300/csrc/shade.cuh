@@ -196,7 +196,7 @@ __device__ __forceinline__ V3 eval_coat(const Mat &m, V3 wo, V3 wi, V3 n)
   const float w = m.clearcoat * 0.25f;
   return F * (w * D * G / denom);
 }
-static __device__ __noinline__ V3 bsdf_eval(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
+static __device__ __forceinline__ V3 bsdf_eval(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
 {
   if (dot(wo, n) <= 0.f || dot(wi, n) <= 0.f)
     return V3{0.f, 0.f, 0.f};
@@ -212,7 +212,7 @@ static __device__ __noinline__ V3 bsdf_eval(const Mat &m, V3 wo, V3 wi, V3 n, V3
   f = f + eval_coat(m, wo, wi, sn);
   return f;
 }
-static __device__ __noinline__ float bsdf_pdf(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
+static __device__ __forceinline__ float bsdf_pdf(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
 {
   if (dot(wo, n) <= 0.f || dot(wi, n) <= 0.f)
     return 0.f;
@@ -264,7 +264,7 @@ struct BSample {
   int lobe;
   float noh;
 };
-static __device__ __noinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3 sn, Rng &rng)
+static __device__ __forceinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3 sn, Rng &rng)
 {
   BSample out{V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, 0.f, false, false, LOBE_NONE, 0.f};
   const BSample none = out;
@@ -549,7 +549,7 @@ __device__ __forceinline__ V3 atlas_sample(const DevScene &sc, int32_t tex, floa
 // SRC = false: the scene has no attribute / sampler / atlas sources, the
 // constants are the parameters (the source branches are not compiled).
 template <bool SRC>
-static __device__ __noinline__ Mat resolve_material(const DevScene &sc, const DevMaterial &dm, const Query &q, float &alpha)
+static __device__ __forceinline__ Mat resolve_material(const DevScene &sc, const DevMaterial &dm, const Query &q, float &alpha)
 {
   Mat m;
   m.base_color = V3{dm.base_color[0], dm.base_color[1], dm.base_color[2]};
@@ -660,7 +660,7 @@ __device__ __forceinline__ V3 env_eval_pdf(const DevScene &sc, V3 dir, bool want
   pdf = want_pdf ? env_texel_pdf(sc, x, y, v) : 0.f;
   return v3(__ldg(sc.env_pixels + size_t(y) * sc.env_w + x));
 }
-static __device__ __noinline__ V3 env_sample(const DevScene &sc, Rng &rng, float &pdf_out)
+static __device__ __forceinline__ V3 env_sample(const DevScene &sc, Rng &rng, float &pdf_out)
 {
   const float u1 = rng.next();
   const float u2 = rng.next();
@@ -752,7 +752,7 @@ struct DirectSample {
 // sample_direct, pathtracer.cpp:270-367
 // FULL = false: no analytic lights and no material sources in the scene.
 template <bool FULL>
-static __device__ __noinline__ DirectSample sample_direct(const DevScene &sc, V3 p, Rng &rng)
+static __device__ __forceinline__ DirectSample sample_direct(const DevScene &sc, V3 p, Rng &rng)
 {
   DirectSample ds{V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, 0.f, 0.f, false, false};
   if (sc.strategy_count == 0)
