@@ -420,7 +420,7 @@ __device__ __forceinline__ int32_t wrap_index(int32_t i, int32_t n, int32_t mode
   }
   return i < 0 ? 0 : (i >= n ? n - 1 : i);
 }
-static __device__ __noinline__ float4 sampler_sample(const DevScene &sc, int32_t id, float4 attr)
+static __device__ __forceinline__ float4 sampler_sample(const DevScene &sc, int32_t id, float4 attr)
 {
   if (id < 0 || uint32_t(id) >= sc.sampler_count)
     return make_float4(0.f, 0.f, 0.f, 1.f);
@@ -484,7 +484,7 @@ __device__ __forceinline__ float4 eval_source(const DevScene &sc, int32_t kind, 
   const int32_t slot = sc.samplers[uint32_t(index)].in_attribute;
   return sampler_sample(sc, index, fetch_attribute(sc, slot, q));
 }
-static __device__ __noinline__ V3 apply_normal_map(const DevScene &sc, int32_t kind, int32_t index, const Query &q, V3 sn)
+static __device__ __forceinline__ V3 apply_normal_map(const DevScene &sc, int32_t kind, int32_t index, const Query &q, V3 sn)
 {
   const float4 c = eval_source(sc, kind, index, q);
   const V3 nm{2.f * c.x - 1.f, 2.f * c.y - 1.f, 2.f * c.z - 1.f};
@@ -699,7 +699,7 @@ __device__ __forceinline__ V3 sphere_point(const DevLight &l, V3 p, Rng &rng)
   concentric_disk(rng, dx, dy);
   return pos + (t * dx + b * dy) * l.radius;
 }
-static __device__ __noinline__ LightSample sample_light(const DevLight &l, V3 p, Rng &rng)
+static __device__ __forceinline__ LightSample sample_light(const DevLight &l, V3 p, Rng &rng)
 {
   const V3 color{l.color[0], l.color[1], l.color[2]};
   const V3 pos{l.position[0], l.position[1], l.position[2]};
