@@ -9,6 +9,7 @@
 #include "bvh8.h"
 #include "cdf_search.cuh"
 #include "traverse.cuh"
+#include "volume_track.cuh"
 
 using namespace phc;
 
@@ -197,5 +198,64 @@ extern "C" int ht_guide_check(const phc_scene_desc *desc, const float *us, uint3
       }
     }
   }
+  return 0;
+}
+
+// The resumable volume tracking of the shading kernels (VolTrack / vt_step,
+// volume_track.cuh) against the plain tracking (vol_sample_scatter,
+// vol_transmittance), both run on the host over the scene's volumes: for
+// every ray the scattering distance and albedo, the transmittance and the
+// random-number state after the tracking must be identical bit for bit.
+// seeds: the initial random-number state per ray.  counts: [0] rays that
+// met a volume event or attenuation, [1] mismatches, [2] vt_step calls.
+extern "C" int ht_volume_check(const phc_scene_desc *desc, const float *orgs, const float *dirs, const float *tmin,
+    const float *tmax, const uint32_t *seeds, uint32_t n, uint64_t *counts)
+{
+  HostScene h;
+  build_host_scene(*desc, h);
+  std::vector<float> values(h.vol_values);
+  for (const HostScene::Span &sp : h.vol_value_spans)
+    values.insert(values.end(), sp.p, sp.p + sp.floats);
+  DevScene sc{};
+  sc.volumes = h.volumes.data();
+  sc.volume_count = uint32_t(h.volumes.size());
+  sc.vol_values = values.data();
+  sc.vol_tf = reinterpret_cast<const float4 *>(h.vol_tf.data());
+  sc.vol_majorants = h.vol_majorants.data();
+  uint64_t events = 0, bad = 0, steps = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const V3 o{orgs[3 * i], orgs[3 * i + 1], orgs[3 * i + 2]};
+    const V3 d{dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+    for (int mode = 0; mode < 2; ++mode) {
+      Rng a(seeds[i]), b(seeds[i]);
+      VolTrack s;
+      vt_init(s, o, d, tmin[i], tmax[i]);
+      bool same = true;
+      if (mode == 0) {
+        V3 albedo{0.f, 0.f, 0.f};
+        const float t = vol_sample_scatter(sc, o, d, tmin[i], tmax[i], a, albedo);
+        while (!s.done) {
+          vt_step<true>(sc, s, b);
+          ++steps;
+        }
+        same = f2u(t) == f2u(s.t_event) && f2u(albedo.x) == f2u(s.albedo.x) &&
+            f2u(albedo.y) == f2u(s.albedo.y) && f2u(albedo.z) == f2u(s.albedo.z);
+        events += t >= 0.f;
+      } else {
+        const float tr = vol_transmittance(sc, o, d, tmin[i], tmax[i], a);
+        while (!s.done) {
+          vt_step<false>(sc, s, b);
+          ++steps;
+        }
+        same = f2u(tr) == f2u(s.tr);
+        events += tr < 1.f;
+      }
+      same = same && a.s == b.s;
+      bad += same ? 0u : 1u;
+    }
+  }
+  counts[0] = events;
+  counts[1] = bad;
+  counts[2] = steps;
   return 0;
 }
