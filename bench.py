@@ -674,9 +674,13 @@ def run_ours(args, world, rank, local):
         "launches": kcount["trace_closest"], "kernel_ms_total": kms["trace_closest"],
     }
     import baseline
-    l2 = baseline.l2_read_gbs()
-    roofline["l2"] = {"peak": l2, "frac": achieved / l2, "unit": "GB/s",
-                      "peak_source": "one-launch read sweeps of a 32 MiB L2-resident buffer, measured in this run"}
+    try:
+        l2 = baseline.l2_read_gbs()
+        roofline["l2"] = {"peak": l2, "frac": achieved / l2, "unit": "GB/s",
+                          "peak_source": "one-launch read sweeps of a 32 MiB L2-resident buffer, measured in this run"}
+    except Exception as e:  # an optional figure: the line is printed without it
+        _log(f"l2 probe failed: {e}")
+        roofline["l2"] = None
 
     _log("e2e and kernel profile done")
     cpu = None
@@ -701,16 +705,25 @@ def run_ours(args, world, rank, local):
         frame = {"pixel_samples": samples / args.steps, "closest_rays": closest / args.steps,
                  "shadow_rays": shadow / args.steps, "render_ms": dev_ms / args.steps, "kernel_ms": kms,
                  "iterations": kcount["trace_closest"] // max(1, kcount["raygen"])}  # per wave
-        kokkos = kokkos_port_vs_ours(p, sc, cam, st, frame)
-        fb = kokkos["frame_bound"]
-        fb["ours_msamples_per_s"] = value
-        fb["speedup_at_least"] = value / fb["reference_msamples_per_s_at_most"]
-        fb["with_bounce_loop"]["speedup_at_least"] = value / fb["with_bounce_loop"]["reference_msamples_per_s_at_most"]
-        _log("kokkos port comparison done")
+        try:
+            kokkos = kokkos_port_vs_ours(p, sc, cam, st, frame)
+            fb = kokkos["frame_bound"]
+            fb["ours_msamples_per_s"] = value
+            fb["speedup_at_least"] = value / fb["reference_msamples_per_s_at_most"]
+            fb["with_bounce_loop"]["speedup_at_least"] = (
+                value / fb["with_bounce_loop"]["reference_msamples_per_s_at_most"])
+            _log("kokkos port comparison done")
+        except Exception as e:  # an optional comparison: the line is printed without it
+            _log(f"kokkos port comparison failed: {e}")
+            kokkos = {"error": str(e)}
     configs = None
     if rank == 0 and not args.no_configs:
-        configs = scene_configs(p)
-        _log("other configurations done")
+        try:
+            configs = scene_configs(p)
+            _log("other configurations done")
+        except Exception as e:  # optional: the line is printed without it
+            _log(f"other configurations failed: {e}")
+            configs = {"error": str(e)}
 
     if rank == 0:
         h2d = C.sizeof(cam) + C.sizeof(st)
