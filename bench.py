@@ -374,6 +374,38 @@ def cpu_baseline(sc, cam, st, spp=1, frames=2):
                       f"({samples} pixel-samples, {dt:.1f} s)"}
 
 
+def cpu_baseline_configs():
+    """The CPU oracle on the other forward configurations, all host threads:
+    the box room at its full 64 spp (512^2, depth 8), the differentiable
+    workload's forward pass at its full 64 spp (256^2, depth 6, homogeneous
+    medium), and the 2M-triangle volume scene at 1 spp of its 1920^2 frame
+    (adaptive sampling off for the sample: its gate opens after 16 samples),
+    Msamples/s per configuration."""
+    import oracle
+    from photon_gb300 import workloads
+    oracle.build()
+    out = {}
+    for name, make, spp in (("box_room_512", workloads.box_room, None),
+                            ("differentiable_256", workloads.differentiable, None),
+                            ("instanced_2m_1920", workloads.instanced_2m, 1)):
+        sc, cam, st = make()
+        s = type(st).from_buffer_copy(bytes(st))
+        if spp:
+            s.pixel_samples = spp
+            s.adaptive_sampling = 0
+        r = oracle.CpuRenderer("oracle")
+        r.set_scene(sc)
+        t = time.perf_counter()
+        r.render(cam, s, True)
+        dt = time.perf_counter() - t
+        samples = s.width * s.height * s.pixel_samples
+        out[name] = {"msamples_per_s": samples / dt / 1e6, "pixel_samples": int(samples), "seconds": dt,
+                     "spp": int(s.pixel_samples), "full_spp": spp is None}
+        r.close()
+        _log(f"cpu baseline: {name} done")
+    return out
+
+
 def batched_vs_plain(p, n_jobs=64, seed=0, check_jobs=8):
     """The 64-job mix: the same render calls one at a time (phc_render per
     renderer) and as one batch (phc_render_batch), wall-clock, scenes
@@ -687,6 +719,11 @@ def run_ours(args, world, rank, local):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, cam, st)
         _log("cpu baseline done")
+        if not args.no_configs:
+            try:
+                cpu["configs"] = cpu_baseline_configs()
+            except Exception as e:  # optional: the line is printed without it
+                _log(f"cpu baseline of the other configurations failed: {e}")
     batched = None
     if rank == 0 and not args.no_batch:
         r.close()
