@@ -6,12 +6,15 @@
 //   Disney BSDF           include/photon/pt/disney_bsdf.h:21-521
 //   lights (point/dir/spot) include/photon/pt/light.h:66-142
 //   environment map       include/photon/pt/environment_map.h:40-155
-//   TF volumes            include/photon/pt/tf_volume.h:43-283
+//   TF volumes            include/photon/pt/tf_volume.h:43-283 (volume_track.cuh)
 //   samplers/attributes   include/photon/pt/sampler.h:73-134,
 //                         src/photon/pt/pathtracer.cpp:111-247
 //   light selection       src/photon/pt/pathtracer.cpp:270-367
 // Read-only scene data goes through the read-only data (texture/L1) path
-// with __ldg.
+// with __ldg.  Every function is inlined into the kernels: each is called once
+// per kernel variant, and calls under the shading kernels' register caps cost
+// register saves and spills (measured: 12% more instructions, 10% slower
+// shading when the BSDF, material and light functions were called).
 #pragma once
 
 #include "cdf_search.cuh"
