@@ -11,10 +11,11 @@
 //                         src/photon/pt/pathtracer.cpp:111-247
 //   light selection       src/photon/pt/pathtracer.cpp:270-367
 // Read-only scene data goes through the read-only data (texture/L1) path
-// with __ldg.  Every function is inlined into the kernels: each is called once
-// per kernel variant, and calls under the shading kernels' register caps cost
-// register saves and spills (measured: 12% more instructions, 10% slower
-// shading when the BSDF, material and light functions were called).
+// with __ldg.  The functions are inlined into the kernels (each has one or
+// two call sites per kernel variant): calls under the shading kernels'
+// register caps cost register saves and spills (measured: 12% more
+// instructions, 10% slower shading when the BSDF, material and light
+// functions were called).
 #pragma once
 
 #include "cdf_search.cuh"
