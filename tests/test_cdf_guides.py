@@ -69,3 +69,30 @@ def test_guides_peaked_environment(host_lib):
     counts = _check(host_lib, sc)
     assert counts[0] & 6 == 6
     assert counts[4] == 0
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (5, 1), (3, 2)])
+def test_guides_tiny_environments(host_lib, shape):
+    """Environments of one row or one column (guide cells span the whole
+    table) still give the bisection's indices."""
+    from photon_gb300 import workloads
+    sc, _, _ = workloads.box_room()
+    h, w = shape
+    rng = np.random.default_rng(h * 10 + w)
+    env = rng.uniform(0.0, 2.0, (h, w, 4)).astype(np.float32)
+    env[..., 3] = 1.0
+    sc.env_pixels = env
+    counts = _check(host_lib, sc)
+    assert counts[0] & 6 == 6
+    assert counts[2] > 0 and counts[4] == 0
+
+
+def test_guides_black_environment(host_lib):
+    """An all-black environment: the CDFs fall back to uniform steps (k / n)."""
+    from photon_gb300 import workloads
+    sc, _, _ = workloads.box_room()
+    env = np.zeros((16, 32, 4), np.float32)
+    env[..., 3] = 1.0
+    sc.env_pixels = env
+    counts = _check(host_lib, sc)
+    assert counts[4] == 0
