@@ -54,6 +54,22 @@ HIT_BYTES = 16    # t, prim, u, v
 # reads stay in L2, so the traffic is the ray/hit queues and grows with the
 # ray count).  The roofline's `traffic` scales it to the average launch.
 TRACE_DRAM_BYTES_PER_RAY = (291.76e6 + 147.45e6) / 8388608
+# Instruction issue of k_trace from the same capture: warp instructions per
+# camera ray (smsp__inst_executed.sum / rays), the fraction of issue slots
+# used, and active threads per warp instruction.
+TRACE_ISSUE = {"warp_instructions_per_ray": 1.831e9 / 8388608, "issue_active": 0.788,
+               "threads_per_warp_instruction": 20.4,
+               "source": "ncu --set full capture of k_trace, bounce iteration 0 of the 500K workload at 8 spp "
+                         "(profiles/k_trace_procedural_500k.md)"}
+# Shading: algorithmic bytes per shaded hit path: queue and sorted index 8,
+# path state 68 (origin+tmin, direction+tmax, throughput+pdf, info, distance),
+# hit 16, triangle indices+material 16, three vertex normals 48, triangle
+# record 48, material parameters 64, continued path 68, shadow record 48.
+SHADE_BYTES_PER_PATH = 8 + 68 + 16 + 16 + 48 + 48 + 64 + 68 + 48
+# DRAM bytes per shaded path of the material-sorted hit-shading kernel, from
+# one ncu capture (1412.8 + 1897.5 MB over the 8.4M hits of iteration 0 at
+# 8 spp, profiles/k_shade_procedural_500k.md).
+SHADE_DRAM_BYTES_PER_PATH = (1412.8e6 + 1897.5e6) / 8388608
 
 
 _T0 = time.perf_counter()
@@ -472,7 +488,10 @@ def batched_vs_plain(p, n_jobs=64, seed=0, check_jobs=8):
             r.close()
     finally:
         p.tuning_set("wave_paths", old)
-    out["ratio"] = out["one_sample_per_wave"]["ratio"]
+    # the headline ratio is against the plain path as shipped (sample lanes);
+    # the one-sample-per-wave ratio is the reference's loop structure
+    out["ratio"] = out["lanes"]["ratio"]
+    out["ratio_vs_one_sample_per_wave"] = out["one_sample_per_wave"]["ratio"]
     out["identical_images"] = out["one_sample_per_wave"]["identical_images"] and out["lanes"]["identical_images"]
     return out
 
@@ -693,8 +712,14 @@ def run_ours(args, world, rank, local):
     achieved = bytes_alg / (ms / 1e3) / 1e9 if ms > 0 else 0.0
     roofline = {
         "kernel": "k_trace (BVH8 closest hit)" if dom != "trace_shadow" else "k_shadow (BVH8 any hit)",
-        "dominant_kernel_by_time": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "dominant_kernel_by_time": dom,
+        # what limits it (ncu): instruction issue over an L2-resident BVH and
+        # triangle set; `frac` is the metric's figure, algorithmic node /
+        # triangle / ray bytes against the measured HBM copy bandwidth
+        "bound": "issue", "memory_level": "l2",
+        "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+        "issue": TRACE_ISSUE,
         "traffic": (TRACE_DRAM_BYTES_PER_RAY * prof["closest_rays"] / max(1, kcount["trace_closest"])
                     if dom != "trace_shadow" else None),
         "traffic_source": "ncu capture of k_trace (profiles/k_trace_procedural_500k.md): 52.4 DRAM bytes per "
@@ -704,6 +729,18 @@ def run_ours(args, world, rank, local):
         "nodes_per_ray": prof["node_visits"] / max(1, prof["closest_rays"]),
         "tris_per_ray": prof["tri_tests"] / max(1, prof["closest_rays"]),
         "launches": kcount["trace_closest"], "kernel_ms_total": kms["trace_closest"],
+    }
+    shade_paths = prof["closest_rays"]
+    shade_gbs = shade_paths * SHADE_BYTES_PER_PATH / (kms["shade"] / 1e3) / 1e9 if kms["shade"] > 0 else 0.0
+    roofline["shade"] = {
+        "kernel": "k_shade (hit and miss shading, material-sorted)", "bound": "latency",
+        "ms_per_frame": kms["shade"], "paths": shade_paths,
+        "algorithmic_bytes_per_path": SHADE_BYTES_PER_PATH,
+        "achieved": shade_gbs, "peak": peak, "unit": "GB/s", "frac": shade_gbs / peak,
+        "dram_bytes_per_path": SHADE_DRAM_BYTES_PER_PATH,
+        "note": "paths = closest-hit rays of the frame, hits and misses (a miss reads fewer bytes, so the "
+                "algorithmic figure is an upper bound); DRAM bytes per path from the ncu capture "
+                "(profiles/k_shade_procedural_500k.md)",
     }
     import baseline
     try:

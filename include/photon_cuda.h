@@ -441,10 +441,14 @@ int phc_accel_create_instanced(phc_accel **out, const float *positions, uint64_t
     const uint32_t *indices, uint64_t triangle_count, const float *normals, const uint32_t *material_ids,
     const phc_object *objects, uint32_t object_count, const phc_instance *instances, uint32_t instance_count);
 void phc_accel_destroy(phc_accel *a);
+/* Largest ray count one phc_trace_* call accepts (PHC_ERR_LIMIT above it). */
+#define PHC_TRACE_MAX_RAYS 0x40000000u
 /* RayBackend::trace_closest (kokkos_backend.cpp:21-61) on device pointers:
    origins/directions are xyz float triples (RayBatch, ray_backend.h:31-37),
    tmin/tmax one float each; a ray with !(tmax > tmin) misses.  Writes n
-   phc_hit_result records.  stream is a cudaStream_t (NULL: the library's). */
+   phc_hit_result records.  stream is a cudaStream_t (NULL: the library's).
+   Blocks until the trace is done; n above PHC_TRACE_MAX_RAYS is rejected
+   with PHC_ERR_LIMIT. */
 int phc_trace_closest(phc_accel *a, const float *origins, const float *directions, const float *tmin,
     const float *tmax, uint32_t n, phc_hit_result *hits, void *stream);
 /* The same traversal with the compact 16-byte hit record the renderer uses:
@@ -463,7 +467,7 @@ int phc_accel_info(const phc_accel *a, uint64_t *node_bytes, uint64_t *tri_bytes
 const char *phc_accel_error(void);
 
 /* Largest ray count phc_trace_closest_compact_static accepts. */
-#define PHC_STATIC_MAX_RAYS 0x40000000u
+#define PHC_STATIC_MAX_RAYS PHC_TRACE_MAX_RAYS
 /* No counterpart in the reference: an allocation-free form of
    phc_trace_closest_compact, with the same arguments and the same results.
    It is for callers that must not allocate device memory while they trace:
@@ -474,11 +478,14 @@ const char *phc_accel_error(void);
    array compiled into the library, which every GPU that loads the library
    holds until the process exits; the accel, rays and hit buffer are the
    caller's as before.  The first call on a device looks the array's device
-   address up (cudaGetSymbolAddress) and caches it, so make that first call
-   before any stream capture.  Every call shares the one array and resets the
-   counter itself: calls that overlap on the GPU (two streams, two threads)
-   race and must be serialised by the caller.  n above PHC_STATIC_MAX_RAYS is
-   rejected with PHC_ERR_LIMIT.  Blocks until the trace is done. */
+   address up (cudaGetSymbolAddress) and caches it per CUDA context (a
+   context made after cudaDeviceReset gets its own lookup); that lookup must
+   not run while a stream of the device is being captured, so make the first
+   call before any stream capture starts.  Every call shares the one array
+   and resets the counter itself: calls that overlap on the GPU (two
+   streams, two threads) race and must be serialised by the caller.  n above
+   PHC_STATIC_MAX_RAYS is rejected with PHC_ERR_LIMIT.  Each call blocks
+   until its trace is done: it synchronises the stream before it returns. */
 int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const float *directions, const float *tmin,
     const float *tmax, uint32_t n, float *hits4, void *stream);
 

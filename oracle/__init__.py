@@ -25,20 +25,25 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_LIB = os.path.join(HERE, "_ref", "libphoton_ref.so")
 ORACLE_LIB = os.path.join(HERE, "_build", "libphoton_oracle.so")
-REFERENCE_DIR = os.environ.get("PHOTON_REFERENCE_DIR", "/root/reference")
+# The reference checkout, when it is not where oracle/Makefile looks (REF).
+REFERENCE_DIR = os.environ.get("PHOTON_REFERENCE_DIR", "")
 
 
 def build(ref: bool | None = None, jobs: int = 8, quiet: bool = True):
-    """Build the restatement (always) and the reference oracle (when the
-    reference checkout exists, or when ref=True)."""
-    if ref is None:
-        ref = os.path.isdir(os.path.join(REFERENCE_DIR, "src", "photon", "pt"))
-    targets = ["oracle"] + (["ref"] if ref else [])
-    out = subprocess.run(["make", "-C", HERE, f"-j{jobs}", f"REF={REFERENCE_DIR}"] + targets,
-                         capture_output=True, text=True)
+    """Build the restatement (always) and the reference oracle: where the
+    reference checkout exists (ref=None), always (ref=True) or never
+    (ref=False)."""
+    targets = ["oracle"] + {None: ["ref-if-present"], True: ["ref"], False: []}[ref]
+    out = subprocess.run(["make", "-C", HERE, f"-j{jobs}"] + ([f"REF={REFERENCE_DIR}"] if REFERENCE_DIR else [])
+                         + targets, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout[-4000:] + out.stderr[-4000:])
     return targets
+
+
+def have_ref() -> bool:
+    """Whether the reference oracle is built (after build())."""
+    return os.path.exists(REF_LIB)
 
 
 _libs = {}

@@ -8,9 +8,12 @@
 #include <stdexcept>
 #include <string>
 
+#include <cuda.h> // driver types only: cuCtxGetCurrent / cuCtxGetId are reached through the runtime
+
 #include "../../include/photon_cuda.h"
 #include "scene_build.h"
 #include "traverse.cuh"
+#include "tuning.h"
 
 using namespace phc;
 
@@ -63,8 +66,9 @@ __global__ void __launch_bounds__(128) k_level_a(DevScene sc, const float *__res
     const uint32_t i = base + (threadIdx.x & 31u);
     if (i >= n)
       continue;
-    const V3 o{orgs[3 * i], orgs[3 * i + 1], orgs[3 * i + 2]};
-    const V3 d{dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+    const size_t i3 = size_t(3) * i;
+    const V3 o{orgs[i3], orgs[i3 + 1], orgs[i3 + 2]};
+    const V3 d{dirs[i3], dirs[i3 + 1], dirs[i3 + 2]};
     const float t0 = tmins[i], t1 = tmaxs[i];
     uint32_t inst = INST_NONE;
     if (MODE == 2) {
@@ -130,16 +134,25 @@ int launch(phc_accel *a, const float *o, const float *d, const float *t0, const 
 {
   if (!a)
     return fail(PHC_ERR_INVALID, "null accel");
+  // the warps' 32-bit batch counter overshoots n by at most one batch per
+  // warp of the grid, which stays far below 2^32 for n up to the limit
+  if (n > PHC_TRACE_MAX_RAYS)
+    return fail(PHC_ERR_LIMIT, "trace: n = " + std::to_string(n) + " rays exceeds the maximum of " +
+        std::to_string(PHC_TRACE_MAX_RAYS) + " per call");
   if (n == 0)
     return PHC_OK;
   if (!o || !d || !t0 || !t1 || !out)
     return fail(PHC_ERR_INVALID, "null ray or output pointer");
-  cudaSetDevice(a->device);
+  cudaError_t e = cudaSetDevice(a->device);
+  if (e != cudaSuccess)
+    return fail(PHC_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : a->stream;
   uint32_t *fetch = reinterpret_cast<uint32_t *>(a->counters + 2);
-  cudaMemsetAsync(a->counters, 0, 4 * sizeof(uint64_t), s);
+  e = cudaMemsetAsync(a->counters, 0, 4 * sizeof(uint64_t), s);
+  if (e != cudaSuccess)
+    return fail(PHC_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
   const int blocks = a->sm_count * 16;
-  const bool count = std::getenv("PHC_TUNE_COUNT_TRAVERSAL") && std::atoi(std::getenv("PHC_TUNE_COUNT_TRAVERSAL"));
+  const bool count = tuning().count_traversal != 0;
   auto *st = reinterpret_cast<unsigned long long *>(a->counters);
   const bool inst = a->scene.dev.inst_count > 0;
   if (count && inst)
@@ -150,14 +163,16 @@ int launch(phc_accel *a, const float *o, const float *d, const float *t0, const 
     k_level_a<MODE, false, true><<<blocks, 128, 0, s>>>(a->scene.dev, o, d, t0, t1, n, out, fetch, st);
   else
     k_level_a<MODE, false><<<blocks, 128, 0, s>>>(a->scene.dev, o, d, t0, t1, n, out, fetch, st);
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e == cudaSuccess)
     e = cudaStreamSynchronize(s);
   if (e != cudaSuccess)
     return fail(PHC_ERR_CUDA, std::string("trace: ") + cudaGetErrorString(e));
   uint64_t c[2] = {0, 0};
   if (count) {
-    cudaMemcpy(c, a->counters, sizeof(c), cudaMemcpyDeviceToHost);
+    e = cudaMemcpy(c, a->counters, sizeof(c), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+      return fail(PHC_ERR_CUDA, std::string("trace counters: ") + cudaGetErrorString(e));
   }
   a->last_nodes = c[0];
   a->last_tris = c[1];
@@ -303,33 +318,77 @@ const char *phc_accel_error(void) { return g_accel_error.c_str(); }
 // file-scope array below instead of memory the accel allocated.  The array is
 // part of the module image: every GPU that loads this library holds these
 // 256 bytes until the process exits.  Host code must not use the array's name
-// as a device address; it asks the runtime for the address once per device.
+// as a device address; it asks the runtime for the address once per device
+// context (static_scratch).
 #define PHC_STATIC_SCRATCH_WORDS 64
 static __device__ __align__(256) uint32_t g_static_scratch[PHC_STATIC_SCRATCH_WORDS];
 
 namespace {
 
-// Device address of g_static_scratch on `device`, looked up on the first call
-// made with that device current and cached (nullptr on failure, err set).
-uint32_t *static_scratch(int device, std::string &err)
+// Identity of the CUDA context current on this thread: cuCtxGetId of
+// cuCtxGetCurrent, both reached through the runtime's driver entry points
+// (the library does not link the driver library itself).  Context ids are
+// unique for the life of the process, so a context created after
+// cudaDeviceReset, or a driver-API caller's own context, never matches an
+// earlier one.  0 when the driver cannot say.
+unsigned long long current_context_id()
 {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  if (!get_current || !get_id)
+    return 0;
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Device address of g_static_scratch in the context current on this thread
+// (the caller has made the accel's device current).  The set-up looks it up
+// with cudaGetSymbolAddress once per device context and caches it under the
+// context's id; nullptr on failure, with err set.  Where the context has no
+// id the address is looked up on every call.
+uint32_t *static_scratch(std::string &err)
+{
+  struct Entry {
+    unsigned long long ctx;
+    uint32_t *ptr;
+  };
   static std::mutex mu;
-  static uint32_t *ptrs[256] = {};
-  if (device < 0 || device >= 256) {
-    err = "device ordinal out of range";
+  static Entry cache[64] = {};
+  static unsigned next = 0;
+  const unsigned long long ctx = current_context_id();
+  std::lock_guard<std::mutex> lock(mu);
+  if (ctx)
+    for (const Entry &e : cache)
+      if (e.ctx == ctx)
+        return e.ptr;
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (e != cudaSuccess) {
+    err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
     return nullptr;
   }
-  std::lock_guard<std::mutex> lock(mu);
-  if (!ptrs[device]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess) {
-      err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
-      return nullptr;
-    }
-    ptrs[device] = static_cast<uint32_t *>(p);
+  if (ctx) {
+    cache[next] = Entry{ctx, static_cast<uint32_t *>(p)};
+    next = (next + 1) % 64;
   }
-  return ptrs[device];
+  return static_cast<uint32_t *>(p);
 }
 
 } // namespace
@@ -351,7 +410,7 @@ extern "C" int phc_trace_closest_compact_static(phc_accel *a, const float *origi
   if (e != cudaSuccess)
     return fail(PHC_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
   std::string err;
-  uint32_t *scratch = static_scratch(a->device, err);
+  uint32_t *scratch = static_scratch(err);
   if (!scratch)
     return fail(PHC_ERR_CUDA, err);
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : a->stream;

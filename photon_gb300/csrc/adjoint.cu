@@ -1055,6 +1055,8 @@ __device__ __forceinline__ void adj_shade_path(const RenderConst &rc, const DevS
 __global__ void __launch_bounds__(128, PHC_ADJ_MIN_BLOCKS) k_adj_shade(const RenderConst *__restrict__ rcp, DevScene sc, AdjPathSoA in,
     AdjPathSoA out, const float4 *__restrict__ hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a)
 {
+  if (wave_failed(wc)) // a traversal warp stopped at its trip cap: its results are incomplete
+    return;
   __shared__ float smat[MAX_SMEM_MATERIALS * NP];
   __shared__ float svol[MAX_VOLUMES * 4];
   Grads g = begin_grads(smat, svol, sc, a);
@@ -1108,6 +1110,8 @@ __global__ void __launch_bounds__(128, PHC_ADJ_MIN_BLOCKS) k_adj_shade(const Ren
 __global__ void __launch_bounds__(128) k_adj_resolve(const RenderConst *__restrict__ rcp, DevScene sc,
     AdjShadowSoA sh, AdjPathSoA next, WaveCounters wc, int it, AdjointArgs a)
 {
+  if (wave_failed(wc)) // a traversal warp stopped at its trip cap: its results are incomplete
+    return;
   __shared__ float smat[MAX_SMEM_MATERIALS * NP];
   __shared__ float svol[MAX_VOLUMES * 4];
   Grads g = begin_grads(smat, svol, sc, a);

@@ -112,7 +112,7 @@ struct phc_renderer {
   uint32_t width{0}, height{0}, samples{0}, sample_counter{0};
   // graph of one wave
   cudaGraphExec_t graph{nullptr};
-  uint64_t graph_key[6]{};
+  uint64_t graph_key[7]{};
   // bumped whenever a buffer a recorded wave graph points to is reallocated
   uint64_t buf_gen{0};
   uint64_t graph_launches{0}; // kernels per replay of the wave graph
@@ -316,6 +316,7 @@ WaveCounters wave_counters(phc_renderer *r, int max_iter)
   wc.wave = c + wave_counter_words(max_iter);
   wc.error = c + wave_counter_words(max_iter) + 1;
   wc.dbg = c + wave_counter_words(max_iter) + 4;
+  wc.trip_cap = uint32_t(tuning().wave_trip_cap);
   return wc;
 }
 // Bytes of the counters reset at the start of every wave (not wave / error).
@@ -613,12 +614,12 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
 
   ck(cudaEventRecord(r->ev0, s), "event");
   // everything the recorded launch sequence depends on
-  const uint64_t key[6] = {uint64_t(npix) | (uint64_t(lanes) << 32),
+  const uint64_t key[7] = {uint64_t(npix) | (uint64_t(lanes) << 32),
       uint64_t(max_iter) | (uint64_t(rc.adaptive) << 32), r->scene_generation,
       uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32),
       uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16) |
           (uint64_t(tu.sort_threshold) << 24),
-      r->buf_gen};
+      r->buf_gen, uint64_t(tu.wave_trip_cap)};
   uint64_t launches = 0;
   KernelTimer timer;
   if (tu.time_kernels) {

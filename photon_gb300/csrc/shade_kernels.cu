@@ -336,6 +336,8 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
     PathSoA in, PathSoA out, const float4 *__restrict__ hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it,
     HitQueues hq)
 {
+  if (wave_failed(wc))
+    return;
   const uint32_t n = PART == 0 ? wc.count[it] : (PART == 1 ? wc.hcount[it] : wc.mcount[it]);
   uint32_t *fetch = wc.fetch + 4 * it + (PART == 2 ? 2 : 1);
   for (;;) {
@@ -398,6 +400,8 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
 __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restrict__ rcp, DevScene sc, PathSoA in,
     const float4 *__restrict__ hits, WaveCounters wc, int it, HitQueues hq)
 {
+  if (wave_failed(wc))
+    return;
   // persistent warps with refill: a lane whose ray is done takes a new one
   // once VOL_REFILL lanes of its warp are idle; every step is one density
   // lookup of every busy lane (vt_step)
@@ -410,7 +414,7 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
   bool busy = false, exhausted = false;
   uint32_t idx = 0, idle = WARP_FULL;
   for (uint32_t trips = 0;; ++trips) {
-    if (trips >= WAVE_TRIP_CAP) { // warp-uniform
+    if (trips >= wc.trip_cap) { // warp-uniform
       if (lane == 0)
         atomicCAS(wc.error, 0u, (WAVE_ERR_VOLUME << 16) | uint32_t(it));
       break;

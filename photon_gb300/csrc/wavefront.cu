@@ -210,6 +210,8 @@ template <bool COUNT, bool SPLIT, bool BATCH, bool INST = false>
 __global__ void __launch_bounds__(128, INST ? PHC_TRACE_MIN_BLOCKS_INST : PHC_TRACE_MIN_BLOCKS) k_trace(DevScene sc, BatchTable bt, PathSoA in, float4 *__restrict__ hits,
     WaveCounters wc, int it, uint64_t *stats, uint32_t refill, HitQueues hq)
 {
+  if (wave_failed(wc))
+    return;
   const uint32_t n = wc.count[it];
   uint32_t *fetch = wc.fetch + 4 * it;
   const uint32_t lane = lane_id();
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(128, INST ? PHC_TRACE_MIN_BLOCKS_INST : PHC_TR
   // (refill, queue appends) run only on trips where some lane finished.
   uint32_t idle = WARP_FULL;
   for (uint32_t trips = 0;; ++trips) {
-    if (trips >= WAVE_TRIP_CAP) { // warp-uniform: every lane counts the same trips
+    if (trips >= wc.trip_cap) { // warp-uniform: every lane counts the same trips
       record_cap(wc, (WAVE_ERR_TRACE << 16) | uint32_t(it), n, *fetch, busy, exhausted, idx, in.ray_o[idx],
           in.ray_d[idx], s, steps, rays, fetch_trips, step_trips, max_steps, max_idx, trips);
       break;
@@ -338,6 +340,8 @@ template <bool BATCH>
 __global__ void __launch_bounds__(256) k_mat_hist(DevScene sc, BatchTable bt, const uint4 *__restrict__ info,
     const float4 *__restrict__ hits, HitQueues hq, WaveCounters wc, int it, uint32_t *bins)
 {
+  if (wave_failed(wc))
+    return;
   __shared__ uint32_t h[MAT_SORT_BINS];
   const uint32_t n = wc.hcount[it];
   if (n < hq.sort_threshold)
@@ -356,6 +360,8 @@ __global__ void __launch_bounds__(256) k_mat_hist(DevScene sc, BatchTable bt, co
 // One block of MAT_SORT_BINS threads: bins[0..) counts -> bins[MAT_SORT_BINS..) starts.
 __global__ void __launch_bounds__(MAT_SORT_BINS) k_mat_scan(HitQueues hq, WaveCounters wc, int it, uint32_t *bins)
 {
+  if (wave_failed(wc))
+    return;
   __shared__ uint32_t t[MAT_SORT_BINS];
   if (wc.hcount[it] < hq.sort_threshold)
     return;
@@ -379,6 +385,8 @@ template <bool BATCH>
 __global__ void __launch_bounds__(256) k_mat_scatter(DevScene sc, BatchTable bt, const uint4 *__restrict__ info,
     const float4 *__restrict__ hits, HitQueues hq, WaveCounters wc, int it, uint32_t *bins)
 {
+  if (wave_failed(wc))
+    return;
   __shared__ uint32_t cnt[MAT_SORT_BINS];
   const uint32_t n = wc.hcount[it];
   if (n < hq.sort_threshold)
@@ -425,6 +433,8 @@ template <bool COUNT, bool BATCH, bool DEFER = false, bool INST = false>
 __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ rcp, DevScene sc, BatchTable bt,
     ShadowSoA sh, Accum acc_param, WaveCounters wc, int it, uint64_t *stats, uint32_t refill)
 {
+  if (wave_failed(wc))
+    return;
   const uint32_t n = wc.scount[it];
   uint32_t *fetch = wc.fetch + 4 * it + 3;
   const uint32_t lane = lane_id();
@@ -440,7 +450,7 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
   // changes only where lanes finish or fetch
   uint32_t idle = WARP_FULL;
   for (uint32_t trips = 0;; ++trips) {
-    if (trips >= WAVE_TRIP_CAP) {
+    if (trips >= wc.trip_cap) {
       record_cap(wc, (WAVE_ERR_SHADOW << 16) | uint32_t(it), n, *fetch, busy, exhausted, idx, sh.a[idx], sh.b[idx],
           s, steps, rays, fetch_trips, step_trips, max_steps, max_idx, trips);
       break;
@@ -532,6 +542,8 @@ template <bool BATCH>
 __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__restrict__ rcp, DevScene sc,
     BatchTable bt, ShadowSoA sh, Accum acc_param, WaveCounters wc, int it)
 {
+  if (wave_failed(wc))
+    return;
   // the unoccluded shadow rays (tmax >= 0) of the iteration: ratio-tracking
   // transmittance (stream dimension 0x10000 + iteration) times the NEE
   // contribution into the path's pixel slot; persistent warps with refill,
@@ -545,7 +557,7 @@ __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__rest
   bool busy = false, exhausted = false;
   uint32_t idx = 0, job = 0, idle = WARP_FULL;
   for (uint32_t trips = 0;; ++trips) {
-    if (trips >= WAVE_TRIP_CAP) { // warp-uniform
+    if (trips >= wc.trip_cap) { // warp-uniform
       if (lane == 0)
         atomicCAS(wc.error, 0u, (WAVE_ERR_VOLUME << 16) | uint32_t(it));
       break;

@@ -75,14 +75,18 @@ struct WaveCounters {
   uint32_t *wave;    // current wave index within the render call
   uint32_t *error;   // sticky error word
   uint32_t *dbg;     // [WAVE_DBG_WORDS] record of the first self-check failure
+  uint32_t trip_cap; // loop trips after which a persistent warp stops (tuning key wave_trip_cap)
 };
 inline size_t wave_counter_words(int max_iter) { return size_t(10 * max_iter + 1); }
 
 // Self-check of the persistent traversal loops: a warp that makes more than
-// WAVE_TRIP_CAP loop trips (each trip is one traversal step of every busy
-// lane; legitimate work needs a few thousand) stops and records
-// (kernel << 16) | iteration in the error word, first writer wins.
+// WaveCounters::trip_cap loop trips (each trip is one traversal step of every
+// busy lane; legitimate work needs a few thousand; default WAVE_TRIP_CAP)
+// stops and records (kernel << 16) | iteration in the error word, first
+// writer wins.  Every later kernel of the wave then returns at entry
+// (wave_failed), so nothing reads the results the stopped warps never wrote.
 constexpr uint32_t WAVE_TRIP_CAP = 1u << 24;
+__device__ __forceinline__ bool wave_failed(const WaveCounters &wc) { return *(volatile uint32_t *)wc.error != 0u; }
 enum : uint32_t { WAVE_ERR_TRACE = 1u, WAVE_ERR_SHADOW = 2u, WAVE_ERR_VOLUME = 3u };
 // A volume-tracking warp takes new rays once this many of its lanes are idle.
 constexpr uint32_t VOL_REFILL = 8u;

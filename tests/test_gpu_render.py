@@ -61,6 +61,38 @@ def test_render_procedural_matches_oracle(photon, oracle_lib, adaptive):
         assert close_fraction(got[f]["depth"], ref.read("depth")) >= MIN_PATH_FRACTION
 
 
+def test_render_procedural_full_frame_matches_oracle(photon, oracle_lib):
+    """The 500K-triangle workload at its full 1024^2 frame, depth 8, one
+    sample per pixel, two frames (sample offsets 0 and 1): 1,048,576 paths
+    per frame on the reference's RNG stream against the oracle, every path
+    and every channel (colour with alpha, depth, normal, albedo) at the
+    per-sample bar (>= 99.9% of paths within 1e-4 relative)."""
+    from photon_gb300 import workloads
+    sc, cam, st = workloads.procedural_500k()
+    assert (st.width, st.height, st.max_depth) == (1024, 1024, 8)
+    st.pixel_samples = 1
+    st.adaptive_sampling = 0
+    r = photon.Renderer()
+    r.set_scene(sc)
+    ref = oracle_lib.CpuRenderer("oracle")
+    ref.set_scene(sc)
+    for f in range(2):
+        r.render(cam, st, True)
+        ref.render(cam, st, True)
+        fracs = {}
+        for ch in ("color", "depth", "normal", "albedo"):
+            g, w = r.read(ch), ref.read(ch)
+            fracs[ch] = close_fraction(g, w)
+            if ch == "color":
+                bad = int((~close_mask(g, w)).sum())
+        print(f"500K workload 1024^2 frame {f}: " + ", ".join(f"{k} {v:.6f}" for k, v in fracs.items()) +
+              f" of {st.width * st.height} paths within 1e-4 ({bad} colour paths outside)")
+        for ch, v in fracs.items():
+            assert v >= MIN_PATH_FRACTION, f"frame {f} {ch}: {v:.6f}"
+    r.close()
+    ref.close()
+
+
 def test_progressive_accumulation(photon, oracle_lib):
     """render() without reset adds samples (RenderBridge.cpp:923-927);
     accumulated_samples counts them; a size change restarts."""
