@@ -447,12 +447,16 @@ def batched_vs_plain(p, n_jobs=64, seed=0, check_jobs=8):
             rs.append(r)
         return rs
 
+    dev = {"plain": 0.0, "batched": 0.0}
+
     def plain(rs, js):
+        dev["plain"] = 0.0
         for r, (sc, cam, st) in zip(rs, js):
             r.render(cam, st, True)
+            dev["plain"] += r.stats()["render_ms"] / 1e3
 
     def batch(rs, js):
-        p.render_batch([(r, cam, st, True) for r, (sc, cam, st) in zip(rs, js)])
+        dev["batched"] = p.render_batch([(r, cam, st, True) for r, (sc, cam, st) in zip(rs, js)])["render_ms"] / 1e3
 
     out = {"jobs": n_jobs, "pixel_samples": samples,
            "mix": f"{n_jobs} seeded procedural scenes, {min(tris)}-{max(tris)} tris (log-uniform), "
@@ -470,6 +474,14 @@ def batched_vs_plain(p, n_jobs=64, seed=0, check_jobs=8):
                 t = time.perf_counter()
                 fn(rs, jobs)
                 res[name + "_s"] = time.perf_counter() - t
+            # device time inside the calls (events around each call's GPU
+            # work) against wall time: what is left between the plain calls
+            # is GPU idle time that batching can remove; the rest it can only
+            # shorten by doing the same paths faster
+            res["plain_device_s"] = dev["plain"]
+            res["plain_idle_frac"] = max(0.0, 1.0 - dev["plain"] / res["plain_s"])
+            res["batched_device_s"] = dev["batched"]
+            res["ratio_bound_from_idle"] = res["plain_s"] / dev["plain"] if dev["plain"] > 0 else None
             res["plain_msamples_per_s"] = samples / res["plain_s"] / 1e6
             res["batched_msamples_per_s"] = samples / res["batched_s"] / 1e6
             res["ratio"] = res["plain_s"] / res["batched_s"]

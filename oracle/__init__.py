@@ -25,6 +25,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_LIB = os.path.join(HERE, "_ref", "libphoton_ref.so")
 ORACLE_LIB = os.path.join(HERE, "_build", "libphoton_oracle.so")
+# the restatement with double-evaluated transcendental functions (a second libm)
+ORACLE_DLIBM_LIB = os.path.join(HERE, "_build", "libphoton_oracle_dlibm.so")
+_LIBS = {"ref": (REF_LIB, "ref_"), "oracle": (ORACLE_LIB, "orc_"), "oracle_dlibm": (ORACLE_DLIBM_LIB, "orc_")}
 # The reference checkout, when it is not where oracle/Makefile looks (REF).
 REFERENCE_DIR = os.environ.get("PHOTON_REFERENCE_DIR", "")
 
@@ -83,8 +86,8 @@ class CpuRenderer:
 
     def __init__(self, which: str = "oracle"):
         self.which = which
-        self.prefix = "ref_" if which == "ref" else "orc_"
-        self.lib = _load(REF_LIB if which == "ref" else ORACLE_LIB, self.prefix)
+        path, self.prefix = _LIBS[which]
+        self.lib = _load(path, self.prefix)
         self.h = self._fn("renderer_create")()
         if not self.h:
             raise RuntimeError(f"{which}: renderer_create failed")

@@ -40,6 +40,33 @@
 namespace orc {
 
 using f32 = float;
+
+// The single-precision transcendental functions of the restatement.  By
+// default they are the host C library's, which is what the reference calls
+// (std::sin on a float, ...).  Built with -DORACLE_LIBM_DOUBLE each is
+// evaluated in double precision and rounded to float instead: a different
+// libm, correctly rounded almost everywhere, which the tests use to measure
+// how much a libm difference alone moves per-sample results (the GPU's
+// CUDA math functions are another such libm).
+namespace lm {
+#ifdef ORACLE_LIBM_DOUBLE
+inline f32 sin(f32 x) { return f32(::sin(double(x))); }
+inline f32 cos(f32 x) { return f32(::cos(double(x))); }
+inline f32 tan(f32 x) { return f32(::tan(double(x))); }
+inline f32 log(f32 x) { return f32(::log(double(x))); }
+inline f32 pow(f32 x, f32 y) { return f32(::pow(double(x), double(y))); }
+inline f32 acos(f32 x) { return f32(::acos(double(x))); }
+inline f32 atan2(f32 y, f32 x) { return f32(::atan2(double(y), double(x))); }
+#else
+inline f32 sin(f32 x) { return std::sin(x); }
+inline f32 cos(f32 x) { return std::cos(x); }
+inline f32 tan(f32 x) { return std::tan(x); }
+inline f32 log(f32 x) { return std::log(x); }
+inline f32 pow(f32 x, f32 y) { return std::pow(x, y); }
+inline f32 acos(f32 x) { return std::acos(x); }
+inline f32 atan2(f32 y, f32 x) { return std::atan2(y, x); }
+#endif
+} // namespace lm
 using u32 = uint32_t;
 using i32 = int32_t;
 
@@ -172,7 +199,7 @@ inline V2 concentric_disk(Rng &rng) // sampling.h:53-76
     r = av;
     theta = (PI / 2.f) - (PI / 4.f) * (u / v);
   }
-  return {r * std::cos(theta), r * std::sin(theta)};
+  return {r * lm::cos(theta), r * lm::sin(theta)};
 }
 inline V3 cosine_hemisphere(const V3 &n, Rng &rng) // sampling.h:78-92 (direction only)
 {
@@ -188,7 +215,7 @@ inline V3 uniform_sphere(Rng &rng) // sampling.h:94-100
   const f32 z = 1.f - 2.f * rng.next_f32();
   const f32 r = std::sqrt(std::fmax(0.f, 1.f - z * z));
   const f32 phi = TWO_PI * rng.next_f32();
-  return {r * std::cos(phi), r * std::sin(phi), z};
+  return {r * lm::cos(phi), r * lm::sin(phi), z};
 }
 
 // ------------------------------------------------------------- material.h
@@ -537,7 +564,7 @@ inline V3 ggx_half(const V3 &n, f32 a, Rng &rng) // disney_bsdf.h:357-375
   const f32 ct = std::sqrt((1.f - r1) / (1.f + (a2 - 1.f) * r1));
   const f32 st = std::sqrt(std::fmax(0.f, 1.f - ct * ct));
   const f32 phi = 2.f * PI * r2;
-  return normalize(t * (st * std::cos(phi)) + b * (st * std::sin(phi)) + n * ct);
+  return normalize(t * (st * lm::cos(phi)) + b * (st * lm::sin(phi)) + n * ct);
 }
 struct BS {
   V3 wi, f;
@@ -617,7 +644,7 @@ BS bsdf_sample(const Mat &m, const V3 &wo, const V3 &n, const V3 &sn, Rng &rng) 
       F = fresnel_dielectric(cos_i, eta);
     } else {
       const f32 f0 = dielectric_f0(m.ior);
-      F = f0 + (1.f - f0) * std::pow(1.f - cos_i, 5.f);
+      F = f0 + (1.f - f0) * lm::pow(1.f - cos_i, 5.f);
     }
     const f32 lobe_weight = t_energy / pt;
     out.pdf = 1.f;
@@ -691,13 +718,13 @@ LS sample_light(const Light &l, const V3 &p, Rng &rng) // light.h:66-142 (point,
   if (l.type == L_DIR) {
     V3 wi = -normalize(l.direction);
     if (l.radius > 0.f) {
-      const f32 cos_max = std::cos(l.radius);
+      const f32 cos_max = lm::cos(l.radius);
       const f32 ct = 1.f - rng.next_f32() * (1.f - cos_max);
       const f32 st = std::sqrt(std::fmax(0.f, 1.f - ct * ct));
       const f32 phi = TWO_PI * rng.next_f32();
       V3 t, b;
       onb(wi, t, b);
-      wi = normalize(t * (st * std::cos(phi)) + b * (st * std::sin(phi)) + wi * ct);
+      wi = normalize(t * (st * lm::cos(phi)) + b * (st * lm::sin(phi)) + wi * ct);
     }
     return {wi, l.color * l.intensity, 1.f, 1e30f};
   }
@@ -710,8 +737,8 @@ LS sample_light(const Light &l, const V3 &p, Rng &rng) // light.h:66-142 (point,
   const V3 spot_dir = normalize(l.direction);
   const V3 from_light = -normalize(center_to);
   const f32 cos_angle = dot(from_light, spot_dir);
-  const f32 cos_inner = std::cos(std::fmax(l.spot_angle - l.spot_falloff, 0.f));
-  const f32 cos_outer = std::cos(l.spot_angle);
+  const f32 cos_inner = lm::cos(std::fmax(l.spot_angle - l.spot_falloff, 0.f));
+  const f32 cos_outer = lm::cos(l.spot_angle);
   f32 falloff = 0.f;
   if (cos_angle >= cos_inner)
     falloff = 1.f;
@@ -746,17 +773,17 @@ struct Env {
   static V2 dir_to_uv(const V3 &d) // environment_map.h:138-147
   {
     const V3 nd = normalize(d);
-    const f32 phi = std::atan2(nd.z, nd.x);
+    const f32 phi = lm::atan2(nd.z, nd.x);
     const f32 y = clampf(nd.y, -1.f, 1.f);
-    const f32 theta = std::acos(y);
+    const f32 theta = lm::acos(y);
     return {(phi + PI) * INV_TWO_PI, theta * INV_PI};
   }
   static V3 uv_to_dir(const V2 &uv) // environment_map.h:149-155
   {
     const f32 phi = uv.x * TWO_PI - PI;
     const f32 theta = uv.y * PI;
-    const f32 st = std::sin(theta);
-    return {st * std::cos(phi), std::cos(theta), st * std::sin(phi)};
+    const f32 st = lm::sin(theta);
+    return {st * lm::cos(phi), lm::cos(theta), st * lm::sin(phi)};
   }
   void texel(const V3 &direction, u32 &x, u32 &y, V2 &uv) const
   {
@@ -807,7 +834,7 @@ struct Env {
     const f32 v = ((f32)row + rng.next_f32()) / (f32)height;
     const V3 dir = to_world(uv_to_dir(V2{u, v}));
     const f32 theta = v * PI;
-    const f32 denom = TWO_PI * PI * std::fmax(std::sin(theta), 1e-6f);
+    const f32 denom = TWO_PI * PI * std::fmax(lm::sin(theta), 1e-6f);
     pdf_out = (row_pdf * col_pdf) * (f32)width * (f32)height / denom;
     return dir;
   }
@@ -821,7 +848,7 @@ struct Env {
     const f32 row_pdf = marginal[y + 1] - marginal[y];
     const f32 col_pdf = cond(y, x + 1) - cond(y, x);
     const f32 theta = uv.y * PI;
-    const f32 denom = TWO_PI * PI * std::fmax(std::sin(theta), 1e-6f);
+    const f32 denom = TWO_PI * PI * std::fmax(lm::sin(theta), 1e-6f);
     return (row_pdf * col_pdf) * (f32)width * (f32)height / denom;
   }
   void build_cdf() // environment_map.cpp:8-65
@@ -834,7 +861,7 @@ struct Env {
       f32 *c = &conditional[size_t(y) * (width + 1)];
       c[0] = 0.f;
       const f32 theta = ((f32)y + 0.5f) * (PI / (f32)height);
-      const f32 st = std::sin(theta);
+      const f32 st = lm::sin(theta);
       f32 sum = 0.f;
       for (u32 x = 0; x < width; ++x) {
         sum += luminance(pixels[size_t(y) * width + x]);
@@ -1016,7 +1043,7 @@ struct VolSet {
       if (bound > 0.f) {
         const f32 inv_bound = 1.f / bound;
         while (lookups < 8192) {
-          t -= std::log(1.f - rng.next_f32()) * inv_bound;
+          t -= lm::log(1.f - rng.next_f32()) * inv_bound;
           if (t >= t_exit)
             break;
           ++lookups;
@@ -1363,7 +1390,7 @@ struct Cam { // camera.h:11-160
   static Cam perspective(const V3 &from, const V3 &at, const V3 &vup, f32 vfov, f32 aspect, f32 aperture, f32 focus)
   {
     const f32 theta = vfov * 3.1415926535f / 180.f;
-    const f32 h = std::tan(theta * 0.5f);
+    const f32 h = lm::tan(theta * 0.5f);
     const f32 vh = 2.f * h;
     const f32 vw = aspect * vh;
     Cam c;

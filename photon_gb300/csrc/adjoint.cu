@@ -396,11 +396,11 @@ __device__ Taps base_color_taps(const DevScene &sc, const DevMaterial &dm, const
       for (int kx = 0; kx < 2; ++kx) {
         const uint32_t x = uint32_t(kx ? i1[0] : i0[0]);
         const float w = (kx ? fr[0] : 1.f - fr[0]) * (wy * wz);
-        const uint32_t ti = si.offset + z * sxy + y * sx + x;
-        t.idx[t.n] = ti;
+        const uint32_t ti = z * sxy + y * sx + x;
+        t.idx[t.n] = si.grad_offset + ti;
         t.w[t.n] = w;
         ++t.n;
-        acc = add4(acc, mul4(__ldg(sc.texels + ti), w));
+        acc = add4(acc, mul4(sampler_texel(sc, si, ti), w));
       }
     }
   }
@@ -516,7 +516,7 @@ __device__ float vol_track_d(const DevScene &sc, const DevVolume &v, V3 org, V3 
       const float inv_bound = 1.f / bound;
       const float cell_start = t;
       while (lookups < 8192) {
-        t -= logf(1.f - rng.next()) * inv_bound;
+        t -= m_log(1.f - rng.next()) * inv_bound;
         if (t >= t_exit)
           break;
         ++lookups;

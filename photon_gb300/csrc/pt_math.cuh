@@ -26,6 +26,23 @@ namespace phc {
 using u32 = uint32_t;
 using i32 = int32_t;
 
+// The transcendental functions of the path-tracing code, in one place: CUDA's
+// single-precision functions on the device (the host's C library in host
+// builds of the same code).  PHC_MATH_DOUBLE (a bit mask: 1 sin / cos,
+// 2 log, 4 acos / atan2, 8 pow, 16 tan) evaluates the selected ones in
+// double precision and rounds to float instead, a build used only to measure
+// how per-sample results depend on the math library.
+#ifndef PHC_MATH_DOUBLE
+#define PHC_MATH_DOUBLE 0
+#endif
+PHC_HD float m_sin(float x) { return (PHC_MATH_DOUBLE & 1) ? float(sin(double(x))) : sinf(x); }
+PHC_HD float m_cos(float x) { return (PHC_MATH_DOUBLE & 1) ? float(cos(double(x))) : cosf(x); }
+PHC_HD float m_log(float x) { return (PHC_MATH_DOUBLE & 2) ? float(log(double(x))) : logf(x); }
+PHC_HD float m_acos(float x) { return (PHC_MATH_DOUBLE & 4) ? float(acos(double(x))) : acosf(x); }
+PHC_HD float m_atan2(float y, float x) { return (PHC_MATH_DOUBLE & 4) ? float(atan2(double(y), double(x))) : atan2f(y, x); }
+PHC_HD float m_pow(float x, float y) { return (PHC_MATH_DOUBLE & 8) ? float(pow(double(x), double(y))) : powf(x, y); }
+PHC_HD float m_tan(float x) { return (PHC_MATH_DOUBLE & 16) ? float(tan(double(x))) : tanf(x); }
+
 // Bit casts and bit scans that compile for the device and, for host-side
 // tests of the same traversal code, for the host.
 PHC_HD uint32_t f2u(float f)
@@ -178,8 +195,8 @@ PHC_HD void concentric_disk(Rng &rng, float &dx, float &dy)
     r = fabsf(v);
     th = (PI / 2.f) - (PI / 4.f) * (u / v);
   }
-  dx = r * cosf(th);
-  dy = r * sinf(th);
+  dx = r * m_cos(th);
+  dy = r * m_sin(th);
 }
 PHC_HD V3 cosine_hemisphere(V3 n, Rng &rng)
 {
@@ -195,7 +212,7 @@ PHC_HD V3 uniform_sphere(Rng &rng)
   const float z = 1.f - 2.f * rng.next();
   const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
   const float phi = TWO_PI * rng.next();
-  return V3{r * cosf(phi), r * sinf(phi), z};
+  return V3{r * m_cos(phi), r * m_sin(phi), z};
 }
 
 } // namespace phc

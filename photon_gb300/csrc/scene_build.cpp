@@ -125,6 +125,43 @@ bool may_emit(const DevMaterial &m)
   return m.src_kind[SRC_EMIT] != 0 || m.emission[0] > 0.f || m.emission[1] > 0.f || m.emission[2] > 0.f;
 }
 
+// RGBA8 images reach the seam as floats k / 255 (the reference's
+// SamplerTable holds fp32 RGBA, sampler.h:56-138; the bridge copies the
+// caller's floats).  When every value of a sampler's texels is one of the
+// 256 floats float(k) / 255 bit for bit (s.u8_decode), its texels are kept
+// as k in 8 bits and the device decodes them through the same table, so
+// lookups return the identical floats from a quarter of the bytes.  Appends
+// to s.texels_u8 and returns true, or leaves it unchanged and returns false.
+bool pack_texels_u8(const float *src, size_t floats, HostScene &s)
+{
+  const size_t at = s.texels_u8.size();
+  s.texels_u8.resize(at + floats);
+  uint8_t *dst = s.texels_u8.data() + at;
+  const float *dec = s.u8_decode.data();
+  int ok = 1;
+#pragma omp parallel for reduction(&& : ok) schedule(static)
+  for (int64_t i = 0; i < int64_t(floats); ++i) {
+    const float x = src[i];
+    const float y = x * 255.f;
+    if (!(y >= 0.f && y <= 255.f)) { // NaN, negative or above 1
+      ok = 0;
+      continue;
+    }
+    const uint32_t k = uint32_t(y + 0.5f);
+    uint32_t a, b;
+    std::memcpy(&a, &x, 4);
+    std::memcpy(&b, dec + k, 4);
+    if (a != b) { // not exactly k / 255 (-0.0 included)
+      ok = 0;
+      continue;
+    }
+    dst[i] = uint8_t(k);
+  }
+  if (!ok)
+    s.texels_u8.resize(at);
+  return ok != 0;
+}
+
 // EnvironmentMap::build_cdf (environment_map.cpp:8-65): row CDFs of texel
 // luminance and a marginal CDF of row sums weighted by sin(theta).
 void build_env_cdf(HostScene &s)
@@ -700,6 +737,7 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     si.size[1] = td.height;
     si.size[2] = 1;
     si.offset = uint32_t(offset);
+    si.grad_offset = uint32_t(offset);
     const size_t n = size_t(td.width) * td.height;
     if (n && !td.rgb)
       throw std::invalid_argument("scene: texture pixels pointer is null");
@@ -714,6 +752,14 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     offset += n;
     s.samplers.push_back(si);
   }
+  // storage offsets: float4 texels (atlas, then fp32 samplers) and uchar4
+  // texels (8-bit samplers); `offset` runs over every sampler in order
+  size_t f_offset = offset;
+  if (!pt && in.sampler_count) {
+    s.u8_decode.resize(256);
+    for (int k = 0; k < 256; ++k)
+      s.u8_decode[size_t(k)] = float(k) / 255.f;
+  }
   for (uint32_t i = 0; !pt && i < in.sampler_count; ++i) {
     const phc_sampler &sd = in.samplers[i];
     DevSampler si{};
@@ -724,7 +770,7 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
       si.wrap[d] = sd.wrap[d] == 1 ? 1 : (sd.wrap[d] == 2 ? 2 : 0);
       si.size[d] = std::max<uint32_t>(sd.size[d], 1);
     }
-    si.offset = uint32_t(offset);
+    si.grad_offset = uint32_t(offset);
     std::memcpy(si.in_t, sd.in_transform, sizeof(si.in_t));
     std::memcpy(si.in_o, sd.in_offset, sizeof(si.in_o));
     std::memcpy(si.out_t, sd.out_transform, sizeof(si.out_t));
@@ -732,13 +778,21 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     const size_t n = sd.texels ? size_t(sd.texel_count) : 0;
     if (si.type != 3 && n < size_t(si.size[0]) * si.size[1] * si.size[2])
       si.type = 3; // incomplete image: a transform keeps lookups in bounds
-    if (n)
-      s.texel_spans.push_back({sd.texels, 4 * n});
+    if (n && si.type != 3 && tuning().texels_u8 && pack_texels_u8(sd.texels, 4 * n, s)) {
+      si.u8 = 1;
+      si.offset = uint32_t(s.texels_u8.size() / 4 - n);
+    } else {
+      si.offset = uint32_t(f_offset);
+      if (n)
+        s.texel_spans.push_back({sd.texels, 4 * n});
+      f_offset += n;
+    }
     offset += n;
     s.samplers.push_back(si);
   }
   if (offset > 0xffffffffull)
     throw std::length_error("scene: too many sampler texels");
+  s.texel_logical_count = offset;
   for (uint32_t i = 0; i < in.light_count; ++i) {
     const phc_light &ld = in.lights[i];
     DevLight l{};
@@ -931,6 +985,8 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   d.samplers = put(h.samplers, s, err);
   d.sampler_count = uint32_t(h.samplers.size());
   d.texels = reinterpret_cast<const float4 *>(put_spans(h.texels, h.texel_spans, s, err));
+  d.texels_u8 = reinterpret_cast<const uchar4 *>(put(h.texels_u8, s, err));
+  d.u8_decode = put(h.u8_decode, s, err);
   d.lights = put(h.lights, s, err);
   d.light_count = uint32_t(h.lights.size());
   d.emissive_ids = put(h.emissive_ids, s, err);
@@ -976,9 +1032,7 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   node_bytes = uint64_t(h.bvh.nodes.size()) * 4;
   tri_bytes = uint64_t(h.bvh.tris.size()) * 4;
   bvh_depth = h.bvh.max_depth;
-  texel_count = uint64_t(h.texels.size() / 4);
-  for (const HostScene::Span &sp : h.texel_spans)
-    texel_count += sp.floats / 4;
+  texel_count = h.texel_logical_count;
   if (!err.empty()) {
     release();
     return err;

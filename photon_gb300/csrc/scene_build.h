@@ -39,6 +39,11 @@ struct HostScene {
     size_t floats;
   };
   std::vector<Span> texel_spans;
+  // 8-bit RGBA texels (4 bytes per texel) of the samplers whose every value
+  // is one of u8_decode's, and that table
+  std::vector<uint8_t> texels_u8;
+  std::vector<float> u8_decode;
+  uint64_t texel_logical_count{0}; // texels in the scene's texel order (atlas or every sampler)
   std::vector<Span> vol_value_spans; // volume fields, likewise
   std::vector<DevLight> lights;
   std::vector<uint32_t> emissive_ids;

@@ -69,6 +69,13 @@ struct DevSampler { // include/photon/pt/sampler.h:49-63
   float in_o[4];
   float out_t[16];
   float out_o[4];
+  // Storage of the texels: u8 = 0: float4 at DevScene::texels + offset;
+  // u8 = 1: uchar4 at DevScene::texels_u8 + offset (images whose every value
+  // is k / 255, decoded through DevScene::u8_decode).  grad_offset is the
+  // sampler's first texel in the scene's texel order (all samplers' texels
+  // in sequence), the index of the adjoint's texel gradients.
+  uint32_t u8;
+  uint32_t grad_offset;
 };
 
 struct DevLight { // include/photon/pt/light.h:19-35 (point, directional, spot)
@@ -118,6 +125,8 @@ struct DevScene {
   const DevSampler *samplers;
   uint32_t sampler_count;
   const float4 *texels;
+  const uchar4 *texels_u8;  // 8-bit RGBA samplers (DevSampler::u8)
+  const float *u8_decode;   // 256 entries: float(k) / 255 (IEEE division)
   const DevLight *lights;
   uint32_t light_count;
   const uint32_t *emissive_ids;

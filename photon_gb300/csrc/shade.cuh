@@ -255,7 +255,7 @@ __device__ __forceinline__ V3 ggx_half(V3 n, float a, Rng &rng)
   const float ct = sqrtf((1.f - r1) / (1.f + (a2 - 1.f) * r1));
   const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
   const float phi = 2.f * PI * r2;
-  return normalize(t * (st * cosf(phi)) + b * (st * sinf(phi)) + n * ct);
+  return normalize(t * (st * m_cos(phi)) + b * (st * m_sin(phi)) + n * ct);
 }
 // Sampled lobe: 1 diffuse, 2 GGX reflection, 3 smooth (delta) specular,
 // 4 dielectric reflection, 5 dielectric transmission, 6 clearcoat.  noh > 0:
@@ -347,7 +347,7 @@ static __device__ __forceinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n,
       F = fresnel_dielectric(cos_i, eta);
     } else {
       const float f0 = dielectric_f0(m.ior);
-      F = f0 + (1.f - f0) * powf(1.f - cos_i, 5.f);
+      F = f0 + (1.f - f0) * m_pow(1.f - cos_i, 5.f);
     }
     const float lobe_weight = t_energy / pt;
     out.pdf = 1.f;
@@ -425,6 +425,18 @@ __device__ __forceinline__ int32_t wrap_index(int32_t i, int32_t n, int32_t mode
   }
   return i < 0 ? 0 : (i >= n ? n - 1 : i);
 }
+// One texel of an image sampler (index within the sampler's texels): fp32
+// RGBA, or 8-bit RGBA decoded through the table of the 256 floats k / 255,
+// which returns the caller's original floats bit for bit.
+__device__ __forceinline__ float4 sampler_texel(const DevScene &sc, const DevSampler &si, uint32_t i)
+{
+  if (si.u8) {
+    const uchar4 t = __ldg(sc.texels_u8 + si.offset + i);
+    return make_float4(__ldg(sc.u8_decode + t.x), __ldg(sc.u8_decode + t.y), __ldg(sc.u8_decode + t.z),
+        __ldg(sc.u8_decode + t.w));
+  }
+  return __ldg(sc.texels + si.offset + i);
+}
 static __device__ __forceinline__ float4 sampler_sample(const DevScene &sc, int32_t id, float4 attr)
 {
   if (id < 0 || uint32_t(id) >= sc.sampler_count)
@@ -457,7 +469,7 @@ static __device__ __forceinline__ float4 sampler_sample(const DevScene &sc, int3
         i1[d] = i0[d];
       }
     }
-    const uint32_t sx = si.size[0], sxy = si.size[0] * si.size[1], base = si.offset;
+    const uint32_t sx = si.size[0], sxy = si.size[0] * si.size[1];
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     const int nz = dims > 2 ? 2 : 1, ny = dims > 1 ? 2 : 1;
     for (int kz = 0; kz < nz; ++kz) {
@@ -466,8 +478,8 @@ static __device__ __forceinline__ float4 sampler_sample(const DevScene &sc, int3
       for (int ky = 0; ky < ny; ++ky) {
         const float wy = dims > 1 ? (ky ? frac[1] : 1.f - frac[1]) : 1.f;
         const uint32_t y = uint32_t(ky ? i1[1] : i0[1]);
-        const float4 a = __ldg(sc.texels + base + z * sxy + y * sx + uint32_t(i0[0]));
-        const float4 b = __ldg(sc.texels + base + z * sxy + y * sx + uint32_t(i1[0]));
+        const float4 a = sampler_texel(sc, si, z * sxy + y * sx + uint32_t(i0[0]));
+        const float4 b = sampler_texel(sc, si, z * sxy + y * sx + uint32_t(i1[0]));
         acc = add4(acc, mul4(add4(mul4(a, 1.f - frac[0]), mul4(b, frac[0])), wy * wz));
       }
     }
@@ -620,9 +632,9 @@ __device__ __forceinline__ V3 mat3_mul(const float *m, V3 d)
 __device__ __forceinline__ void env_texel(const DevScene &sc, V3 dir, uint32_t &x, uint32_t &y, float &v)
 {
   const V3 nd = normalize(mat3_mul(sc.env_w2t, dir));
-  const float phi = atan2f(nd.z, nd.x);
+  const float phi = m_atan2(nd.z, nd.x);
   const float yy = fminf(fmaxf(nd.y, -1.f), 1.f);
-  const float theta = acosf(yy);
+  const float theta = m_acos(yy);
   const float u = (phi + PI) * INV_TWO_PI;
   v = theta * INV_PI;
   const float xf = u * float(sc.env_w);
@@ -645,7 +657,7 @@ __device__ __forceinline__ float env_texel_pdf(const DevScene &sc, uint32_t x, u
   const float *c = sc.env_conditional + size_t(y) * (sc.env_w + 1);
   const float col_pdf = __ldg(c + x + 1) - __ldg(c + x);
   const float theta = v * PI;
-  const float denom = TWO_PI * PI * fmaxf(sinf(theta), 1e-6f);
+  const float denom = TWO_PI * PI * fmaxf(m_sin(theta), 1e-6f);
   return (row_pdf * col_pdf) * float(sc.env_w) * float(sc.env_h) / denom;
 }
 __device__ __forceinline__ float env_pdf(const DevScene &sc, V3 dir)
@@ -679,10 +691,10 @@ static __device__ __forceinline__ V3 env_sample(const DevScene &sc, Rng &rng, fl
   const float v = (float(row) + rng.next()) / float(sc.env_h);
   const float phi = u * TWO_PI - PI;
   const float theta = v * PI;
-  const float st = sinf(theta);
-  const V3 d = mat3_mul(sc.env_t2w, V3{st * cosf(phi), cosf(theta), st * sinf(phi)});
+  const float st = m_sin(theta);
+  const V3 d = mat3_mul(sc.env_t2w, V3{st * m_cos(phi), m_cos(theta), st * m_sin(phi)});
   const float theta2 = v * PI;
-  const float denom = TWO_PI * PI * fmaxf(sinf(theta2), 1e-6f);
+  const float denom = TWO_PI * PI * fmaxf(m_sin(theta2), 1e-6f);
   pdf_out = (row_pdf * col_pdf) * float(sc.env_w) * float(sc.env_h) / denom;
   return d;
 }
@@ -712,13 +724,13 @@ static __device__ __forceinline__ LightSample sample_light(const DevLight &l, V3
   if (l.type == 1) {
     V3 wi = -normalize(dirv);
     if (l.radius > 0.f) {
-      const float cos_max = cosf(l.radius);
+      const float cos_max = m_cos(l.radius);
       const float ct = 1.f - rng.next() * (1.f - cos_max);
       const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
       const float phi = TWO_PI * rng.next();
       V3 t, b;
       onb(wi, t, b);
-      wi = normalize(t * (st * cosf(phi)) + b * (st * sinf(phi)) + wi * ct);
+      wi = normalize(t * (st * m_cos(phi)) + b * (st * m_sin(phi)) + wi * ct);
     }
     return LightSample{wi, color * l.intensity, 1.f, 1e30f};
   }
@@ -732,8 +744,8 @@ static __device__ __forceinline__ LightSample sample_light(const DevLight &l, V3
     const V3 spot_dir = normalize(dirv);
     const V3 from_light = -normalize(center_to);
     const float ca = dot(from_light, spot_dir);
-    const float ci = cosf(fmaxf(l.spot_angle - l.spot_falloff, 0.f));
-    const float co = cosf(l.spot_angle);
+    const float ci = m_cos(fmaxf(l.spot_angle - l.spot_falloff, 0.f));
+    const float co = m_cos(l.spot_angle);
     float falloff = 0.f;
     if (ca >= ci)
       falloff = 1.f;

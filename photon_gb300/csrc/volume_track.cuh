@@ -153,7 +153,7 @@ static PHC_HD_NOINLINE float vol_track(const DevScene &sc, const DevVolume &v, V
     if (bound > 0.f) {
       const float inv_bound = 1.f / bound;
       while (lookups < 8192) {
-        t -= logf(1.f - rng.next()) * inv_bound;
+        t -= m_log(1.f - rng.next()) * inv_bound;
         if (t >= t_exit)
           break;
         ++lookups;
@@ -404,7 +404,7 @@ PHC_HD void vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
       vt_next_cell<SCATTER>(sc, s);
       continue;
     }
-    s.t -= logf(1.f - rng.next()) * s.inv_bound;
+    s.t -= m_log(1.f - rng.next()) * s.inv_bound;
     if (s.t >= s.t_exit) {
       vt_next_cell<SCATTER>(sc, s);
       continue;

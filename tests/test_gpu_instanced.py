@@ -113,3 +113,43 @@ def test_instanced_full_size_renders(photon):
     assert img[..., :3].mean() > 0.0
     assert r.accumulated_samples() == 32
     r.close()
+
+
+def test_rgba8_texels_match_fp32_storage(photon):
+    """Samplers whose texels are all k / 255 are stored as 8-bit RGBA on the
+    device (tuning key texels_u8) and decoded through the table of those
+    floats: every channel of every frame is bit-identical to the same scene
+    stored as fp32 texels, and the scene takes about a quarter of the texel
+    bytes."""
+    import torch
+    from photon_gb300 import tuning_get, tuning_set
+    sc, cam, st0 = _small()
+    st = type(st0).from_buffer_copy(bytes(st0))
+    st.pixel_samples = 2
+    old = tuning_get("texels_u8")
+    out, mem = {}, {}
+    try:
+        for mode in (1, 0):
+            tuning_set("texels_u8", mode)
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
+            r = photon.Renderer()
+            r.set_scene(sc)
+            torch.cuda.synchronize()
+            mem[mode] = free0 - torch.cuda.mem_get_info()[0]
+            frames = []
+            for _ in range(2):
+                r.render(cam, st, True)
+                frames.append({ch: r.read(ch).copy() for ch in ("color", "depth", "normal", "albedo")})
+            out[mode] = frames
+            r.close()
+    finally:
+        tuning_set("texels_u8", old)
+    for f in range(2):
+        for ch in ("color", "depth", "normal", "albedo"):
+            a, b = out[1][f][ch], out[0][f][ch]
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (f, ch)
+    texel_bytes = sum(len(t) * 16 for _, t in sc.samplers)
+    print(f"scene device memory: {mem[1] / 2**20:.1f} MiB with 8-bit texels, {mem[0] / 2**20:.1f} MiB fp32 "
+          f"({texel_bytes / 2**20:.1f} MiB of fp32 texels)")
+    assert mem[0] - mem[1] >= 0.6 * texel_bytes
