@@ -342,6 +342,21 @@ int phc_read_normal(phc_renderer *r, float *xyz);
 int phc_read_albedo(phc_renderer *r, float *rgb);
 /* Counters of the last phc_render call. */
 int phc_render_stats_get(const phc_renderer *r, phc_render_stats *out);
+/* Scene tables the sampling reads, as built on the device at phc_set_scene
+   (no reference counterpart; for checking them against the host builders of
+   the same tables): the volumes' macro-cell majorant grids, the environment
+   map's marginal and conditional CDFs, the emissive triangles' selection CDF
+   and the per-primitive light pdf.  *count receives the table's length in
+   floats; its floats are copied to host_out when host_out is not NULL and
+   capacity (floats) holds them, else PHC_ERR_LIMIT. */
+enum {
+  PHC_TABLE_MAJORANTS = 0,
+  PHC_TABLE_ENV_MARGINAL = 1,
+  PHC_TABLE_ENV_CONDITIONAL = 2,
+  PHC_TABLE_EMISSIVE_CDF = 3,
+  PHC_TABLE_PRIM_LIGHT_PDF = 4
+};
+int phc_scene_table(const phc_renderer *r, int32_t table, float *host_out, uint64_t capacity, uint64_t *count);
 
 /* One render call of a batch: the arguments of phc_render. */
 typedef struct phc_job {
@@ -367,9 +382,12 @@ const char *phc_last_error(const phc_renderer *r);
    bridge's perceptual roughness; GGX alpha = roughness^2), metallic,
    specTrans (transmission), sheen, clearcoat.  Per volume: density scale,
    albedo r, g, b (the transfer function's colour, taken as constant over the
-   volume).  Per texel: r, g, b, 0, for the texels of every sampler in the
-   order of phc_scene_desc::samplers (sampler i's texels follow those of
-   samplers 0..i-1). */
+   volume).  Per texel: the gradient of each of its four channels (r, g, b,
+   a), for the texels of every sampler in the order of
+   phc_scene_desc::samplers (sampler i's texels follow those of samplers
+   0..i-1); a texel collects the gradient of every parameter its sampler
+   feeds (base colour through channels r, g, b of the sampler's output;
+   roughness, metallic and specTrans through output channel r). */
 #define PHC_ADJ_MATERIAL_PARAMS 8
 #define PHC_ADJ_VOLUME_PARAMS 4
 #define PHC_ADJ_MAX_VOLUMES 4
@@ -395,7 +413,9 @@ typedef struct phc_adjoint_grads {
    selection, Russian roulette, MIS weights, clamps and stochastic
    transparency are held constant; visibility (edge) derivatives are not
    computed.  Parameters that come from attributes get no gradient; a base
-   colour from an image sampler sends its gradient to the texels.  Leaves
+   colour, roughness, metallic or specTrans read from an image sampler sends
+   its gradient to that sampler's texels (through the sampler's output
+   transform and the clamps of the material resolution).  Leaves
    the accumulated frame and the sample counter unchanged.  Every output
    buffer is host memory and is overwritten.  Volume gradients need
    volume_count <= PHC_ADJ_MAX_VOLUMES (else PHC_ERR_LIMIT). */

@@ -1,7 +1,8 @@
 // Path-replay adjoint (no reference counterpart: the reference has no
 // derivatives).  Gradients of an image loss with respect to the Disney
 // parameters of the materials (base colour, roughness, metallic, specTrans,
-// sheen, clearcoat), the base-colour texels of sampler textures, and the
+// sheen, clearcoat), the texels of the image samplers those parameters are
+// read from (base colour, roughness, metallic, specTrans), and the
 // extinction scale and albedo of homogeneous volumes.
 //
 // Path replay backpropagation (Vicini, Speierer and Jakob, "Path Replay
@@ -35,9 +36,9 @@
 //
 // Material gradients gather in a per-thread cache of the current material,
 // then in block shared memory, then one global atomic per block and
-// parameter; volume gradients in shared memory; texel gradients go straight
-// to global memory with atomics (taps of neighbouring pixels rarely coincide
-// within a warp).
+// parameter; volume gradients in shared memory; texel gradients go to
+// global memory with warp-aggregated atomics (lanes adding to the same texel
+// channel combine first, warp_add).
 #include "adjoint.h"
 #include "dual.cuh"
 #include "wave_common.cuh"
@@ -339,77 +340,109 @@ __device__ __forceinline__ void add_mat(Grads &g, uint32_t m, const float *gp, u
       g.cache[k] += gp[k];
 }
 
-// Base-colour texture taps at a hit: texel indices, weights and the chain
-// factor d base_i / d acc_j (out transform, clamp at 0) of sampler_sample.
-struct Taps {
-  int n;
+// Adds v to *p, the lanes of the warp that add to the same address at this
+// call first combined (one atomic per distinct address instead of one per
+// lane: neighbouring paths read the same texels).  Every lane converged here
+// calls it; `on` says whether it has a value.
+__device__ __forceinline__ void warp_add(float *p, float v, bool on, unsigned act)
+{
+  const unsigned long long key = on ? reinterpret_cast<unsigned long long>(p) : 0ull;
+  const unsigned grp = __match_any_sync(act, key);
+  float sum = 0.f;
+  for (unsigned m = grp; m; m &= m - 1u)
+    sum += __shfl_sync(grp, v, __ffs(int(m)) - 1);
+  if (on && lane_id() == uint32_t(__ffs(int(grp)) - 1) && sum != 0.f && sum == sum)
+    atomicAdd(p, sum);
+}
+
+// Texel gradients of one parameter source read from an image sampler at a
+// hit: the sampler's taps (texels and bilinear / trilinear weights, as
+// sampler_sample reads them) times the chain factor d param_c / d acc_j of
+// resolve_material (the out transform, then max(., 0) for the base colour,
+// the clamp to [0, 1] for roughness / metallic / specTrans) times the
+// parameter gradients gpc[c] (three channels for the base colour, one for
+// the scalars).  No-op for lanes without such a source (has = false); all
+// lanes of `act` call it.
+__device__ void scatter_source(float4 *texels, const DevScene &sc, bool has, int32_t id, int nch, const Query &q,
+    const float *gpc, unsigned act)
+{
+  int n = 0;
   uint32_t idx[8];
   float w[8];
-  float dbase[3][4];
-};
-__device__ Taps base_color_taps(const DevScene &sc, const DevMaterial &dm, const Query &q)
-{
-  Taps t;
-  t.n = 0;
-  if (dm.src_kind[SRC_BASE] != 2)
-    return t;
-  const int32_t id = dm.src_index[SRC_BASE];
-  if (id < 0 || uint32_t(id) >= sc.sampler_count)
-    return t;
-  const DevSampler &si = sc.samplers[uint32_t(id)];
-  if (si.type == 3)
-    return t;
-  const float4 attr = fetch_attribute(sc, si.in_attribute, q);
-  float4 c = mat4_mul(si.in_t, attr);
-  c.x += si.in_o[0];
-  c.y += si.in_o[1];
-  c.z += si.in_o[2];
-  const int dims = si.type == 0 ? 1 : (si.type == 1 ? 2 : 3);
-  const float coord[3] = {c.x, c.y, c.z};
-  int32_t i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0};
-  float fr[3] = {0.f, 0.f, 0.f};
-  for (int d = 0; d < dims; ++d) {
-    const int32_t n = int32_t(si.size[d]);
-    float x = coord[d];
-    if (!(x > -1e6f && x < 1e6f))
-      x = 0.f;
-    if (si.linear) {
-      const float f = x * float(n) - 0.5f;
-      const float fl = floorf(f);
-      fr[d] = f - fl;
-      i0[d] = wrap_index(int32_t(fl), n, si.wrap[d]);
-      i1[d] = wrap_index(int32_t(fl) + 1, n, si.wrap[d]);
-    } else {
-      i0[d] = wrap_index(int32_t(floorf(x * float(n))), n, si.wrap[d]);
-      i1[d] = i0[d];
-    }
-  }
-  const uint32_t sx = si.size[0], sxy = si.size[0] * si.size[1];
-  const int nz = dims > 2 ? 2 : 1, ny = dims > 1 ? 2 : 1;
-  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int kz = 0; kz < nz; ++kz) {
-    const float wz = dims > 2 ? (kz ? fr[2] : 1.f - fr[2]) : 1.f;
-    const uint32_t z = uint32_t(kz ? i1[2] : i0[2]);
-    for (int ky = 0; ky < ny; ++ky) {
-      const float wy = dims > 1 ? (ky ? fr[1] : 1.f - fr[1]) : 1.f;
-      const uint32_t y = uint32_t(ky ? i1[1] : i0[1]);
-      for (int kx = 0; kx < 2; ++kx) {
-        const uint32_t x = uint32_t(kx ? i1[0] : i0[0]);
-        const float w = (kx ? fr[0] : 1.f - fr[0]) * (wy * wz);
-        const uint32_t ti = z * sxy + y * sx + x;
-        t.idx[t.n] = si.grad_offset + ti;
-        t.w[t.n] = w;
-        ++t.n;
-        acc = add4(acc, mul4(sampler_texel(sc, si, ti), w));
+  float chain[3][4];
+  for (int c = 0; c < 3; ++c)
+    for (int j = 0; j < 4; ++j)
+      chain[c][j] = 0.f;
+  const DevSampler *sp = nullptr;
+  if (has && id >= 0 && uint32_t(id) < sc.sampler_count && sc.samplers[uint32_t(id)].type != 3)
+    sp = sc.samplers + uint32_t(id);
+  if (sp) {
+    const DevSampler &si = *sp;
+    const float4 attr = fetch_attribute(sc, si.in_attribute, q);
+    float4 c = mat4_mul(si.in_t, attr);
+    c.x += si.in_o[0];
+    c.y += si.in_o[1];
+    c.z += si.in_o[2];
+    const int dims = si.type == 0 ? 1 : (si.type == 1 ? 2 : 3);
+    const float coord[3] = {c.x, c.y, c.z};
+    int32_t i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0};
+    float fr[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < dims; ++d) {
+      const int32_t nn = int32_t(si.size[d]);
+      float x = coord[d];
+      if (!(x > -1e6f && x < 1e6f))
+        x = 0.f;
+      if (si.linear) {
+        const float f = x * float(nn) - 0.5f;
+        const float fl = floorf(f);
+        fr[d] = f - fl;
+        i0[d] = wrap_index(int32_t(fl), nn, si.wrap[d]);
+        i1[d] = wrap_index(int32_t(fl) + 1, nn, si.wrap[d]);
+      } else {
+        i0[d] = wrap_index(int32_t(floorf(x * float(nn))), nn, si.wrap[d]);
+        i1[d] = i0[d];
       }
     }
+    const uint32_t sx = si.size[0], sxy = si.size[0] * si.size[1];
+    const int nz = dims > 2 ? 2 : 1, ny = dims > 1 ? 2 : 1;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int kz = 0; kz < nz; ++kz) {
+      const float wz = dims > 2 ? (kz ? fr[2] : 1.f - fr[2]) : 1.f;
+      const uint32_t z = uint32_t(kz ? i1[2] : i0[2]);
+      for (int ky = 0; ky < ny; ++ky) {
+        const float wy = dims > 1 ? (ky ? fr[1] : 1.f - fr[1]) : 1.f;
+        const uint32_t y = uint32_t(ky ? i1[1] : i0[1]);
+        for (int kx = 0; kx < 2; ++kx) {
+          const uint32_t x = uint32_t(kx ? i1[0] : i0[0]);
+          const float wt = (kx ? fr[0] : 1.f - fr[0]) * (wy * wz);
+          const uint32_t ti = z * sxy + y * sx + x;
+          idx[n] = si.grad_offset + ti;
+          w[n] = wt;
+          ++n;
+          acc = add4(acc, mul4(sampler_texel(sc, si, ti), wt));
+        }
+      }
+    }
+    const float4 out = mat4_mul(si.out_t, acc);
+    const float o[3] = {out.x + si.out_o[0], out.y + si.out_o[1], out.z + si.out_o[2]};
+    for (int cc = 0; cc < nch; ++cc) {
+      // base colour: max(o, 0); scalars: clamp01(o) (roughness: the
+      // perceptual value, which the adjoint's gradient is taken against)
+      const bool live = nch == 3 ? o[cc] > 0.f : (o[cc] > 0.f && o[cc] < 1.f);
+      for (int j = 0; j < 4; ++j)
+        chain[cc][j] = live ? si.out_t[4 * cc + j] * gpc[cc] : 0.f;
+    }
   }
-  const float4 out = mat4_mul(si.out_t, acc);
-  const float o[3] = {out.x + si.out_o[0], out.y + si.out_o[1], out.z + si.out_o[2]};
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 4; ++j)
-      t.dbase[i][j] = o[i] > 0.f ? si.out_t[4 * i + j] : 0.f;
-  return t;
+  // the warp's lanes walk the taps together; lanes with fewer (or none) add nothing
+  __syncwarp(act);
+  const int n_max = int(__reduce_max_sync(act, uint32_t(n)));
+  for (int t = 0; t < n_max; ++t) {
+    float *tp = reinterpret_cast<float *>(texels + (t < n ? idx[t] : 0u));
+    for (int j = 0; j < 4; ++j) {
+      const float v = t < n ? w[t] * (chain[0][j] + chain[1][j] + chain[2][j]) : 0.f;
+      warp_add(tp + j, v, t < n && v != 0.f && v == v, act);
+    }
+  }
 }
 
 // gp += sum_c k_c * (d f_c / d theta) / f_c
@@ -438,26 +471,38 @@ __device__ __forceinline__ void add_dlog(const D &x, float K, float *gp)
     gp[p] += s * x.d[p];
 }
 
-// Scatters a vertex's parameter gradient gp into its material (constant
-// parameters) and, for a base colour read from an image, its texels.
-__device__ void scatter_grads(Grads &g, const DevMaterial &dm, uint32_t mat_id, const Taps &taps, const float *gp)
+// Scatters a vertex's parameter gradient gp into its material (the
+// parameters it takes as constants) and, for parameters read from image
+// samplers (base colour, roughness, metallic, specTrans), into their texels.
+// All lanes converged here call it (the texel scatter is warp-cooperative).
+__device__ void scatter_grads(Grads &g, const DevScene &sc, const DevMaterial &dm, uint32_t mat_id, const Query &q,
+    const float *gp, bool on = true)
 {
   const int src_of[NP] = {SRC_BASE, SRC_BASE, SRC_BASE, SRC_ROUGH, SRC_METAL, SRC_TRANS, -1, -1};
-  uint32_t allowed = 0;
+  if (on) {
+    uint32_t allowed = 0;
 #pragma unroll
-  for (int p = 0; p < NP; ++p)
-    if (src_of[p] < 0 || dm.src_kind[src_of[p]] == 0)
-      allowed |= 1u << p;
-  add_mat(g, mat_id, gp, allowed);
-  if (taps.n > 0 && g.texels) {
-    for (int t = 0; t < taps.n; ++t) {
-      float *tp = reinterpret_cast<float *>(g.texels + taps.idx[t]);
-      for (int j = 0; j < 3; ++j) {
-        const float v = taps.w[t] * (gp[0] * taps.dbase[0][j] + gp[1] * taps.dbase[1][j] + gp[2] * taps.dbase[2][j]);
-        if (v != 0.f && v == v)
-          atomicAdd(tp + j, v);
-      }
-    }
+    for (int p = 0; p < NP; ++p)
+      if (src_of[p] < 0 || dm.src_kind[src_of[p]] == 0)
+        allowed |= 1u << p;
+    add_mat(g, mat_id, gp, allowed);
+  }
+  if (!g.texels)
+    return;
+  const unsigned act = __activemask();
+  const bool any_src = on && (dm.src_kind[SRC_BASE] == 2 || dm.src_kind[SRC_ROUGH] == 2 ||
+      dm.src_kind[SRC_METAL] == 2 || dm.src_kind[SRC_TRANS] == 2);
+  if (!__any_sync(act, any_src))
+    return;
+  const float gb[3] = {gp[0], gp[1], gp[2]};
+  scatter_source(g.texels, sc, on && dm.src_kind[SRC_BASE] == 2, dm.src_index[SRC_BASE], 3, q, gb, act);
+  const int scalars[3] = {SRC_ROUGH, SRC_METAL, SRC_TRANS};
+  for (int k = 0; k < 3; ++k) {
+    const bool has = on && dm.src_kind[scalars[k]] == 2;
+    if (!__any_sync(act, has))
+      continue;
+    const float gs[3] = {gp[3 + k], 0.f, 0.f};
+    scatter_source(g.texels, sc, has, dm.src_index[scalars[k]], 1, q, gs, act);
   }
 }
 
@@ -656,21 +701,19 @@ __device__ __forceinline__ void put_vtx(const VtxSoA &v, uint32_t i, const Query
   v.p[i] = f4(q.p, 0.f);
   v.sn[i] = f4(q.sn, 0.f);
 }
-// The material and base-colour taps of a stored vertex; false: none stored.
-__device__ bool get_vtx(const DevScene &sc, const VtxSoA &v, uint32_t i, uint32_t &mat, Taps &taps)
+// The material and hit query of a stored vertex; false: none stored.
+__device__ bool get_vtx(const DevScene &sc, const VtxSoA &v, uint32_t i, uint32_t &mat, Query &q)
 {
   const uint4 q4 = v.q[i];
   if (!(q4.w & ADJ_VTX_VALID))
     return false;
   mat = q4.w & ~ADJ_VTX_VALID;
-  Query q;
   q.prim = q4.x;
   q.vidx = __ldg(sc.prim_vidx + q4.x);
   q.b1 = __uint_as_float(q4.y);
   q.b2 = __uint_as_float(q4.z);
   q.p = v3(v.p[i]);
   q.sn = v3(v.sn[i]);
-  taps = base_color_taps(sc, sc.materials[mat], q);
   return true;
 }
 
@@ -685,12 +728,12 @@ __device__ void mis_prev(Grads &g, const DevScene &sc, const AdjPathSoA &in, uin
   if (K == 0.f)
     return;
   uint32_t mat;
-  Taps taps;
-  if (!get_vtx(sc, in.v, i, mat, taps))
+  Query q;
+  if (!get_vtx(sc, in.v, i, mat, q))
     return;
   const float4 a = in.g0[i], b = in.g1[i];
   const float gp[NP] = {K * a.x, K * a.y, K * a.z, K * a.w, K * b.x, K * b.y, K * b.z, K * b.w};
-  scatter_grads(g, sc.materials[mat], mat, taps, gp);
+  scatter_grads(g, sc, sc.materials[mat], mat, q, gp);
 }
 
 // What one replayed path hands on: its continuation and its shadow ray.
@@ -917,7 +960,6 @@ __device__ __forceinline__ void adj_shade_path(const RenderConst &rc, const DevS
     return;
   }
   const MatD md = make_matd(mat);
-  const Taps taps = base_color_taps(sc, dm, q);
   float gnee[NP];
 #pragma unroll
   for (int k = 0; k < NP; ++k)
@@ -999,7 +1041,7 @@ __device__ __forceinline__ void adj_shade_path(const RenderConst &rc, const DevS
         add_dlog(dh, Kc, gc);
       }
     }
-    scatter_grads(g, dm, ha.material_id, taps, grem);
+    scatter_grads(g, sc, dm, ha.material_id, q, grem);
   }
   if (has_sh) { // per unit transmittance: the NEE gradient minus the part the sample's term took
     sh.g0 = make_float4(gnee[0] - gc[0], gnee[1] - gc[1], gnee[2] - gc[2], gnee[3] - gc[3]);
@@ -1150,11 +1192,11 @@ __global__ void __launch_bounds__(128) k_adj_resolve(const RenderConst *__restri
     const V3 delta{dI.x * a.inv_spp, dI.y * a.inv_spp, dI.z * a.inv_spp};
     add_vol(g, dlt, sc.volume_count, dot(delta, c));
     uint32_t mat;
-    Taps taps;
-    if (get_vtx(sc, sh.v, i, mat, taps)) {
+    Query q;
+    if (get_vtx(sc, sh.v, i, mat, q)) {
       const float4 u = sh.g0[i], w = sh.g1[i];
       const float gp[NP] = {T * u.x, T * u.y, T * u.z, T * u.w, T * w.x, T * w.y, T * w.z, T * w.w};
-      scatter_grads(g, sc.materials[mat], mat, taps, gp);
+      scatter_grads(g, sc, sc.materials[mat], mat, q, gp);
     }
   }
   end_grads(g, sc, a);

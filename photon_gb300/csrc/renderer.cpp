@@ -1338,6 +1338,31 @@ int phc_render_stats_get(const phc_renderer *r, phc_render_stats *out)
   return PHC_OK;
 }
 
+int phc_scene_table(const phc_renderer *r, int32_t table, float *host_out, uint64_t capacity, uint64_t *count)
+{
+  if (!r || !count)
+    return set_error(nullptr, PHC_ERR_INVALID, "null argument");
+  if (table < PHC_TABLE_MAJORANTS || table > PHC_TABLE_PRIM_LIGHT_PDF)
+    return set_error(nullptr, PHC_ERR_INVALID, "unknown scene table " + std::to_string(table));
+  if (!r->has_scene)
+    return set_error(nullptr, PHC_ERR_NO_SCENE, "no scene");
+  const DevScene &d = r->scene.dev;
+  const float *src[5] = {d.vol_majorants, d.env_marginal, d.env_conditional, d.emissive_cdf, d.prim_light_pdf};
+  const uint64_t n = r->scene.table_floats[table];
+  *count = n;
+  if (!host_out || n == 0)
+    return PHC_OK;
+  if (capacity < n)
+    return set_error(nullptr, PHC_ERR_LIMIT, "scene table: " + std::to_string(n) + " floats, capacity " +
+        std::to_string(capacity));
+  cudaError_t e = cudaSetDevice(r->device);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(host_out, src[table], n * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess)
+    return set_error(nullptr, PHC_ERR_CUDA, std::string("scene table: ") + cudaGetErrorString(e));
+  return PHC_OK;
+}
+
 const char *phc_last_error(const phc_renderer *r) { return r ? r->error.c_str() : g_error.c_str(); }
 
 } // extern "C"

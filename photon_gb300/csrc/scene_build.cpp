@@ -6,6 +6,7 @@
 // identical CDFs, majorants and light densities, then uploaded to HBM.
 #include "scene_build.h"
 #include "bvh_gpu.h"
+#include "scene_tables.cuh"
 #include "tuning.h"
 
 #include <algorithm>
@@ -323,76 +324,38 @@ void build_volumes(const phc_scene_desc &in, HostScene &s)
       for (int d = 0; d < 3; ++d)
         if (sub[d] > 0)
           v.macro_dims[d] = std::min<uint32_t>(std::max<uint32_t>((v.dims[d] + 2) / 4, 1), 128);
-    const float *vals = vd.values;
-    auto node = [&](uint32_t x, uint32_t y, uint32_t z) {
-      x = std::min(x, v.dims[0] - 1);
-      y = std::min(y, v.dims[1] - 1);
-      z = std::min(z, v.dims[2] - 1);
-      return vals[(size_t(z) * v.dims[1] + y) * v.dims[0] + x];
-    };
-    auto interp = [&](float gx, float gy, float gz) {
-      const uint32_t x = uint32_t(gx), y = uint32_t(gy), z = uint32_t(gz);
-      const float fx = gx - float(x), fy = gy - float(y), fz = gz - float(z);
-      const float c00 = node(x, y, z) * (1.f - fx) + node(x + 1, y, z) * fx;
-      const float c10 = node(x, y + 1, z) * (1.f - fx) + node(x + 1, y + 1, z) * fx;
-      const float c01 = node(x, y, z + 1) * (1.f - fx) + node(x + 1, y, z + 1) * fx;
-      const float c11 = node(x, y + 1, z + 1) * (1.f - fx) + node(x + 1, y + 1, z + 1) * fx;
-      return (c00 * (1.f - fy) + c10 * fy) * (1.f - fz) + (c01 * (1.f - fy) + c11 * fy) * fz;
-    };
+    MajorantJob job{};
+    for (int d = 0; d < 3; ++d) {
+      job.dims[d] = v.dims[d];
+      job.macro_dims[d] = v.macro_dims[d];
+      job.sub[d] = sub[d];
+    }
+    job.refined = refined ? 1u : 0u;
+    job.complete = complete ? 1u : 0u;
+    job.table = uint32_t(table);
+    job.value_lo = vd.value_range[0];
+    job.range = range;
+    job.density_scale = vd.density_scale;
+    job.max_opacity = max_opacity;
     const size_t cells_total = size_t(v.macro_dims[0]) * v.macro_dims[1] * v.macro_dims[2];
     const size_t base = s.vol_majorants.size();
     s.vol_majorants.resize(base + cells_total);
+    if (tuning().gpu_tables && nvals) { // computed on the device from the uploaded field (upload)
+      s.majorant_tasks.push_back({job, uint32_t(base), uint32_t(value_offset), uint32_t(tf_offset)});
+    } else {
+      const float *vals = vd.values;
+      const float *tf = vd.transfer;
+      auto alpha = [&](size_t t) { return tf[4 * t + 3]; };
 #pragma omp parallel for schedule(dynamic, 1)
-    for (int64_t mz = 0; mz < int64_t(v.macro_dims[2]); ++mz)
-      for (uint32_t my = 0; my < v.macro_dims[1]; ++my)
-        for (uint32_t mx = 0; mx < v.macro_dims[0]; ++mx) {
-          float bound = 0.f;
-          if (complete && table > 0) {
-            const uint32_t m[3] = {mx, my, uint32_t(mz)};
-            float vmin = std::numeric_limits<float>::max(), vmax = -std::numeric_limits<float>::max();
-            if (refined) {
-              for (int corner = 0; corner < 8; ++corner) {
-                float g[3];
-                for (int d = 0; d < 3; ++d)
-                  g[d] = float(m[d] + ((corner >> d) & 1)) / float(sub[d]);
-                const float value = interp(g[0], g[1], g[2]);
-                vmin = std::min(vmin, value);
-                vmax = std::max(vmax, value);
-              }
-            } else {
-              uint32_t first[3], last[3];
-              for (int d = 0; d < 3; ++d) {
-                const float cells = float(v.dims[d] > 1 ? v.dims[d] - 1 : 1);
-                const float lo = float(m[d]) / float(v.macro_dims[d]) * cells;
-                const float hi = float(m[d] + 1) / float(v.macro_dims[d]) * cells;
-                first[d] = uint32_t(std::max(std::floor(lo) - 1.f, 0.f));
-                last[d] = std::min<uint32_t>(uint32_t(std::ceil(hi)) + 1, v.dims[d] - 1);
-              }
-              for (uint32_t z = first[2]; z <= last[2]; ++z)
-                for (uint32_t y = first[1]; y <= last[1]; ++y)
-                  for (uint32_t x = first[0]; x <= last[0]; ++x) {
-                    const float value = vals[(size_t(z) * v.dims[1] + y) * v.dims[0] + x];
-                    vmin = std::min(vmin, value);
-                    vmax = std::max(vmax, value);
-                  }
-            }
-            auto tpos = [&](float value) {
-              float x = range != 0.f ? (value - vd.value_range[0]) / range : 0.f;
-              x = std::min(std::max(x, 0.f), 1.f);
-              return x * float(table - 1);
-            };
-            const size_t i0 = size_t(std::floor(tpos(vmin)));
-            const size_t i1 = std::min(size_t(std::ceil(tpos(vmax))), table - 1);
-            for (size_t t = i0; t <= i1; ++t)
-              bound = std::max(bound, vd.transfer[4 * t + 3]);
-            if (!(vmin <= vmax))
-              bound = max_opacity;
+      for (int64_t mz = 0; mz < int64_t(v.macro_dims[2]); ++mz)
+        for (uint32_t my = 0; my < v.macro_dims[1]; ++my)
+          for (uint32_t mx = 0; mx < v.macro_dims[0]; ++mx) {
+            const size_t cell = (size_t(mz) * v.macro_dims[1] + my) * v.macro_dims[0] + mx;
+            s.vol_majorants[base + cell] = majorant_cell(job, vals, alpha, mx, my, uint32_t(mz));
           }
-          const size_t cell = (size_t(mz) * v.macro_dims[1] + my) * v.macro_dims[0] + mx;
-          s.vol_majorants[base + cell] = bound * vd.density_scale * 1.01f;
-        }
+    }
     if (nvals)
-      s.vol_value_spans.push_back({vals, nvals}); // copied to the device from the caller's array
+      s.vol_value_spans.push_back({vd.values, nvals}); // copied to the device from the caller's array
     value_offset += nvals;
     tf_offset += table;
     s.volumes.push_back(v);
@@ -1009,7 +972,12 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   d.volume_count = uint32_t(h.volumes.size());
   d.vol_values = put_spans(h.vol_values, h.vol_value_spans, s, err);
   d.vol_tf = reinterpret_cast<const float4 *>(put(h.vol_tf, s, err));
-  d.vol_majorants = put(h.vol_majorants, s, err);
+  float *majorants = put(h.vol_majorants, s, err);
+  d.vol_majorants = majorants;
+  for (const HostScene::MajorantTask &t : h.majorant_tasks)
+    if (err.empty())
+      err = launch_majorants(t.job, d.vol_values + t.data_offset, d.vol_tf + t.tf_offset,
+          majorants + t.macro_offset, s);
   d.strategy_count = h.strategy_count;
   d.eps = h.eps;
   d.inst_w2o = reinterpret_cast<const float4 *>(put(h.inst_w2o, s, err));
@@ -1033,6 +1001,11 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   tri_bytes = uint64_t(h.bvh.tris.size()) * 4;
   bvh_depth = h.bvh.max_depth;
   texel_count = h.texel_logical_count;
+  table_floats[PHC_TABLE_MAJORANTS] = h.vol_majorants.size();
+  table_floats[PHC_TABLE_ENV_MARGINAL] = h.env_marginal.size();
+  table_floats[PHC_TABLE_ENV_CONDITIONAL] = h.env_conditional.size();
+  table_floats[PHC_TABLE_EMISSIVE_CDF] = h.emissive_cdf.size();
+  table_floats[PHC_TABLE_PRIM_LIGHT_PDF] = h.prim_light_pdf.size();
   if (!err.empty()) {
     release();
     return err;

@@ -10,6 +10,7 @@
 #include "../../include/photon_cuda.h"
 #include "bvh8.h"
 #include "scene_types.h"
+#include "scene_tables.cuh"
 
 namespace phc {
 
@@ -55,6 +56,14 @@ struct HostScene {
   std::vector<uint32_t> emissive_guide, env_mguide, env_cguide;
   float env_w2t[9]{1, 0, 0, 0, 1, 0, 0, 0, 1}, env_t2w[9]{1, 0, 0, 0, 1, 0, 0, 0, 1};
   std::vector<DevVolume> volumes;
+  // majorant grids the upload computes on the device (tuning key gpu_tables):
+  // the grid's parameters and its offsets in vol_majorants / vol_values /
+  // vol_tf (transfer-function entries)
+  struct MajorantTask {
+    MajorantJob job;
+    uint32_t macro_offset, data_offset, tf_offset;
+  };
+  std::vector<MajorantTask> majorant_tasks;
   std::vector<float> vol_values, vol_tf, vol_majorants;
   uint32_t strategy_count{0};
   float eps{1e-3f};
@@ -80,6 +89,7 @@ struct DeviceScene {
   uint64_t node_bytes{0}, tri_bytes{0};
   uint64_t texel_count{0};
   uint32_t bvh_depth{0};
+  uint64_t table_floats[5]{}; // lengths of the tables phc_scene_table reads (PHC_TABLE_*)
   ~DeviceScene();
   void release();
   // Returns an empty string on success, else the failure message.
@@ -90,5 +100,10 @@ private:
   float *put_spans(const std::vector<float> &owned, const std::vector<HostScene::Span> &spans, cudaStream_t s,
       std::string &err);
 };
+
+// Launches the majorant grid of one volume on the device (scene_tables.cu);
+// returns an empty string on success, else the failure message.
+std::string launch_majorants(const MajorantJob &job, const float *vals, const float4 *tf, float *out,
+    cudaStream_t stream);
 
 } // namespace phc

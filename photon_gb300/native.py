@@ -37,6 +37,7 @@ SIGNATURES = {
     "phc_read_normal": (C.c_int, [vp, vp]),
     "phc_read_albedo": (C.c_int, [vp, vp]),
     "phc_render_stats_get": (C.c_int, [vp, vp]),
+    "phc_scene_table": (C.c_int, [vp, C.c_int32, vp, C.c_uint64, C.POINTER(C.c_uint64)]),
     "phc_render_batch": (C.c_int, [vp, C.c_uint32, vp]),
     "phc_last_error": (C.c_char_p, [vp]),
     "phc_adjoint": (C.c_int, [vp, vp, vp, C.c_uint32, vp, vp]),

@@ -127,6 +127,19 @@ class Renderer:
             out["color"] = img
         return out
 
+    TABLES = {"majorants": 0, "env_marginal": 1, "env_conditional": 2, "emissive_cdf": 3, "prim_light_pdf": 4}
+
+    def scene_table(self, name: str):
+        """One of the scene's device tables (phc_scene_table) as a float32 array."""
+        import numpy as np
+        which = self.TABLES[name]
+        n = C.c_uint64(0)
+        self._check(self.lib.phc_scene_table(self.h, which, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.float32)
+        if n.value:
+            self._check(self.lib.phc_scene_table(self.h, which, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
     def stats(self) -> dict:
         s = _abi.RenderStats()
         self._check(self.lib.phc_render_stats_get(self.h, C.byref(s)))

@@ -349,15 +349,17 @@ DIFF_MATERIALS = 8
 DIFF_TEXTURE = 512
 
 
-def differentiable(seed=0, res=256, spp=64, depth=6, texture=DIFF_TEXTURE, target=False):
+def differentiable(seed=0, res=256, spp=64, depth=6, texture=DIFF_TEXTURE, target=False, param_textures=False):
     """Differentiable workload: ~50K triangles of displaced icospheres and tori
     on a ground plane, 8 materials whose base colour is a texture x texture
     fp32 value-noise image (sampler i for material i, uv in attribute 0) with
     scalar roughness / metallic / specTrans / sheen / clearcoat, a soft sky
     environment and a homogeneous box medium (constant transfer function of
     albedo 0.8, density scale 0.5).  target=True gives the perturbed
-    parameters a reference image is rendered from.  Returns
-    (SceneData, camera, settings)."""
+    parameters a reference image is rendered from.  param_textures=True
+    also reads roughness (materials 0-3), metallic (4-6) and specTrans (7)
+    from texture x texture value-noise images (channel r; samplers 8-15).
+    Returns (SceneData, camera, settings)."""
     rng = np.random.default_rng(seed)
     mb = _MeshBuilder()
     uvs = []
@@ -440,6 +442,23 @@ def differentiable(seed=0, res=256, spp=64, depth=6, texture=DIFF_TEXTURE, targe
         vol.density_scale = 0.5 * float(trng.uniform(0.8, 1.2))
         albedo = np.clip(albedo * trng.uniform(0.9, 1.1, 3), 0, 1).astype(np.float32)
     tf = np.array([list(albedo) + [1.0], list(albedo) + [1.0]], np.float32)
+    if param_textures:
+        xrng = np.random.default_rng(seed + 13)
+        for i, m in enumerate(mats):
+            field, lo, hi = (("roughness_src", 0.25, 0.85) if i < 4 else
+                             ("metallic_src", 0.05, 0.5) if i < 7 else ("transmission_src", 0.05, 0.3))
+            tex = np.zeros((texture, texture, 4), np.float32)
+            tex[..., 0] = lo + (hi - lo) * value_noise(xrng, texture)[..., 0]
+            tex[..., 3] = 1.0
+            s = _abi.sampler_default()
+            s.type = 1
+            s.in_attribute = 0
+            s.linear = 1
+            s.wrap[:] = (1, 1, 0)
+            s.size[:] = (texture, texture, 1)
+            src = getattr(m, field)
+            src.kind, src.index = 2, len(samplers)
+            samplers.append((s, tex.reshape(-1, 4)))
     sc.materials = mats
     sc.samplers = samplers
     sc.volumes = [(vol, np.ones(8, np.float32), tf)]

@@ -62,6 +62,11 @@ GpuBvh8 build_bvh8_gpu(const float4 *, const uint4 *, uint32_t, cudaStream_t)
 {
   throw std::runtime_error("the host harness builds no BVH on the GPU");
 }
+// Likewise the GPU majorant grid (scene_tables.cu).
+std::string launch_majorants(const MajorantJob &, const float *, const float4 *, float *, cudaStream_t)
+{
+  return "the host harness builds no tables on the GPU";
+}
 } // namespace phc
 
 extern "C" int ht_trace_instanced(const phc_scene_desc *desc, const float *orgs, const float *dirs,

@@ -55,9 +55,9 @@ def _adjoint(photon, sc, cam, st, wt, **kw):
     return g
 
 
-def _diff_small(res=40, spp=8, texture=64):
+def _diff_small(res=40, spp=8, texture=64, param_textures=False):
     from photon_gb300 import workloads
-    return workloads.differentiable(res=res, spp=spp, depth=6, texture=texture)
+    return workloads.differentiable(res=res, spp=spp, depth=6, texture=texture, param_textures=param_textures)
 
 
 def test_primal_pass_is_the_render(photon):
@@ -184,13 +184,44 @@ def test_fd_texel_directions(photon):
     assert np.all(np.abs(adj - fd) <= FD_REL_TOL * np.abs(fd) + 1e-6), (adj, fd)
 
 
-def test_gpu_adjoint_matches_fp64_cpu_adjoint(photon, oracle_lib):
+def test_fd_parameter_texture_directions(photon):
+    """Texel gradients of roughness (materials 0-3), metallic (4-6) and
+    specTrans (7) read from textures, along a uniform raise of a whole
+    texture's r channel (the channel those parameters read)."""
+    sc, cam, st = _diff_small(res=32, spp=4096, param_textures=True)
+    wt = _weights(st.height, st.width)
+    g = _adjoint(photon, sc, cam, st, wt)["texels"]
+    h = 1e-2
+    counts = [t.shape[0] for _, t in sc.samplers]
+    offs = np.concatenate([[0], np.cumsum(counts)])
+    adj, fd = [], []
+    for i in (8, 11, 12, 15):  # roughness, roughness, metallic, specTrans
+        rec, tex = sc.samplers[i]
+        base = tex.copy()
+        v = np.zeros_like(base)
+        v[:, 0] = 1.0
+        sc.samplers[i] = (rec, base + h * v)
+        lp = _loss(photon, sc, cam, st, wt)
+        sc.samplers[i] = (rec, base - h * v)
+        lm = _loss(photon, sc, cam, st, wt)
+        sc.samplers[i] = (rec, base)
+        fd.append((lp - lm) / (2 * h))
+        adj.append(float(np.sum(g[offs[i]:offs[i + 1]].astype(np.float64) * v)))
+    adj, fd = np.array(adj), np.array(fd)
+    print("parameter texture directions: adjoint", adj, "fd", fd)
+    assert np.all(np.abs(adj - fd) <= FD_REL_TOL * np.abs(fd) + 1e-6), (adj, fd)
+
+
+@pytest.mark.parametrize("param_textures", [False, True])
+def test_gpu_adjoint_matches_fp64_cpu_adjoint(photon, oracle_lib, param_textures):
     """The GPU adjoint against the FP64 CPU adjoint (oracle/adjoint_fp64.inc:
     the same paths replayed by the oracle, derivatives by central differences
     in double of each weight's forward formula) on the same pixel samples:
     every scalar material parameter, the medium's density and albedo, and the
-    texels along three random directions."""
-    sc, cam, st = _diff_small(res=16, spp=16)
+    texels along three random directions; with param_textures, roughness,
+    metallic and specTrans are read from textures too, and their texels are
+    part of the directions."""
+    sc, cam, st = _diff_small(res=16, spp=16, param_textures=param_textures)
     wt = _weights(st.height, st.width)
     g = _adjoint(photon, sc, cam, st, wt)
     ref = oracle_lib.CpuRenderer("oracle")
