@@ -52,6 +52,7 @@ extern "C" int ht_trace(const float *pos, uint64_t nv, const uint32_t *idx, uint
 // as the shading kernels compute them (hit_attributes).
 #include "scene_build.h"
 #include "bvh_gpu.h"
+#include "tuning.h"
 
 #include <stdexcept>
 
@@ -62,10 +63,16 @@ GpuBvh8 build_bvh8_gpu(const float4 *, const uint4 *, uint32_t, cudaStream_t)
 {
   throw std::runtime_error("the host harness builds no BVH on the GPU");
 }
-// Likewise the GPU majorant grid (scene_tables.cu).
+// Likewise the GPU majorant grid (scene_tables.cu): the harness has every
+// table built on the host (host_scene).
 std::string launch_majorants(const MajorantJob &, const float *, const float4 *, float *, cudaStream_t)
 {
   return "the host harness builds no tables on the GPU";
+}
+void host_scene(const phc_scene_desc &desc, HostScene &h)
+{
+  tuning().gpu_tables = 0;
+  build_host_scene(desc, h);
 }
 } // namespace phc
 
@@ -74,7 +81,7 @@ extern "C" int ht_trace_instanced(const phc_scene_desc *desc, const float *orgs,
     uint64_t *stats)
 {
   HostScene h;
-  build_host_scene(*desc, h);
+  host_scene(*desc, h);
   DevScene sc{};
   sc.nodes = reinterpret_cast<const uint4 *>(h.bvh.nodes.data());
   sc.tris = reinterpret_cast<const float4 *>(h.bvh.tris.data());
@@ -138,7 +145,7 @@ extern "C" int ht_trace_instanced(const phc_scene_desc *desc, const float *orgs,
 extern "C" int ht_guide_check(const phc_scene_desc *desc, const float *us, uint32_t n, uint64_t *counts)
 {
   HostScene h;
-  build_host_scene(*desc, h);
+  host_scene(*desc, h);
   for (int k = 0; k < 5; ++k)
     counts[k] = 0;
   counts[0] = (h.emissive_guide.empty() ? 0u : 1u) | (h.env_mguide.empty() ? 0u : 2u) |
@@ -217,7 +224,7 @@ extern "C" int ht_volume_check(const phc_scene_desc *desc, const float *orgs, co
     const float *tmax, const uint32_t *seeds, uint32_t n, uint64_t *counts)
 {
   HostScene h;
-  build_host_scene(*desc, h);
+  host_scene(*desc, h);
   std::vector<float> values(h.vol_values);
   for (const HostScene::Span &sp : h.vol_value_spans)
     values.insert(values.end(), sp.p, sp.p + sp.floats);
