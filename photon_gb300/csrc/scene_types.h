@@ -46,8 +46,20 @@ struct DevMaterial {
   int32_t base_color_alpha;
   int32_t base_tex;  // atlas texture of the base colour (pt::Material::base_color_tex), -1: none
   int32_t alpha_tex; // atlas texture of alpha (pt::Material::alpha_tex), -1: none
-  int32_t pad_;
+  uint32_t shade_class; // shading kernel class (SHADE_CLASS_LOBES), set by the scene build
 };
+
+// Lobes a material's BSDF can have.  A bit is clear only where the scene
+// build proved that lobe's weight and value exactly +0 for every direction
+// (material_lobes), so a shading kernel compiled without it returns the
+// same results for that material.
+enum : uint32_t { LB_DIFF = 1u, LB_SPEC = 2u, LB_TRANS = 4u, LB_COAT = 8u, LB_SHEEN = 16u, LB_ALL = 31u };
+// Material classes with a hit-shading kernel of their own: class c is
+// shaded with the lobes SHADE_CLASS_LOBES[c]; a material goes to the first
+// class (from 1) whose lobes include its own, else to class 0 (all lobes).
+constexpr uint32_t SHADE_CLASSES = 8;
+constexpr uint32_t SHADE_CLASS_LOBES[SHADE_CLASSES] = {LB_ALL, LB_SPEC | LB_COAT, LB_DIFF | LB_SPEC | LB_COAT,
+    LB_TRANS | LB_COAT, LB_SPEC | LB_TRANS | LB_COAT, LB_SPEC, LB_DIFF | LB_SPEC, LB_DIFF};
 
 enum : int32_t { SRC_BASE = 0, SRC_ALPHA = 1, SRC_METAL = 2, SRC_ROUGH = 3, SRC_EMIT = 4, SRC_TRANS = 5, SRC_NORMAL = 6 };
 enum : int32_t {

@@ -116,23 +116,33 @@ __device__ __forceinline__ float diffuse_scale(const Mat &m, float NoV)
   return 1.f - (f0d + (f90d - f0d) * c2 * c2 * c);
 }
 __device__ __forceinline__ bool spec_is_delta(const Mat &m) { return m.roughness < 0.001f; }
+// LOBES (an LB_* mask, scene_types.h): the lobes the material can have; a
+// lobe outside it has weight exactly +0 (material_lobes proves it on the
+// host), so its code is left out without changing a result.
+template <uint32_t LOBES = LB_ALL>
 __device__ __forceinline__ void lobe_weights(const Mat &m, float NoV, float &wd, float &ws, float &wt, float &wc)
 {
   const float opaque = 1.f - saturate(m.transmission);
   const float dielectric = 1.f - saturate(m.metallic);
-  const float diffuse_energy = dielectric * opaque * diffuse_scale(m, NoV);
-  const float base_lum = lum(m.base_color);
-  wd = diffuse_energy > 0.f ? diffuse_energy * fmaxf(base_lum, 0.05f) : 0.f;
-  if (m.sheen > 0.f && dielectric * opaque > 0.f)
-    wd += 0.1f * m.sheen;
-  V3 F0, F90;
-  spec_f0_f90(m, F0, F90);
-  const V3 F = schlick(NoV, F0, F90);
-  const float spec = lum(F);
-  ws = spec > 0.f ? fmaxf(spec, 0.05f) : 0.f;
-  wt = saturate(m.transmission) * dielectric;
+  wd = 0.f;
+  if (LOBES & LB_DIFF) {
+    const float diffuse_energy = dielectric * opaque * diffuse_scale(m, NoV);
+    const float base_lum = lum(m.base_color);
+    wd = diffuse_energy > 0.f ? diffuse_energy * fmaxf(base_lum, 0.05f) : 0.f;
+    if (m.sheen > 0.f && dielectric * opaque > 0.f)
+      wd += 0.1f * m.sheen;
+  }
+  ws = 0.f;
+  if (LOBES & LB_SPEC) {
+    V3 F0, F90;
+    spec_f0_f90(m, F0, F90);
+    const V3 F = schlick(NoV, F0, F90);
+    const float spec = lum(F);
+    ws = spec > 0.f ? fmaxf(spec, 0.05f) : 0.f;
+  }
+  wt = (LOBES & LB_TRANS) ? saturate(m.transmission) * dielectric : 0.f;
   wc = 0.f;
-  if (m.clearcoat > 0.f) {
+  if ((LOBES & LB_COAT) && m.clearcoat > 0.f) {
     const float c = 1.f - saturate(NoV);
     const float c2 = c * c;
     wc = fmaxf(m.clearcoat * 0.25f * (0.04f + 0.96f * c2 * c2 * c), 0.02f);
@@ -201,6 +211,10 @@ __device__ __forceinline__ V3 eval_coat(const Mat &m, V3 wo, V3 wi, V3 n)
   const float w = m.clearcoat * 0.25f;
   return F * (w * D * G / denom);
 }
+// The lobes outside LOBES evaluate to exactly +0 (eval_diffuse, eval_spec
+// with F0 = F90 = 0, eval_sheen, eval_coat return +0 vectors for them), and
+// f + (+0) = f: leaving them out returns the same f.
+template <uint32_t LOBES = LB_ALL>
 static __device__ __forceinline__ V3 bsdf_eval(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
 {
   if (dot(wo, n) <= 0.f || dot(wi, n) <= 0.f)
@@ -210,13 +224,16 @@ static __device__ __forceinline__ V3 bsdf_eval(const Mat &m, V3 wo, V3 wi, V3 n,
   if (NoL <= 0.f || NoV <= 0.f)
     return V3{0.f, 0.f, 0.f};
   const float a = fmaxf(m.roughness, 0.001f);
-  V3 f = eval_diffuse(m, NoL, NoV);
-  if (!spec_is_delta(m))
+  V3 f = (LOBES & LB_DIFF) ? eval_diffuse(m, NoL, NoV) : V3{0.f, 0.f, 0.f};
+  if ((LOBES & LB_SPEC) && !spec_is_delta(m))
     f = f + eval_spec(m, wo, wi, sn, a);
-  f = f + eval_sheen(m, wo, wi, sn);
-  f = f + eval_coat(m, wo, wi, sn);
+  if (LOBES & LB_SHEEN)
+    f = f + eval_sheen(m, wo, wi, sn);
+  if (LOBES & LB_COAT)
+    f = f + eval_coat(m, wo, wi, sn);
   return f;
 }
+template <uint32_t LOBES = LB_ALL>
 static __device__ __forceinline__ float bsdf_pdf(const Mat &m, V3 wo, V3 wi, V3 n, V3 sn)
 {
   if (dot(wo, n) <= 0.f || dot(wi, n) <= 0.f)
@@ -227,19 +244,19 @@ static __device__ __forceinline__ float bsdf_pdf(const Mat &m, V3 wo, V3 wi, V3 
     return 0.f;
   const float a = fmaxf(m.roughness, 0.001f);
   float wd, ws, wt, wc;
-  lobe_weights(m, NoV, wd, ws, wt, wc);
+  lobe_weights<LOBES>(m, NoV, wd, ws, wt, wc);
   const float sum = wd + ws + wt + wc;
   if (sum <= 0.f)
     return 0.f;
   const float pd = wd / sum, ps = ws / sum, pc = wc / sum;
   float pdf = 0.f;
-  if (pd > 0.f)
+  if ((LOBES & LB_DIFF) && pd > 0.f)
     pdf += pd * (NoL * INV_PI);
-  if (ps > 0.f && !spec_is_delta(m)) {
+  if ((LOBES & LB_SPEC) && ps > 0.f && !spec_is_delta(m)) {
     const V3 h = normalize(wi + wo);
     pdf += ps * ggx_pdf_refl(saturate(dot(sn, h)), saturate(dot(wo, h)), a);
   }
-  if (pc > 0.f) {
+  if ((LOBES & LB_COAT) && pc > 0.f) {
     const V3 h = normalize(wi + wo);
     pdf += pc * ggx_pdf_refl(saturate(dot(sn, h)), saturate(dot(wo, h)), fmaxf(m.clearcoat_roughness, 0.001f));
   }
@@ -269,6 +286,10 @@ struct BSample {
   int lobe;
   float noh;
 };
+// A lobe outside LOBES has probability exactly 0, so its branch is never
+// taken (xi >= 0, and the sums of the selection thresholds are unchanged by
+// +0 terms); leaving it out returns the same sample.
+template <uint32_t LOBES = LB_ALL>
 static __device__ __forceinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n, V3 sn, Rng &rng)
 {
   BSample out{V3{0.f, 0.f, 0.f}, V3{0.f, 0.f, 0.f}, 0.f, false, false, LOBE_NONE, 0.f};
@@ -285,7 +306,7 @@ static __device__ __forceinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n,
     wt = 1.f;
     wc = 0.f;
   } else {
-    lobe_weights(m, NoV, wd, ws, wt, wc);
+    lobe_weights<LOBES>(m, NoV, wd, ws, wt, wc);
     t_energy = wt;
   }
   const float sum = wd + ws + wt + wc;
@@ -293,15 +314,15 @@ static __device__ __forceinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n,
     return out;
   const float pd = wd / sum, ps = ws / sum, pt = wt / sum, pc = wc / sum;
   const float xi = rng.next();
-  if (xi < pd) {
+  if ((LOBES & LB_DIFF) && xi < pd) {
     out.wi = cosine_hemisphere(sn, rng);
     out.diff = true;
     out.lobe = LOBE_DIFFUSE;
-    out.f = bsdf_eval(m, wo, out.wi, n, sn);
-    out.pdf = bsdf_pdf(m, wo, out.wi, n, sn);
+    out.f = bsdf_eval<LOBES>(m, wo, out.wi, n, sn);
+    out.pdf = bsdf_pdf<LOBES>(m, wo, out.wi, n, sn);
     return out;
   }
-  if (xi < pd + ps) {
+  if ((LOBES & LB_SPEC) && xi < pd + ps) {
     if (spec_is_delta(m)) {
       out.wi = reflect(-wo, sn);
       if (dot(out.wi, n) <= 0.f)
@@ -320,12 +341,12 @@ static __device__ __forceinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n,
     out.wi = reflect(-wo, h);
     if (dot(out.wi, n) <= 0.f)
       return none;
-    out.f = bsdf_eval(m, wo, out.wi, n, sn);
-    out.pdf = bsdf_pdf(m, wo, out.wi, n, sn);
+    out.f = bsdf_eval<LOBES>(m, wo, out.wi, n, sn);
+    out.pdf = bsdf_pdf<LOBES>(m, wo, out.wi, n, sn);
     out.lobe = LOBE_GLOSSY;
     return out;
   }
-  if (xi < pd + ps + pt && m.transmission > 0.f) {
+  if ((LOBES & LB_TRANS) && xi < pd + ps + pt && m.transmission > 0.f) {
     const V3 nn = front ? n : n * -1.f;
     V3 snf = front ? sn : sn * -1.f;
     if (dot(snf, wo) <= 0.f)
@@ -380,13 +401,13 @@ static __device__ __forceinline__ BSample bsdf_sample(const Mat &m, V3 wo, V3 n,
     out.lobe = LOBE_TRANS;
     return out;
   }
-  if (pc > 0.f) {
+  if ((LOBES & LB_COAT) && pc > 0.f) {
     const V3 h = ggx_half(sn, fmaxf(m.clearcoat_roughness, 0.001f), rng);
     out.wi = reflect(-wo, h);
     if (dot(out.wi, n) <= 0.f)
       return none;
-    out.f = bsdf_eval(m, wo, out.wi, n, sn);
-    out.pdf = bsdf_pdf(m, wo, out.wi, n, sn);
+    out.f = bsdf_eval<LOBES>(m, wo, out.wi, n, sn);
+    out.pdf = bsdf_pdf<LOBES>(m, wo, out.wi, n, sn);
     out.lobe = LOBE_COAT;
     return out;
   }

