@@ -39,6 +39,7 @@ using i32 = int32_t;
 // path measurably (tracking distances, environment directions).
 PHC_HD float m_sin(float x) { return acc_sin(x); }
 PHC_HD float m_cos(float x) { return acc_cos(x); }
+PHC_HD void m_sincos(float x, float &s, float &c) { acc_sincos(x, s, c); }
 PHC_HD float m_log(float x) { return logf(x); }
 PHC_HD float m_acos(float x) { return acosf(x); }
 PHC_HD float m_atan2(float y, float x) { return atan2f(y, x); }
@@ -197,8 +198,10 @@ PHC_HD void concentric_disk(Rng &rng, float &dx, float &dy)
     r = fabsf(v);
     th = (PI / 2.f) - (PI / 4.f) * (u / v);
   }
-  dx = r * m_cos(th);
-  dy = r * m_sin(th);
+  float sth, cth;
+  m_sincos(th, sth, cth);
+  dx = r * cth;
+  dy = r * sth;
 }
 PHC_HD V3 cosine_hemisphere(V3 n, Rng &rng)
 {
@@ -214,7 +217,9 @@ PHC_HD V3 uniform_sphere(Rng &rng)
   const float z = 1.f - 2.f * rng.next();
   const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
   const float phi = TWO_PI * rng.next();
-  return V3{r * m_cos(phi), r * m_sin(phi), z};
+  float sp, cp;
+  m_sincos(phi, sp, cp);
+  return V3{r * cp, r * sp, z};
 }
 
 } // namespace phc

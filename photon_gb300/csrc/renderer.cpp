@@ -313,6 +313,7 @@ WaveCounters wave_counters(phc_renderer *r, int max_iter)
   wc.mcount = c + (3 * max_iter + 1);
   wc.fetch = c + (4 * max_iter + 1);
   wc.vfetch = c + (8 * max_iter + 1);
+  wc.cfetch = c + (10 * max_iter + 1);
   wc.wave = c + wave_counter_words(max_iter);
   wc.error = c + wave_counter_words(max_iter) + 1;
   wc.dbg = c + wave_counter_words(max_iter) + 4;
@@ -364,8 +365,11 @@ struct KernelTimer {
 
 // One wave: counter reset, raygen, per iteration trace / shade / shadow, end.
 // Returns the number of kernel launches.
+// wave_paths: paths of one wave (lanes x pixels); the material sort and the
+// class kernels are recorded only where an iteration can reach the sort
+// threshold.
 uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, const RenderConst *rc, uint32_t npix,
-    int max_iter, int adaptive, bool counting, KernelTimer *tm = nullptr)
+    size_t wave_paths, int max_iter, int adaptive, bool counting, KernelTimer *tm = nullptr)
 {
   const WaveCounters wc = wave_counters(r, max_iter);
   ck(cudaMemsetAsync(wc.count, 0, per_wave_counter_bytes(max_iter), s), "reset counters");
@@ -394,11 +398,14 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
     hq.vscatter = r->vol_scatter.as<float4>();
     hq.vrng = r->vol_rng.as<uint32_t>();
   }
-  const bool sort = split && tu.sort_threshold > 0;
+  const bool sort = split && tu.sort_threshold > 0 && wave_paths >= size_t(tu.sort_threshold);
+  // lean scenes: the hit queue sorted by shading class, one kernel per class
+  const bool classes = sort && !full && tu.shade_classes;
   const size_t bin_words = size_t(2) * MAT_SORT_BINS;
   if (sort) { // sort_bins sized by ensure_wave_buffers (no allocation while a graph is captured)
     hq.sorted = r->hitq_sorted.as<uint32_t>();
     hq.sort_threshold = uint32_t(tu.sort_threshold);
+    hq.classes = classes ? 1u : 0u;
     ck(cudaMemsetAsync(r->sort_bins.p, 0, size_t(max_iter) * bin_words * 4, s), "reset sort bins");
   }
   uint64_t launches = 2;
@@ -416,8 +423,16 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
       launches += 3;
     }
     if (split) {
-      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 1}, hq); });
-      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 2}, hq); });
+      HitQueues hqi = hq;
+      if (classes) // the scatter leaves each bin's end in the upper half of the iteration's bins
+        hqi.cls_end = r->sort_bins.as<uint32_t>() + size_t(it) * bin_words + MAT_SORT_BINS;
+      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 1}, hqi); });
+      if (classes) {
+        for (uint32_t c = 1; c < SHADE_CLASSES; ++c)
+          timed(2, [&] { launch_shade_class(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, c, hqi); });
+        launches += SHADE_CLASSES - 1;
+      }
+      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 2}, hqi); });
       launches += 4;
     } else {
       if (vol_pre) {
@@ -618,13 +633,13 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
       uint64_t(max_iter) | (uint64_t(rc.adaptive) << 32), r->scene_generation,
       uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32),
       uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16) |
-          (uint64_t(tu.sort_threshold) << 24),
+          (uint64_t(tu.shade_classes) << 23) | (uint64_t(tu.sort_threshold) << 24),
       r->buf_gen, uint64_t(tu.wave_trip_cap)};
   uint64_t launches = 0;
   KernelTimer timer;
   if (tu.time_kernels) {
     for (uint32_t wv = 0; wv < waves; ++wv)
-      launches += record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting, &timer);
+      launches += record_wave(r, s, cfg, drc, npix, plan.slots, max_iter, rc.adaptive, counting, &timer);
   } else if (tu.use_graph) {
     if (!r->graph || std::memcmp(key, r->graph_key, sizeof(key)) != 0) {
       if (r->graph) {
@@ -634,7 +649,7 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
       cudaGraph_t g = nullptr;
       ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
       try {
-        r->graph_launches = record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
+        r->graph_launches = record_wave(r, s, cfg, drc, npix, plan.slots, max_iter, rc.adaptive, counting);
       } catch (...) {
         cudaStreamEndCapture(s, &g);
         if (g)
@@ -653,7 +668,7 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
     launches = uint64_t(waves) * r->graph_launches;
   } else {
     for (uint32_t wv = 0; wv < waves; ++wv)
-      launches += record_wave(r, s, cfg, drc, npix, max_iter, rc.adaptive, counting);
+      launches += record_wave(r, s, cfg, drc, npix, plan.slots, max_iter, rc.adaptive, counting);
   }
   const Frame fr = frame_of(r);
   if (tu.time_kernels)
@@ -1041,7 +1056,7 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
     ck(cudaMemsetAsync(r->nsamp.p, 0, size_t(cnt) * npix * 4, s), "reset accumulators");
     ck(cudaMemsetAsync(r->aov_a.p, 0, size_t(cnt) * npix * 16, s), "reset accumulators");
     ck(cudaMemsetAsync(wc.wave, 0, 8, s), "reset wave");
-    record_wave(r, s, cfg, drc, npix, max_iter, 0, false);
+    record_wave(r, s, cfg, drc, npix, size_t(cnt) * npix, max_iter, 0, false);
     // pass 2: the replay, bounce by bounce
     ck(cudaMemsetAsync(wc.count, 0, per_wave_counter_bytes(max_iter), s), "reset counters");
     ck(cudaMemsetAsync(wc.wave, 0, 4, s), "reset wave");

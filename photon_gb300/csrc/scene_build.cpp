@@ -69,6 +69,59 @@ DevMaterial convert_material(const phc_material &in)
   return m;
 }
 
+// The lobes a material's BSDF can have (LB_*), from the constants the lean
+// and full shading kernels read (resolve_material clamps metallic and
+// specTrans to [0, 1]).  A bit is cleared only where the shading code gives
+// that lobe exactly +0 for every direction:
+//   diffuse (and the sheen share of its weight): weight and value carry the
+//     factor (1 - metallic)(1 - specTrans), 0 here, times finite terms;
+//   specular reflection: with metallic 0 and the dielectric F0 / F90 scaled
+//     by the opacity both 0, F0 = F90 = +0, so its weight and value are +0;
+//   transmission: its branch needs specTrans > 0;
+//   clear coat, sheen: their code returns +0 for clearcoat <= 0, for
+//     sheen <= 0 or metallic >= 1.
+// Materials whose base colour, metallic or specTrans come from attributes or
+// textures, or with non-finite constants, keep every lobe.
+uint32_t material_lobes(const DevMaterial &m)
+{
+  if (m.src_kind[SRC_BASE] != 0 || m.src_kind[SRC_METAL] != 0 || m.src_kind[SRC_TRANS] != 0 || m.base_tex >= 0)
+    return LB_ALL;
+  const float vals[9] = {m.base_color[0], m.base_color[1], m.base_color[2], m.metallic, m.transmission,
+      m.specular, m.ior, m.clearcoat, m.sheen};
+  for (float v : vals)
+    if (!std::isfinite(v))
+      return LB_ALL;
+  auto clamp01 = [](float x) { return x < 0.f ? 0.f : (x > 1.f ? 1.f : x); };
+  const float metallic = clamp01(m.metallic), trans = clamp01(m.transmission);
+  const float dielectric = 1.f - metallic, opaque = 1.f - trans;
+  uint32_t lb = 0;
+  if (dielectric * opaque > 0.f)
+    lb |= LB_DIFF;
+  const float scale = std::fmax(2.f * m.specular, 0.f);
+  const float a = (1.f - m.ior) / (1.f + m.ior);
+  const float f0d = std::fmin(a * a * scale, 1.f) * opaque;
+  const float f90d = std::fmin(scale, 1.f) * opaque;
+  if (!(metallic == 0.f && f0d == 0.f && f90d == 0.f))
+    lb |= LB_SPEC;
+  if (trans > 0.f)
+    lb |= LB_TRANS;
+  if (m.clearcoat > 0.f)
+    lb |= LB_COAT;
+  if (m.sheen > 0.f && metallic < 1.f)
+    lb |= LB_SHEEN;
+  return lb;
+}
+
+// The shading class of a material: the first class from 1 whose lobes
+// include the material's, else class 0 (every lobe).
+uint32_t shade_class_of(uint32_t lobes)
+{
+  for (uint32_t c = 1; c < SHADE_CLASSES; ++c)
+    if ((lobes & ~SHADE_CLASS_LOBES[c]) == 0u)
+      return c;
+  return 0u;
+}
+
 // photon::pt::Material{} defaults (material.h:35-82), used when the scene has
 // no material at all (RenderBridge.cpp:518-519).
 DevMaterial default_material()
@@ -689,6 +742,8 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
   }
   if (s.materials.empty())
     s.materials.push_back(default_material());
+  for (DevMaterial &m : s.materials)
+    m.shade_class = shade_class_of(material_lobes(m));
   // samplers (RenderBridge.cpp:527-571); a pt scene has atlas textures
   // (texture.h:11-65) in their place, RGB widened to float4
   size_t offset = 0;

@@ -272,7 +272,9 @@ __device__ __forceinline__ V3 ggx_half(V3 n, float a, Rng &rng)
   const float ct = sqrtf((1.f - r1) / (1.f + (a2 - 1.f) * r1));
   const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
   const float phi = 2.f * PI * r2;
-  return normalize(t * (st * m_cos(phi)) + b * (st * m_sin(phi)) + n * ct);
+  float sp, cp;
+  m_sincos(phi, sp, cp);
+  return normalize(t * (st * cp) + b * (st * sp) + n * ct);
 }
 // Sampled lobe: 1 diffuse, 2 GGX reflection, 3 smooth (delta) specular,
 // 4 dielectric reflection, 5 dielectric transmission, 6 clearcoat.  noh > 0:
@@ -712,10 +714,12 @@ static __device__ __forceinline__ V3 env_sample(const DevScene &sc, Rng &rng, fl
   const float v = (float(row) + rng.next()) / float(sc.env_h);
   const float phi = u * TWO_PI - PI;
   const float theta = v * PI;
-  const float st = m_sin(theta);
-  const V3 d = mat3_mul(sc.env_t2w, V3{st * m_cos(phi), m_cos(theta), st * m_sin(phi)});
-  const float theta2 = v * PI;
-  const float denom = TWO_PI * PI * fmaxf(m_sin(theta2), 1e-6f);
+  float st, ct, sp, cp;
+  m_sincos(theta, st, ct);
+  m_sincos(phi, sp, cp);
+  const V3 d = mat3_mul(sc.env_t2w, V3{st * cp, ct, st * sp});
+  // the pdf's sin(theta) (the same angle: v * PI again)
+  const float denom = TWO_PI * PI * fmaxf(st, 1e-6f);
   pdf_out = (row_pdf * col_pdf) * float(sc.env_w) * float(sc.env_h) / denom;
   return d;
 }
@@ -751,7 +755,9 @@ static __device__ __forceinline__ LightSample sample_light(const DevLight &l, V3
       const float phi = TWO_PI * rng.next();
       V3 t, b;
       onb(wi, t, b);
-      wi = normalize(t * (st * m_cos(phi)) + b * (st * m_sin(phi)) + wi * ct);
+      float sp, cp;
+      m_sincos(phi, sp, cp);
+      wi = normalize(t * (st * cp) + b * (st * sp) + wi * ct);
     }
     return LightSample{wi, color * l.intensity, 1.f, 1e30f};
   }

@@ -17,10 +17,11 @@
 //     remainder r kept as an unevaluated sum of two floats (float-float,
 //     Dekker's error-free sum and product; the product through fmaf);
 //   * Taylor series of sin and cos on |r| <= pi/4 (the coefficients are
-//     1 / n!), the leading coefficients and every product that carries them
-//     in float-float, the small tail terms in plain float;
-//   * one final float rounding of hi + lo, whose error before rounding is
-//     below 2^-40 relative.
+//     1 / n!), the terms above 2^-9 of the result in float-float, the small
+//     tail terms in plain float;
+//   * one final float rounding, whose error before rounding is below 2^-35
+//     relative.
+// Call sites that need both use acc_sincos (one reduction, both series).
 // Arguments with |x| > 8 (no call site passes one) and non-finite ones
 // return CUDA's (or the host library's) sinf / cosf.
 #pragma once
@@ -83,55 +84,80 @@ PHC_HD int ff_reduce_pio2(float x, FFloat &r)
   return int(k);
 }
 
-// sin(r) and cos(r) as float-float for |r| <= pi/4 + a little: Taylor
-// series through r^13 / 13! and r^14 / 14! (truncation below 2^-41).
-PHC_HD void ff_sincos_poly(FFloat r, FFloat &s, FFloat &c)
+// sin(r) and cos(r) for |r| <= pi/4 + a little (r = r.hi + r.lo), rounded
+// once to float: Taylor series through r^13 / 13! and r^14 / 14!
+// (truncation below 2^-41).  The terms above 2^-9 of the result (r, r^3/3!,
+// r^5/5! for the sine; 1, z/2, z^2/4! for the cosine, z = r^2) are formed as
+// float-float with exact products (fmaf); the rest in float, whose error is
+// then below 2^-35 of the result.
+PHC_HD void ff_sincos_poly(FFloat r, float &sn, float &cs)
 {
-  const FFloat z = ff_mul(r, r);
-  const float zh = z.hi;
-  // sin r = r + r z (-1/3! + z (1/5! + z (-1/7! + z (1/9! + z (-1/11! + z / 13!)))))
-  const float qs = -0x1.a01a02p-13f + zh * (0x1.71de3ap-19f + zh * (-0x1.ae6456p-26f + zh * 0x1.612462p-33f));
-  const FFloat us = ff_add(ff(0x1.111112p-7f, -0x1.dddddep-32f), ff_mul(z, ff(qs)));
-  const FFloat ps = ff_add(ff(-0x1.555556p-3f, 0x1.555556p-28f), ff_mul(z, us));
-  s = ff_add(r, ff_mul(ff_mul(r, z), ps));
-  // cos r = 1 + z (-1/2 + z (1/4! + z (-1/6! + z (1/8! + z (-1/10! + z (1/12! - z / 14!))))))
-  const float qc = -0x1.6c16c2p-10f +
-      zh * (0x1.a01a02p-16f + zh * (-0x1.27e4fcp-22f + zh * (0x1.1eed8ep-29f + zh * -0x1.93974ap-37f)));
-  const FFloat uc = ff_add(ff(0x1.555556p-5f, -0x1.555556p-30f), ff_mul(z, ff(qc)));
-  const FFloat rc = ff_add(ff(-0.5f), ff_mul(z, uc));
-  c = ff_add(ff(1.f), ff_mul(z, rc));
+  // z = r^2 = zh + zl
+  const float zh = r.hi * r.hi;
+  const float zl = fmaf(r.hi, r.hi, -zh) + 2.f * r.hi * r.lo;
+  // sine: r^3 = p + pe, r^5 = q + qe, -r^3/3! = t + te, r^5/5! = u + ue
+  const float p = r.hi * zh;
+  const float pe = fmaf(r.hi, zh, -p) + fmaf(r.hi, zl, r.lo * zh);
+  const float q = p * zh;
+  const float qe = fmaf(p, zh, -q) + fmaf(p, zl, pe * zh);
+  const float t = p * -0x1.555556p-3f;
+  const float te = fmaf(p, -0x1.555556p-3f, -t) + fmaf(p, 0x1.555556p-28f, pe * -0x1.555556p-3f);
+  const float u = q * 0x1.111112p-7f;
+  const float ue = fmaf(q, 0x1.111112p-7f, -u) + fmaf(q, -0x1.dddddep-32f, qe * 0x1.111112p-7f);
+  // r^7 (-1/7! + z (1/9! - z (1/11! - z / 13!)))
+  const float st = q * zh * fmaf(zh, fmaf(zh, fmaf(zh, 0x1.612462p-33f, -0x1.ae6456p-26f), 0x1.71de3ap-19f),
+      -0x1.a01a02p-13f);
+  const FFloat sa = ff_two_sum(r.hi, t);
+  const FFloat sb = ff_fast_sum(sa.hi, u);
+  sn = sb.hi + (((sa.lo + sb.lo) + (r.lo + te)) + (ue + st));
+  // cosine: -z/2 = -(zh + zl)/2 exactly, z^2 = w + we, z^2/4! = v + ve
+  const float w = zh * zh;
+  const float we = fmaf(zh, zh, -w) + 2.f * zh * zl;
+  const float v = w * 0x1.555556p-5f;
+  const float ve = fmaf(w, 0x1.555556p-5f, -v) + fmaf(w, -0x1.555556p-30f, we * 0x1.555556p-5f);
+  // z^3 (-1/6! + z (1/8! - z (1/10! - z (1/12! - z / 14!))))
+  const float ct = w * zh *
+      fmaf(zh, fmaf(zh, fmaf(zh, fmaf(zh, -0x1.93974ap-37f, 0x1.1eed8ep-29f), -0x1.27e4fcp-22f), 0x1.a01a02p-16f),
+          -0x1.6c16c2p-10f);
+  const FFloat ca = ff_two_sum(1.f, -0.5f * zh);
+  const FFloat cb = ff_fast_sum(ca.hi, v);
+  cs = cb.hi + (((ca.lo + cb.lo) + (-0.5f * zl + ve)) + ct);
+}
+
+// sin(x) and cos(x) together (one reduction, both series).
+PHC_HD void acc_sincos(float x, float &sn, float &cs)
+{
+  if (!(fabsf(x) <= 8.f)) {
+    sn = sinf(x);
+    cs = cosf(x);
+    return;
+  }
+  FFloat r;
+  const int k = ff_reduce_pio2(x, r);
+  float s, c;
+  ff_sincos_poly(r, s, c);
+  switch (k & 3) {
+  case 0: sn = s; cs = c; break;
+  case 1: sn = c; cs = -s; break;
+  case 2: sn = -s; cs = -c; break;
+  default: sn = -c; cs = s; break;
+  }
+  if (x == 0.f)
+    sn = x; // sin(+-0) = +-0
 }
 
 PHC_HD float acc_sin(float x)
 {
-  if (!(fabsf(x) <= 8.f))
-    return sinf(x);
-  if (x == 0.f)
-    return x; // sin(+-0) = +-0
-  FFloat r, s, c;
-  const int k = ff_reduce_pio2(x, r);
-  ff_sincos_poly(r, s, c);
-  switch (k & 3) {
-  case 0: return s.hi + s.lo;
-  case 1: return c.hi + c.lo;
-  case 2: return -(s.hi + s.lo);
-  default: return -(c.hi + c.lo);
-  }
+  float s, c;
+  acc_sincos(x, s, c);
+  return s;
 }
 
 PHC_HD float acc_cos(float x)
 {
-  if (!(fabsf(x) <= 8.f))
-    return cosf(x);
-  FFloat r, s, c;
-  const int k = ff_reduce_pio2(x, r);
-  ff_sincos_poly(r, s, c);
-  switch (k & 3) {
-  case 0: return c.hi + c.lo;
-  case 1: return -(s.hi + s.lo);
-  case 2: return -(c.hi + c.lo);
-  default: return s.hi + s.lo;
-  }
+  float s, c;
+  acc_sincos(x, s, c);
+  return c;
 }
 
 } // namespace phc

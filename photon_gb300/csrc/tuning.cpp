@@ -35,6 +35,7 @@ const Key *keys(size_t &n)
       {"trace_refill", "PHC_TUNE_TRACE_REFILL", 1, 32, nullptr, &g_tuning.trace_refill},
       {"split_shade", "PHC_TUNE_SPLIT_SHADE", 0, 1, nullptr, &g_tuning.split_shade},
       {"shade_lean", "PHC_TUNE_SHADE_LEAN", 0, 1, nullptr, &g_tuning.shade_lean},
+      {"shade_classes", "PHC_TUNE_SHADE_CLASSES", 0, 1, nullptr, &g_tuning.shade_classes},
       {"batch_wave_paths", "PHC_TUNE_BATCH_WAVE_PATHS", 1024, int64_t(1) << 30, &g_tuning.batch_wave_paths, nullptr},
       {"sort_threshold", "PHC_TUNE_SORT_THRESHOLD", 0, int64_t(1) << 30, &g_tuning.sort_threshold, nullptr},
       {"gpu_bvh", "PHC_TUNE_GPU_BVH", 0, 1, nullptr, &g_tuning.gpu_bvh},

@@ -22,6 +22,7 @@ struct Tuning {
   int trace_refill{8};               // closest-hit warps refill once this many lanes idle (32: never)
   int split_shade{1};                // misses and hits shaded by separate kernels (no-volume scenes)
   int shade_lean{1};                 // lean shading kernels for scenes without volumes/sources/lights
+  int shade_classes{1};              // lean scenes: hit queue sorted by shading class, one kernel per class
   int64_t batch_wave_paths{1 << 25}; // paths per wave of a batched render
   int64_t sort_threshold{1 << 18};   // sort the hit queue by material when it holds this many hits (0: never)
   int gpu_bvh{1};                    // build the BVH8 on the GPU (bvh_gpu.cu), read at scene build

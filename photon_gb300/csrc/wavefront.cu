@@ -324,16 +324,20 @@ __global__ void __launch_bounds__(128, INST ? PHC_TRACE_MIN_BLOCKS_INST : PHC_TR
 // from one atomic).  Order within a bin is not preserved; every path's result
 // is independent of the order it is shaded in.
 // Bin of a queued hit: its material (batched renders: job and material).
+// Sorting by shading class (hq.classes): the class's bins, then the material.
 template <bool BATCH>
 __device__ __forceinline__ uint32_t hit_bin(const DevScene &sc, const BatchTable &bt, const uint4 *info,
-    const float4 *hits, uint32_t qi)
+    const float4 *hits, const HitQueues &hq, uint32_t qi)
 {
   const uint32_t prim = __float_as_uint(hits[qi].y);
   if (BATCH) {
     const uint32_t job = info[qi].w >> BATCH_JOB_SHIFT;
     return (job * 1031u + __ldg(&bt.jobs[job].sc.prim_vidx[prim].w)) % MAT_SORT_BINS;
   }
-  return __ldg(&sc.prim_vidx[prim].w) % MAT_SORT_BINS;
+  const uint32_t mat = __ldg(&sc.prim_vidx[prim].w);
+  if (hq.classes)
+    return __ldg(&sc.materials[mat].shade_class) * MAT_CLASS_BINS + mat % MAT_CLASS_BINS;
+  return mat % MAT_SORT_BINS;
 }
 
 template <bool BATCH>
@@ -350,7 +354,7 @@ __global__ void __launch_bounds__(256) k_mat_hist(DevScene sc, BatchTable bt, co
     h[b] = 0u;
   __syncthreads();
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    atomicAdd(&h[hit_bin<BATCH>(sc, bt, info, hits, hq.hitq[i])], 1u);
+    atomicAdd(&h[hit_bin<BATCH>(sc, bt, info, hits, hq, hq.hitq[i])], 1u);
   __syncthreads();
   for (uint32_t b = threadIdx.x; b < MAT_SORT_BINS; b += blockDim.x)
     if (h[b])
@@ -403,7 +407,7 @@ __global__ void __launch_bounds__(256) k_mat_scatter(DevScene sc, BatchTable bt,
       const uint32_t i = c0 + k * blockDim.x + threadIdx.x;
       const bool live = i < n;
       q[k] = live ? hq.hitq[i] : 0u;
-      bin[k] = live ? hit_bin<BATCH>(sc, bt, info, hits, q[k]) : 0xffffffffu;
+      bin[k] = live ? hit_bin<BATCH>(sc, bt, info, hits, hq, q[k]) : 0xffffffffu;
       const uint32_t grp = __match_any_sync(WARP_FULL, bin[k]);
       const uint32_t leader = uint32_t(__ffs(int(grp)) - 1);
       uint32_t r = 0;

@@ -72,12 +72,13 @@ struct WaveCounters {
   uint32_t *mcount;  // [max_iter] closest-hit results that missed (split queues)
   uint32_t *fetch;   // [4 * max_iter] work counters: trace, shade (all/hits), shade misses, shadow
   uint32_t *vfetch;  // [2 * max_iter] work counters: volume scattering, shadow transmittance
+  uint32_t *cfetch;  // [SHADE_CLASSES * max_iter] work counters of the class hit-shading kernels
   uint32_t *wave;    // current wave index within the render call
   uint32_t *error;   // sticky error word
   uint32_t *dbg;     // [WAVE_DBG_WORDS] record of the first self-check failure
   uint32_t trip_cap; // loop trips after which a persistent warp stops (tuning key wave_trip_cap)
 };
-inline size_t wave_counter_words(int max_iter) { return size_t(10 * max_iter + 1); }
+inline size_t wave_counter_words(int max_iter) { return size_t((10 + SHADE_CLASSES) * max_iter + 1); }
 
 // Self-check of the persistent traversal loops: a warp that makes more than
 // WaveCounters::trip_cap loop trips (each trip is one traversal step of every
@@ -113,8 +114,16 @@ struct HitQueues {
   // path's random-number state after it, from which shading continues.
   float4 *vscatter = nullptr;
   uint32_t *vrng = nullptr;
+  // Sorting by shading class (lean scenes): bins are grouped per class
+  // (MAT_CLASS_BINS each, class-major), and after the sort cls_end[b] is
+  // the end of bin b's run in `sorted`, so class c's hits are the run
+  // [cls_end[c * MAT_CLASS_BINS - 1] (0 for c = 0), cls_end[(c + 1) *
+  // MAT_CLASS_BINS - 1]), shaded by that class's kernel.
+  uint32_t classes = 0;
+  const uint32_t *cls_end = nullptr;
 };
 constexpr uint32_t MAT_SORT_BINS = 1024; // materials map to bin = id % MAT_SORT_BINS
+constexpr uint32_t MAT_CLASS_BINS = MAT_SORT_BINS / SHADE_CLASSES; // sorting by class: bin = class * this + id % this
 
 // Shading kernel variants: FULL compiles volumes, material sources and
 // analytic lights; PART 0 shades every path, 1 the hit queue, 2 the misses.
@@ -180,6 +189,11 @@ void launch_trace(const LaunchCfg &c, cudaStream_t s, DevScene sc, PathSoA in, f
     uint64_t *stats, int refill, HitQueues hq);
 void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in, PathSoA out,
     const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, ShadeVariant v, HitQueues hq);
+// The lean hit-shading kernel of shading class cls (1 .. SHADE_CLASSES - 1)
+// over its run of the class-sorted hit queue (hq.cls_end); class 0 is
+// launch_shade's lean hit kernel.
+void launch_shade_class(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,
+    PathSoA out, const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, uint32_t cls, HitQueues hq);
 // Delta tracking of every path of iteration `it` through the scene's volumes
 // (the first step of pt_shade for volume scenes), into hq.vscatter / hq.vrng.
 void launch_vol_scatter(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,

@@ -168,22 +168,34 @@ def test_empty_scene_renders_background(photon):
     assert np.all(np.isinf(r.read("depth")))
 
 
-def test_material_sorted_shading_keeps_images(photon):
-    """Shading the hit queue in material order changes no pixel."""
+@pytest.mark.parametrize("scene", ["procedural_500k", "box_room"])
+def test_material_sorted_shading_keeps_images(photon, scene):
+    """Shading the hit queue unsorted, sorted by material, and sorted by
+    shading class with one kernel per class (each compiled without the lobes
+    its materials cannot have) gives the same image bit for bit.  The sizes
+    make the first iterations' hit queues pass the sort threshold."""
     from photon_gb300 import tuning_get, tuning_set, workloads
-    sc, cam, st = workloads.procedural_500k()
-    st.width = st.height = 128
-    st.pixel_samples = 8
-    old = tuning_get("sort_threshold")
+    if scene == "box_room":
+        sc, cam, st = workloads.box_room()
+        st.width = st.height = 512
+        st.pixel_samples = 2
+    else:
+        sc, cam, st = workloads.procedural_500k()
+        st.width = st.height = 256
+        st.pixel_samples = 8
+    old = (tuning_get("sort_threshold"), tuning_get("shade_classes"))
     try:
         imgs = []
-        for thr in (0, 1):
+        for thr, cls in ((0, 0), (1, 0), (1, 1), (1 << 18, 1)):
             tuning_set("sort_threshold", thr)
+            tuning_set("shade_classes", cls)
             r = photon.Renderer()
             r.set_scene(sc)
             r.render(cam, st, True)
             imgs.append(r.read("color").copy())
             r.close()
-        assert np.array_equal(imgs[0].view(np.uint32), imgs[1].view(np.uint32))
+        for k in range(1, len(imgs)):
+            assert np.array_equal(imgs[0].view(np.uint32), imgs[k].view(np.uint32)), k
     finally:
-        tuning_set("sort_threshold", old)
+        tuning_set("sort_threshold", old[0])
+        tuning_set("shade_classes", old[1])
