@@ -70,6 +70,9 @@ SHADE_BYTES_PER_PATH = 8 + 68 + 16 + 16 + 48 + 48 + 64 + 68 + 48
 # one ncu capture (1412.8 + 1897.5 MB over the 8.4M hits of iteration 0 at
 # 8 spp, profiles/k_shade_procedural_500k.md).
 SHADE_DRAM_BYTES_PER_PATH = (1412.8e6 + 1897.5e6) / 8388608
+# Volume tracking: one density lookup reads the 8 grid values of its
+# trilinear cell and the 2 transfer-function entries it interpolates.
+VOL_LOOKUP_BYTES = 8 * 4 + 2 * 16
 
 
 _T0 = time.perf_counter()
@@ -206,14 +209,29 @@ def scene_configs(p, reps=1):
         k = ms.index(m)
         p.tuning_set("time_kernels", 1)  # per-kind device time of one more render
         r.render(cam, st, True)
-        kinds = r.stats()["kernel_ms"]
+        kinds = dict(zip(p._abi.KERNEL_KIND_NAMES, r.stats()["kernel_ms"]))
         p.tuning_set("time_kernels", 0)
         out[name] = {"triangles": int(sc.triangle_count), "res": [st.width, st.height],
                      "spp": st.pixel_samples, "depth": st.max_depth, "adaptive": int(st.adaptive_sampling),
                      "render_ms": m, "pixel_samples": int(samples[k]),
                      "msamples_per_s": samples[k] / (m / 1e3) / 1e6, "upload_s": upload,
-                     "kernel_ms": dict(zip(["raygen", "trace_closest", "shade", "trace_shadow", "wave_end+resolve"],
-                                           kinds))}
+                     "kernel_ms": kinds}
+        if sc.volumes:
+            # the tracking kernels' algorithmic bytes: per density lookup the
+            # 8 grid values of its trilinear cell and the 2 transfer-function
+            # entries it interpolates (the lookups counted on the device)
+            p.tuning_set("count_traversal", 1)
+            r.render(cam, st, True)
+            lookups = r.stats()["volume_lookups"]
+            p.tuning_set("count_traversal", 0)
+            vol_ms = kinds["volume_scatter"] + kinds["shadow_transmittance"]
+            peak, peak_kind = peaks()
+            gbs = lookups * VOL_LOOKUP_BYTES / (vol_ms / 1e3) / 1e9 if vol_ms > 0 else 0.0
+            out[name]["roofline"] = {
+                "kernel": "k_vol_scatter + k_shadow_volume (delta / ratio tracking)", "bound": "latency",
+                "density_lookups": int(lookups), "lookups_per_pixel_sample": lookups / max(1, samples[k]),
+                "bytes_per_lookup": VOL_LOOKUP_BYTES, "ms_per_frame": vol_ms, "achieved": gbs, "peak": peak,
+                "unit": "GB/s", "frac": gbs / peak, "peak_source": f"{peak_kind} hbm_gbs"}
         r.close()
         del sc
     return out
@@ -463,7 +481,10 @@ def batched_vs_plain(p, n_jobs=64, seed=0, check_jobs=8):
                   "128^2-1024^2, 4-64 spp, depth 4-12"}
     _log("batched: jobs generated")
     try:
+        t = time.perf_counter()
         rs = make(jobs)
+        torch.cuda.synchronize()
+        out["upload_s"] = time.perf_counter() - t  # 64 phc_set_scene calls: host tables, GPU BVH8 build
         _log("batched: scenes uploaded")
         for label, wave_paths in (("one_sample_per_wave", 1024), ("lanes", old)):
             p.tuning_set("wave_paths", wave_paths)
@@ -706,7 +727,7 @@ def run_ours(args, world, rank, local):
     p.tuning_set("count_traversal", 0)
     for k in ("node_visits", "tri_tests", "shadow_node_visits", "shadow_tri_tests"):
         prof[k] = cnt[k]
-    kinds = ["raygen", "trace_closest", "shade", "trace_shadow", "wave_end+resolve"]
+    kinds = list(p._abi.KERNEL_KIND_NAMES)
     kms = dict(zip(kinds, prof["kernel_ms"]))
     kcount = dict(zip(kinds, prof["kernel_count"]))
     # algorithmic bytes of the traversal kernels

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define PHC_ABI_VERSION 1
+#define PHC_ABI_VERSION 2
 
 enum {
   PHC_OK = 0,
@@ -284,6 +284,7 @@ typedef struct phc_settings {
 } phc_settings;
 
 /* Counters of the last render call, read by phc_render_stats. */
+#define PHC_KERNEL_KINDS 7
 typedef struct phc_render_stats {
   uint64_t pixel_samples;   /* pixel-samples traced (adaptive: started ones)  */
   uint64_t closest_rays;    /* rays given to closest-hit traversal            */
@@ -295,10 +296,14 @@ typedef struct phc_render_stats {
   uint64_t shadow_tri_tests;
   double render_ms;         /* device time of the render call                 */
   uint64_t kernel_launches; /* kernels launched by the call (graph nodes too) */
-  /* Device time per kernel kind (raygen, closest-hit trace, shade, shadow,
-     wave end + resolve) when the "time_kernels" tuning key is 1, else 0. */
-  double kernel_ms[5];
-  uint64_t kernel_count[5];
+  /* Device time per kernel kind when the "time_kernels" tuning key is 1,
+     else 0: raygen, closest-hit trace, shade (with the material sort), shadow
+     (any hit), wave end + resolve, the volume-scattering pre-pass, the shadow
+     transmittance of volume scenes. */
+  double kernel_ms[PHC_KERNEL_KINDS];
+  uint64_t kernel_count[PHC_KERNEL_KINDS];
+  uint64_t volume_lookups;  /* density lookups of the volume-tracking kernels
+                               (when "count_traversal" is 1)                   */
 } phc_render_stats;
 
 /* ------------------------------------------------------------------ defaults */

@@ -152,14 +152,20 @@ class Settings(C.Structure):
     ]
 
 
+# kernel kinds of RenderStats.kernel_ms (phc_render_stats)
+KERNEL_KINDS = 7
+KERNEL_KIND_NAMES = ("raygen", "trace_closest", "shade", "trace_shadow", "wave_end+resolve", "volume_scatter",
+                     "shadow_transmittance")
+
+
 class RenderStats(C.Structure):
     _fields_ = [
         ("pixel_samples", C.c_uint64), ("closest_rays", C.c_uint64),
         ("shadow_rays", C.c_uint64), ("node_visits", C.c_uint64),
         ("tri_tests", C.c_uint64), ("shadow_node_visits", C.c_uint64),
         ("shadow_tri_tests", C.c_uint64), ("render_ms", C.c_double),
-        ("kernel_launches", C.c_uint64), ("kernel_ms", C.c_double * 5),
-        ("kernel_count", C.c_uint64 * 5),
+        ("kernel_launches", C.c_uint64), ("kernel_ms", C.c_double * KERNEL_KINDS),
+        ("kernel_count", C.c_uint64 * KERNEL_KINDS), ("volume_lookups", C.c_uint64),
     ]
 
 

@@ -329,8 +329,8 @@ struct KernelTimer {
   std::vector<cudaEvent_t> ev;
   std::vector<int> kind;
   size_t used{0};
-  double ms[5]{};
-  uint64_t count[5]{};
+  double ms[PHC_KERNEL_KINDS]{};
+  uint64_t count[PHC_KERNEL_KINDS]{};
   ~KernelTimer()
   {
     for (cudaEvent_t e : ev)
@@ -436,15 +436,17 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
       launches += 4;
     } else {
       if (vol_pre) {
-        timed(2, [&] { launch_vol_scatter(cfg, s, rc, sc, in, hits, wc, it, hq); });
+        timed(5, [&] { launch_vol_scatter(cfg, s, rc, sc, in, hits, wc, it, hq, counting ? stats + 7 : nullptr); });
         launches += 1;
       }
       timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 0}, hq); });
       launches += 3;
     }
     timed(3, [&] { launch_shadow(cfg, s, rc, sc, sh, ac, wc, it, counting ? stats + 5 : nullptr, tu.trace_refill); });
-    if (sc.volume_count > 0)
-      launches += 1; // k_shadow_volume
+    if (sc.volume_count > 0) {
+      timed(6, [&] { launch_shadow_volume(cfg, s, rc, sc, sh, ac, wc, it, counting ? stats + 7 : nullptr); });
+      launches += 1;
+    }
   }
   timed(4, [&] { launch_wave_end(s, rc, ac, wc, npix, adaptive, max_iter, stats); });
   if (tm)
@@ -702,7 +704,8 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
   r->last.shadow_node_visits = stats[5];
   r->last.shadow_tri_tests = stats[6];
   r->last.kernel_launches = launches;
-  for (int k = 0; k < 5; ++k) {
+  r->last.volume_lookups = stats[7];
+  for (int k = 0; k < PHC_KERNEL_KINDS; ++k) {
     r->last.kernel_ms[k] = timer.ms[k];
     r->last.kernel_count[k] = timer.count[k];
   }

@@ -12,8 +12,9 @@ namespace {
 // would use (dimension 1 + iteration), whose state after the tracking goes
 // with the result.  Tracking loops differ in length from path to path; in a
 // kernel of their own they no longer hold the lanes of the shading code.
+// lookups (or nullptr): density lookups made, added up over the grid.
 __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restrict__ rcp, DevScene sc, PathSoA in,
-    const float4 *__restrict__ hits, WaveCounters wc, int it, HitQueues hq)
+    const float4 *__restrict__ hits, WaveCounters wc, int it, HitQueues hq, unsigned long long *lookups)
 {
   if (wave_failed(wc))
     return;
@@ -27,7 +28,7 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
   VolTrack s;
   Rng rng(1u);
   bool busy = false, exhausted = false;
-  uint32_t idx = 0, idle = WARP_FULL;
+  uint32_t idx = 0, idle = WARP_FULL, nlook = 0;
   for (uint32_t trips = 0;; ++trips) {
     if (trips >= wc.trip_cap) { // warp-uniform
       if (lane == 0)
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
       continue;
     }
     if (busy) {
-      vt_step<true>(sc, s, rng);
+      nlook += vt_step<true>(sc, s, rng) ? 1u : 0u;
       if (s.done) {
         hq.vscatter[idx] = make_float4(s.t_event, s.albedo.x, s.albedo.y, s.albedo.z);
         hq.vrng[idx] = rng.s;
@@ -70,14 +71,20 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
     __syncwarp(); // every lane back from the step's divergent work before the vote
     idle = __ballot_sync(WARP_FULL, !busy);
   }
+  if (lookups) { // the loop ends for the whole warp at once
+    const uint32_t w = __reduce_add_sync(WARP_FULL, nlook);
+    if (lane == 0)
+      atomicAdd(lookups, (unsigned long long)w);
+  }
 }
 
 } // namespace
 
 void launch_vol_scatter(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,
-    const float4 *hits, WaveCounters wc, int it, HitQueues hq)
+    const float4 *hits, WaveCounters wc, int it, HitQueues hq, uint64_t *lookups)
 {
-  k_vol_scatter<<<c.blocks_trace, 128, 0, s>>>(rc, sc, in, hits, wc, it, hq);
+  k_vol_scatter<<<c.blocks_trace, 128, 0, s>>>(rc, sc, in, hits, wc, it, hq,
+      reinterpret_cast<unsigned long long *>(lookups));
 }
 
 void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in, PathSoA out,

@@ -324,17 +324,17 @@ PHC_HD void vt_next_cell(const DevScene &sc, VolTrack &s)
 }
 
 // Advances the ray to its next density lookup and makes it; sets s.done when
-// the tracking is over.
+// the tracking is over.  Returns whether it made a lookup.
 template <bool SCATTER>
-PHC_HD void vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
+PHC_HD bool vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
 {
   for (int pass = 0; pass < 4096 + 64; ++pass) { // bounded work per call (a pass ends a cell or a volume)
     if (s.done)
-      return;
+      return false;
     if (!s.in_vol) { // enter the next volume the segment crosses
       if (s.vi >= sc.volume_count) {
         s.done = true;
-        return;
+        return false;
       }
       const DevVolume &v = sc.volumes[s.vi];
       if (v.majorant <= 0.f || v.tf_size == 0) {
@@ -425,9 +425,10 @@ PHC_HD void vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
         }
       }
     }
-    return;
+    return true;
   }
   // a long run of empty cells: the state is kept and the next call resumes it
+  return false;
 }
 
 } // namespace phc

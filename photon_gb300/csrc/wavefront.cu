@@ -542,9 +542,10 @@ __global__ void __launch_bounds__(128) k_shadow(const RenderConst *__restrict__ 
 // The unoccluded shadow rays of volume scenes (tmax >= 0 after k_shadow):
 // contribution times the ratio-tracking transmittance of the volumes along
 // [0, tmax] (stream dimension 0x10000 + iteration), added to the path's slot.
+// lookups (or nullptr): density lookups made, added up over the grid.
 template <bool BATCH>
 __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__restrict__ rcp, DevScene sc,
-    BatchTable bt, ShadowSoA sh, Accum acc_param, WaveCounters wc, int it)
+    BatchTable bt, ShadowSoA sh, Accum acc_param, WaveCounters wc, int it, unsigned long long *lookups)
 {
   if (wave_failed(wc))
     return;
@@ -559,7 +560,7 @@ __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__rest
   VolTrack s;
   Rng rng(1u);
   bool busy = false, exhausted = false;
-  uint32_t idx = 0, job = 0, idle = WARP_FULL;
+  uint32_t idx = 0, job = 0, idle = WARP_FULL, nlook = 0;
   for (uint32_t trips = 0;; ++trips) {
     if (trips >= wc.trip_cap) { // warp-uniform
       if (lane == 0)
@@ -596,7 +597,7 @@ __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__rest
     }
     if (busy) {
       const DevScene &S = BATCH ? bt.jobs[job].sc : sc;
-      vt_step<false>(S, s, rng);
+      nlook += vt_step<false>(S, s, rng) ? 1u : 0u;
       if (s.done) {
         busy = false;
         const Accum &acc = BATCH ? bt.jobs[job].acc : acc_param;
@@ -614,6 +615,11 @@ __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__rest
     }
     __syncwarp(); // every lane back from the step's divergent work before the vote
     idle = __ballot_sync(WARP_FULL, !busy);
+  }
+  if (lookups) { // the loop ends for the whole warp at once
+    const uint32_t w = __reduce_add_sync(WARP_FULL, nlook);
+    if (lane == 0)
+      atomicAdd(lookups, (unsigned long long)w);
   }
 }
 
@@ -768,8 +774,13 @@ void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, De
     k_shadow<true, false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, stats, r);
   else
     k_shadow<false, false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it, nullptr, r);
-  if (sc.volume_count > 0)
-    k_shadow_volume<false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, none, sh, acc, wc, it);
+}
+
+void launch_shadow_volume(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh,
+    Accum acc, WaveCounters wc, int it, uint64_t *lookups)
+{
+  k_shadow_volume<false><<<c.blocks_trace, 128, 0, s>>>(rc, sc, BatchTable{}, sh, acc, wc, it,
+      reinterpret_cast<unsigned long long *>(lookups));
 }
 
 void launch_raygen_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA out, WaveCounters wc)
@@ -820,7 +831,7 @@ void launch_shadow_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, Shad
   const uint32_t r = uint32_t(refill < 1 ? 1 : (refill > 32 ? 32 : refill));
   k_shadow<false, true><<<c.blocks_trace, 128, 0, s>>>(nullptr, DevScene{}, bt, sh, Accum{}, wc, it, nullptr, r);
   if (volumes)
-    k_shadow_volume<true><<<c.blocks_trace, 128, 0, s>>>(nullptr, DevScene{}, bt, sh, Accum{}, wc, it);
+    k_shadow_volume<true><<<c.blocks_trace, 128, 0, s>>>(nullptr, DevScene{}, bt, sh, Accum{}, wc, it, nullptr);
 }
 
 void launch_wave_end(cudaStream_t s, const RenderConst *rc, Accum acc, WaveCounters wc, uint32_t npix, int adaptive,

@@ -196,10 +196,15 @@ void launch_shade_class(const LaunchCfg &c, cudaStream_t s, const RenderConst *r
     PathSoA out, const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, uint32_t cls, HitQueues hq);
 // Delta tracking of every path of iteration `it` through the scene's volumes
 // (the first step of pt_shade for volume scenes), into hq.vscatter / hq.vrng.
+// lookups (or nullptr): the density lookups are added to it.
 void launch_vol_scatter(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,
-    const float4 *hits, WaveCounters wc, int it, HitQueues hq);
+    const float4 *hits, WaveCounters wc, int it, HitQueues hq, uint64_t *lookups);
 void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh, Accum acc,
     WaveCounters wc, int it, uint64_t *stats, int refill);
+// Volume scenes, after launch_shadow: ratio-tracking transmittance of the
+// unoccluded shadow rays times their contribution, into the pixel slots.
+void launch_shadow_volume(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh,
+    Accum acc, WaveCounters wc, int it, uint64_t *lookups);
 // Counting sort of iteration it's hit queue by material (when hcount[it] >=
 // hq.sort_threshold): bins = 2 * MAT_SORT_BINS words of scratch.
 void launch_material_sort(const LaunchCfg &c, cudaStream_t s, DevScene sc, const float4 *hits, HitQueues hq,

@@ -92,7 +92,7 @@ def test_tuning_round_trip(photon):
 
 def test_entry_points_reject_bad_arguments_without_gpu(photon):
     lib = photon.load()
-    assert lib.phc_abi_version() == 1
+    assert lib.phc_abi_version() == 2
     assert lib.phc_create(None) == -1                      # PHC_ERR_INVALID
     assert lib.phc_set_scene(None, None) == -1
     assert lib.phc_render(None, None, None, 1) == -1
