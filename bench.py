@@ -183,7 +183,7 @@ def barrier(world):
         dist.barrier()
 
 
-def scene_configs(p, reps=1):
+def scene_configs(p, reps=1, only=None, spp=0):
     """The other single-GPU forward configurations, one render each after a
     warm-up, device time: the box room (about 36 triangles, 512^2, 64 spp,
     depth 8) and the 2M-triangle instanced scene (12 RGBA8 2048^2 noise
@@ -192,7 +192,11 @@ def scene_configs(p, reps=1):
     from photon_gb300 import workloads
     out = {}
     for name, make in (("box_room_512", workloads.box_room), ("instanced_2m_1920", workloads.instanced_2m)):
+        if only and name != only:
+            continue
         sc, cam, st = make()
+        if spp:
+            st.pixel_samples = spp
         _log(f"configs: {name} generated")
         r = p.Renderer()
         t = time.perf_counter()
@@ -875,7 +879,19 @@ def main():
                     help="skip the Level-A comparison with the reference's Kokkos BVH back-end restated for the GPU")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the box-room and 2M-triangle instanced configurations")
+    ap.add_argument("--config-only", default="", choices=["", "box_room_512", "instanced_2m_1920"],
+                    help="render only this configuration (one warm-up and one timed render) and print its record "
+                         "(profiling a small case; not a bench line)")
+    ap.add_argument("--config-spp", type=int, default=0, help="samples per pixel of --config-only")
     args = ap.parse_args()
+    if args.config_only:
+        import torch
+        torch.cuda.set_device(0)
+        from photon_gb300 import build as pbuild
+        pbuild.build()
+        import photon_gb300 as p
+        print(json.dumps(scene_configs(p, only=args.config_only, spp=args.config_spp)), flush=True)
+        return
     world, rank, local = dist_setup(args.gpus if args.impl == "ours" else 0)
     if args.impl == "reference":
         run_reference(args, world, rank)
