@@ -527,7 +527,15 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
    read at the next scene upload), "gpu_bvh" (0/1: build the BVH8 of
    single-level scenes on the GPU, leaves of one triangle, read at the next
    scene upload), "batch_wave_paths", "use_graph" (0/1),
-   "count_traversal" (0/1), "time_kernels" (0/1).  Returns PHC_ERR_INVALID
+   "count_traversal" (0/1: node / triangle / density-lookup counters),
+   "time_kernels" (0/1), "shade_classes" (0/1: lean scenes sort the hit queue
+   by shading class and shade each class with a kernel compiled for its
+   lobes), "texels_u8" (0/1: keep samplers whose texels are all k / 255 as
+   8-bit RGBA, read at the next scene upload), "gpu_tables" (0/1: build the
+   volume majorant grids on the GPU, read at the next scene upload),
+   "vol_refill" (a volume-tracking warp takes new rays once this many lanes
+   are idle), "wave_trip_cap" (loop trips after which a persistent warp stops
+   with PHC_ERR_DEVICE; a self-check).  Returns PHC_ERR_INVALID
    for an unknown key or out-of-range value; get returns -1 for an unknown
    key.  Settings are process-wide and read at the start of each call. */
 int phc_tuning_set(const char *key, int64_t value);

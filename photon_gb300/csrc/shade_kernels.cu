@@ -19,8 +19,9 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
   if (wave_failed(wc))
     return;
   // persistent warps with refill: a lane whose ray is done takes a new one
-  // once VOL_REFILL lanes of its warp are idle; every step is one density
-  // lookup of every busy lane (vt_step)
+  // once wc.vol_refill lanes of its warp are idle; every trip is one pass of
+  // every busy lane's tracking (vt_pass: a macro-cell step or a density
+  // lookup)
   const uint32_t n = wc.count[it];
   uint32_t *fetch = wc.vfetch + 2 * it;
   const uint32_t lane = lane_id();
@@ -35,7 +36,7 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
         atomicCAS(wc.error, 0u, (WAVE_ERR_VOLUME << 16) | uint32_t(it));
       break;
     }
-    if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= VOL_REFILL)) {
+    if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= wc.vol_refill)) {
       __syncwarp();
       const uint32_t k = uint32_t(__popc(idle));
       const uint32_t base = warp_fetch(fetch, k);
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
       continue;
     }
     if (busy) {
-      nlook += vt_step<true>(sc, s, rng) ? 1u : 0u;
+      nlook += vt_pass<true>(sc, s, rng) == VT_LOOKUP ? 1u : 0u;
       if (s.done) {
         hq.vscatter[idx] = make_float4(s.t_event, s.albedo.x, s.albedo.y, s.albedo.z);
         hq.vrng[idx] = rng.s;

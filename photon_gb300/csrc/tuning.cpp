@@ -33,6 +33,7 @@ const Key *keys(size_t &n)
       {"max_leaf", "PHC_TUNE_MAX_LEAF", 1, 3, nullptr, &g_tuning.max_leaf},
       {"time_kernels", "PHC_TUNE_TIME_KERNELS", 0, 1, nullptr, &g_tuning.time_kernels},
       {"trace_refill", "PHC_TUNE_TRACE_REFILL", 1, 32, nullptr, &g_tuning.trace_refill},
+      {"vol_refill", "PHC_TUNE_VOL_REFILL", 1, 32, nullptr, &g_tuning.vol_refill},
       {"split_shade", "PHC_TUNE_SPLIT_SHADE", 0, 1, nullptr, &g_tuning.split_shade},
       {"shade_lean", "PHC_TUNE_SHADE_LEAN", 0, 1, nullptr, &g_tuning.shade_lean},
       {"shade_classes", "PHC_TUNE_SHADE_CLASSES", 0, 1, nullptr, &g_tuning.shade_classes},

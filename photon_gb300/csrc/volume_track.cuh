@@ -323,30 +323,34 @@ PHC_HD void vt_next_cell(const DevScene &sc, VolTrack &s)
   ++s.visited;
 }
 
-// Advances the ray to its next density lookup and makes it; sets s.done when
-// the tracking is over.  Returns whether it made a lookup.
+// One unit of the tracking: entering a volume, setting up or leaving a
+// macro cell, or one delta-tracking step with its density lookup.  The
+// persistent kernels make one pass per lane and loop trip, so that a lane
+// walking a long run of empty cells does not hold the warp's other lanes
+// (each lane still makes its own operations and random draws in order).
+enum : int { VT_CONTINUE = 0, VT_LOOKUP = 1, VT_DONE = 2 };
 template <bool SCATTER>
-PHC_HD bool vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
+PHC_HD int vt_pass(const DevScene &sc, VolTrack &s, Rng &rng)
 {
-  for (int pass = 0; pass < 4096 + 64; ++pass) { // bounded work per call (a pass ends a cell or a volume)
+  {
     if (s.done)
-      return false;
+      return VT_DONE;
     if (!s.in_vol) { // enter the next volume the segment crosses
       if (s.vi >= sc.volume_count) {
         s.done = true;
-        return false;
+        return VT_DONE;
       }
       const DevVolume &v = sc.volumes[s.vi];
       if (v.majorant <= 0.f || v.tf_size == 0) {
         ++s.vi;
-        continue;
+        return VT_CONTINUE;
       }
       s.org = vol_point(v, s.ro);
       s.dir = vol_vector(v, s.rd);
       float t0 = s.tmin, t1 = SCATTER ? s.t_limit : s.tmax;
       if (!vol_clip(v, s.org, s.dir, t0, t1)) {
         ++s.vi;
-        continue;
+        return VT_CONTINUE;
       }
       // the macro-cell walk of vol_track, from t0
       const float o[3] = {s.org.x, s.org.y, s.org.z}, d[3] = {s.dir.x, s.dir.y, s.dir.z};
@@ -385,7 +389,7 @@ PHC_HD bool vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
     if (!s.cell_ready) { // the top of vol_track's outer loop
       if (s.visited >= 4096) {
         vt_end_volume<SCATTER>(s, -1.f, V3{0.f, 0.f, 0.f});
-        continue;
+        return s.done ? VT_DONE : VT_CONTINUE;
       }
       s.axis = s.t_next[0] < s.t_next[1] ? (s.t_next[0] < s.t_next[2] ? 0 : 2) : (s.t_next[1] < s.t_next[2] ? 1 : 2);
       const float tn = s.axis == 0 ? s.t_next[0] : (s.axis == 1 ? s.t_next[1] : s.t_next[2]);
@@ -395,19 +399,20 @@ PHC_HD bool vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
       s.cell_ready = true;
       if (!(s.bound > 0.f)) {
         vt_next_cell<SCATTER>(sc, s);
-        continue;
+        return s.done ? VT_DONE : VT_CONTINUE;
       }
       s.inv_bound = 1.f / s.bound;
+      return VT_CONTINUE;
     }
     // one delta-tracking step of the cell
     if (s.lookups >= 8192) {
       vt_next_cell<SCATTER>(sc, s);
-      continue;
+      return s.done ? VT_DONE : VT_CONTINUE;
     }
     s.t -= m_log(1.f - rng.next()) * s.inv_bound;
     if (s.t >= s.t_exit) {
       vt_next_cell<SCATTER>(sc, s);
-      continue;
+      return s.done ? VT_DONE : VT_CONTINUE;
     }
     ++s.lookups;
     const float4 c = vol_classify(sc, v, s.org + s.dir * s.t);
@@ -425,9 +430,22 @@ PHC_HD bool vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
         }
       }
     }
-    return true;
+    return VT_LOOKUP;
   }
-  // a long run of empty cells: the state is kept and the next call resumes it
+}
+
+// Advances the ray to its next density lookup and makes it (passes until a
+// lookup, at most 4096 + 64 per call: a longer run of empty cells resumes at
+// the next call); sets s.done when the tracking is over.  Returns whether it
+// made a lookup.
+template <bool SCATTER>
+PHC_HD bool vt_step(const DevScene &sc, VolTrack &s, Rng &rng)
+{
+  for (int pass = 0; pass < 4096 + 64; ++pass) {
+    const int r = vt_pass<SCATTER>(sc, s, rng);
+    if (r != VT_CONTINUE)
+      return r == VT_LOOKUP;
+  }
   return false;
 }
 

@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__rest
   // the unoccluded shadow rays (tmax >= 0) of the iteration: ratio-tracking
   // transmittance (stream dimension 0x10000 + iteration) times the NEE
   // contribution into the path's pixel slot; persistent warps with refill,
-  // one density lookup per busy lane and step, as in k_vol_scatter
+  // one tracking pass per busy lane and trip, as in k_vol_scatter
   const uint32_t n = wc.scount[it];
   uint32_t *fetch = wc.vfetch + 2 * it + 1;
   const uint32_t lane = lane_id();
@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__rest
         atomicCAS(wc.error, 0u, (WAVE_ERR_VOLUME << 16) | uint32_t(it));
       break;
     }
-    if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= VOL_REFILL)) {
+    if (!exhausted && (idle == WARP_FULL || uint32_t(__popc(idle)) >= wc.vol_refill)) {
       __syncwarp();
       const uint32_t k = uint32_t(__popc(idle));
       const uint32_t base = warp_fetch(fetch, k);
@@ -597,7 +597,7 @@ __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__rest
     }
     if (busy) {
       const DevScene &S = BATCH ? bt.jobs[job].sc : sc;
-      nlook += vt_step<false>(S, s, rng) ? 1u : 0u;
+      nlook += vt_pass<false>(S, s, rng) == VT_LOOKUP ? 1u : 0u;
       if (s.done) {
         busy = false;
         const Accum &acc = BATCH ? bt.jobs[job].acc : acc_param;

@@ -77,6 +77,7 @@ struct WaveCounters {
   uint32_t *error;   // sticky error word
   uint32_t *dbg;     // [WAVE_DBG_WORDS] record of the first self-check failure
   uint32_t trip_cap; // loop trips after which a persistent warp stops (tuning key wave_trip_cap)
+  uint32_t vol_refill; // a volume-tracking warp takes new rays once this many lanes are idle (tuning key vol_refill)
 };
 inline size_t wave_counter_words(int max_iter) { return size_t((10 + SHADE_CLASSES) * max_iter + 1); }
 
@@ -89,8 +90,6 @@ inline size_t wave_counter_words(int max_iter) { return size_t((10 + SHADE_CLASS
 constexpr uint32_t WAVE_TRIP_CAP = 1u << 24;
 __device__ __forceinline__ bool wave_failed(const WaveCounters &wc) { return *(volatile uint32_t *)wc.error != 0u; }
 enum : uint32_t { WAVE_ERR_TRACE = 1u, WAVE_ERR_SHADOW = 2u, WAVE_ERR_VOLUME = 3u };
-// A volume-tracking warp takes new rays once this many of its lanes are idle.
-constexpr uint32_t VOL_REFILL = 8u;
 // dbg words: queue length, fetch counter, busy ballot, exhausted, then for
 // the warp's first busy lane: ray index, origin xyz, tmax, direction xyz,
 // stack depth, group base, group hits, group internal mask, steps of the ray.
