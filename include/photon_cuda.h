@@ -534,7 +534,8 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
    8-bit RGBA, read at the next scene upload), "gpu_tables" (0/1: build the
    volume majorant grids on the GPU, read at the next scene upload),
    "vol_refill" (a volume-tracking warp takes new rays once this many lanes
-   are idle), "wave_trip_cap" (loop trips after which a persistent warp stops
+   are idle), "vol_passes" (volume tracking: at most this many macro-cell
+   steps or lookups per lane and loop trip), "wave_trip_cap" (loop trips after which a persistent warp stops
    with PHC_ERR_DEVICE; a self-check).  Returns PHC_ERR_INVALID
    for an unknown key or out-of-range value; get returns -1 for an unknown
    key.  Settings are process-wide and read at the start of each call. */

@@ -319,6 +319,7 @@ WaveCounters wave_counters(phc_renderer *r, int max_iter)
   wc.dbg = c + wave_counter_words(max_iter) + 4;
   wc.trip_cap = uint32_t(tuning().wave_trip_cap);
   wc.vol_refill = uint32_t(tuning().vol_refill);
+  wc.vol_passes = uint32_t(tuning().vol_passes);
   return wc;
 }
 // Bytes of the counters reset at the start of every wave (not wave / error).
@@ -637,7 +638,7 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
       uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32),
       uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16) |
           (uint64_t(tu.shade_classes) << 23) | (uint64_t(tu.sort_threshold) << 24),
-      r->buf_gen, uint64_t(tu.wave_trip_cap) | (uint64_t(tu.vol_refill) << 40)};
+      r->buf_gen, uint64_t(tu.wave_trip_cap) | (uint64_t(tu.vol_refill) << 32) | (uint64_t(tu.vol_passes) << 40)};
   uint64_t launches = 0;
   KernelTimer timer;
   if (tu.time_kernels) {

@@ -19,9 +19,9 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
   if (wave_failed(wc))
     return;
   // persistent warps with refill: a lane whose ray is done takes a new one
-  // once wc.vol_refill lanes of its warp are idle; every trip is one pass of
-  // every busy lane's tracking (vt_pass: a macro-cell step or a density
-  // lookup)
+  // once wc.vol_refill lanes of its warp are idle; every trip is at most
+  // wc.vol_passes passes of every busy lane's tracking (vt_pass: a macro-cell
+  // step or a density lookup), ending at its next lookup
   const uint32_t n = wc.count[it];
   uint32_t *fetch = wc.vfetch + 2 * it;
   const uint32_t lane = lane_id();
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
       continue;
     }
     if (busy) {
-      nlook += vt_pass<true>(sc, s, rng) == VT_LOOKUP ? 1u : 0u;
+      nlook += vt_passes<true>(sc, s, rng, wc.vol_passes) == VT_LOOKUP ? 1u : 0u;
       if (s.done) {
         hq.vscatter[idx] = make_float4(s.t_event, s.albedo.x, s.albedo.y, s.albedo.z);
         hq.vrng[idx] = rng.s;

@@ -34,6 +34,7 @@ const Key *keys(size_t &n)
       {"time_kernels", "PHC_TUNE_TIME_KERNELS", 0, 1, nullptr, &g_tuning.time_kernels},
       {"trace_refill", "PHC_TUNE_TRACE_REFILL", 1, 32, nullptr, &g_tuning.trace_refill},
       {"vol_refill", "PHC_TUNE_VOL_REFILL", 1, 32, nullptr, &g_tuning.vol_refill},
+      {"vol_passes", "PHC_TUNE_VOL_PASSES", 1, 1 << 16, nullptr, &g_tuning.vol_passes},
       {"split_shade", "PHC_TUNE_SPLIT_SHADE", 0, 1, nullptr, &g_tuning.split_shade},
       {"shade_lean", "PHC_TUNE_SHADE_LEAN", 0, 1, nullptr, &g_tuning.shade_lean},
       {"shade_classes", "PHC_TUNE_SHADE_CLASSES", 0, 1, nullptr, &g_tuning.shade_classes},

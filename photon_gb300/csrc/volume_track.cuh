@@ -323,11 +323,12 @@ PHC_HD void vt_next_cell(const DevScene &sc, VolTrack &s)
   ++s.visited;
 }
 
-// One unit of the tracking: entering a volume, setting up or leaving a
-// macro cell, or one delta-tracking step with its density lookup.  The
-// persistent kernels make one pass per lane and loop trip, so that a lane
-// walking a long run of empty cells does not hold the warp's other lanes
-// (each lane still makes its own operations and random draws in order).
+// One unit of the tracking: entering a volume, leaving a macro cell or
+// stepping over an empty one, or one delta-tracking step with its density
+// lookup (after setting up its cell).  The persistent kernels make at most
+// a few passes per lane and loop trip (vt_passes), so that a lane walking a
+// long run of empty cells does not hold the warp's other lanes (each lane
+// still makes its own operations and random draws in order).
 enum : int { VT_CONTINUE = 0, VT_LOOKUP = 1, VT_DONE = 2 };
 template <bool SCATTER>
 PHC_HD int vt_pass(const DevScene &sc, VolTrack &s, Rng &rng)
@@ -402,7 +403,6 @@ PHC_HD int vt_pass(const DevScene &sc, VolTrack &s, Rng &rng)
         return s.done ? VT_DONE : VT_CONTINUE;
       }
       s.inv_bound = 1.f / s.bound;
-      return VT_CONTINUE;
     }
     // one delta-tracking step of the cell
     if (s.lookups >= 8192) {
@@ -432,6 +432,17 @@ PHC_HD int vt_pass(const DevScene &sc, VolTrack &s, Rng &rng)
     }
     return VT_LOOKUP;
   }
+}
+
+// Up to max_passes passes, stopping at a density lookup or the end of the
+// tracking; returns the last pass's result.
+template <bool SCATTER>
+PHC_HD int vt_passes(const DevScene &sc, VolTrack &s, Rng &rng, uint32_t max_passes)
+{
+  int r = VT_CONTINUE;
+  for (uint32_t k = 0; k < max_passes && r == VT_CONTINUE; ++k)
+    r = vt_pass<SCATTER>(sc, s, rng);
+  return r;
 }
 
 // Advances the ray to its next density lookup and makes it (passes until a

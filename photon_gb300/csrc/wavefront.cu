@@ -597,7 +597,7 @@ __global__ void __launch_bounds__(128) k_shadow_volume(const RenderConst *__rest
     }
     if (busy) {
       const DevScene &S = BATCH ? bt.jobs[job].sc : sc;
-      nlook += vt_pass<false>(S, s, rng) == VT_LOOKUP ? 1u : 0u;
+      nlook += vt_passes<false>(S, s, rng, wc.vol_passes) == VT_LOOKUP ? 1u : 0u;
       if (s.done) {
         busy = false;
         const Accum &acc = BATCH ? bt.jobs[job].acc : acc_param;

@@ -78,6 +78,7 @@ struct WaveCounters {
   uint32_t *dbg;     // [WAVE_DBG_WORDS] record of the first self-check failure
   uint32_t trip_cap; // loop trips after which a persistent warp stops (tuning key wave_trip_cap)
   uint32_t vol_refill; // a volume-tracking warp takes new rays once this many lanes are idle (tuning key vol_refill)
+  uint32_t vol_passes; // tracking passes per lane and loop trip at most (tuning key vol_passes)
 };
 inline size_t wave_counter_words(int max_iter) { return size_t((10 + SHADE_CLASSES) * max_iter + 1); }
 
