@@ -21,7 +21,7 @@ struct Tuning {
   int time_kernels{0};               // CUDA events around every launch (no graph), per-kind times
   int trace_refill{8};               // closest-hit warps refill once this many lanes idle (32: never)
   int vol_refill{8};                 // volume-tracking warps refill once this many lanes idle
-  int vol_passes{4};                 // volume tracking: passes per lane and loop trip at most
+  int vol_passes{1};                 // volume tracking: passes per lane and loop trip at most
   int split_shade{1};                // misses and hits shaded by separate kernels (no-volume scenes)
   int shade_lean{1};                 // lean shading kernels for scenes without volumes/sources/lights
   int shade_classes{1};              // lean scenes: hit queue sorted by shading class, one kernel per class
