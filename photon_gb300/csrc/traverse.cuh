@@ -95,31 +95,11 @@ PHC_HD float byte_f(uint32_t w, int j)
 }
 
 #ifdef __CUDA_ARCH__
-// Paired fp32 arithmetic (sm_100+ .f32x2 forms): each element is rounded
-// exactly as the scalar instruction would round it, so the box tests below
-// make the same decisions as the host restatement with half the issue slots.
-__device__ __forceinline__ unsigned long long pk2(float lo, float hi)
-{
-  unsigned long long r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void upk2(unsigned long long v, float &lo, float &hi)
-{
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b)
-{
-  unsigned long long r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
-{
-  unsigned long long r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
+// Paired fp32 arithmetic (sm_100+ FADD2 / FFMA2 through __fadd2_rn /
+// __ffma2_rn on float2): each element is rounded exactly as the scalar
+// instruction would round it, so the box tests below make the same
+// decisions as the host restatement with half the issue slots.  Three-input
+// min / max in one instruction:
 __device__ __forceinline__ float max3f(float a, float b, float c)
 {
   float r;
@@ -174,11 +154,11 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
   tri_hits = 0u;
   uint32_t slots = 0u; // SLOTS: bit s set when the ray overlaps child box s
 #ifdef __CUDA_ARCH__
-  // (near, far) of one axis as a pair: q = (2^23 + byte) - 2^23 exactly, then
-  // t = fma(q, a, b) per element.
-  const unsigned long long m23 = pk2(-8388608.f, -8388608.f);
-  const unsigned long long ax2 = pk2(ax, ax), ay2 = pk2(ay, ay), az2 = pk2(az, az);
-  const unsigned long long bx2 = pk2(bx, bx), by2 = pk2(by, by), bz2 = pk2(bz, bz);
+  // (near, far) of one axis as a float2: q = (2^23 + byte) - 2^23 exactly,
+  // then t = fma(q, a, b) per element.
+  const float2 m23 = make_float2(-8388608.f, -8388608.f);
+  const float2 ax2 = make_float2(ax, ax), ay2 = make_float2(ay, ay), az2 = make_float2(az, az);
+  const float2 bx2 = make_float2(bx, bx), by2 = make_float2(by, by), bz2 = make_float2(bz, bz);
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const uint32_t m4 = h ? w1.w : w1.z;
@@ -188,10 +168,10 @@ PHC_HD void intersect_node(const uint4 *__restrict__ nodes, uint32_t ni, V3 o, V
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const uint32_t mb = (m4 >> (8 * j)) & 0xffu;
-      float tnx, tfx, tny, tfy, tnz, tfz;
-      upk2(fma2(add2(pk2(byte_f23(nxw, j), byte_f23(fxw, j)), m23), ax2, bx2), tnx, tfx);
-      upk2(fma2(add2(pk2(byte_f23(nyw, j), byte_f23(fyw, j)), m23), ay2, by2), tny, tfy);
-      upk2(fma2(add2(pk2(byte_f23(nzw, j), byte_f23(fzw, j)), m23), az2, bz2), tnz, tfz);
+      const float2 tx = __ffma2_rn(__fadd2_rn(make_float2(byte_f23(nxw, j), byte_f23(fxw, j)), m23), ax2, bx2);
+      const float2 ty = __ffma2_rn(__fadd2_rn(make_float2(byte_f23(nyw, j), byte_f23(fyw, j)), m23), ay2, by2);
+      const float2 tz = __ffma2_rn(__fadd2_rn(make_float2(byte_f23(nzw, j), byte_f23(fzw, j)), m23), az2, bz2);
+      const float tnx = tx.x, tfx = tx.y, tny = ty.x, tfy = ty.y, tnz = tz.x, tfz = tz.y;
       const float t0 = fmaxf(max3f(tnx, tny, tnz), tmin);
       const float t1 = fminf(min3f(tfx, tfy, tfz), tmax);
       if constexpr (SLOTS) {
