@@ -532,7 +532,9 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
    by shading class and shade each class with a kernel compiled for its
    lobes), "texels_u8" (0/1: keep samplers whose texels are all k / 255 as
    8-bit RGBA, read at the next scene upload), "gpu_tables" (0/1: build the
-   volume majorant grids on the GPU, read at the next scene upload),
+   volume majorant grids, the environment and emissive CDFs with their
+   search guides, and the 8-bit texels on the GPU, equal to the host-built
+   tables bit for bit; read at the next scene upload),
    "vol_refill" (a volume-tracking warp takes new rays once this many lanes
    are idle), "vol_passes" (volume tracking: at most this many macro-cell
    steps or lookups per lane and loop trip), "wave_trip_cap" (loop trips after which a persistent warp stops

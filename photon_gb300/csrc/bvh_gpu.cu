@@ -18,9 +18,11 @@
 //      area are broken by the pair's indices, so the globally smallest pair
 //      is always mutual and every iteration merges;
 //   4. the binary tree collapsed into the 8-wide quantised nodes level by
-//      level, each node taking the up to eight descendants of largest area,
-//      the octant slot order and the outward-rounded 8-bit child grid of the
-//      host builder.
+//      level, each node taking the up to eight descendants of largest area
+//      (subtrees of more than max_leaf primitives opened first), the octant
+//      slot order and the outward-rounded 8-bit child grid of the host
+//      builder; a descendant with at most max_leaf primitives (1..3) is one
+//      leaf child.
 //
 // The result is deterministic except for where nodes and leaf records land
 // in memory (atomic allocation order), which changes no traversal result.
@@ -315,7 +317,32 @@ struct Collapse {
   float4 *tris;        // 3 per triangle record
   uint32_t *counters;  // [0] nodes, [1] triangle records, [2] next queue length, [3] overflow
   uint32_t node_cap;
+  int max_leaf;        // triangles per leaf child (1..3)
 };
+
+// The primitives of BVH2 subtree v when it has at most `limit` leaves (at
+// most 3): their count, with the primitives in `prims` in left-to-right
+// order; limit + 1 when it has more.
+__device__ int subtree_prims(const int2 *__restrict__ nchild, int v, int limit, int *prims)
+{
+  int stack[4], sp = 0, n = 0;
+  stack[sp++] = v;
+  while (sp > 0) {
+    const int u = stack[--sp];
+    const int2 c = nchild[u];
+    if (c.x < 0) {
+      if (n == limit)
+        return limit + 1;
+      prims[n++] = c.y;
+    } else {
+      if (sp + 2 > 4)
+        return limit + 1;
+      stack[sp++] = c.y;
+      stack[sp++] = c.x;
+    }
+  }
+  return n;
+}
 
 __device__ __forceinline__ float node_area(const float *nbox, int v)
 {
@@ -340,15 +367,22 @@ __global__ void __launch_bounds__(128) k_collapse(Collapse c, const uint2 *__res
     ch[k++] = c.nchild[root].x;
     ch[k++] = c.nchild[root].y;
   }
-  while (k < 8) { // open the internal child of largest area
+  // small[i]: internal child i has at most max_leaf primitives (it becomes
+  // one leaf child unless a free slot opens it)
+  int prims[3];
+  auto small = [&](int v) { return c.max_leaf > 1 && subtree_prims(c.nchild, v, c.max_leaf, prims) <= c.max_leaf; };
+  while (k < 8) { // open the internal child of largest area, larger subtrees first
     int best = -1;
     float best_a = -1.f;
+    bool best_small = true;
     for (int i = 0; i < k; ++i)
       if (c.nchild[ch[i]].x >= 0) {
         const float a = node_area(c.nbox, ch[i]);
-        if (a > best_a) {
+        const bool sm = small(ch[i]);
+        if (best < 0 || (best_small && !sm) || (sm == best_small && a > best_a)) {
           best_a = a;
           best = i;
+          best_small = sm;
         }
       }
     if (best < 0)
@@ -418,16 +452,27 @@ __global__ void __launch_bounds__(128) k_collapse(Collapse c, const uint2 *__res
     e[a] = uint8_t(ex + 127);
     scale[a] = ex == -127 ? 0.0 : ldexp(1.0, ex);
   }
+  // leaf children: single primitives, and internal children of at most
+  // max_leaf primitives (lcount[s] primitives each)
   uint32_t internal = 0, leaves = 0;
   uint8_t imask = 0;
+  int lcount[8];
   for (int s = 0; s < 8; ++s) {
+    lcount[s] = 0;
     if (child_at[s] < 0)
       continue;
-    if (c.nchild[child_at[s]].x >= 0) {
+    const int v = child_at[s];
+    if (c.nchild[v].x < 0)
+      lcount[s] = 1;
+    else if (c.max_leaf > 1) {
+      const int m = subtree_prims(c.nchild, v, c.max_leaf, prims);
+      lcount[s] = m <= c.max_leaf ? m : 0;
+    }
+    if (lcount[s] == 0) {
       imask |= uint8_t(1u << s);
       ++internal;
     } else {
-      ++leaves;
+      leaves += uint32_t(lcount[s]);
     }
   }
   uint32_t child_base = 0, tri_base = 0;
@@ -458,19 +503,25 @@ __global__ void __launch_bounds__(128) k_collapse(Collapse c, const uint2 *__res
       q[a][s] = uint8_t(fmin(fmax(lo, 0.0), 255.0));
       q[3 + a][s] = uint8_t(fmin(fmax(hi, 0.0), 255.0));
     }
-    if (c.nchild[v].x >= 0) {
+    if (lcount[s] == 0) {
       meta[s] = 0x80;
       qout[qo++] = make_uint2(next_child++, uint32_t(v));
     } else {
-      meta[s] = uint8_t((1u << 5) | tri_off);
-      const uint32_t prim = uint32_t(c.nchild[v].y);
-      const uint4 vi = c.vidx[prim];
-      const float4 v0 = c.pos[vi.x], v1 = c.pos[vi.y], v2 = c.pos[vi.z];
-      float4 *r = c.tris + 3 * size_t(tri_base + tri_off);
-      r[0] = make_float4(v0.x, v0.y, v0.z, __uint_as_float(prim));
-      r[1] = make_float4(v1.x - v0.x, v1.y - v0.y, v1.z - v0.z, 0.f);
-      r[2] = make_float4(v2.x - v0.x, v2.y - v0.y, v2.z - v0.z, 0.f);
-      ++tri_off;
+      meta[s] = uint8_t((uint32_t(lcount[s]) << 5) | tri_off);
+      if (c.nchild[v].x < 0)
+        prims[0] = c.nchild[v].y;
+      else
+        subtree_prims(c.nchild, v, c.max_leaf, prims);
+      for (int j = 0; j < lcount[s]; ++j) {
+        const uint32_t prim = uint32_t(prims[j]);
+        const uint4 vi = c.vidx[prim];
+        const float4 v0 = c.pos[vi.x], v1 = c.pos[vi.y], v2 = c.pos[vi.z];
+        float4 *r = c.tris + 3 * size_t(tri_base + tri_off);
+        r[0] = make_float4(v0.x, v0.y, v0.z, __uint_as_float(prim));
+        r[1] = make_float4(v1.x - v0.x, v1.y - v0.y, v1.z - v0.z, 0.f);
+        r[2] = make_float4(v2.x - v0.x, v2.y - v0.y, v2.z - v0.z, 0.f);
+        ++tri_off;
+      }
     }
   }
   uint32_t *w = c.nodes + size_t(ni) * 20;
@@ -515,7 +566,7 @@ uint32_t grid_of(uint32_t n, uint32_t block) { return std::max<uint32_t>(1u, std
 
 } // namespace
 
-GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t n, cudaStream_t s)
+GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t n, cudaStream_t s, int max_leaf)
 {
   if (n == 0)
     throw std::runtime_error("gpu bvh build: no triangles");
@@ -607,7 +658,7 @@ GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t
   const uint2 first = make_uint2(0u, root);
   ck(cudaMemcpyAsync(q[0].p, &first, sizeof(first), cudaMemcpyHostToDevice, s), "first queue entry");
   Collapse col{nbox.as<float>(), nchild.as<int2>(), positions, prim_vidx, nodes_buf.as<uint32_t>(),
-      tris_buf.as<float4>(), ctr.as<uint32_t>(), out.node_cap};
+      tris_buf.as<float4>(), ctr.as<uint32_t>(), out.node_cap, std::min(std::max(max_leaf, 1), 3)};
   uint32_t nq = 1, depth = 0;
   int qc = 0;
   while (nq > 0) {

@@ -1,6 +1,6 @@
 // GPU construction of the BVH8 (bvh_gpu.cu): Morton sort, parallel
 // locally-ordered clustering, collapse into the quantised 8-wide nodes of
-// bvh8.h with leaves of one triangle.
+// bvh8.h with leaf children of up to max_leaf triangles.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -16,7 +16,9 @@ struct GpuBvh8 {
 };
 
 // positions: float4 per vertex; prim_vidx: (i0, i1, i2, material) per
-// triangle, both on the device.  Blocks on `s` until the build is done.
-GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t triangle_count, cudaStream_t s);
+// triangle, both on the device; max_leaf: triangles per leaf child (1..3).
+// Blocks on `s` until the build is done.
+GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t triangle_count, cudaStream_t s,
+    int max_leaf = 1);
 
 } // namespace phc

@@ -216,6 +216,14 @@ bool pack_texels_u8(const float *src, size_t floats, HostScene &s)
   return ok != 0;
 }
 
+// sin(theta) of row y of an environment map of h rows, with the host C
+// library's sinf as the reference evaluates it (environment_map.cpp:31).
+static float env_row_sin(uint32_t y, uint32_t h)
+{
+  const float PI = 3.14159265358979323846f;
+  return std::sin(((float)y + 0.5f) * (PI / (float)h));
+}
+
 // EnvironmentMap::build_cdf (environment_map.cpp:8-65): row CDFs of texel
 // luminance and a marginal CDF of row sums weighted by sin(theta).
 void build_env_cdf(HostScene &s)
@@ -224,15 +232,14 @@ void build_env_cdf(HostScene &s)
   s.env_marginal.assign(h + 1, 0.f);
   s.env_conditional.assign(size_t(h) * (w + 1), 0.f);
   std::vector<float> row_w(h, 0.f);
-  const float PI = 3.14159265358979323846f;
   for (uint32_t y = 0; y < h; ++y) {
     float *c = &s.env_conditional[size_t(y) * (w + 1)];
     c[0] = 0.f;
-    const float st = std::sin(((float)y + 0.5f) * (PI / (float)h));
+    const float st = env_row_sin(y, h);
     float sum = 0.f;
     for (uint32_t x = 0; x < w; ++x) {
       const float *p = &s.env_pixels4[(size_t(y) * w + x) * 4];
-      sum += lum(p[0], p[1], p[2]);
+      sum += tbl_lum(p[0], p[1], p[2]);
       c[x + 1] = sum;
     }
     if (sum > 0.f) {
@@ -311,7 +318,7 @@ void build_search_guides(HostScene &s)
     }
     s.emissive_guide[G] = ne - 1;
   }
-  if (s.has_env && s.env_w > 0 && s.env_h > 0) {
+  if (s.has_env && s.env_w > 0 && s.env_h > 0 && !s.env_rgb) {
     const uint32_t w = s.env_w, h = s.env_h;
     bool ok = non_decreasing(s.env_marginal.data(), h + 1);
     for (uint32_t y = 0; ok && y < h; ++y)
@@ -777,6 +784,12 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     s.u8_decode.resize(256);
     for (int k = 0; k < 256; ++k)
       s.u8_decode[size_t(k)] = float(k) / 255.f;
+    // room for every sampler's texels, so that packing never moves the array
+    size_t cap = 0;
+    for (uint32_t i = 0; i < in.sampler_count; ++i)
+      cap += in.samplers[i].texels ? 4 * size_t(in.samplers[i].texel_count) : 0;
+    if (tuning().texels_u8 && !tuning().gpu_tables)
+      s.texels_u8.reserve(cap);
   }
   for (uint32_t i = 0; !pt && i < in.sampler_count; ++i) {
     const phc_sampler &sd = in.samplers[i];
@@ -796,7 +809,13 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     const size_t n = sd.texels ? size_t(sd.texel_count) : 0;
     if (si.type != 3 && n < size_t(si.size[0]) * si.size[1] * si.size[2])
       si.type = 3; // incomplete image: a transform keeps lookups in bounds
-    if (n && si.type != 3 && tuning().texels_u8 && pack_texels_u8(sd.texels, 4 * n, s)) {
+    const bool try_u8 = n && si.type != 3 && tuning().texels_u8;
+    if (try_u8 && tuning().gpu_tables) { // packed and checked by the upload
+      si.u8 = 1;
+      si.offset = uint32_t(s.texels_u8_device);
+      s.texel_pack_tasks.push_back({sd.texels, n, uint32_t(s.samplers.size()), s.texels_u8_device});
+      s.texels_u8_device += n;
+    } else if (try_u8 && pack_texels_u8(sd.texels, 4 * n, s)) {
       si.u8 = 1;
       si.offset = uint32_t(s.texels_u8.size() / 4 - n);
     } else {
@@ -829,13 +848,20 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     s.env_w = env.width;
     s.env_h = env.height;
     const size_t n = size_t(env.width) * env.height;
-    s.env_pixels4.resize(n * 4);
-    for (size_t k = 0; k < n; ++k) {
-      for (int c = 0; c < 3; ++c) {
-        const float v = env.pixels[3 * k + c];
-        s.env_pixels4[4 * k + c] = std::isfinite(v) && v > 0.f ? v : 0.f;
+    if (tuning().gpu_tables) { // texels and CDFs built by the upload
+      s.env_rgb = env.pixels;
+      s.env_row_sin.resize(env.height);
+      for (uint32_t y = 0; y < env.height; ++y)
+        s.env_row_sin[y] = env_row_sin(y, env.height);
+    } else {
+      s.env_pixels4.resize(n * 4);
+      for (size_t k = 0; k < n; ++k) {
+        for (int c = 0; c < 3; ++c) {
+          const float v = env.pixels[3 * k + c];
+          s.env_pixels4[4 * k + c] = std::isfinite(v) && v > 0.f ? v : 0.f;
+        }
+        s.env_pixels4[4 * k + 3] = 0.f;
       }
-      s.env_pixels4[4 * k + 3] = 0.f;
     }
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 3; ++c) {
@@ -844,7 +870,8 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
       }
     if (pt && pt->env_map_to_world_given) // pbrt_to_photon.cpp:455-466
       std::memcpy(s.env_t2w, pt->env_map_to_world, sizeof(s.env_t2w));
-    build_env_cdf(s);
+    if (!s.env_rgb)
+      build_env_cdf(s);
     s.has_env = true;
     s.env_visible = env.visible != 0;
   }
@@ -853,15 +880,15 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
   // and area densities (pathtracer.cpp:439-487)
   std::vector<uint32_t> ids;
   std::vector<float> areas;
-  if (!empty) {
+  const bool instanced = pt && pt->instance_count && pt->object_count;
+  s.emissive_on_gpu = !empty && !instanced && tuning().gpu_tables; // built by the upload
+  if (!empty && !s.emissive_on_gpu) {
     for (size_t t = 0; t < tc; ++t) {
       const uint32_t mid = s.material_ids[t];
-      if (!may_emit(s.materials[mid]))
+      if (!tbl_may_emit(s.materials[mid]))
         continue;
-      const F3 p0 = f3(&pos3[3 * size_t(s.indices[3 * t])]);
-      const F3 p1 = f3(&pos3[3 * size_t(s.indices[3 * t + 1])]);
-      const F3 p2 = f3(&pos3[3 * size_t(s.indices[3 * t + 2])]);
-      const float area = 0.5f * len(crs(sub(p1, p0), sub(p2, p0)));
+      const float area = tbl_tri_area(&pos3[3 * size_t(s.indices[3 * t])], &pos3[3 * size_t(s.indices[3 * t + 1])],
+          &pos3[3 * size_t(s.indices[3 * t + 2])]);
       if (!(area > 0.f))
         continue;
       ids.push_back(uint32_t(t));
@@ -873,15 +900,7 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
     std::vector<double> weights(n, 0.0);
     double total_w = 0.0;
     for (uint32_t i = 0; i < n; ++i) {
-      const DevMaterial &m = s.materials[s.material_ids[ids[i]]];
-      const bool constant = m.src_kind[SRC_EMIT] == 0;
-      const float power = constant
-          ? lum(m.emission[0] * m.emission_strength, m.emission[1] * m.emission_strength,
-                m.emission[2] * m.emission_strength)
-          : m.emission_strength;
-      weights[i] = double(areas[i]) * double(power > 1e-6f ? power : 1e-6f);
-      if (!(areas[i] > 0.f))
-        weights[i] = 0.0;
+      weights[i] = tbl_emit_weight(s.materials[s.material_ids[ids[i]]], areas[i]);
       total_w += weights[i];
     }
     if (total_w > 0.0) {
@@ -908,7 +927,6 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
   s.strategy_count = uint32_t(s.lights.size()) + (s.emissive_cdf.empty() ? 0u : 1u) + (s.has_env ? 1u : 0u);
   build_search_guides(s);
   s.scene_normals = !empty && in.normals;
-  const bool instanced = pt && pt->instance_count && pt->object_count;
   if (tuning().gpu_bvh && !instanced && !empty) {
     s.bvh_on_gpu = true; // single-level scenes: the upload builds the BVH8 on the GPU
     return;
@@ -931,7 +949,7 @@ void DeviceScene::release()
   bytes = 0;
 }
 
-template <class T> T *DeviceScene::put(const std::vector<T> &v, cudaStream_t s, std::string &err)
+template <class T, class A> T *DeviceScene::put(const std::vector<T, A> &v, cudaStream_t s, std::string &err)
 {
   if (v.empty() || !err.empty())
     return nullptr;
@@ -983,6 +1001,222 @@ float *DeviceScene::put_spans(const std::vector<float> &owned, const std::vector
   return dst;
 }
 
+template <class T> T *DeviceScene::alloc(size_t n, std::string &err, bool keep)
+{
+  if (!err.empty() || n == 0)
+    return nullptr;
+  void *p = nullptr;
+  const cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  if (keep) {
+    allocations.push_back(p);
+    bytes += n * sizeof(T);
+  }
+  return static_cast<T *>(p);
+}
+
+// The environment and emitter tables of h built on the device
+// (scene_tables.cu; h.env_rgb, h.emissive_on_gpu) into d, with the host
+// builders' arithmetic and order, so that they equal the host tables bit for
+// bit.  Reads the emitter count, the emitters' weights and the
+// monotonicity flags back (waits for the stream); sets the guides only for
+// non-decreasing CDFs, and the emitter tables only when their weights sum
+// above 0, as the host does.
+std::string DeviceScene::device_tables(const HostScene &h, DevScene &d, cudaStream_t s)
+{
+  std::string err;
+  std::vector<void *> scratch;
+  auto tmp = [&](size_t bytes_) -> void * {
+    void *p = alloc<uint8_t>(bytes_, err, false);
+    if (p)
+      scratch.push_back(p);
+    return p;
+  };
+  auto ck = [&](cudaError_t e, const char *what) {
+    if (e != cudaSuccess && err.empty())
+      err = std::string(what) + ": " + cudaGetErrorString(e);
+  };
+  uint32_t *flags = static_cast<uint32_t *>(tmp(16)); // bad, count
+  double tw = 0.0;                                       // the emitters' total weight
+  if (flags)
+    ck(cudaMemsetAsync(flags, 0, 16, s), "table flags");
+  const uint32_t w = h.env_w, eh = h.env_h;
+  uint32_t *mguide = nullptr, *cguide = nullptr;
+  if (h.env_rgb && err.empty()) {
+    EnvTablesJob j{};
+    const size_t n = size_t(w) * eh;
+    float *rgb = static_cast<float *>(tmp(n * 3 * sizeof(float)));
+    float *row_sin = static_cast<float *>(tmp(eh * sizeof(float)));
+    j.row_weight = static_cast<float *>(tmp(eh * sizeof(float)));
+    if (err.empty()) {
+      ck(cudaMemcpyAsync(rgb, h.env_rgb, n * 3 * sizeof(float), cudaMemcpyHostToDevice, s), "environment texels");
+      ck(cudaMemcpyAsync(row_sin, h.env_row_sin.data(), eh * sizeof(float), cudaMemcpyHostToDevice, s),
+          "environment rows");
+    }
+    j.rgb = rgb;
+    j.row_sin = row_sin;
+    j.w = w;
+    j.h = eh;
+    j.pixels = alloc<float4>(n, err);
+    j.conditional = alloc<float>(size_t(eh) * (w + 1), err);
+    j.marginal = alloc<float>(size_t(eh) + 1, err);
+    j.mguide = mguide = alloc<uint32_t>((1u << ENV_MGUIDE_BITS) + 1, err);
+    j.cguide = cguide = alloc<uint32_t>(size_t(eh) * ((1u << ENV_CGUIDE_BITS) + 1), err);
+    j.bad = flags;
+    if (err.empty())
+      err = launch_env_tables(j, s);
+    d.env_pixels = j.pixels;
+    d.env_conditional = j.conditional;
+    d.env_marginal = j.marginal;
+    table_floats[PHC_TABLE_ENV_MARGINAL] = size_t(eh) + 1;
+    table_floats[PHC_TABLE_ENV_CONDITIONAL] = size_t(eh) * (w + 1);
+  }
+  EmissiveJob ej{};
+  uint32_t counts[4] = {0, 0, 0, 0};
+  const uint32_t tc = uint32_t(h.prim_vidx.size() / 4);
+  if (h.emissive_on_gpu && err.empty() && tc) {
+    ej.pos = d.positions;
+    ej.vidx = d.prim_vidx;
+    ej.mats = d.materials;
+    ej.tc = tc;
+    ej.flag = static_cast<uint32_t *>(tmp(size_t(tc) * sizeof(uint32_t)));
+    ej.count = flags + 1;
+    ej.bad = flags;
+    if (err.empty())
+      err = launch_emissive_ids(ej, s);
+    if (err.empty()) {
+      ck(cudaMemcpyAsync(counts, flags, 8, cudaMemcpyDeviceToHost, s), "emitter count");
+      ck(cudaStreamSynchronize(s), "emitter count");
+    }
+    ej.n = counts[1];
+    if (ej.n && err.empty()) {
+      ej.ids = alloc<uint32_t>(ej.n, err);
+      ej.weight = static_cast<double *>(tmp(size_t(ej.n) * sizeof(double)));
+      ej.prefix = static_cast<double *>(tmp(size_t(ej.n) * sizeof(double)));
+      ej.cdf = alloc<float>(ej.n, err);
+      ej.pdf = alloc<float>(tc, err);
+      ej.guide = alloc<uint32_t>((1u << EMISSIVE_GUIDE_BITS) + 1, err);
+      if (err.empty())
+        ck(cudaMemsetAsync(ej.pdf, 0, size_t(tc) * sizeof(float), s), "emitter densities");
+      if (err.empty())
+        err = launch_emissive_weights(ej, s);
+      // the running sum of the weights is sequential in the reference's
+      // double order: one host core runs it (about 1 ns per emitter, against
+      // tens of ns for one GPU thread's dependent FP64 adds), between a read
+      // of the weights and an upload of the sums
+      std::vector<double> w(err.empty() ? ej.n : 0);
+      if (err.empty()) {
+        ck(cudaMemcpyAsync(w.data(), ej.weight, w.size() * sizeof(double), cudaMemcpyDeviceToHost, s),
+            "emitter weights");
+        ck(cudaStreamSynchronize(s), "emitter weights");
+      }
+      if (err.empty()) {
+        for (double &x : w) {
+          tw += x;
+          x = tw;
+        }
+        ck(cudaMemcpyAsync(ej.prefix, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, s),
+            "emitter sums");
+      }
+      if (err.empty())
+        err = launch_emissive_tables(ej, tw, s);
+    }
+  }
+  if (err.empty()) {
+    ck(cudaMemcpyAsync(counts, flags, 8, cudaMemcpyDeviceToHost, s), "table flags");
+    ck(cudaStreamSynchronize(s), "device tables");
+  }
+  for (void *p : scratch)
+    cudaFree(p);
+  if (!err.empty())
+    return err;
+  if (h.env_rgb) {
+    const bool ok = (counts[0] & 3u) == 0;
+    d.env_mguide = ok ? mguide : nullptr;
+    d.env_cguide = ok ? cguide : nullptr;
+  }
+  if (h.emissive_on_gpu) {
+    const bool any = ej.n > 0 && tw > 0.0;
+    d.emissive_ids = any ? ej.ids : nullptr;
+    d.emissive_cdf = any ? ej.cdf : nullptr;
+    d.prim_light_pdf = any ? ej.pdf : nullptr;
+    d.emissive_count = any ? ej.n : 0u;
+    d.emissive_guide = any && ej.n > 1 && (counts[0] & 4u) == 0 ? ej.guide : nullptr;
+    d.strategy_count = h.strategy_count + (any ? 1u : 0u);
+    table_floats[PHC_TABLE_EMISSIVE_CDF] = any ? ej.n : 0;
+    table_floats[PHC_TABLE_PRIM_LIGHT_PDF] = any ? tc : 0;
+  }
+  return std::string();
+}
+
+// The samplers of h.texel_pack_tasks: the packing kernel reads their fp32
+// texels through a staging buffer and writes the uchar4 array and a flag
+// per sampler; a sampler whose flag is set is switched to fp32 storage
+// (samplers[i].u8 = 0, its texels appended to the float4 array's spans).
+// Waits for the stream.
+const uchar4 *DeviceScene::pack_texels(const HostScene &h, std::vector<DevSampler> &samplers,
+    std::vector<HostScene::Span> &spans, const float *dec, cudaStream_t s, std::string &err)
+{
+  constexpr size_t kStage = size_t(1) << 23; // texels per staging copy (128 MiB)
+  const size_t n_tasks = h.texel_pack_tasks.size();
+  size_t most = 0;
+  for (const HostScene::TexelPackTask &t : h.texel_pack_tasks)
+    most = std::max(most, t.texels);
+  void *out = nullptr, *stage = nullptr, *bad = nullptr;
+  cudaError_t e = cudaMalloc(&out, h.texels_u8_device * sizeof(uchar4));
+  if (e == cudaSuccess) {
+    allocations.push_back(out);
+    bytes += h.texels_u8_device * sizeof(uchar4);
+    e = cudaMalloc(&bad, n_tasks * sizeof(uint32_t));
+  }
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(bad, 0, n_tasks * sizeof(uint32_t), s);
+  uchar4 *dst = static_cast<uchar4 *>(out);
+  // the caller's texels are staged (a kernel reading them in place through
+  // the host's page tables measured slower on a first upload: 4 GB/s)
+  for (size_t i = 0; i < n_tasks && e == cudaSuccess && err.empty(); ++i) {
+    const HostScene::TexelPackTask &t = h.texel_pack_tasks[i];
+    if (!stage)
+      e = cudaMalloc(&stage, std::min(most, kStage) * sizeof(float4));
+    for (size_t at = 0; at < t.texels && e == cudaSuccess && err.empty(); at += kStage) {
+      const size_t m = std::min(kStage, t.texels - at);
+      e = cudaMemcpyAsync(stage, t.src + 4 * at, m * sizeof(float4), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess)
+        err = launch_pack_texels_u8(static_cast<const float4 *>(stage), m, dec, dst + t.u8_offset + at,
+            static_cast<uint32_t *>(bad) + i, s);
+    }
+  }
+  std::vector<uint32_t> flags(n_tasks, 0);
+  if (e == cudaSuccess && err.empty())
+    e = cudaMemcpyAsync(flags.data(), bad, n_tasks * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && err.empty())
+    e = cudaStreamSynchronize(s);
+  if (stage)
+    cudaFree(stage);
+  if (bad)
+    cudaFree(bad);
+  if (e != cudaSuccess && err.empty())
+    err = std::string("texel packing: ") + cudaGetErrorString(e);
+  if (!err.empty())
+    return nullptr;
+  size_t f_end = h.texels.size() / 4;
+  for (const HostScene::Span &sp : spans)
+    f_end += sp.floats / 4;
+  for (size_t i = 0; i < n_tasks; ++i) {
+    if (!flags[i])
+      continue;
+    const HostScene::TexelPackTask &t = h.texel_pack_tasks[i];
+    samplers[t.sampler].u8 = 0;
+    samplers[t.sampler].offset = uint32_t(f_end);
+    spans.push_back({t.src, 4 * t.texels});
+    f_end += t.texels;
+  }
+  return dst;
+}
+
 std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
 {
   release();
@@ -1000,11 +1234,16 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   d.material_count = uint32_t(h.materials.size());
   d.attr_values = reinterpret_cast<const float4 *>(put(h.attr_values, s, err));
   std::memcpy(d.attr_offset, h.attr_offset, sizeof(d.attr_offset));
-  d.samplers = put(h.samplers, s, err);
-  d.sampler_count = uint32_t(h.samplers.size());
-  d.texels = reinterpret_cast<const float4 *>(put_spans(h.texels, h.texel_spans, s, err));
-  d.texels_u8 = reinterpret_cast<const uchar4 *>(put(h.texels_u8, s, err));
   d.u8_decode = put(h.u8_decode, s, err);
+  std::vector<DevSampler> samplers = h.samplers;
+  std::vector<HostScene::Span> texel_spans = h.texel_spans;
+  if (h.texel_pack_tasks.empty())
+    d.texels_u8 = reinterpret_cast<const uchar4 *>(put(h.texels_u8, s, err));
+  else if (err.empty())
+    d.texels_u8 = pack_texels(h, samplers, texel_spans, d.u8_decode, s, err);
+  d.samplers = put(samplers, s, err);
+  d.sampler_count = uint32_t(samplers.size());
+  d.texels = reinterpret_cast<const float4 *>(put_spans(h.texels, texel_spans, s, err));
   d.lights = put(h.lights, s, err);
   d.light_count = uint32_t(h.lights.size());
   d.emissive_ids = put(h.emissive_ids, s, err);
@@ -1061,13 +1300,16 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   table_floats[PHC_TABLE_ENV_CONDITIONAL] = h.env_conditional.size();
   table_floats[PHC_TABLE_EMISSIVE_CDF] = h.emissive_cdf.size();
   table_floats[PHC_TABLE_PRIM_LIGHT_PDF] = h.prim_light_pdf.size();
+  if (err.empty() && (h.env_rgb || h.emissive_on_gpu))
+    err = device_tables(h, d, s);
   if (!err.empty()) {
     release();
     return err;
   }
   if (h.bvh_on_gpu) {
     try {
-      const GpuBvh8 g = build_bvh8_gpu(d.positions, d.prim_vidx, uint32_t(h.prim_vidx.size() / 4), s);
+      const GpuBvh8 g = build_bvh8_gpu(d.positions, d.prim_vidx, uint32_t(h.prim_vidx.size() / 4), s,
+          tuning().max_leaf);
       allocations.push_back(g.nodes);
       allocations.push_back(g.tris);
       bytes += size_t(g.node_cap) * 80 + size_t(g.tri_count) * 48;

@@ -1,6 +1,9 @@
 // Scene tables built on the GPU at upload, with the same code as the host
 // builders (these functions are __host__ __device__): the macro-cell
-// majorant grid of a transfer-function volume (RenderBridge.cpp:668-780).
+// majorant grid of a transfer-function volume (RenderBridge.cpp:668-780),
+// the environment map's row and marginal CDFs (environment_map.cpp:8-65),
+// the emissive triangles' selection CDF and area densities
+// (pathtracer.cpp:439-487), and the guide tables of the CDF searches.
 // Every operation is an IEEE add, multiply, divide, floor, ceil or compare
 // (the translation units are compiled without contraction), so the device
 // tables are bit-identical to the host's.
@@ -11,6 +14,7 @@
 #include <cstdint>
 
 #include "pt_math.cuh"
+#include "scene_types.h"
 
 namespace phc {
 
@@ -105,6 +109,73 @@ PHC_HD float majorant_cell(const MajorantJob &j, const float *vals, Alpha alpha,
       bound = j.max_opacity;
   }
   return bound * j.density_scale * 1.01f;
+}
+
+// Luminance weights of the environment CDF and the emitters' power
+// (environment_map.cpp:20, pathtracer.cpp:455).
+PHC_HD float tbl_lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+
+// A material that can emit (RenderBridge.cpp:780-813): positive strength and
+// a textured or positive emission colour.
+PHC_HD bool tbl_may_emit(const DevMaterial &m)
+{
+  if (m.emission_strength <= 0.f)
+    return false;
+  return m.src_kind[SRC_EMIT] != 0 || m.emission[0] > 0.f || m.emission[1] > 0.f || m.emission[2] > 0.f;
+}
+
+// Area of the triangle (p0, p1, p2): half the length of the cross product
+// of its edges from p0.
+PHC_HD float tbl_tri_area(const float *p0, const float *p1, const float *p2)
+{
+  const float ax = p1[0] - p0[0], ay = p1[1] - p0[1], az = p1[2] - p0[2];
+  const float bx = p2[0] - p0[0], by = p2[1] - p0[1], bz = p2[2] - p0[2];
+  const float cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+  return 0.5f * sqrtf(cx * cx + cy * cy + cz * cz);
+}
+
+// Selection weight of an emissive triangle of the given area: area times
+// the emitter's power (constant emission: the luminance of colour times
+// strength; textured: the strength), the power floored at 1e-6.
+PHC_HD double tbl_emit_weight(const DevMaterial &m, float area)
+{
+  const bool constant = m.src_kind[SRC_EMIT] == 0;
+  const float power = constant ? tbl_lum(m.emission[0] * m.emission_strength, m.emission[1] * m.emission_strength,
+                                     m.emission[2] * m.emission_strength)
+                               : m.emission_strength;
+  return area > 0.f ? double(area) * double(power > 1e-6f ? power : 1e-6f) : 0.0;
+}
+
+// Guide entries of non-decreasing CDFs, for the grid point u = k / G.
+// guide_le: max{i in [0, n - 1] : cdf[i] <= u}, 0 when none (the row /
+// column searches, environment_map.h:62-104); guide_gt: min({i in [0, n - 2]
+// : cdf[i] > u} U {n - 1}) (the emissive search, pathtracer.cpp:296-306).
+// The host builder walks the CDF in order; on a non-decreasing CDF these
+// bisections return the same indices.
+PHC_HD uint32_t guide_le(const float *cdf, uint32_t n, float u)
+{
+  uint32_t lo = 1, hi = n; // first i in [1, n) with cdf[i] > u, n when none
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (cdf[mid] <= u)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo - 1;
+}
+
+PHC_HD uint32_t guide_gt(const float *cdf, uint32_t n, float u)
+{
+  uint32_t lo = 0, hi = n - 1; // first i in [0, n - 1) with cdf[i] > u, n - 1 when none
+  while (lo < hi) {
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (cdf[mid] <= u)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
 }
 
 } // namespace phc

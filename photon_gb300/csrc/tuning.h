@@ -28,7 +28,7 @@ struct Tuning {
   int64_t batch_wave_paths{1 << 25}; // paths per wave of a batched render
   int64_t sort_threshold{1 << 18};   // sort the hit queue by material when it holds this many hits (0: never)
   int gpu_bvh{1};                    // build the BVH8 on the GPU (bvh_gpu.cu), read at scene build
-  int gpu_tables{1};                 // build the volume majorant grids on the GPU (scene_tables.cu), read at scene build
+  int gpu_tables{1};                 // build majorant grids, env / emissive CDFs and 8-bit texels on the GPU (scene_tables.cu), read at scene build
   int texels_u8{1};                  // keep samplers whose texels are all k / 255 as 8-bit RGBA, read at scene build
   int64_t wave_trip_cap{1 << 24};    // loop trips after which a persistent wave kernel's warp stops with
                                      // PHC_ERR_DEVICE (a self-check; lowered only to test that path)

@@ -69,6 +69,20 @@ std::string launch_majorants(const MajorantJob &, const float *, const float4 *,
 {
   return "the host harness builds no tables on the GPU";
 }
+std::string launch_pack_texels_u8(const float4 *, size_t, const float *, uchar4 *, uint32_t *, cudaStream_t)
+{
+  return "the host harness packs no texels on the GPU";
+}
+std::string launch_env_tables(const EnvTablesJob &, cudaStream_t) { return "the host harness builds no tables on the GPU"; }
+std::string launch_emissive_ids(const EmissiveJob &, cudaStream_t) { return "the host harness builds no tables on the GPU"; }
+std::string launch_emissive_weights(const EmissiveJob &, cudaStream_t)
+{
+  return "the host harness builds no tables on the GPU";
+}
+std::string launch_emissive_tables(const EmissiveJob &, double, cudaStream_t)
+{
+  return "the host harness builds no tables on the GPU";
+}
 void host_scene(const phc_scene_desc &desc, HostScene &h)
 {
   tuning().gpu_tables = 0;

@@ -115,22 +115,18 @@ def test_instanced_full_size_renders(photon):
     r.close()
 
 
-def test_rgba8_texels_match_fp32_storage(photon):
-    """Samplers whose texels are all k / 255 are stored as 8-bit RGBA on the
-    device (tuning key texels_u8) and decoded through the table of those
-    floats: every channel of every frame is bit-identical to the same scene
-    stored as fp32 texels, and the scene takes about a quarter of the texel
-    bytes."""
+def _render_modes(photon, sc, cam, st, modes):
+    """Renders two frames of the scene under each (texels_u8, gpu_tables)
+    mode; returns the frames' four channels and the device memory the scene
+    took, per mode."""
     import torch
     from photon_gb300 import tuning_get, tuning_set
-    sc, cam, st0 = _small()
-    st = type(st0).from_buffer_copy(bytes(st0))
-    st.pixel_samples = 2
-    old = tuning_get("texels_u8")
+    old = (tuning_get("texels_u8"), tuning_get("gpu_tables"))
     out, mem = {}, {}
     try:
-        for mode in (1, 0):
-            tuning_set("texels_u8", mode)
+        for mode in modes:
+            tuning_set("texels_u8", mode[0])
+            tuning_set("gpu_tables", mode[1])
             torch.cuda.synchronize()
             free0 = torch.cuda.mem_get_info()[0]
             r = photon.Renderer()
@@ -144,12 +140,63 @@ def test_rgba8_texels_match_fp32_storage(photon):
             out[mode] = frames
             r.close()
     finally:
-        tuning_set("texels_u8", old)
+        tuning_set("texels_u8", old[0])
+        tuning_set("gpu_tables", old[1])
+    return out, mem
+
+
+def _same_frames(a, b):
     for f in range(2):
         for ch in ("color", "depth", "normal", "albedo"):
-            a, b = out[1][f][ch], out[0][f][ch]
-            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (f, ch)
+            assert np.array_equal(a[f][ch].view(np.uint32), b[f][ch].view(np.uint32)), (f, ch)
+
+
+def test_rgba8_texels_match_fp32_storage(photon):
+    """Samplers whose texels are all k / 255 are stored as 8-bit RGBA on the
+    device (tuning key texels_u8) and decoded through the table of those
+    floats: every channel of every frame is bit-identical to the same scene
+    stored as fp32 texels, whether the upload packs the texels on the device
+    (tuning key gpu_tables, the default) or on the host, and the scene takes
+    about a quarter of the texel bytes."""
+    sc, cam, st0 = _small()
+    st = type(st0).from_buffer_copy(bytes(st0))
+    st.pixel_samples = 2
+    dev, host, fp32 = (1, 1), (1, 0), (0, 1)
+    out, mem = _render_modes(photon, sc, cam, st, (dev, host, fp32))
+    _same_frames(out[dev], out[fp32])
+    _same_frames(out[host], out[fp32])
     texel_bytes = sum(len(t) * 16 for _, t in sc.samplers)
-    print(f"scene device memory: {mem[1] / 2**20:.1f} MiB with 8-bit texels, {mem[0] / 2**20:.1f} MiB fp32 "
+    print(f"scene device memory: {mem[dev] / 2**20:.1f} MiB with 8-bit texels packed on the device, "
+          f"{mem[host] / 2**20:.1f} MiB packed on the host, {mem[fp32] / 2**20:.1f} MiB fp32 "
           f"({texel_bytes / 2**20:.1f} MiB of fp32 texels)")
-    assert mem[0] - mem[1] >= 0.6 * texel_bytes
+    assert mem[fp32] - mem[dev] >= 0.6 * texel_bytes
+    assert mem[fp32] - mem[host] >= 0.6 * texel_bytes
+
+
+def test_rgba8_packing_falls_back_to_fp32(photon):
+    """A sampler with values that are not k / 255 (0.5 on every 7th texel's
+    green channel, or -0.0 on every 11th texel's red channel) keeps fp32
+    storage: the device packer flags it, the upload moves it to the float4
+    array, and the images equal the all-fp32 scene's bit for bit; the other
+    samplers stay 8-bit."""
+    import copy
+    sc0, cam, st0 = _small()
+    sc = copy.copy(sc0)
+    sc.samplers = list(sc0.samplers)
+    planted = []
+    for i, v, step, ch in ((0, 0.5, 7, 1), (len(sc.samplers) - 1, -0.0, 11, 0)):
+        rec, t = sc.samplers[i]
+        t = np.array(t, np.float32, copy=True).reshape(-1, 4)
+        t[::step, ch] = v
+        sc.samplers[i] = (rec, t)
+        planted.append(i)
+    st = type(st0).from_buffer_copy(bytes(st0))
+    st.pixel_samples = 2
+    dev, host, fp32 = (1, 1), (1, 0), (0, 1)
+    out, mem = _render_modes(photon, sc, cam, st, (dev, host, fp32))
+    _same_frames(out[dev], out[fp32])
+    _same_frames(out[host], out[fp32])
+    kept = sum(len(t) * 16 for i, (_, t) in enumerate(sc.samplers) if i not in planted)
+    print(f"planted samplers {planted}: {mem[dev] / 2**20:.1f} MiB (device packing), "
+          f"{mem[host] / 2**20:.1f} MiB (host), {mem[fp32] / 2**20:.1f} MiB fp32")
+    assert mem[fp32] - mem[host] >= 0.6 * kept
