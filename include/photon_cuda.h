@@ -523,10 +523,11 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
    idle), "split_shade" (0/1: hits and misses shaded by separate kernels),
    "shade_lean" (0/1: lean shading kernels for scenes without volumes /
    sources / lights), "sort_threshold" (sort the hit queue by material when it
-   holds at least this many hits; 0: never), "max_leaf" (1..3, BVH8 leaf size,
-   read at the next scene upload), "gpu_bvh" (0/1: build the BVH8 of
-   single-level scenes on the GPU, leaves of one triangle, read at the next
-   scene upload), "batch_wave_paths", "use_graph" (0/1),
+   holds at least this many hits; 0: never), "max_leaf" (1..3, leaf size of the
+   host-built BVH8, read at the next scene upload), "gpu_bvh" (0/1: build
+   the BVH8 of single-level scenes on the GPU, read at the next scene
+   upload), "gpu_max_leaf" (1..3, leaf size of the GPU-built BVH8, read at
+   the next scene upload), "batch_wave_paths", "use_graph" (0/1),
    "count_traversal" (0/1: node / triangle / density-lookup counters),
    "time_kernels" (0/1), "shade_classes" (0/1: lean scenes sort the hit queue
    by shading class and shade each class with a kernel compiled for its

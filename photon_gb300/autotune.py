@@ -4,8 +4,8 @@ Coordinate descent on one workload: each key in turn takes every candidate
 value of SPACE with the other keys fixed, and keeps the value with the lowest
 median device time of a render call (phc_render's render_ms, after a warm-up
 call).  Passes repeat until a pass changes nothing or `passes` is reached.
-"max_leaf" and "gpu_bvh" change the BVH8 and are applied by re-uploading the
-scene.
+"max_leaf", "gpu_bvh" and "gpu_max_leaf" change the BVH8 and are applied by
+re-uploading the scene.
 
 The reference has no tunables on this path; the keys are this renderer's:
 queue capacity (wave_paths), persistent grid sizes of the traversal and
@@ -32,8 +32,9 @@ SPACE = {
     "sort_threshold": [0, 1 << 12, 1 << 14, 1 << 16, 1 << 18, 1 << 20],
     "max_leaf": [1, 2, 3],
     "gpu_bvh": [0, 1],
+    "gpu_max_leaf": [1, 2, 3],
 }
-SCENE_KEYS = {"max_leaf", "gpu_bvh"}  # read at scene upload
+SCENE_KEYS = {"max_leaf", "gpu_bvh", "gpu_max_leaf"}  # read at scene upload
 
 
 class RenderTimer:

@@ -17,7 +17,7 @@ struct Tuning {
   int shade_blocks_per_sm{16};       // persistent grid of the shading kernel (128 threads; capped by occupancy)
   int use_graph{1};                  // replay each wave as a CUDA graph
   int count_traversal{0};            // node-visit / triangle-test counters (roofline runs)
-  int max_leaf{1};                   // triangles per BVH8 leaf child (1..3), read at scene build
+  int max_leaf{1};                   // triangles per leaf child of the host-built BVH8 (1..3), read at scene build
   int time_kernels{0};               // CUDA events around every launch (no graph), per-kind times
   int trace_refill{8};               // closest-hit warps refill once this many lanes idle (32: never)
   int vol_refill{8};                 // volume-tracking warps refill once this many lanes idle
@@ -28,6 +28,7 @@ struct Tuning {
   int64_t batch_wave_paths{1 << 25}; // paths per wave of a batched render
   int64_t sort_threshold{1 << 18};   // sort the hit queue by material when it holds this many hits (0: never)
   int gpu_bvh{1};                    // build the BVH8 on the GPU (bvh_gpu.cu), read at scene build
+  int gpu_max_leaf{2};               // triangles per leaf child of the GPU-built BVH8 (1..3), read at scene build
   int gpu_tables{1};                 // build majorant grids, env / emissive CDFs and 8-bit texels on the GPU (scene_tables.cu), read at scene build
   int texels_u8{1};                  // keep samplers whose texels are all k / 255 as 8-bit RGBA, read at scene build
   int64_t wave_trip_cap{1 << 24};    // loop trips after which a persistent wave kernel's warp stops with

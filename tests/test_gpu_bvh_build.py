@@ -16,13 +16,17 @@ from tests.parity import MIN_PATH_FRACTION, close_fraction
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture
-def gpu_bvh(photon):
+@pytest.fixture(params=[1, 2, 3], ids=lambda m: f"leaf{m}")
+def gpu_bvh(photon, request):
+    """The GPU builder, with leaf children of up to 1, 2 or 3 triangles
+    (tuning key gpu_max_leaf)."""
     from photon_gb300 import tuning_get, tuning_set
-    old = tuning_get("gpu_bvh")
+    old = (tuning_get("gpu_bvh"), tuning_get("gpu_max_leaf"))
     tuning_set("gpu_bvh", 1)
+    tuning_set("gpu_max_leaf", request.param)
     yield
-    tuning_set("gpu_bvh", old)
+    tuning_set("gpu_bvh", old[0])
+    tuning_set("gpu_max_leaf", old[1])
 
 
 def _to_dev(*arrs):
