@@ -510,7 +510,8 @@ const char *phc_accel_error(void);
    and resets the counter itself: calls that overlap on the GPU (two
    streams, two threads) race and must be serialised by the caller.  n above
    PHC_STATIC_MAX_RAYS is rejected with PHC_ERR_LIMIT.  Each call blocks
-   until its trace is done: it synchronises the stream before it returns. */
+   until its trace is done: it synchronises the stream before it returns,
+   so no call can be captured into a CUDA graph. */
 int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const float *directions, const float *tmin,
     const float *tmax, uint32_t n, float *hits4, void *stream);
 
