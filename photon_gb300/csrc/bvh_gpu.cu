@@ -12,7 +12,8 @@
 //   3. a binary tree by parallel locally-ordered clustering (Meister and
 //      Bittner, "Parallel Locally-Ordered Clustering for Bounding Volume
 //      Hierarchy Construction", IEEE TVCG 2018): every cluster finds, among
-//      the RADIUS clusters on each side in Morton order, the one whose merged
+//      the `radius` clusters on each side in Morton order (2, 4, 8, 16 or 32;
+//      tuning key ploc_radius), the one whose merged
 //      box has the least surface area; mutual pairs merge; the survivors are
 //      compacted in order; repeat until one cluster is left.  Ties in the
 //      area are broken by the pair's indices, so the globally smallest pair
@@ -39,10 +40,6 @@
 namespace phc {
 namespace {
 
-#ifndef PHC_PLOC_RADIUS
-#define PHC_PLOC_RADIUS 16
-#endif
-constexpr int RADIUS = PHC_PLOC_RADIUS; // PLOC search radius (clusters on each side)
 constexpr int SORT_BLOCK = 256;
 constexpr int TILE = 256;    // clusters per block of the neighbour search
 
@@ -225,6 +222,7 @@ __global__ void k_leaves(const float *__restrict__ boxes, const uint32_t *__rest
 
 // Nearest neighbour of every cluster within RADIUS on each side; the pair
 // order is (merged area, smaller index, larger index).
+template <int RADIUS>
 __global__ void __launch_bounds__(TILE) k_ploc_nn(const float *__restrict__ cbox, uint32_t n, uint32_t *__restrict__ nn)
 {
   __shared__ float sb[TILE + 2 * RADIUS][6];
@@ -566,7 +564,8 @@ uint32_t grid_of(uint32_t n, uint32_t block) { return std::max<uint32_t>(1u, std
 
 } // namespace
 
-GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t n, cudaStream_t s, int max_leaf)
+GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t n, cudaStream_t s, int max_leaf,
+    int radius)
 {
   if (n == 0)
     throw std::runtime_error("gpu bvh build: no triangles");
@@ -618,7 +617,17 @@ GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t
   int c = 0;
   uint32_t counts[4];
   for (int iter = 0; count > 1; ++iter) {
-    k_ploc_nn<<<(count + TILE - 1) / TILE, TILE, 0, s>>>(cbox[c].as<float>(), count, nn.as<uint32_t>());
+    const unsigned nb = (count + TILE - 1) / TILE;
+    if (radius <= 2)
+      k_ploc_nn<2><<<nb, TILE, 0, s>>>(cbox[c].as<float>(), count, nn.as<uint32_t>());
+    else if (radius <= 4)
+      k_ploc_nn<4><<<nb, TILE, 0, s>>>(cbox[c].as<float>(), count, nn.as<uint32_t>());
+    else if (radius <= 8)
+      k_ploc_nn<8><<<nb, TILE, 0, s>>>(cbox[c].as<float>(), count, nn.as<uint32_t>());
+    else if (radius <= 16)
+      k_ploc_nn<16><<<nb, TILE, 0, s>>>(cbox[c].as<float>(), count, nn.as<uint32_t>());
+    else
+      k_ploc_nn<32><<<nb, TILE, 0, s>>>(cbox[c].as<float>(), count, nn.as<uint32_t>());
     k_ploc_flags<<<grid_of(count, 256), 256, 0, s>>>(nn.as<uint32_t>(), count, mflag.as<uint32_t>(),
         kflag.as<uint32_t>());
     ck(cudaMemcpyAsync(mrank.p, mflag.p, size_t(count) * 4, cudaMemcpyDeviceToDevice, s), "copy merge flags");

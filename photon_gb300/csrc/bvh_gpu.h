@@ -16,9 +16,10 @@ struct GpuBvh8 {
 };
 
 // positions: float4 per vertex; prim_vidx: (i0, i1, i2, material) per
-// triangle, both on the device; max_leaf: triangles per leaf child (1..3).
+// triangle, both on the device; max_leaf: triangles per leaf child (1..3);
+// radius: clusters searched on each side by the clustering (2..32).
 // Blocks on `s` until the build is done.
 GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t triangle_count, cudaStream_t s,
-    int max_leaf = 1);
+    int max_leaf = 1, int radius = 16);
 
 } // namespace phc

@@ -29,6 +29,7 @@ struct Tuning {
   int64_t sort_threshold{1 << 18};   // sort the hit queue by material when it holds this many hits (0: never)
   int gpu_bvh{1};                    // build the BVH8 on the GPU (bvh_gpu.cu), read at scene build
   int gpu_max_leaf{2};               // triangles per leaf child of the GPU-built BVH8 (1..3), read at scene build
+  int ploc_radius{4};                // clusters searched on each side by the GPU build's clustering (2..32)
   int gpu_tables{1};                 // build majorant grids, env / emissive CDFs and 8-bit texels on the GPU (scene_tables.cu), read at scene build
   int texels_u8{1};                  // keep samplers whose texels are all k / 255 as 8-bit RGBA, read at scene build
   int64_t wave_trip_cap{1 << 24};    // loop trips after which a persistent wave kernel's warp stops with

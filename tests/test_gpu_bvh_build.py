@@ -16,17 +16,19 @@ from tests.parity import MIN_PATH_FRACTION, close_fraction
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=[1, 2, 3], ids=lambda m: f"leaf{m}")
+@pytest.fixture(params=[(1, 4), (2, 4), (3, 4), (2, 2), (2, 32)], ids=lambda p: f"leaf{p[0]}-radius{p[1]}")
 def gpu_bvh(photon, request):
     """The GPU builder, with leaf children of up to 1, 2 or 3 triangles
-    (tuning key gpu_max_leaf)."""
+    (tuning key gpu_max_leaf) and clustering radii 2, 4 and 32 (ploc_radius)."""
     from photon_gb300 import tuning_get, tuning_set
-    old = (tuning_get("gpu_bvh"), tuning_get("gpu_max_leaf"))
+    keys = ("gpu_bvh", "gpu_max_leaf", "ploc_radius")
+    old = {k: tuning_get(k) for k in keys}
     tuning_set("gpu_bvh", 1)
-    tuning_set("gpu_max_leaf", request.param)
+    tuning_set("gpu_max_leaf", request.param[0])
+    tuning_set("ploc_radius", request.param[1])
     yield
-    tuning_set("gpu_bvh", old[0])
-    tuning_set("gpu_max_leaf", old[1])
+    for k, v in old.items():
+        tuning_set(k, v)
 
 
 def _to_dev(*arrs):
