@@ -146,7 +146,8 @@ __global__ void __launch_bounds__(SORT_BLOCK) k_digit_hist(const uint32_t *__res
 }
 
 // Exclusive scan of `count` words in place by one block (sequential chunks,
-// in order, so the result is independent of the block size).
+// in order, so the result is independent of the block size): the scan of
+// the tile sums below.
 __global__ void __launch_bounds__(1024) k_scan_inplace(uint32_t *__restrict__ v, uint32_t count, uint32_t *total)
 {
   __shared__ uint32_t part[1024];
@@ -171,6 +172,84 @@ __global__ void __launch_bounds__(1024) k_scan_inplace(uint32_t *__restrict__ v,
   }
   if (threadIdx.x == 1023 && total)
     *total = part[1023];
+}
+
+// Multi-block exclusive scan: tiles of SCAN_TILE words, one block each;
+// the tile sums, their scan by one block, then each tile's scan from its
+// offset.  Integer sums, so the result is exact whatever the tiling.
+constexpr int SCAN_T = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_T * SCAN_ITEMS;
+
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t x, uint32_t &block_total)
+{
+  __shared__ uint32_t warp_sum[SCAN_T / 32];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t inc = x;
+  for (uint32_t off = 1; off < 32u; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+    if (lane >= off)
+      inc += y;
+  }
+  if (lane == 31u)
+    warp_sum[warp] = inc;
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+  for (uint32_t w = 0; w < SCAN_T / 32; ++w) {
+    const uint32_t v = warp_sum[w];
+    before += w < warp ? v : 0u;
+    all += v;
+  }
+  __syncthreads(); // warp_sum is reused by the next call
+  block_total = all;
+  return before + inc - x;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_tile_sums(const uint32_t *__restrict__ in, uint32_t n,
+    uint32_t *__restrict__ sums)
+{
+  const size_t base = size_t(blockIdx.x) * SCAN_TILE;
+  uint32_t s = 0;
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    const size_t i = base + size_t(k) * SCAN_T + threadIdx.x;
+    if (i < n)
+      s += in[i];
+  }
+  uint32_t total;
+  block_exclusive(s, total);
+  if (threadIdx.x == 0)
+    sums[blockIdx.x] = total;
+}
+
+// Padded shared index: thread t's SCAN_ITEMS consecutive words fall in
+// different banks.
+__device__ __forceinline__ uint32_t scan_pad(uint32_t i) { return i + (i >> 5); }
+
+__global__ void __launch_bounds__(SCAN_T) k_tile_scan(const uint32_t *in, uint32_t n,
+    const uint32_t *__restrict__ offsets, uint32_t *out)
+{
+  __shared__ uint32_t tile[SCAN_TILE + SCAN_TILE / 32];
+  const size_t base = size_t(blockIdx.x) * SCAN_TILE;
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    const uint32_t j = uint32_t(k) * SCAN_T + threadIdx.x;
+    tile[scan_pad(j)] = base + j < n ? in[base + j] : 0u;
+  }
+  __syncthreads();
+  uint32_t v[SCAN_ITEMS], local = 0;
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    v[k] = tile[scan_pad(threadIdx.x * SCAN_ITEMS + k)];
+    local += v[k];
+  }
+  uint32_t total;
+  uint32_t run = offsets[blockIdx.x] + block_exclusive(local, total);
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    tile[scan_pad(threadIdx.x * SCAN_ITEMS + k)] = run;
+    run += v[k];
+  }
+  __syncthreads();
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    const uint32_t j = uint32_t(k) * SCAN_T + threadIdx.x;
+    if (base + j < n)
+      out[base + j] = tile[scan_pad(j)];
+  }
 }
 
 __global__ void __launch_bounds__(SORT_BLOCK) k_digit_scatter(const uint32_t *__restrict__ kin,
@@ -564,6 +643,18 @@ uint32_t grid_of(uint32_t n, uint32_t block) { return std::max<uint32_t>(1u, std
 
 } // namespace
 
+size_t scan_u32_scratch(uint32_t n) { return (size_t(n) + SCAN_TILE - 1) / SCAN_TILE; }
+
+void scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, uint32_t *scratch, cudaStream_t s)
+{
+  if (n == 0)
+    return;
+  const uint32_t tiles = uint32_t(scan_u32_scratch(n));
+  k_tile_sums<<<tiles, SCAN_T, 0, s>>>(in, n, scratch);
+  k_scan_inplace<<<1, 1024, 0, s>>>(scratch, tiles, total);
+  k_tile_scan<<<tiles, SCAN_T, 0, s>>>(in, n, scratch, out);
+}
+
 GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t n, cudaStream_t s, int max_leaf,
     int radius)
 {
@@ -580,6 +671,8 @@ GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t
   }
   const uint32_t nb = (n + SORT_BLOCK - 1) / SORT_BLOCK;
   alloc(hist, size_t(nb) * 256 * 4, "histogram");
+  DevBuf scan_tmp;
+  alloc(scan_tmp, std::max(scan_u32_scratch(nb * 256), scan_u32_scratch(n)) * 4, "scan tile sums");
   alloc(total, 16, "total");
   // scene centroid bounds start at (+max, -max) in the ordered encoding
   const uint32_t init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
@@ -590,7 +683,7 @@ GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t
   int cur = 0;
   for (int shift = 0; shift < 32; shift += 8) {
     k_digit_hist<<<nb, SORT_BLOCK, 0, s>>>(keys[cur].as<uint32_t>(), n, shift, hist.as<uint32_t>(), nb);
-    k_scan_inplace<<<1, 1024, 0, s>>>(hist.as<uint32_t>(), nb * 256, nullptr);
+    scan_u32(hist.as<uint32_t>(), hist.as<uint32_t>(), nb * 256, nullptr, scan_tmp.as<uint32_t>(), s);
     k_digit_scatter<<<nb, SORT_BLOCK, 0, s>>>(keys[cur].as<uint32_t>(), vals[cur].as<uint32_t>(), n, shift,
         hist.as<uint32_t>(), nb, keys[cur ^ 1].as<uint32_t>(), vals[cur ^ 1].as<uint32_t>());
     cur ^= 1;
@@ -630,10 +723,8 @@ GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t
       k_ploc_nn<32><<<nb, TILE, 0, s>>>(cbox[c].as<float>(), count, nn.as<uint32_t>());
     k_ploc_flags<<<grid_of(count, 256), 256, 0, s>>>(nn.as<uint32_t>(), count, mflag.as<uint32_t>(),
         kflag.as<uint32_t>());
-    ck(cudaMemcpyAsync(mrank.p, mflag.p, size_t(count) * 4, cudaMemcpyDeviceToDevice, s), "copy merge flags");
-    ck(cudaMemcpyAsync(krank.p, kflag.p, size_t(count) * 4, cudaMemcpyDeviceToDevice, s), "copy keep flags");
-    k_scan_inplace<<<1, 1024, 0, s>>>(mrank.as<uint32_t>(), count, total.as<uint32_t>());
-    k_scan_inplace<<<1, 1024, 0, s>>>(krank.as<uint32_t>(), count, total.as<uint32_t>() + 1);
+    scan_u32(mflag.as<uint32_t>(), mrank.as<uint32_t>(), count, total.as<uint32_t>(), scan_tmp.as<uint32_t>(), s);
+    scan_u32(kflag.as<uint32_t>(), krank.as<uint32_t>(), count, total.as<uint32_t>() + 1, scan_tmp.as<uint32_t>(), s);
     k_ploc_write<<<grid_of(count, 256), 256, 0, s>>>(nn.as<uint32_t>(), count, mflag.as<uint32_t>(),
         mrank.as<uint32_t>(), kflag.as<uint32_t>(), krank.as<uint32_t>(), node_base, cid[c].as<uint32_t>(),
         cbox[c].as<float>(), cid[c ^ 1].as<uint32_t>(), cbox[c ^ 1].as<float>(), nbox.as<float>(),

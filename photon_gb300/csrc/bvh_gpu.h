@@ -22,4 +22,10 @@ struct GpuBvh8 {
 GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t triangle_count, cudaStream_t s,
     int max_leaf = 1, int radius = 16);
 
+// Exclusive scan of n words (in == out allowed) on the device, in three
+// launches on `s`; *total (if not null) receives the sum.  scratch holds
+// scan_u32_scratch(n) words.
+size_t scan_u32_scratch(uint32_t n);
+void scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, uint32_t *scratch, cudaStream_t s);
+
 } // namespace phc

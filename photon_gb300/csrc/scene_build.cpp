@@ -1083,6 +1083,8 @@ std::string DeviceScene::device_tables(const HostScene &h, DevScene &d, cudaStre
     ej.mats = d.materials;
     ej.tc = tc;
     ej.flag = static_cast<uint32_t *>(tmp(size_t(tc) * sizeof(uint32_t)));
+    ej.rank = static_cast<uint32_t *>(tmp(size_t(tc) * sizeof(uint32_t)));
+    ej.scan_scratch = static_cast<uint32_t *>(tmp(scan_u32_scratch(tc) * sizeof(uint32_t)));
     ej.count = flags + 1;
     ej.bad = flags;
     if (err.empty())

@@ -167,8 +167,8 @@ std::string launch_env_tables(const EnvTablesJob &job, cudaStream_t stream);
 
 // The emissive triangles' tables on the device (scene_tables.cu), in three
 // launches: flags of the triangles whose material may emit and whose area
-// is positive, and their number (count[0] = n); their ids in triangle order
-// and their weights; then, from the running sum of the weights (computed by
+// is positive, their exclusive scan and their number (count[0] = n); their
+// ids in triangle order and their weights; then, from the running sum of the weights (computed by
 // the caller, in the reference's double order, into prefix) and its total,
 // the CDF, the per-triangle area densities and the guide (bad |= 4 when the
 // CDF is not non-decreasing).
@@ -178,6 +178,8 @@ struct EmissiveJob {
   const DevMaterial *mats;
   uint32_t tc;       // triangles
   uint32_t *flag;    // tc (scratch)
+  uint32_t *rank;    // tc (scratch): exclusive scan of flag
+  uint32_t *scan_scratch; // scan_u32_scratch(tc) words
   uint32_t *ids;     // n
   uint32_t *count;
   uint32_t n;        // emitters

@@ -5,6 +5,7 @@
 
 #include "scene_build.h"
 #include "scene_tables.cuh"
+#include "bvh_gpu.h"
 
 namespace phc {
 namespace {
@@ -170,33 +171,14 @@ __global__ void __launch_bounds__(256) k_emissive_flags(const float4 *__restrict
   }
 }
 
-// The flagged triangles' ids in triangle order, by one block: each thread
-// takes a contiguous chunk, the chunk counts are scanned, and each thread
-// writes its ids from its offset.  count[0] = the number of ids.
-__global__ void __launch_bounds__(1024) k_emissive_compact(const uint32_t *__restrict__ flag, uint32_t tc,
-    uint32_t *__restrict__ ids, uint32_t *__restrict__ count)
+// The flagged triangles' ids in triangle order: rank is the exclusive scan
+// of the flags.
+__global__ void __launch_bounds__(256) k_emissive_ids(const uint32_t *__restrict__ flag,
+    const uint32_t *__restrict__ rank, uint32_t tc, uint32_t *__restrict__ ids)
 {
-  __shared__ uint32_t part[1024];
-  const uint32_t per = (tc + 1023u) / 1024u;
-  const uint32_t b = min(tc, threadIdx.x * per), e = min(tc, b + per);
-  uint32_t n = 0;
-  for (uint32_t t = b; t < e; ++t)
-    n += flag[t];
-  part[threadIdx.x] = n;
-  __syncthreads();
-  for (uint32_t off = 1; off < 1024u; off <<= 1) {
-    const uint32_t x = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
-    __syncthreads();
-    part[threadIdx.x] += x;
-    __syncthreads();
-  }
-  uint32_t at = part[threadIdx.x] - n;
-  if (ids)
-    for (uint32_t t = b; t < e; ++t)
-      if (flag[t])
-        ids[at++] = t;
-  if (threadIdx.x == 1023)
-    *count = part[1023];
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < tc; t += gridDim.x * blockDim.x)
+    if (flag[t])
+      ids[rank[t]] = t;
 }
 
 // Selection weight of each emitter (one thread per emitter).
@@ -269,14 +251,14 @@ std::string launch_env_tables(const EnvTablesJob &j, cudaStream_t s)
 std::string launch_emissive_ids(const EmissiveJob &j, cudaStream_t s)
 {
   k_emissive_flags<<<grid_for(j.tc, 256, 8), 256, 0, s>>>(j.pos, j.vidx, j.mats, j.tc, j.flag);
-  k_emissive_compact<<<1, 1024, 0, s>>>(j.flag, j.tc, j.ids, j.count);
+  scan_u32(j.flag, j.rank, j.tc, j.count, j.scan_scratch, s);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? std::string() : std::string("emissive ids: ") + cudaGetErrorString(e);
 }
 
 std::string launch_emissive_weights(const EmissiveJob &j, cudaStream_t s)
 {
-  k_emissive_compact<<<1, 1024, 0, s>>>(j.flag, j.tc, j.ids, j.count);
+  k_emissive_ids<<<grid_for(j.tc, 256, 8), 256, 0, s>>>(j.flag, j.rank, j.tc, j.ids);
   k_emissive_weights<<<grid_for(j.n, 256, 8), 256, 0, s>>>(j.pos, j.vidx, j.mats, j.ids, j.n, j.weight);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? std::string() : std::string("emissive weights: ") + cudaGetErrorString(e);

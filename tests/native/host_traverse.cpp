@@ -74,6 +74,8 @@ std::string launch_pack_texels_u8(const float4 *, size_t, const float *, uchar4 
   return "the host harness packs no texels on the GPU";
 }
 std::string launch_env_tables(const EnvTablesJob &, cudaStream_t) { return "the host harness builds no tables on the GPU"; }
+size_t scan_u32_scratch(uint32_t n) { return n; }
+void scan_u32(const uint32_t *, uint32_t *, uint32_t, uint32_t *, uint32_t *, cudaStream_t) {}
 std::string launch_emissive_ids(const EmissiveJob &, cudaStream_t) { return "the host harness builds no tables on the GPU"; }
 std::string launch_emissive_weights(const EmissiveJob &, cudaStream_t)
 {
