@@ -436,37 +436,36 @@ __global__ void __launch_bounds__(128) k_collapse(Collapse c, const uint2 *__res
     return;
   const uint32_t ni = qin[t].x;
   const int root = int(qin[t].y);
+  // candidates: child v, whether it is internal, its area, and whether it
+  // has at most max_leaf primitives (it becomes one leaf child unless a free
+  // slot opens it), each found once when the candidate is added
   int ch[8];
-  int k = 0;
-  if (c.nchild[root].x < 0) {
-    ch[k++] = root; // a leaf root: one leaf child
-  } else {
-    ch[k++] = c.nchild[root].x;
-    ch[k++] = c.nchild[root].y;
-  }
-  // small[i]: internal child i has at most max_leaf primitives (it becomes
-  // one leaf child unless a free slot opens it)
+  bool inner[8], sm[8];
+  float ar[8];
   int prims[3];
-  auto small = [&](int v) { return c.max_leaf > 1 && subtree_prims(c.nchild, v, c.max_leaf, prims) <= c.max_leaf; };
+  int k = 0;
+  auto add = [&](int slot, int v) {
+    ch[slot] = v;
+    inner[slot] = c.nchild[v].x >= 0;
+    ar[slot] = inner[slot] ? node_area(c.nbox, v) : 0.f;
+    sm[slot] = inner[slot] && c.max_leaf > 1 && subtree_prims(c.nchild, v, c.max_leaf, prims) <= c.max_leaf;
+  };
+  if (c.nchild[root].x < 0) {
+    add(k++, root); // a leaf root: one leaf child
+  } else {
+    add(k++, c.nchild[root].x);
+    add(k++, c.nchild[root].y);
+  }
   while (k < 8) { // open the internal child of largest area, larger subtrees first
     int best = -1;
-    float best_a = -1.f;
-    bool best_small = true;
     for (int i = 0; i < k; ++i)
-      if (c.nchild[ch[i]].x >= 0) {
-        const float a = node_area(c.nbox, ch[i]);
-        const bool sm = small(ch[i]);
-        if (best < 0 || (best_small && !sm) || (sm == best_small && a > best_a)) {
-          best_a = a;
-          best = i;
-          best_small = sm;
-        }
-      }
+      if (inner[i] && (best < 0 || (sm[best] && !sm[i]) || (sm[i] == sm[best] && ar[i] > ar[best])))
+        best = i;
     if (best < 0)
       break;
     const int2 cc = c.nchild[ch[best]];
-    ch[best] = cc.x;
-    ch[k++] = cc.y;
+    add(best, cc.x);
+    add(k++, cc.y);
   }
   float nlo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, nhi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
   for (int i = 0; i < k; ++i)
