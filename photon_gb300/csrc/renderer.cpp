@@ -98,7 +98,7 @@ struct phc_renderer {
   // wavefront buffers
   size_t cap_paths{0};
   Buf st_o[2], st_d[2], st_tp[2], st_info[2], st_dist[2], hits, sh_a, sh_b, sh_c, hitq, missq, hitq_sorted;
-  Buf vol_scatter, vol_rng; // scenes with volumes: k_vol_scatter results per path
+  Buf vol_scatter, vol_rng, vol_q; // scenes with volumes: k_vol_scatter results per path, scattering queue
   size_t cap_vol{0};
   Buf hit_inst; // instance slot per hit (scenes with instances)
   Buf sort_bins; // per bounce iteration: material-sort counts and starts
@@ -262,6 +262,7 @@ void ensure_paths(phc_renderer *r, size_t n)
     r->buf_gen++;
     ck(r->vol_scatter.ensure(r->cap_paths * 16), "alloc volume scattering");
     ck(r->vol_rng.ensure(r->cap_paths * 4), "alloc volume scattering");
+    ck(r->vol_q.ensure(r->cap_paths * 4), "alloc volume scattering");
     r->cap_vol = r->cap_paths;
   }
 }
@@ -314,6 +315,8 @@ WaveCounters wave_counters(phc_renderer *r, int max_iter)
   wc.fetch = c + (4 * max_iter + 1);
   wc.vfetch = c + (8 * max_iter + 1);
   wc.cfetch = c + (10 * max_iter + 1);
+  wc.vcount = c + ((10 + SHADE_CLASSES) * max_iter + 1);
+  wc.vqfetch = c + ((11 + SHADE_CLASSES) * max_iter + 1);
   wc.wave = c + wave_counter_words(max_iter);
   wc.error = c + wave_counter_words(max_iter) + 1;
   wc.dbg = c + wave_counter_words(max_iter) + 4;
@@ -394,13 +397,21 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
   const bool split = (sc.features & SCENE_VOLUMES) == 0 && tu.split_shade;
   HitQueues hq = split ? HitQueues{r->hitq.as<uint32_t>(), r->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
   hq.inst = r->hit_inst.as<uint32_t>();
-  // volume scenes: delta tracking in its own kernel ahead of the shading
+  // volume scenes: delta tracking in its own kernel ahead of the shading;
+  // with split_volume it routes every path to the scattering, hit or miss
+  // queue, each shaded by its own kernel
   const bool vol_pre = full && !split && sc.volume_count > 0 && r->cap_vol >= r->cap_paths && r->cap_vol > 0;
+  const bool vsplit = vol_pre && tu.split_volume;
   if (vol_pre) {
     hq.vscatter = r->vol_scatter.as<float4>();
     hq.vrng = r->vol_rng.as<uint32_t>();
   }
-  const bool sort = split && tu.sort_threshold > 0 && wave_paths >= size_t(tu.sort_threshold);
+  if (vsplit) {
+    hq.hitq = r->hitq.as<uint32_t>();
+    hq.missq = r->missq.as<uint32_t>();
+    hq.vscatq = r->vol_q.as<uint32_t>();
+  }
+  const bool sort = (split || vsplit) && tu.sort_threshold > 0 && wave_paths >= size_t(tu.sort_threshold);
   // lean scenes: the hit queue sorted by shading class, one kernel per class
   const bool classes = sort && !full && tu.shade_classes;
   const size_t bin_words = size_t(2) * MAT_SORT_BINS;
@@ -417,7 +428,16 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
   for (int it = 0; it < max_iter; ++it) {
     const PathSoA in = path_soa(r, it & 1), out = path_soa(r, (it + 1) & 1);
     float4 *hits = r->hits.as<float4>();
-    timed(1, [&] { launch_trace(cfg, s, sc, in, hits, wc, it, counting ? stats + 3 : nullptr, tu.trace_refill, hq); });
+    HitQueues hq_trace = hq;
+    if (vsplit) // the tracking pre-pass writes the queues
+      hq_trace.hitq = hq_trace.missq = nullptr;
+    timed(1, [&] {
+      launch_trace(cfg, s, sc, in, hits, wc, it, counting ? stats + 3 : nullptr, tu.trace_refill, hq_trace);
+    });
+    if (vsplit) {
+      timed(5, [&] { launch_vol_scatter(cfg, s, rc, sc, in, hits, wc, it, hq, counting ? stats + 7 : nullptr); });
+      launches += 1;
+    }
     if (sort) {
       timed(2, [&] {
         launch_material_sort(cfg, s, sc, hits, hq, wc, it, r->sort_bins.as<uint32_t>() + size_t(it) * bin_words);
@@ -436,6 +456,11 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
       }
       timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 2}, hqi); });
       launches += 4;
+    } else if (vsplit) {
+      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 3}, hq); });
+      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 1}, hq); });
+      timed(2, [&] { launch_shade(cfg, s, rc, sc, in, out, hits, sh, ac, wc, it, ShadeVariant{full, 2}, hq); });
+      launches += 3;
     } else {
       if (vol_pre) {
         timed(5, [&] { launch_vol_scatter(cfg, s, rc, sc, in, hits, wc, it, hq, counting ? stats + 7 : nullptr); });
@@ -638,7 +663,8 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
       uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32),
       uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16) |
           (uint64_t(tu.shade_classes) << 23) | (uint64_t(tu.sort_threshold) << 24),
-      r->buf_gen, uint64_t(tu.wave_trip_cap) | (uint64_t(tu.vol_refill) << 32) | (uint64_t(tu.vol_passes) << 40)};
+      r->buf_gen, uint64_t(tu.wave_trip_cap) | (uint64_t(tu.vol_refill) << 32) | (uint64_t(tu.vol_passes) << 40) |
+          (uint64_t(tu.split_volume) << 60)};
   uint64_t launches = 0;
   KernelTimer timer;
   if (tu.time_kernels) {

@@ -12,8 +12,10 @@ namespace {
 // would use (dimension 1 + iteration), whose state after the tracking goes
 // with the result.  Tracking loops differ in length from path to path; in a
 // kernel of their own they no longer hold the lanes of the shading code.
+// With split queues (hq.vscatq) every path then joins the queue of its
+// outcome (it scatters, reaches its hit, or escapes).
 // lookups (or nullptr): density lookups made, added up over the grid.
-__global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restrict__ rcp, DevScene sc, PathSoA in,
+__global__ void __launch_bounds__(128, 7) k_vol_scatter(const RenderConst *__restrict__ rcp, DevScene sc, PathSoA in,
     const float4 *__restrict__ hits, WaveCounters wc, int it, HitQueues hq, unsigned long long *lookups)
 {
   if (wave_failed(wc))
@@ -28,7 +30,7 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
   const uint32_t lt_mask = (1u << lane) - 1u;
   VolTrack s;
   Rng rng(1u);
-  bool busy = false, exhausted = false;
+  bool busy = false, exhausted = false, lane_hit = false;
   uint32_t idx = 0, idle = WARP_FULL, nlook = 0;
   for (uint32_t trips = 0;; ++trips) {
     if (trips >= wc.trip_cap) { // warp-uniform
@@ -49,8 +51,8 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
           const uint4 info = in.info[idx];
           const float4 ro4 = in.ray_o[idx], rd4 = in.ray_d[idx], hit = hits[idx];
           rng = path_rng(info.x % rcp->npix, info.y, 1u + uint32_t(it));
-          const bool is_hit = __float_as_uint(hit.y) != 0xffffffffu;
-          vt_init(s, v3(ro4), v3(rd4), ro4.w, is_hit ? hit.x : rd4.w);
+          lane_hit = __float_as_uint(hit.y) != 0xffffffffu;
+          vt_init(s, v3(ro4), v3(rd4), ro4.w, lane_hit ? hit.x : rd4.w);
           busy = true;
         }
       }
@@ -61,15 +63,29 @@ __global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restri
         break;
       continue;
     }
+    uint32_t route = 0u; // the path finished on this trip: 1 it scatters, 2 it hits, 3 it misses
     if (busy) {
       nlook += vt_passes<true>(sc, s, rng, wc.vol_passes) == VT_LOOKUP ? 1u : 0u;
       if (s.done) {
         hq.vscatter[idx] = make_float4(s.t_event, s.albedo.x, s.albedo.y, s.albedo.z);
         hq.vrng[idx] = rng.s;
         busy = false;
+        route = s.t_event >= 0.f ? 1u : (lane_hit ? 2u : 3u);
       }
     }
     __syncwarp(); // every lane back from the step's divergent work before the vote
+    if (hq.vscatq != nullptr && __ballot_sync(WARP_FULL, route != 0u) != 0u) {
+      // split queues: each finished path joins the queue of its outcome
+      const uint32_t a = warp_append(wc.vcount + it, route == 1u);
+      if (route == 1u)
+        hq.vscatq[a] = idx;
+      const uint32_t b = warp_append(wc.hcount + it, route == 2u);
+      if (route == 2u)
+        hq.hitq[b] = idx;
+      const uint32_t m = warp_append(wc.mcount + it, route == 3u);
+      if (route == 3u)
+        hq.missq[m] = idx;
+    }
     idle = __ballot_sync(WARP_FULL, !busy);
   }
   if (lookups) { // the loop ends for the whole warp at once
@@ -98,8 +114,10 @@ void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, Dev
       k_shade<true, 0, false><<<b, 128, 0, s>>>(rc, sc, none, in, out, hits, sh, acc, wc, it, hq);
     else if (v.part == 1)
       k_shade<true, 1, false><<<b, 128, 0, s>>>(rc, sc, none, in, out, hits, sh, acc, wc, it, hq);
-    else
+    else if (v.part == 2)
       k_shade<true, 2, false><<<b, 128, 0, s>>>(rc, sc, none, in, out, hits, sh, acc, wc, it, hq);
+    else
+      k_shade<true, 3, false><<<b, 128, 0, s>>>(rc, sc, none, in, out, hits, sh, acc, wc, it, hq);
   } else {
     if (v.part == 0)
       k_shade<false, 0, false><<<b, 128, 0, s>>>(rc, sc, none, in, out, hits, sh, acc, wc, it, hq);

@@ -13,6 +13,9 @@
 //                 kernels over the index queues the trace kernel wrote
 //                 (scenes without volumes, where a miss cannot scatter);
 //   PART 0        every path of the iteration (volume scenes);
+//   PART 3        volume scenes with split queues: the paths that scatter in
+//                 a volume, while those that reach their surface hit or
+//                 escape go to PART 1 / 2 (the tracking pre-pass routes them);
 //   CLS           lean hit kernels specialised to the lobes of a shading
 //                 class (scene_types.h), each over its class's run of the
 //                 class-sorted hit queue: smaller kernels with fewer live
@@ -63,6 +66,8 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
   const uint32_t prim = __float_as_uint(hit.y);
   const bool is_hit = PART == 1 ? true : (PART == 2 ? false : prim != 0xffffffffu);
   Rng rng = path_rng(pixel, sample_index, 1u + uint32_t(it));
+  if (FULL && (PART == 1 || PART == 2) && pre) // split volume queues: the path did not scatter
+    rng = Rng(pre->rng);
   // The slot's radiance and alpha, read only on the branches that update them
   // (a secondary hit on a surface that does not emit toward the ray leaves
   // them alone): one scattered 16-byte load and four live registers fewer
@@ -79,7 +84,7 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
   };
 
   // Scattering inside a volume in front of the surface (pathtracer.cpp:789-858)
-  if (FULL && PART == 0 && sc.volume_count > 0) {
+  if (FULL && (PART == 0 || PART == 3) && sc.volume_count > 0) {
     V3 albedo{0.f, 0.f, 0.f};
     float t_sc;
     if (pre) { // tracked by k_vol_scatter: continue its random-number stream
@@ -142,6 +147,8 @@ __device__ __forceinline__ void shade_path(const RenderConst &rc, const DevScene
       return;
     }
   }
+  if (PART == 3) // the scattering queue holds only paths that scatter
+    return;
 
   if (PART != 1 && !is_hit) { // miss (pathtracer.cpp:860-899)
     a = acc.acc[slot];
@@ -353,7 +360,8 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
   static_assert(CLS == 0 || (PART == 1 && !FULL && !BATCH), "class kernels are lean hit kernels");
   if (wave_failed(wc))
     return;
-  const uint32_t n_all = PART == 0 ? wc.count[it] : (PART == 1 ? wc.hcount[it] : wc.mcount[it]);
+  const uint32_t n_all =
+      PART == 0 ? wc.count[it] : (PART == 1 ? wc.hcount[it] : (PART == 2 ? wc.mcount[it] : wc.vcount[it]));
   const bool sorted = PART == 1 && hq.sort_threshold != 0u && n_all >= hq.sort_threshold;
   uint32_t lo = 0, n = n_all;
   if (PART == 1 && hq.cls_end && sorted) {
@@ -362,7 +370,8 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
   } else if (CLS != 0) {
     return;
   }
-  uint32_t *fetch = CLS == 0 ? wc.fetch + 4 * it + (PART == 2 ? 2 : 1) : wc.cfetch + it * SHADE_CLASSES + CLS;
+  uint32_t *fetch = CLS != 0 ? wc.cfetch + it * SHADE_CLASSES + CLS
+                             : (PART == 3 ? wc.vqfetch + it : wc.fetch + 4 * it + (PART == 2 ? 2 : 1));
   for (;;) {
     const uint32_t base = warp_fetch(fetch);
     if (base >= n)
@@ -373,7 +382,10 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
     ShadowRec sr;
     uint32_t job_bits = 0;
     if (j < n) {
-      const uint32_t i = PART == 0 ? j : (PART == 1 ? (sorted ? hq.sorted[lo + j] : hq.hitq[j]) : hq.missq[j]);
+      const uint32_t i = PART == 0 ? j
+          : PART == 1          ? (sorted ? hq.sorted[lo + j] : hq.hitq[j])
+          : PART == 2          ? hq.missq[j]
+                               : hq.vscatq[j];
       const uint4 info = in.info[i];
       if (BATCH) {
         job_bits = info.w & ~((1u << BATCH_JOB_SHIFT) - 1u);
@@ -383,7 +395,7 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
       } else {
         const uint32_t inst = (PART != 2 && sc.inst_count) ? hq.inst[i] : INST_NONE;
         VolPre pre;
-        const bool has_pre = FULL && PART == 0 && hq.vscatter != nullptr;
+        const bool has_pre = FULL && hq.vscatter != nullptr; // volume scenes (PART 1 / 2: split queues)
         if (has_pre) {
           pre.s = hq.vscatter[i];
           pre.rng = hq.vrng[i];

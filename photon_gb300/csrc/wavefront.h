@@ -73,6 +73,8 @@ struct WaveCounters {
   uint32_t *fetch;   // [4 * max_iter] work counters: trace, shade (all/hits), shade misses, shadow
   uint32_t *vfetch;  // [2 * max_iter] work counters: volume scattering, shadow transmittance
   uint32_t *cfetch;  // [SHADE_CLASSES * max_iter] work counters of the class hit-shading kernels
+  uint32_t *vcount;  // [max_iter] paths that scatter in a volume (volume scenes, split queues)
+  uint32_t *vqfetch; // [max_iter] work counters of the shading of those paths
   uint32_t *wave;    // current wave index within the render call
   uint32_t *error;   // sticky error word
   uint32_t *dbg;     // [WAVE_DBG_WORDS] record of the first self-check failure
@@ -80,7 +82,7 @@ struct WaveCounters {
   uint32_t vol_refill; // a volume-tracking warp takes new rays once this many lanes are idle (tuning key vol_refill)
   uint32_t vol_passes; // tracking passes per lane and loop trip at most (tuning key vol_passes)
 };
-inline size_t wave_counter_words(int max_iter) { return size_t((10 + SHADE_CLASSES) * max_iter + 1); }
+inline size_t wave_counter_words(int max_iter) { return size_t((12 + SHADE_CLASSES) * max_iter + 1); }
 
 // Self-check of the persistent traversal loops: a warp that makes more than
 // WaveCounters::trip_cap loop trips (each trip is one traversal step of every
@@ -114,6 +116,11 @@ struct HitQueues {
   // path's random-number state after it, from which shading continues.
   float4 *vscatter = nullptr;
   uint32_t *vrng = nullptr;
+  // Volume scenes with split queues: k_vol_scatter routes every path, once
+  // its tracking is done, to vscatq (it scatters in a volume; wc.vcount),
+  // hitq or missq (it reaches its surface hit / escapes; wc.hcount /
+  // wc.mcount), and the closest-hit kernel writes no queue.
+  uint32_t *vscatq = nullptr;
   // Sorting by shading class (lean scenes): bins are grouped per class
   // (MAT_CLASS_BINS each, class-major), and after the sort cls_end[b] is
   // the end of bin b's run in `sorted`, so class c's hits are the run
@@ -126,7 +133,8 @@ constexpr uint32_t MAT_SORT_BINS = 1024; // materials map to bin = id % MAT_SORT
 constexpr uint32_t MAT_CLASS_BINS = MAT_SORT_BINS / SHADE_CLASSES; // sorting by class: bin = class * this + id % this
 
 // Shading kernel variants: FULL compiles volumes, material sources and
-// analytic lights; PART 0 shades every path, 1 the hit queue, 2 the misses.
+// analytic lights; PART 0 shades every path, 1 the hit queue, 2 the misses,
+// 3 the paths that scatter in a volume (FULL only).
 struct ShadeVariant {
   bool full;
   int part;
