@@ -522,9 +522,9 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
    "trace_blocks_per_sm", "shade_blocks_per_sm" (persistent grid sizes),
    "trace_refill" (a traversal warp takes new rays once this many lanes are
    idle), "split_shade" (0/1: hits and misses shaded by separate kernels),
-   "split_volume" (0/1: in volume scenes the tracking pre-pass routes the
-   paths that scatter in a volume, reach their surface hit or escape to
-   separate queues, each shaded by its own kernel),
+   "split_volume" (0/1: in volume scenes the paths that scatter in a
+   volume, reach their surface hit or escape go, after the tracking
+   pre-pass, to separate queues, each shaded by its own kernel),
    "shade_lean" (0/1: lean shading kernels for scenes without volumes /
    sources / lights), "sort_threshold" (sort the hit queue by material when it
    holds at least this many hits; 0: never), "max_leaf" (1..3, leaf size of the

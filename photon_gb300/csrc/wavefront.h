@@ -116,10 +116,10 @@ struct HitQueues {
   // path's random-number state after it, from which shading continues.
   float4 *vscatter = nullptr;
   uint32_t *vrng = nullptr;
-  // Volume scenes with split queues: k_vol_scatter routes every path, once
-  // its tracking is done, to vscatq (it scatters in a volume; wc.vcount),
-  // hitq or missq (it reaches its surface hit / escapes; wc.hcount /
-  // wc.mcount), and the closest-hit kernel writes no queue.
+  // Volume scenes with split queues: after k_vol_scatter, k_vol_route puts
+  // every path in vscatq (it scatters in a volume; wc.vcount), hitq or missq
+  // (it reaches its surface hit / escapes; wc.hcount / wc.mcount), and the
+  // closest-hit kernel writes no queue.
   uint32_t *vscatq = nullptr;
   // Sorting by shading class (lean scenes): bins are grouped per class
   // (MAT_CLASS_BINS each, class-major), and after the sort cls_end[b] is
@@ -207,6 +207,7 @@ void launch_shade_class(const LaunchCfg &c, cudaStream_t s, const RenderConst *r
 // lookups (or nullptr): the density lookups are added to it.
 void launch_vol_scatter(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,
     const float4 *hits, WaveCounters wc, int it, HitQueues hq, uint64_t *lookups);
+void launch_vol_route(const LaunchCfg &c, cudaStream_t s, const float4 *hits, WaveCounters wc, int it, HitQueues hq);
 void launch_shadow(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, ShadowSoA sh, Accum acc,
     WaveCounters wc, int it, uint64_t *stats, int refill);
 // Volume scenes, after launch_shadow: ratio-tracking transmittance of the
