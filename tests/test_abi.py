@@ -78,13 +78,19 @@ def test_defaults_are_the_bridges(photon):
 
 def test_tuning_round_trip(photon):
     p = photon
-    for key, val in (("wave_paths", 1 << 20), ("trace_refill", 12), ("split_shade", 0), ("batch_wave_paths", 99999)):
+    for key, val in (("wave_paths", 1 << 20), ("trace_refill", 12), ("split_shade", 0), ("batch_wave_paths", 99999),
+                     ("gpu_max_leaf", 3), ("ploc_radius", 16), ("split_volume", 0), ("gpu_tables", 0),
+                     ("texels_u8", 0), ("shade_classes", 0), ("vol_refill", 4), ("vol_passes", 2)):
         old = p.tuning_get(key)
         p.tuning_set(key, val)
         assert p.tuning_get(key) == val
         p.tuning_set(key, old)
-    with pytest.raises(ValueError):
-        p.tuning_set("trace_refill", 0)
+    for key, bad in (("trace_refill", 0), ("gpu_max_leaf", 4), ("ploc_radius", 1), ("ploc_radius", 33),
+                     ("split_volume", 2)):
+        old = p.tuning_get(key)
+        with pytest.raises(ValueError):
+            p.tuning_set(key, bad)
+        assert p.tuning_get(key) == old
     with pytest.raises(ValueError):
         p.tuning_set("no_such_key", 1)
     assert p.tuning_get("no_such_key") == -1
