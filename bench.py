@@ -890,7 +890,17 @@ def main():
                     help="render only this configuration (one warm-up and one timed render) and print its record "
                          "(profiling a small case; not a bench line)")
     ap.add_argument("--config-spp", type=int, default=0, help="samples per pixel of --config-only")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the adjoint/forward measurement and print its record (profiling; not a bench line)")
     args = ap.parse_args()
+    if args.adjoint_only:
+        import torch
+        torch.cuda.set_device(0)
+        from photon_gb300 import build as pbuild
+        pbuild.build()
+        import photon_gb300 as p
+        print(json.dumps(adjoint_vs_forward(p)), flush=True)
+        return
     if args.config_only:
         import torch
         torch.cuda.set_device(0)

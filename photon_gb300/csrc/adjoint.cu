@@ -1094,8 +1094,13 @@ __device__ __forceinline__ void adj_shade_path(const RenderConst &rc, const DevS
 #ifndef PHC_ADJ_MIN_BLOCKS
 #define PHC_ADJ_MIN_BLOCKS 8
 #endif
+// hq.hitq (optional): the closest-hit kernel's hit / miss queues, the hits
+// sorted by material when there are at least hq.sort_threshold of them; the
+// paths are then replayed hits first, in that order, then the misses, so
+// that a warp's lanes mostly run one material's code.
 __global__ void __launch_bounds__(128, PHC_ADJ_MIN_BLOCKS) k_adj_shade(const RenderConst *__restrict__ rcp, DevScene sc, AdjPathSoA in,
-    AdjPathSoA out, const float4 *__restrict__ hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a)
+    AdjPathSoA out, const float4 *__restrict__ hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a,
+    HitQueues hq)
 {
   if (wave_failed(wc)) // a traversal warp stopped at its trip cap: its results are incomplete
     return;
@@ -1113,8 +1118,15 @@ __global__ void __launch_bounds__(128, PHC_ADJ_MIN_BLOCKS) k_adj_shade(const Ren
     bool cont = false, has_sh = false;
     AdjNext nx;
     AdjShadow sr;
-    if (j < n)
-      adj_shade_path(rc, sc, in, j, hits[j], it, a, g, cont, nx, has_sh, sr);
+    if (j < n) {
+      uint32_t i = j;
+      if (hq.hitq) {
+        const uint32_t hc = wc.hcount[it];
+        const bool sorted = hq.sorted != nullptr && hq.sort_threshold != 0u && hc >= hq.sort_threshold;
+        i = j < hc ? (sorted ? hq.sorted[j] : hq.hitq[j]) : hq.missq[j - hc];
+      }
+      adj_shade_path(rc, sc, in, i, hits[i], it, a, g, cont, nx, has_sh, sr);
+    }
     const uint32_t o = warp_append(wc.count + it + 1, cont);
     if (cont) {
       out.p.ray_o[o] = nx.o;
@@ -1223,9 +1235,9 @@ __global__ void __launch_bounds__(256) k_adj_finish(uint32_t slots, AdjointArgs 
 } // namespace
 
 void launch_adj_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, AdjPathSoA in,
-    AdjPathSoA out, const float4 *hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a)
+    AdjPathSoA out, const float4 *hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a, HitQueues hq)
 {
-  k_adj_shade<<<c.blocks_shade, 128, 0, s>>>(rc, sc, in, out, hits, sh, wc, it, a);
+  k_adj_shade<<<c.blocks_shade, 128, 0, s>>>(rc, sc, in, out, hits, sh, wc, it, a, hq);
 }
 
 void launch_adj_resolve(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, AdjShadowSoA sh,

@@ -61,7 +61,8 @@ struct AdjointArgs {
 };
 
 void launch_adj_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, AdjPathSoA in,
-    AdjPathSoA out, const float4 *hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a);
+    AdjPathSoA out, const float4 *hits, AdjShadowSoA sh, WaveCounters wc, int it, AdjointArgs a,
+    HitQueues hq);
 void launch_adj_resolve(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, AdjShadowSoA sh,
     AdjPathSoA next, WaveCounters wc, int it, AdjointArgs a);
 void launch_adj_finish(cudaStream_t s, int blocks, uint32_t slots, AdjointArgs a);

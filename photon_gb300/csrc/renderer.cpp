@@ -1096,11 +1096,23 @@ void adjoint_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st
     ck(cudaMemsetAsync(wc.wave, 0, 4, s), "reset wave");
     ck(cudaMemsetAsync(q.collected, 0, size_t(cnt) * npix * 16, s), "reset adjoint");
     launch_raygen(cfg, s, drc, sc, q.path[0].p, accum(r), wc);
+    // the replay's hits sorted by material (tuning key adjoint_sort)
+    HitQueues rq{nullptr, nullptr};
+    const size_t bin_words = size_t(2) * MAT_SORT_BINS;
+    if (tu.adjoint_sort && tu.sort_threshold > 0) {
+      rq.hitq = r->hitq.as<uint32_t>();
+      rq.missq = r->missq.as<uint32_t>();
+      rq.sorted = r->hitq_sorted.as<uint32_t>();
+      rq.sort_threshold = uint32_t(tu.sort_threshold);
+      ck(cudaMemsetAsync(r->sort_bins.p, 0, size_t(max_iter) * bin_words * 4, s), "reset sort bins");
+    }
     for (int it = 0; it < max_iter; ++it) {
       const AdjPathSoA &in = q.path[it & 1], &out = q.path[(it + 1) & 1];
       float4 *hits = r->hits.as<float4>();
-      launch_trace(cfg, s, sc, in.p, hits, wc, it, nullptr, tu.trace_refill, HitQueues{nullptr, nullptr});
-      launch_adj_shade(acfg, s, drc, sc, in, out, hits, q.shadow, wc, it, a);
+      launch_trace(cfg, s, sc, in.p, hits, wc, it, nullptr, tu.trace_refill, rq);
+      if (rq.hitq)
+        launch_material_sort(cfg, s, sc, hits, rq, wc, it, r->sort_bins.as<uint32_t>() + size_t(it) * bin_words);
+      launch_adj_shade(acfg, s, drc, sc, in, out, hits, q.shadow, wc, it, a, rq);
       launch_shadow_deferred(cfg, s, sc, q.shadow.s, wc, it, tu.trace_refill);
       launch_adj_resolve(acfg, s, drc, sc, q.shadow, out, wc, it, a);
     }
