@@ -189,7 +189,6 @@ def scene_configs(p, reps=1, only=None, spp=0):
     depth 8) and the 2M-triangle instanced scene (12 RGBA8 2048^2 noise
     textures, 256^3 fBm volume, 1920^2, 256 spp, depth 12, adaptive
     sampling, so Msamples/s counts the pixel samples actually traced)."""
-    import torch
     from photon_gb300 import workloads
     out = {}
     for name, make in (("box_room_512", workloads.box_room), ("instanced_2m_1920", workloads.instanced_2m)):
@@ -237,12 +236,6 @@ def scene_configs(p, reps=1, only=None, spp=0):
                 "density_lookups": int(lookups), "lookups_per_pixel_sample": lookups / max(1, samples[k]),
                 "bytes_per_lookup": VOL_LOOKUP_BYTES, "ms_per_frame": vol_ms, "achieved": gbs, "peak": peak,
                 "unit": "GB/s", "frac": gbs / peak, "peak_source": f"{peak_kind} hbm_gbs"}
-        r.close()
-        torch.cuda.synchronize()
-        r = p.Renderer()  # the same upload again, in a new renderer: without the process's first-use costs
-        t = time.perf_counter()
-        r.set_scene(sc)
-        out[name]["upload_warm_s"] = time.perf_counter() - t
         r.close()
         del sc
     return out
