@@ -412,7 +412,8 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
     hq.vscatq = r->vol_q.as<uint32_t>();
   }
   // (volume scenes' hit queues stay unsorted: sorting them measured slower,
-  // 238.6 against 239.9 Msamples/s on the 2M scene)
+  // 238.6 against 239.9 Msamples/s on the 2M scene, and 238.6 when only the
+  // bounces after the first are sorted, their shading 0.94 -> 1.02-1.04 s)
   const bool sort = split && tu.sort_threshold > 0 && wave_paths >= size_t(tu.sort_threshold);
   // lean scenes: the hit queue sorted by shading class, one kernel per class
   const bool classes = sort && !full && tu.shade_classes;
