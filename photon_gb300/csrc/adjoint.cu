@@ -1092,7 +1092,7 @@ __device__ __forceinline__ void adj_shade_path(const RenderConst &rc, const DevS
 // Minimum resident 128-thread blocks per SM for the replay shading kernel
 // (caps its registers; see k_shade).
 #ifndef PHC_ADJ_MIN_BLOCKS
-#define PHC_ADJ_MIN_BLOCKS 8
+#define PHC_ADJ_MIN_BLOCKS 10
 #endif
 // hq.hitq (optional): the closest-hit kernel's hit / miss queues, the hits
 // sorted by material when there are at least hq.sort_threshold of them; the
