@@ -13,7 +13,7 @@ namespace {
 // with the result.  Tracking loops differ in length from path to path; in a
 // kernel of their own they no longer hold the lanes of the shading code.
 // lookups (or nullptr): density lookups made, added up over the grid.
-__global__ void __launch_bounds__(128, 7) k_vol_scatter(const RenderConst *__restrict__ rcp, DevScene sc, PathSoA in,
+__global__ void __launch_bounds__(128) k_vol_scatter(const RenderConst *__restrict__ rcp, DevScene sc, PathSoA in,
     const float4 *__restrict__ hits, WaveCounters wc, int it, HitQueues hq, unsigned long long *lookups)
 {
   if (wave_failed(wc))
