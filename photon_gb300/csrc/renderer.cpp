@@ -414,7 +414,12 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
   // (volume scenes' hit queues stay unsorted: sorting them measured slower,
   // 238.6 against 239.9 Msamples/s on the 2M scene, and 238.6 when only the
   // bounces after the first are sorted, their shading 0.94 -> 1.02-1.04 s)
-  const bool sort = split && tu.sort_threshold > 0 && wave_paths >= size_t(tu.sort_threshold);
+  // scenes whose materials all fall in one shading class run the same
+  // shading code for every hit: sorting gains nothing there and the
+  // shading's reads through the sorted order cost (box room 1503 against
+  // 1813 Msamples/s)
+  const bool sort = split && r->scene.shade_class_count > 1 && tu.sort_threshold > 0 &&
+      wave_paths >= size_t(tu.sort_threshold);
   // lean scenes: the hit queue sorted by shading class, one kernel per class
   const bool classes = sort && !full && tu.shade_classes;
   const size_t bin_words = size_t(2) * MAT_SORT_BINS;

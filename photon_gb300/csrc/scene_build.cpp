@@ -1297,6 +1297,10 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   tri_bytes = uint64_t(h.bvh.tris.size()) * 4;
   bvh_depth = h.bvh.max_depth;
   texel_count = h.texel_logical_count;
+  uint32_t class_mask = 0u;
+  for (const DevMaterial &m : h.materials)
+    class_mask |= 1u << (m.shade_class % SHADE_CLASSES);
+  shade_class_count = uint32_t(__builtin_popcount(class_mask));
   table_floats[PHC_TABLE_MAJORANTS] = h.vol_majorants.size();
   table_floats[PHC_TABLE_ENV_MARGINAL] = h.env_marginal.size();
   table_floats[PHC_TABLE_ENV_CONDITIONAL] = h.env_conditional.size();

@@ -125,6 +125,7 @@ struct DeviceScene {
   size_t bytes{0};
   uint64_t node_bytes{0}, tri_bytes{0};
   uint64_t texel_count{0};
+  uint32_t shade_class_count{0}; // distinct shading classes among the materials
   uint32_t bvh_depth{0};
   uint64_t table_floats[5]{}; // lengths of the tables phc_scene_table reads (PHC_TABLE_*)
   ~DeviceScene();
