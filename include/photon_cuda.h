@@ -526,7 +526,9 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
    volume, reach their surface hit or escape go, after the tracking
    pre-pass, to separate queues, each shaded by its own kernel),
    "adjoint_sort" (0/1: the adjoint's replay shades the hits of each bounce
-   sorted by material, hits before misses),
+   sorted by material, hits before misses), "class_threshold" (waves of at
+   least this many paths shade their hits with the shading-class kernels;
+   smaller waves use one lean hit kernel),
    "shade_lean" (0/1: lean shading kernels for scenes without volumes /
    sources / lights), "sort_threshold" (sort the hit queue by material when it
    holds at least this many hits; 0: never), "max_leaf" (1..3, leaf size of the

@@ -112,7 +112,7 @@ struct phc_renderer {
   uint32_t width{0}, height{0}, samples{0}, sample_counter{0};
   // graph of one wave
   cudaGraphExec_t graph{nullptr};
-  uint64_t graph_key[7]{};
+  uint64_t graph_key[8]{};
   // bumped whenever a buffer a recorded wave graph points to is reallocated
   uint64_t buf_gen{0};
   uint64_t graph_launches{0}; // kernels per replay of the wave graph
@@ -421,7 +421,9 @@ uint64_t record_wave(phc_renderer *r, cudaStream_t s, const LaunchCfg &cfg, cons
   const bool sort = split && r->scene.shade_class_count > 1 && tu.sort_threshold > 0 &&
       wave_paths >= size_t(tu.sort_threshold);
   // lean scenes: the hit queue sorted by shading class, one kernel per class
-  const bool classes = sort && !full && tu.shade_classes;
+  // (waves below class_threshold paths keep one lean hit kernel: the class
+  // kernels' launches and tails cost more than they save on small waves)
+  const bool classes = sort && !full && tu.shade_classes && wave_paths >= size_t(tu.class_threshold);
   const size_t bin_words = size_t(2) * MAT_SORT_BINS;
   if (sort) { // sort_bins sized by ensure_wave_buffers (no allocation while a graph is captured)
     hq.sorted = r->hitq_sorted.as<uint32_t>();
@@ -667,13 +669,14 @@ void render_impl(phc_renderer *r, const phc_camera &cam, const phc_settings &st,
 
   ck(cudaEventRecord(r->ev0, s), "event");
   // everything the recorded launch sequence depends on
-  const uint64_t key[7] = {uint64_t(npix) | (uint64_t(lanes) << 32),
+  const uint64_t key[8] = {uint64_t(npix) | (uint64_t(lanes) << 32),
       uint64_t(max_iter) | (uint64_t(rc.adaptive) << 32), r->scene_generation,
       uint64_t(counting) | (uint64_t(cfg.blocks_trace) << 8) | (uint64_t(cfg.blocks_shade) << 32),
       uint64_t(tu.trace_refill) | (uint64_t(tu.split_shade) << 8) | (uint64_t(tu.shade_lean) << 16) |
           (uint64_t(tu.shade_classes) << 23) | (uint64_t(tu.sort_threshold) << 24),
       r->buf_gen, uint64_t(tu.wave_trip_cap) | (uint64_t(tu.vol_refill) << 32) | (uint64_t(tu.vol_passes) << 40) |
-          (uint64_t(tu.split_volume) << 60)};
+          (uint64_t(tu.split_volume) << 60),
+      uint64_t(tu.class_threshold)};
   uint64_t launches = 0;
   KernelTimer timer;
   if (tu.time_kernels) {
@@ -809,7 +812,7 @@ BatchPlan plan_batch(const std::vector<phc_renderer *> &rs, const std::vector<Jo
 }
 
 void record_batch_wave(phc_renderer *lead, cudaStream_t s, const LaunchCfg &cfg, const BatchTable &bt, int max_iter,
-    uint32_t features)
+    uint32_t features, uint32_t max_items)
 {
   const Tuning &tu = tuning();
   const WaveCounters wc = wave_counters(lead, max_iter);
@@ -821,10 +824,13 @@ void record_batch_wave(phc_renderer *lead, cudaStream_t s, const LaunchCfg &cfg,
   HitQueues hq =
       split ? HitQueues{lead->hitq.as<uint32_t>(), lead->missq.as<uint32_t>()} : HitQueues{nullptr, nullptr};
   const bool sort = split && tu.sort_threshold > 0;
+  // lean batches: the hit queue sorted by shading class, one kernel per class
+  const bool classes = sort && !full && tu.shade_classes && max_items >= uint64_t(tu.class_threshold);
   const size_t bin_words = size_t(2) * MAT_SORT_BINS;
   if (sort) { // sort_bins sized by ensure_wave_buffers
     hq.sorted = lead->hitq_sorted.as<uint32_t>();
     hq.sort_threshold = uint32_t(tu.sort_threshold);
+    hq.classes = classes ? 1u : 0u;
     ck(cudaMemsetAsync(lead->sort_bins.p, 0, size_t(max_iter) * bin_words * 4, s), "reset sort bins");
   }
   float4 *hits = lead->hits.as<float4>();
@@ -836,8 +842,14 @@ void record_batch_wave(phc_renderer *lead, cudaStream_t s, const LaunchCfg &cfg,
       launch_material_sort_batch(cfg, s, bt, in.info, hits, hq, wc, it,
           lead->sort_bins.as<uint32_t>() + size_t(it) * bin_words);
     if (split) {
-      launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 1}, hq);
-      launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 2}, hq);
+      HitQueues hqi = hq;
+      if (classes) // the scatter leaves each bin's end in the upper half of the iteration's bins
+        hqi.cls_end = lead->sort_bins.as<uint32_t>() + size_t(it) * bin_words + MAT_SORT_BINS;
+      launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 1}, hqi);
+      if (classes)
+        for (uint32_t c = 1; c < SHADE_CLASSES; ++c)
+          launch_shade_class_batch(cfg, s, bt, in, out, hits, sh, wc, it, c, hqi);
+      launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 2}, hqi);
     } else {
       launch_shade_batch(cfg, s, bt, in, out, hits, sh, wc, it, ShadeVariant{full, 0}, hq);
     }
@@ -915,7 +927,7 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
     cudaGraphExec_t ge = nullptr;
     ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
     try {
-      record_batch_wave(lead, s, cfg, bt, bp.max_iter, bp.features);
+      record_batch_wave(lead, s, cfg, bt, bp.max_iter, bp.features, bp.max_items);
     } catch (...) {
       cudaStreamEndCapture(s, &g);
       if (g)
@@ -941,7 +953,7 @@ void render_batch_impl(const phc_job *jobs, uint32_t n, phc_render_stats *out_st
     cudaGraphExecDestroy(ge);
   } else {
     for (uint32_t wv = 0; wv < waves; ++wv)
-      record_batch_wave(lead, s, cfg, bt, bp.max_iter, bp.features);
+      record_batch_wave(lead, s, cfg, bt, bp.max_iter, bp.features, bp.max_items);
   }
   for (size_t j = 0; j < rs.size(); ++j)
     launch_resolve(s, accum(rs[j]), frame_of(rs[j]), plans[j].npix, plans[j].lanes, float(plans[j].rc.spp),

@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
     PathSoA in, PathSoA out, const float4 *__restrict__ hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it,
     HitQueues hq)
 {
-  static_assert(CLS == 0 || (PART == 1 && !FULL && !BATCH), "class kernels are lean hit kernels");
+  static_assert(CLS == 0 || (PART == 1 && !FULL), "class kernels are lean hit kernels");
   if (wave_failed(wc))
     return;
   const uint32_t n_all =
@@ -390,8 +390,8 @@ __global__ void __launch_bounds__(128, FULL ? PHC_SHADE_MIN_BLOCKS_FULL : PHC_SH
       if (BATCH) {
         job_bits = info.w & ~((1u << BATCH_JOB_SHIFT) - 1u);
         const BatchJob &J = bt.jobs[info.w >> BATCH_JOB_SHIFT];
-        shade_path<FULL, PART>(J.rc, J.sc, in.ray_o[i], in.ray_d[i], in.tp[i], info, in.pdist[i], hits[i], J.acc,
-            it, cont, np, has_sh, sr);
+        shade_path<FULL, PART, SHADE_CLASS_LOBES[CLS]>(J.rc, J.sc, in.ray_o[i], in.ray_d[i], in.tp[i], info,
+            in.pdist[i], hits[i], J.acc, it, cont, np, has_sh, sr);
       } else {
         const uint32_t inst = (PART != 2 && sc.inst_count) ? hq.inst[i] : INST_NONE;
         VolPre pre;

@@ -38,6 +38,7 @@ const Key *keys(size_t &n)
       {"split_shade", "PHC_TUNE_SPLIT_SHADE", 0, 1, nullptr, &g_tuning.split_shade},
       {"split_volume", "PHC_TUNE_SPLIT_VOLUME", 0, 1, nullptr, &g_tuning.split_volume},
       {"adjoint_sort", "PHC_TUNE_ADJOINT_SORT", 0, 1, nullptr, &g_tuning.adjoint_sort},
+      {"class_threshold", "PHC_TUNE_CLASS_THRESHOLD", 0, int64_t(1) << 30, &g_tuning.class_threshold, nullptr},
       {"shade_lean", "PHC_TUNE_SHADE_LEAN", 0, 1, nullptr, &g_tuning.shade_lean},
       {"shade_classes", "PHC_TUNE_SHADE_CLASSES", 0, 1, nullptr, &g_tuning.shade_classes},
       {"batch_wave_paths", "PHC_TUNE_BATCH_WAVE_PATHS", 1024, int64_t(1) << 30, &g_tuning.batch_wave_paths, nullptr},

@@ -25,6 +25,7 @@ struct Tuning {
   int split_shade{1};                // misses and hits shaded by separate kernels (no-volume scenes)
   int split_volume{1};               // volume scenes: scattering, hit and miss paths shaded by separate kernels
   int adjoint_sort{1};               // the adjoint replay shades its hits sorted by material
+  int64_t class_threshold{1 << 26};  // waves of at least this many paths shade hits with the class kernels
   int shade_lean{1};                 // lean shading kernels for scenes without volumes/sources/lights
   int shade_classes{1};              // lean scenes: hit queue sorted by shading class, one kernel per class
   int64_t batch_wave_paths{1 << 25}; // paths per wave of a batched render

@@ -332,7 +332,10 @@ __device__ __forceinline__ uint32_t hit_bin(const DevScene &sc, const BatchTable
   const uint32_t prim = __float_as_uint(hits[qi].y);
   if (BATCH) {
     const uint32_t job = info[qi].w >> BATCH_JOB_SHIFT;
-    return (job * 1031u + __ldg(&bt.jobs[job].sc.prim_vidx[prim].w)) % MAT_SORT_BINS;
+    const uint32_t mat = __ldg(&bt.jobs[job].sc.prim_vidx[prim].w);
+    if (hq.classes)
+      return __ldg(&bt.jobs[job].sc.materials[mat].shade_class) * MAT_CLASS_BINS + (job * 1031u + mat) % MAT_CLASS_BINS;
+    return (job * 1031u + mat) % MAT_SORT_BINS;
   }
   const uint32_t mat = __ldg(&sc.prim_vidx[prim].w);
   if (hq.classes)

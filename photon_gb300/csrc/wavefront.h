@@ -202,6 +202,9 @@ void launch_shade(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, Dev
 // launch_shade's lean hit kernel.
 void launch_shade_class(const LaunchCfg &c, cudaStream_t s, const RenderConst *rc, DevScene sc, PathSoA in,
     PathSoA out, const float4 *hits, ShadowSoA sh, Accum acc, WaveCounters wc, int it, uint32_t cls, HitQueues hq);
+// The batched wavefront's class kernels (shade_classes_batch.cu).
+void launch_shade_class_batch(const LaunchCfg &c, cudaStream_t s, BatchTable bt, PathSoA in, PathSoA out,
+    const float4 *hits, ShadowSoA sh, WaveCounters wc, int it, uint32_t cls, HitQueues hq);
 // Delta tracking of every path of iteration `it` through the scene's volumes
 // (the first step of pt_shade for volume scenes), into hq.vscatter / hq.vrng.
 // lookups (or nullptr): the density lookups are added to it.

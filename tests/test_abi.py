@@ -80,7 +80,8 @@ def test_tuning_round_trip(photon):
     p = photon
     for key, val in (("wave_paths", 1 << 20), ("trace_refill", 12), ("split_shade", 0), ("batch_wave_paths", 99999),
                      ("gpu_max_leaf", 3), ("ploc_radius", 16), ("split_volume", 0), ("gpu_tables", 0),
-                     ("texels_u8", 0), ("shade_classes", 0), ("vol_refill", 4), ("vol_passes", 2), ("adjoint_sort", 0)):
+                     ("texels_u8", 0), ("shade_classes", 0), ("vol_refill", 4), ("vol_passes", 2), ("adjoint_sort", 0),
+                     ("class_threshold", 1 << 20)):
         old = p.tuning_get(key)
         p.tuning_set(key, val)
         assert p.tuning_get(key) == val

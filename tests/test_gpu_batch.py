@@ -81,3 +81,35 @@ def test_batch_with_adaptive_job_and_errors(photon):
     c = photon.Renderer()  # no scene
     with pytest.raises(PhotonError, match="NO_SCENE"):
         photon.render_batch([(b, cam2, st2, True), (c, cam2, st2, True)])
+
+
+def test_batch_class_kernels_match_plain(photon):
+    """Lean jobs only (procedural Disney materials of several shading
+    classes), with the material sort and the class kernels forced on for
+    every wave (tuning keys sort_threshold 1, class_threshold 0): the
+    batched wavefront's class kernels (shade_classes_batch.cu) leave every
+    job with the image its own render gives, bit for bit."""
+    from photon_gb300 import tuning_get, tuning_set, workloads
+    keys = {"sort_threshold": 1, "class_threshold": 0}
+    old = {k: tuning_get(k) for k in keys}
+    try:
+        for k, v in keys.items():
+            tuning_set(k, v)
+        jobs = list(workloads.batched_jobs(seed=5, n=6, max_tris=30_000, min_res=32, max_res=64, spp=(2, 6)))
+        plain, batch = [], []
+        for sc, cam, st in jobs:
+            a = photon.Renderer()
+            a.set_scene(sc)
+            b = photon.Renderer()
+            b.set_scene(sc)
+            plain.append(a)
+            batch.append(b)
+        for r, (sc, cam, st) in zip(plain, jobs):
+            r.render(cam, st, True)
+        photon.render_batch([(r, cam, st, True) for r, (sc, cam, st) in zip(batch, jobs)])
+        for k, (a, b) in enumerate(zip(plain, batch)):
+            for ch in CHANNELS:
+                assert np.array_equal(_bits(a.read(ch)), _bits(b.read(ch))), f"job {k} {ch}"
+    finally:
+        for k, v in old.items():
+            tuning_set(k, v)
