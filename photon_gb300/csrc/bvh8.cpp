@@ -454,10 +454,8 @@ void build_bvh8_boxes(const float *boxes, uint64_t count, Bvh8Host &out, int max
   build_from_refs(b, nullptr, nullptr, out);
 }
 
-void build_prim_records(const float *positions, const uint32_t *indices, uint64_t triangle_count,
-    std::vector<float> &prim_geo)
+void build_prim_records(const float *positions, const uint32_t *indices, uint64_t triangle_count, float *prim_geo)
 {
-  prim_geo.resize(size_t(triangle_count) * 12);
 #pragma omp parallel for schedule(static)
   for (int64_t t = 0; t < int64_t(triangle_count); ++t) {
     const float *v0 = &positions[3 * size_t(indices[3 * size_t(t) + 0])];

@@ -50,8 +50,7 @@ void build_bvh8(const float *positions, uint64_t vertex_count, const uint32_t *i
 void build_bvh8_boxes(const float *boxes, uint64_t count, Bvh8Host &out, int max_leaf = 1);
 
 // Per-primitive triangle records (v0, e1, e2 as in the leaf records) in
-// primitive order, for shading.
-void build_prim_records(const float *positions, const uint32_t *indices, uint64_t triangle_count,
-    std::vector<float> &prim_geo);
+// primitive order, for shading: 12 floats per triangle into prim_geo.
+void build_prim_records(const float *positions, const uint32_t *indices, uint64_t triangle_count, float *prim_geo);
 
 } // namespace phc

@@ -512,8 +512,8 @@ void build_instancing(const phc_pt_scene &pt, bool has_scene_tris, const float l
       s.prim_vidx.push_back(vbase + ob.indices[3 * t + 2]);
       s.prim_vidx.push_back(mat);
     }
-    std::vector<float> geo;
-    build_prim_records(ob.positions, ob.indices, ob.triangle_count, geo);
+    std::vector<float> geo(size_t(ob.triangle_count) * 12);
+    build_prim_records(ob.positions, ob.indices, ob.triangle_count, geo.data());
     for (size_t t = 0; t < ob.triangle_count; ++t) { // record ids are global primitive ids
       const uint32_t id = prim_base + uint32_t(t);
       std::memcpy(&geo[12 * t + 3], &id, 4);
@@ -665,52 +665,66 @@ void build_host_scene(const phc_scene_desc &in, HostScene &s)
   }
   if (tc > 0x3fffffffull || vc > 0xffffffffull)
     throw std::length_error("scene: too many triangles or vertices");
-  std::vector<float> pos3(vc * 3);
+  // the per-vertex and per-triangle arrays, each filled by one parallel loop
+  // (element by element the same values as a sequential copy)
+  HostVec<float> pos3(vc * 3);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < int64_t(vc * 3); ++i)
+    pos3[size_t(i)] = empty ? 0.f : in.positions[i];
+  // the scene's extent, in vertex order (RenderBridge.cpp:815-820)
   float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
   for (size_t i = 0; i < vc; ++i)
     for (int a = 0; a < 3; ++a) {
-      const float p = empty ? 0.f : in.positions[3 * i + a];
-      pos3[3 * i + a] = p;
+      const float p = pos3[3 * i + a];
       lo[a] = lo[a] < p ? lo[a] : p;
       hi[a] = hi[a] > p ? hi[a] : p;
     }
   s.indices.resize(tc * 3);
-  for (size_t i = 0; i < tc * 3; ++i) {
+  int bad_index = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad_index)
+  for (int64_t i = 0; i < int64_t(tc * 3); ++i) {
     const uint32_t v = empty ? uint32_t(i) : in.indices[i];
-    if (v >= vc)
-      throw std::out_of_range("scene: vertex index out of range");
-    s.indices[i] = v;
+    bad_index |= v >= vc ? 1 : 0;
+    s.indices[size_t(i)] = v;
   }
+  if (bad_index)
+    throw std::out_of_range("scene: vertex index out of range");
   const uint32_t material_count = uint32_t(std::max<size_t>(in.material_count, 1));
   s.material_ids.resize(tc);
-  for (size_t i = 0; i < tc; ++i) {
-    const uint32_t id = (!empty && in.material_ids && i < in.material_id_count) ? in.material_ids[i] : 0u;
-    s.material_ids[i] = id < material_count ? id : 0u;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < int64_t(tc); ++i) {
+    const uint32_t id =
+        (!empty && in.material_ids && uint64_t(i) < in.material_id_count) ? in.material_ids[i] : 0u;
+    s.material_ids[size_t(i)] = id < material_count ? id : 0u;
   }
   s.positions4.resize(vc * 4);
-  for (size_t i = 0; i < vc; ++i) {
-    s.positions4[4 * i] = pos3[3 * i];
-    s.positions4[4 * i + 1] = pos3[3 * i + 1];
-    s.positions4[4 * i + 2] = pos3[3 * i + 2];
-    s.positions4[4 * i + 3] = 0.f;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < int64_t(vc); ++i) {
+    s.positions4[4 * size_t(i)] = pos3[3 * size_t(i)];
+    s.positions4[4 * size_t(i) + 1] = pos3[3 * size_t(i) + 1];
+    s.positions4[4 * size_t(i) + 2] = pos3[3 * size_t(i) + 2];
+    s.positions4[4 * size_t(i) + 3] = 0.f;
   }
   if (!empty && in.normals) {
     s.normals4.resize(vc * 4);
-    for (size_t i = 0; i < vc; ++i) {
-      s.normals4[4 * i] = in.normals[3 * i];
-      s.normals4[4 * i + 1] = in.normals[3 * i + 1];
-      s.normals4[4 * i + 2] = in.normals[3 * i + 2];
-      s.normals4[4 * i + 3] = 0.f;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < int64_t(vc); ++i) {
+      s.normals4[4 * size_t(i)] = in.normals[3 * i];
+      s.normals4[4 * size_t(i) + 1] = in.normals[3 * i + 1];
+      s.normals4[4 * size_t(i) + 2] = in.normals[3 * i + 2];
+      s.normals4[4 * size_t(i) + 3] = 0.f;
     }
   }
   s.prim_vidx.resize(tc * 4);
-  for (size_t t = 0; t < tc; ++t) {
-    s.prim_vidx[4 * t] = s.indices[3 * t];
-    s.prim_vidx[4 * t + 1] = s.indices[3 * t + 1];
-    s.prim_vidx[4 * t + 2] = s.indices[3 * t + 2];
-    s.prim_vidx[4 * t + 3] = s.material_ids[t];
+#pragma omp parallel for schedule(static)
+  for (int64_t t = 0; t < int64_t(tc); ++t) {
+    s.prim_vidx[4 * size_t(t)] = s.indices[3 * size_t(t)];
+    s.prim_vidx[4 * size_t(t) + 1] = s.indices[3 * size_t(t) + 1];
+    s.prim_vidx[4 * size_t(t) + 2] = s.indices[3 * size_t(t) + 2];
+    s.prim_vidx[4 * size_t(t) + 3] = s.material_ids[size_t(t)];
   }
-  build_prim_records(pos3.data(), s.indices.data(), tc, s.prim_geo);
+  s.prim_geo.resize(tc * 12);
+  build_prim_records(pos3.data(), s.indices.data(), tc, s.prim_geo.data());
   const phc_pt_scene *pt = in.pt;
   if (pt) {
     if (in.material_count && !pt->materials)

@@ -32,6 +32,10 @@ template <class T> struct UninitAlloc : std::allocator<T> {
   }
 };
 
+// Host arrays of a scene's geometry: filled by parallel loops right after
+// they are sized.
+template <class T> using HostVec = std::vector<T, UninitAlloc<T>>;
+
 // Sets the message phc_global_error returns on this thread.
 void set_global_error(const std::string &msg);
 
@@ -39,12 +43,12 @@ void set_global_error(const std::string &msg);
 // builds (RenderBridge.cpp:441-826) plus the light tables of
 // PathTracer::build_light_tables (pathtracer.cpp:411-503).
 struct HostScene {
-  std::vector<float> positions4;      // vertices as float4
-  std::vector<uint32_t> indices;      // 3 per triangle
-  std::vector<uint32_t> material_ids; // clamped like the bridge
-  std::vector<float> normals4;        // empty: none
-  std::vector<uint32_t> prim_vidx;    // (i0, i1, i2, material) per triangle
-  std::vector<float> prim_geo;        // 12 floats per triangle
+  HostVec<float> positions4;      // vertices as float4
+  HostVec<uint32_t> indices;      // 3 per triangle
+  HostVec<uint32_t> material_ids; // clamped like the bridge
+  HostVec<float> normals4;        // empty: none
+  HostVec<uint32_t> prim_vidx;    // (i0, i1, i2, material) per triangle
+  HostVec<float> prim_geo;        // 12 floats per triangle
   std::vector<DevMaterial> materials;
   std::vector<float> attr_values;     // float4
   int32_t attr_offset[5]{-1, -1, -1, -1, -1};
