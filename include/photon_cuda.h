@@ -537,7 +537,11 @@ int phc_trace_closest_compact_static(phc_accel *a, const float *origins, const f
    upload), "gpu_max_leaf" (1..3, leaf size of the GPU-built BVH8, read at
    the next scene upload), "ploc_radius" (2..32: clusters the GPU build's
    clustering searches on each side, rounded up to 2, 4, 8, 16 or 32; read
-   at the next scene upload), "batch_wave_paths", "use_graph" (0/1),
+   at the next scene upload), "collapse_tri_cost" (0..10000: a triangle
+   test's cost in percent of a node visit, with which the GPU build chooses
+   each wide node's children by the surface-area cost of the whole tree,
+   default 30; 0: the largest subtrees are opened first; read at the next
+   scene upload), "batch_wave_paths", "use_graph" (0/1),
    "count_traversal" (0/1: node / triangle / density-lookup counters),
    "time_kernels" (0/1), "shade_classes" (0/1: lean scenes sort the hit queue
    by shading class and shade each class with a kernel compiled for its

@@ -4,8 +4,8 @@ Coordinate descent on one workload: each key in turn takes every candidate
 value of SPACE with the other keys fixed, and keeps the value with the lowest
 median device time of a render call (phc_render's render_ms, after a warm-up
 call).  Passes repeat until a pass changes nothing or `passes` is reached.
-"max_leaf", "gpu_bvh", "gpu_max_leaf" and "ploc_radius" change the BVH8 and
-are applied by re-uploading the scene.
+"max_leaf", "gpu_bvh", "gpu_max_leaf", "ploc_radius" and "collapse_tri_cost"
+change the BVH8 and are applied by re-uploading the scene.
 
 The reference has no tunables on this path; the keys are this renderer's:
 queue capacity (wave_paths), persistent grid sizes of the traversal and
@@ -34,8 +34,9 @@ SPACE = {
     "gpu_bvh": [0, 1],
     "gpu_max_leaf": [1, 2, 3],
     "ploc_radius": [2, 4, 8, 16, 32],
+    "collapse_tri_cost": [0, 20, 30, 50],
 }
-SCENE_KEYS = {"max_leaf", "gpu_bvh", "gpu_max_leaf", "ploc_radius"}  # read at scene upload
+SCENE_KEYS = {"max_leaf", "gpu_bvh", "gpu_max_leaf", "ploc_radius", "collapse_tri_cost"}  # read at scene upload
 
 
 class RenderTimer:

@@ -23,7 +23,13 @@
 //      (subtrees of more than max_leaf primitives opened first), the octant
 //      slot order and the outward-rounded 8-bit child grid of the host
 //      builder; a descendant with at most max_leaf primitives (1..3) is one
-//      leaf child.
+//      leaf child.  With a triangle cost (tuning key collapse_tri_cost) the
+//      descendants are chosen instead by the surface-area cost of the whole
+//      wide tree (the dynamic program of Ylitie, Karras and Laine,
+//      "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
+//      BVHs", HPG 2017): bottom-up, the cheapest way to cover every
+//      binary subtree with 1..8 slots, then the collapse follows those
+//      choices from the root down.
 //
 // The result is deterministic except for where nodes and leaf records land
 // in memory (atomic allocation order), which changes no traversal result.
@@ -617,6 +623,303 @@ __global__ void __launch_bounds__(128) k_collapse(Collapse c, const uint2 *__res
   }
 }
 
+// ---------------------------------------------------------------- stage 4a
+// The collapse's surface-area program.  cost(u, j), for j = 1..8: the least
+// expected cost of covering binary subtree u with at most j child slots of
+// its wide parent, each slot holding a descendant w of u as a leaf child
+// (area(w) x primitives x tri_cost, when it has at most max_leaf primitives)
+// or as a wide inner node (area(w) x 1 + the cheapest cover of w's two
+// subtrees by 8 slots); for j >= 2 u may also be opened, its two subtrees
+// sharing the j slots.  A binary leaf (one primitive) is always a one-
+// primitive leaf child.  One launch per clustering iteration's new nodes:
+// their children come from earlier iterations, so they are final.
+struct CollapseDp {
+  float *cost;     // 8 per internal node: cost(v, j + 1)
+  uint8_t *split;  // 8 per internal node, entry j for j + 1 slots: 0 = v fills one slot, k = v opened, k slots
+                   // for its left subtree
+  uchar4 *info;    // per internal node: x = the split of v as a wide inner node, y = 1 when v fills one slot as a
+                   // leaf child, z = its primitives (at most 255)
+};
+
+__device__ __forceinline__ float dp_cost(const CollapseDp &d, const float *nbox, uint32_t n, int u, int j, float ct)
+{
+  return uint32_t(u) < n ? node_area(nbox, u) * ct : d.cost[8 * size_t(uint32_t(u) - n) + j];
+}
+
+// The program's entries of internal node v (its children's are final).
+__device__ void collapse_dp_node(const CollapseDp &d, const float *__restrict__ nbox, const int2 *__restrict__ nchild,
+    uint32_t n, uint32_t v, float ct, int max_leaf)
+{
+  const int2 c = nchild[v];
+  float cl[8], cr[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    cl[j] = dp_cost(d, nbox, n, c.x, j, ct);
+    cr[j] = dp_cost(d, nbox, n, c.y, j, ct);
+  }
+  const uint32_t pl = uint32_t(c.x) < n ? 1u : d.info[uint32_t(c.x) - n].z;
+  const uint32_t pr = uint32_t(c.y) < n ? 1u : d.info[uint32_t(c.y) - n].z;
+  const uint32_t p = min(pl + pr, 255u);
+  // open v: the cheapest share of j slots between its subtrees (j = 2..8)
+  float sc[8];
+  uint8_t sk[8];
+  sc[0] = 3.4e38f;
+  sk[0] = 0;
+#pragma unroll
+  for (int j = 2; j <= 8; ++j) {
+    float best = 3.4e38f;
+    int bk = 1;
+#pragma unroll
+    for (int k = 1; k < j; ++k) {
+      const float x = cl[k - 1] + cr[j - k - 1];
+      if (x < best) {
+        best = x;
+        bk = k;
+      }
+    }
+    sc[j - 1] = best;
+    sk[j - 1] = uint8_t(bk);
+  }
+  const float a = node_area(nbox, int(v));
+  const float c_inner = a + sc[7];
+  const bool leaf = p <= uint32_t(max_leaf) && a * float(p) * ct <= c_inner;
+  const float self = leaf ? a * float(p) * ct : c_inner;
+  float *co = d.cost + 8 * size_t(v - n);
+  uint8_t *sp = d.split + 8 * size_t(v - n);
+  co[0] = self;
+  sp[0] = 0;
+#pragma unroll
+  for (int j = 1; j < 8; ++j) {
+    const bool open = sc[j] < self;
+    co[j] = open ? sc[j] : self;
+    sp[j] = open ? sk[j] : 0;
+  }
+  d.info[v - n] = make_uchar4(sk[7], leaf ? 1 : 0, uint8_t(p), 0);
+}
+
+__global__ void __launch_bounds__(128) k_collapse_dp(CollapseDp d, const float *__restrict__ nbox,
+    const int2 *__restrict__ nchild, uint32_t n, uint32_t lo, uint32_t hi, float ct, int max_leaf)
+{
+  for (uint32_t v = lo + blockIdx.x * blockDim.x + threadIdx.x; v < hi; v += gridDim.x * blockDim.x)
+    if (v >= n)
+      collapse_dp_node(d, nbox, nchild, n, v, ct, max_leaf);
+}
+
+// One wide node from its k candidates ch[i] (lc[i] primitives as a leaf
+// child, 0 for an inner node): octant slots, quantised child boxes, the leaf
+// records and the queue entries of the inner children, as k_collapse does.
+__device__ void write_wide_node(const Collapse &c, uint32_t ni, const int *ch, const int *lc, int k, uint2 *qout)
+{
+  int prims[3];
+  float nlo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, nhi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  for (int i = 0; i < k; ++i)
+    for (int a = 0; a < 3; ++a) {
+      nlo[a] = fminf(nlo[a], c.nbox[6 * size_t(ch[i]) + a]);
+      nhi[a] = fmaxf(nhi[a], c.nbox[6 * size_t(ch[i]) + 3 + a]);
+    }
+  // octant slots, greedily by the smallest cost (the host builder's rule)
+  float pc[3];
+  for (int a = 0; a < 3; ++a)
+    pc[a] = 0.5f * (nlo[a] + nhi[a]);
+  float cost[8][8];
+  for (int i = 0; i < k; ++i) {
+    float cc[3];
+    for (int a = 0; a < 3; ++a)
+      cc[a] = 0.5f * (c.nbox[6 * size_t(ch[i]) + a] + c.nbox[6 * size_t(ch[i]) + 3 + a]) - pc[a];
+    for (int s = 0; s < 8; ++s) {
+      const float dx = (s & 4) ? -1.f : 1.f, dy = (s & 2) ? -1.f : 1.f, dz = (s & 1) ? -1.f : 1.f;
+      cost[i][s] = cc[0] * dx + cc[1] * dy + cc[2] * dz;
+    }
+  }
+  int child_at[8], cand_at[8];
+  for (int s = 0; s < 8; ++s)
+    child_at[s] = cand_at[s] = -1;
+  uint32_t used_c = 0u, used_s = 0u;
+  for (int it = 0; it < k; ++it) {
+    float best = 3.4e38f;
+    int bc = -1, bs = -1;
+    for (int i = 0; i < k; ++i) {
+      if (used_c & (1u << i))
+        continue;
+      for (int s = 0; s < 8; ++s) {
+        if (used_s & (1u << s))
+          continue;
+        if (cost[i][s] < best || bc < 0) {
+          best = cost[i][s];
+          bc = i;
+          bs = s;
+        }
+      }
+    }
+    used_c |= 1u << bc;
+    used_s |= 1u << bs;
+    child_at[bs] = ch[bc];
+    cand_at[bs] = bc;
+  }
+  // quantisation grid (double, exact powers of two: outward rounding)
+  uint8_t e[3];
+  double scale[3];
+  for (int a = 0; a < 3; ++a) {
+    const double ext = double(nhi[a]) - double(nlo[a]);
+    int ex = -127;
+    if (ext > 0.0) {
+      ex = int(ceil(log2(ext / 255.0)));
+      while (ldexp(255.0, ex) < ext)
+        ++ex;
+      while (ex > -127 && ldexp(255.0, ex - 1) >= ext)
+        --ex;
+    }
+    ex = min(max(ex, -127), 127);
+    e[a] = uint8_t(ex + 127);
+    scale[a] = ex == -127 ? 0.0 : ldexp(1.0, ex);
+  }
+  // leaf children: single primitives, and internal children of at most
+  // max_leaf primitives (lcount[s] primitives each)
+  uint32_t internal = 0, leaves = 0;
+  uint8_t imask = 0;
+  int lcount[8];
+  for (int s = 0; s < 8; ++s) {
+    lcount[s] = 0;
+    if (child_at[s] < 0)
+      continue;
+    lcount[s] = lc[cand_at[s]];
+    if (lcount[s] == 0) {
+      imask |= uint8_t(1u << s);
+      ++internal;
+    } else {
+      leaves += uint32_t(lcount[s]);
+    }
+  }
+  uint32_t child_base = 0, tri_base = 0;
+  if (internal)
+    child_base = atomicAdd(&c.counters[0], internal);
+  if (leaves)
+    tri_base = atomicAdd(&c.counters[1], leaves);
+  if (child_base + internal > c.node_cap) {
+    atomicExch(&c.counters[3], 1u);
+    return;
+  }
+  uint32_t q_out_base = 0;
+  if (internal)
+    q_out_base = atomicAdd(&c.counters[2], internal);
+  uint8_t meta[8] = {}, q[6][8] = {};
+  uint32_t next_child = child_base, tri_off = 0, qo = q_out_base;
+  for (int s = 0; s < 8; ++s) {
+    const int v = child_at[s];
+    if (v < 0)
+      continue;
+    const float *b = c.nbox + 6 * size_t(v);
+    for (int a = 0; a < 3; ++a) {
+      double lo = 0.0, hi = 0.0;
+      if (scale[a] > 0.0) {
+        lo = floor((double(b[a]) - double(nlo[a])) / scale[a]);
+        hi = ceil((double(b[3 + a]) - double(nlo[a])) / scale[a]);
+      }
+      q[a][s] = uint8_t(fmin(fmax(lo, 0.0), 255.0));
+      q[3 + a][s] = uint8_t(fmin(fmax(hi, 0.0), 255.0));
+    }
+    if (lcount[s] == 0) {
+      meta[s] = 0x80;
+      qout[qo++] = make_uint2(next_child++, uint32_t(v));
+    } else {
+      meta[s] = uint8_t((uint32_t(lcount[s]) << 5) | tri_off);
+      if (c.nchild[v].x < 0) {
+        prims[0] = c.nchild[v].y;
+      } else if (subtree_prims(c.nchild, v, c.max_leaf, prims) != lcount[s]) { // cannot happen
+        atomicExch(&c.counters[3], 2u);
+        return;
+      }
+      for (int j = 0; j < lcount[s]; ++j) {
+        const uint32_t prim = uint32_t(prims[j]);
+        const uint4 vi = c.vidx[prim];
+        const float4 v0 = c.pos[vi.x], v1 = c.pos[vi.y], v2 = c.pos[vi.z];
+        float4 *r = c.tris + 3 * size_t(tri_base + tri_off);
+        r[0] = make_float4(v0.x, v0.y, v0.z, __uint_as_float(prim));
+        r[1] = make_float4(v1.x - v0.x, v1.y - v0.y, v1.z - v0.z, 0.f);
+        r[2] = make_float4(v2.x - v0.x, v2.y - v0.y, v2.z - v0.z, 0.f);
+        ++tri_off;
+      }
+    }
+  }
+  uint32_t *w = c.nodes + size_t(ni) * 20;
+  w[0] = __float_as_uint(nlo[0]);
+  w[1] = __float_as_uint(nlo[1]);
+  w[2] = __float_as_uint(nlo[2]);
+  w[3] = uint32_t(e[0]) | (uint32_t(e[1]) << 8) | (uint32_t(e[2]) << 16) | (uint32_t(imask) << 24);
+  w[4] = child_base;
+  w[5] = tri_base;
+  w[6] = uint32_t(meta[0]) | (uint32_t(meta[1]) << 8) | (uint32_t(meta[2]) << 16) | (uint32_t(meta[3]) << 24);
+  w[7] = uint32_t(meta[4]) | (uint32_t(meta[5]) << 8) | (uint32_t(meta[6]) << 16) | (uint32_t(meta[7]) << 24);
+  for (int r = 0; r < 6; ++r) {
+    w[8 + 2 * r] = uint32_t(q[r][0]) | (uint32_t(q[r][1]) << 8) | (uint32_t(q[r][2]) << 16) |
+        (uint32_t(q[r][3]) << 24);
+    w[9 + 2 * r] = uint32_t(q[r][4]) | (uint32_t(q[r][5]) << 8) | (uint32_t(q[r][6]) << 16) |
+        (uint32_t(q[r][7]) << 24);
+  }
+}
+
+// One wide node per thread, its children chosen by the surface-area program
+// (k_collapse_dp): the root's two subtrees share the 8 slots as the program
+// chose; each (subtree, slots) entry either fills one slot or, when the
+// program opened it for that many slots, becomes two entries whose slots add
+// up to its own, so at most 8 entries are ever pending.
+struct CollapseSah {
+  const uint8_t *split; // CollapseDp::split
+  const uchar4 *info;   // CollapseDp::info
+  uint32_t n;           // primitives (the binary leaves 0..n-1)
+};
+
+__global__ void __launch_bounds__(128) k_collapse_sah(Collapse c, CollapseSah p, const uint2 *__restrict__ qin,
+    uint32_t nq, uint2 *__restrict__ qout)
+{
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq)
+    return;
+  const uint32_t ni = qin[t].x;
+  const int root = int(qin[t].y);
+  int ch[8], lc[8];
+  for (int i = 0; i < 8; ++i)
+    ch[i] = lc[i] = 0;
+  int k = 0;
+  if (uint32_t(root) < p.n) { // a leaf root: one leaf child
+    ch[k] = root;
+    lc[k++] = 1;
+  } else {
+    int stk[8], slots[8], sp = 0;
+    const int split = min(max(int(p.info[uint32_t(root) - p.n].x), 1), 7);
+    stk[sp] = c.nchild[root].y;
+    slots[sp++] = 8 - split;
+    stk[sp] = c.nchild[root].x;
+    slots[sp++] = split;
+    while (sp > 0) {
+      --sp;
+      const int u = stk[sp], j = slots[sp];
+      const bool bin_leaf = uint32_t(u) < p.n;
+      const int open = bin_leaf || j < 2 ? 0 : int(p.split[8 * size_t(uint32_t(u) - p.n) + size_t(j - 1)]);
+      if (open >= 1 && open < j && sp + 2 <= 8) {
+        stk[sp] = c.nchild[u].y;
+        slots[sp++] = j - open;
+        stk[sp] = c.nchild[u].x;
+        slots[sp++] = open;
+        continue;
+      }
+      if (k == 8) { // cannot happen: the entries' slots add up to 8
+        atomicExch(&c.counters[3], 2u);
+        return;
+      }
+      ch[k] = u;
+      if (bin_leaf) {
+        lc[k] = 1;
+      } else {
+        const uchar4 in = p.info[uint32_t(u) - p.n];
+        lc[k] = in.y ? int(in.z) : 0;
+      }
+      ++k;
+    }
+  }
+  write_wide_node(c, ni, ch, lc, k, qout);
+}
+
 struct DevBuf {
   void *p{nullptr};
   ~DevBuf()
@@ -655,7 +958,7 @@ void scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, ui
 }
 
 GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t n, cudaStream_t s, int max_leaf,
-    int radius)
+    int radius, float tri_cost)
 {
   if (n == 0)
     throw std::runtime_error("gpu bvh build: no triangles");
@@ -708,6 +1011,7 @@ GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t
   uint32_t count = n, node_base = n;
   int c = 0;
   uint32_t counts[4];
+  std::vector<uint32_t> iter_base{n}; // the internal nodes each iteration made: [base[i], base[i + 1])
   for (int iter = 0; count > 1; ++iter) {
     const unsigned nb = (count + TILE - 1) / TILE;
     if (radius <= 2)
@@ -733,6 +1037,7 @@ GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t
     if (counts[0] == 0 || counts[1] >= count)
       throw std::runtime_error("gpu bvh build: clustering made no progress");
     node_base += counts[0];
+    iter_base.push_back(node_base);
     count = counts[1];
     c ^= 1;
   }
@@ -756,18 +1061,41 @@ GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t
   ck(cudaMemcpyAsync(ctr.p, c0, sizeof(c0), cudaMemcpyHostToDevice, s), "collapse counters");
   const uint2 first = make_uint2(0u, root);
   ck(cudaMemcpyAsync(q[0].p, &first, sizeof(first), cudaMemcpyHostToDevice, s), "first queue entry");
+  const int leaf_max = std::min(std::max(max_leaf, 1), 3);
+  // the surface-area program, bottom-up one clustering iteration at a time
+  DevBuf dp_cost, dp_split, dp_info;
+  const uint32_t inner = node_base - n;
+  if (tri_cost > 0.f && inner > 0) {
+    alloc(dp_cost, size_t(inner) * 8 * 4, "collapse costs");
+    alloc(dp_split, size_t(inner) * 8, "collapse splits");
+    alloc(dp_info, size_t(inner) * 4, "collapse choices");
+    const CollapseDp d{dp_cost.as<float>(), dp_split.as<uint8_t>(), dp_info.as<uchar4>()};
+    for (size_t i = 0; i + 1 < iter_base.size(); ++i) {
+      const uint32_t lo = iter_base[i], hi = iter_base[i + 1];
+      k_collapse_dp<<<grid_of(hi - lo, 128), 128, 0, s>>>(d, nbox.as<float>(), nchild.as<int2>(), n, lo, hi,
+          tri_cost, leaf_max);
+    }
+    ck(cudaGetLastError(), "collapse program");
+  }
   Collapse col{nbox.as<float>(), nchild.as<int2>(), positions, prim_vidx, nodes_buf.as<uint32_t>(),
-      tris_buf.as<float4>(), ctr.as<uint32_t>(), out.node_cap, std::min(std::max(max_leaf, 1), 3)};
+      tris_buf.as<float4>(), ctr.as<uint32_t>(), out.node_cap, leaf_max};
+  const CollapseSah sah{dp_split.as<uint8_t>(), dp_info.as<uchar4>(), n};
   uint32_t nq = 1, depth = 0;
   int qc = 0;
   while (nq > 0) {
     ++depth;
     if (depth > 1000)
       throw std::runtime_error("gpu bvh build: collapse did not end");
-    k_collapse<<<(nq + 127) / 128, 128, 0, s>>>(col, q[qc].as<uint2>(), nq, q[qc ^ 1].as<uint2>());
+    if (dp_split.p)
+      k_collapse_sah<<<(nq + 127) / 128, 128, 0, s>>>(col, sah, q[qc].as<uint2>(), nq, q[qc ^ 1].as<uint2>());
+    else
+      k_collapse<<<(nq + 127) / 128, 128, 0, s>>>(col, q[qc].as<uint2>(), nq, q[qc ^ 1].as<uint2>());
+    ck(cudaGetLastError(), "collapse launch");
     uint32_t cc[4];
     ck(cudaMemcpyAsync(cc, ctr.p, 16, cudaMemcpyDeviceToHost, s), "read collapse counters");
     ck(cudaStreamSynchronize(s), "collapse level");
+    if (cc[3] == 2)
+      throw std::runtime_error("gpu bvh build: the collapse's surface-area choices are inconsistent");
     if (cc[3])
       throw std::runtime_error("gpu bvh build: node capacity exceeded");
     nq = cc[2];

@@ -17,10 +17,12 @@ struct GpuBvh8 {
 
 // positions: float4 per vertex; prim_vidx: (i0, i1, i2, material) per
 // triangle, both on the device; max_leaf: triangles per leaf child (1..3);
-// radius: clusters searched on each side by the clustering (2..32).
-// Blocks on `s` until the build is done.
+// radius: clusters searched on each side by the clustering (2..32);
+// tri_cost: a triangle test's cost relative to a node visit for the
+// collapse's surface-area program, 0 for the greedy collapse (largest
+// subtrees opened first).  Blocks on `s` until the build is done.
 GpuBvh8 build_bvh8_gpu(const float4 *positions, const uint4 *prim_vidx, uint32_t triangle_count, cudaStream_t s,
-    int max_leaf = 1, int radius = 16);
+    int max_leaf = 1, int radius = 16, float tri_cost = 0.f);
 
 // Exclusive scan of n words (in == out allowed) on the device, in three
 // launches on `s`; *total (if not null) receives the sum.  scratch holds

@@ -1329,7 +1329,7 @@ std::string DeviceScene::upload(const HostScene &h, cudaStream_t s)
   if (h.bvh_on_gpu) {
     try {
       const GpuBvh8 g = build_bvh8_gpu(d.positions, d.prim_vidx, uint32_t(h.prim_vidx.size() / 4), s,
-          tuning().gpu_max_leaf, tuning().ploc_radius);
+          tuning().gpu_max_leaf, tuning().ploc_radius, 0.01f * float(tuning().collapse_tri_cost));
       allocations.push_back(g.nodes);
       allocations.push_back(g.tris);
       bytes += size_t(g.node_cap) * 80 + size_t(g.tri_count) * 48;

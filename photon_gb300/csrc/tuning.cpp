@@ -46,6 +46,7 @@ const Key *keys(size_t &n)
       {"gpu_bvh", "PHC_TUNE_GPU_BVH", 0, 1, nullptr, &g_tuning.gpu_bvh},
       {"gpu_max_leaf", "PHC_TUNE_GPU_MAX_LEAF", 1, 3, nullptr, &g_tuning.gpu_max_leaf},
       {"ploc_radius", "PHC_TUNE_PLOC_RADIUS", 2, 32, nullptr, &g_tuning.ploc_radius},
+      {"collapse_tri_cost", "PHC_TUNE_COLLAPSE_TRI_COST", 0, 10000, nullptr, &g_tuning.collapse_tri_cost},
       {"gpu_tables", "PHC_TUNE_GPU_TABLES", 0, 1, nullptr, &g_tuning.gpu_tables},
       {"texels_u8", "PHC_TUNE_TEXELS_U8", 0, 1, nullptr, &g_tuning.texels_u8},
       {"wave_trip_cap", "PHC_TUNE_WAVE_TRIP_CAP", 1, int64_t(1) << 30, &g_tuning.wave_trip_cap, nullptr},

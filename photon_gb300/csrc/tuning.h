@@ -33,6 +33,8 @@ struct Tuning {
   int gpu_bvh{1};                    // build the BVH8 on the GPU (bvh_gpu.cu), read at scene build
   int gpu_max_leaf{2};               // triangles per leaf child of the GPU-built BVH8 (1..3), read at scene build
   int ploc_radius{4};                // clusters searched on each side by the GPU build's clustering (2..32)
+  int collapse_tri_cost{30};         // GPU build: triangle test / node visit cost in percent for the collapse's
+                                     // surface-area program; 0: greedy collapse (read at scene build)
   int gpu_tables{1};                 // build majorant grids, env / emissive CDFs and 8-bit texels on the GPU (scene_tables.cu), read at scene build
   int texels_u8{1};                  // keep samplers whose texels are all k / 255 as 8-bit RGBA, read at scene build
   int64_t wave_trip_cap{1 << 24};    // loop trips after which a persistent wave kernel's warp stops with

@@ -59,7 +59,7 @@ extern "C" int ht_trace(const float *pos, uint64_t nv, const uint32_t *idx, uint
 namespace phc {
 // The harness never uploads a scene, so the GPU builder (bvh_gpu.cu, compiled
 // by nvcc) is not linked in; scene_build.cpp's upload refers to it.
-GpuBvh8 build_bvh8_gpu(const float4 *, const uint4 *, uint32_t, cudaStream_t, int, int)
+GpuBvh8 build_bvh8_gpu(const float4 *, const uint4 *, uint32_t, cudaStream_t, int, int, float)
 {
   throw std::runtime_error("the host harness builds no BVH on the GPU");
 }

@@ -81,13 +81,13 @@ def test_tuning_round_trip(photon):
     for key, val in (("wave_paths", 1 << 20), ("trace_refill", 12), ("split_shade", 0), ("batch_wave_paths", 99999),
                      ("gpu_max_leaf", 3), ("ploc_radius", 16), ("split_volume", 0), ("gpu_tables", 0),
                      ("texels_u8", 0), ("shade_classes", 0), ("vol_refill", 4), ("vol_passes", 2), ("adjoint_sort", 0),
-                     ("class_threshold", 1 << 20)):
+                     ("class_threshold", 1 << 20), ("collapse_tri_cost", 30)):
         old = p.tuning_get(key)
         p.tuning_set(key, val)
         assert p.tuning_get(key) == val
         p.tuning_set(key, old)
     for key, bad in (("trace_refill", 0), ("gpu_max_leaf", 4), ("ploc_radius", 1), ("ploc_radius", 33),
-                     ("split_volume", 2)):
+                     ("split_volume", 2), ("collapse_tri_cost", -1), ("collapse_tri_cost", 10001)):
         old = p.tuning_get(key)
         with pytest.raises(ValueError):
             p.tuning_set(key, bad)

@@ -16,16 +16,21 @@ from tests.parity import MIN_PATH_FRACTION, close_fraction
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=[(1, 4), (2, 4), (3, 4), (2, 2), (2, 32)], ids=lambda p: f"leaf{p[0]}-radius{p[1]}")
+@pytest.fixture(params=[(1, 4, 0), (2, 4, 0), (3, 4, 0), (2, 2, 0), (2, 32, 0), (1, 4, 30), (2, 4, 30), (3, 4, 30),
+                        (2, 4, 5), (2, 4, 300)],
+                ids=lambda p: f"leaf{p[0]}-radius{p[1]}-tricost{p[2]}")
 def gpu_bvh(photon, request):
     """The GPU builder, with leaf children of up to 1, 2 or 3 triangles
-    (tuning key gpu_max_leaf) and clustering radii 2, 4 and 32 (ploc_radius)."""
+    (tuning key gpu_max_leaf), clustering radii 2, 4 and 32 (ploc_radius),
+    and the greedy collapse or the surface-area collapse at triangle costs
+    of 0.05, 0.3 and 3 node visits (collapse_tri_cost)."""
     from photon_gb300 import tuning_get, tuning_set
-    keys = ("gpu_bvh", "gpu_max_leaf", "ploc_radius")
+    keys = ("gpu_bvh", "gpu_max_leaf", "ploc_radius", "collapse_tri_cost")
     old = {k: tuning_get(k) for k in keys}
     tuning_set("gpu_bvh", 1)
     tuning_set("gpu_max_leaf", request.param[0])
     tuning_set("ploc_radius", request.param[1])
+    tuning_set("collapse_tri_cost", request.param[2])
     yield
     for k, v in old.items():
         tuning_set(k, v)
