@@ -32,7 +32,7 @@ struct Tuning {
   int64_t sort_threshold{1 << 18};   // sort the hit queue by material when it holds this many hits (0: never)
   int gpu_bvh{1};                    // build the BVH8 on the GPU (bvh_gpu.cu), read at scene build
   int gpu_max_leaf{2};               // triangles per leaf child of the GPU-built BVH8 (1..3), read at scene build
-  int ploc_radius{4};                // clusters searched on each side by the GPU build's clustering (2..32)
+  int ploc_radius{8};                // clusters searched on each side by the GPU build's clustering (2..32)
   int collapse_tri_cost{30};         // GPU build: triangle test / node visit cost in percent for the collapse's
                                      // surface-area program; 0: greedy collapse (read at scene build)
   int gpu_tables{1};                 // build majorant grids, env / emissive CDFs and 8-bit texels on the GPU (scene_tables.cu), read at scene build
