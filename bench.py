@@ -49,16 +49,16 @@ TRI_BYTES = 48    # one triangle record (v0, e1, e2 as float4)
 RAY_BYTES = 32    # origin+tmin, direction+tmax
 HIT_BYTES = 16    # t, prim, u, v
 # DRAM bytes per closest-hit ray of k_trace, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum = 281.65 + 144.30 MB over the
+# (dram__bytes_read.sum + dram__bytes_write.sum = 282.24 + 144.83 MB over the
 # 8,388,608 camera rays of bounce iteration 0 at 8 spp; the node and triangle
 # reads stay in L2, so the traffic is the ray/hit queues and grows with the
 # ray count).  The roofline's `traffic` scales it to the average launch.
-TRACE_DRAM_BYTES_PER_RAY = (281.65e6 + 144.30e6) / 8388608
+TRACE_DRAM_BYTES_PER_RAY = (282.24e6 + 144.83e6) / 8388608
 # Instruction issue of k_trace from the same capture: warp instructions per
 # camera ray (smsp__inst_executed.sum / rays), the fraction of issue slots
 # used, and active threads per warp instruction.
-TRACE_ISSUE = {"warp_instructions_per_ray": 1.665e9 / 8388608, "issue_active": 0.789,
-               "threads_per_warp_instruction": 19.7,
+TRACE_ISSUE = {"warp_instructions_per_ray": 1.597e9 / 8388608, "issue_active": 0.793,
+               "threads_per_warp_instruction": 20.0,
                "source": "ncu --set full capture of k_trace, bounce iteration 0 of the 500K workload at 8 spp "
                          "(profiles/k_trace_procedural_500k.md)"}
 # Shading: algorithmic bytes per shaded hit path: queue and sorted index 8,
@@ -759,8 +759,9 @@ def run_ours(args, world, rank, local):
         "issue": TRACE_ISSUE,
         "traffic": (TRACE_DRAM_BYTES_PER_RAY * prof["closest_rays"] / max(1, kcount["trace_closest"])
                     if dom != "trace_shadow" else None),
-        "traffic_source": "ncu capture of k_trace (profiles/k_trace_procedural_500k.md): 51.5 DRAM bytes per "
-                          "ray, times the rays of the average launch of this frame",
+        "traffic_source": f"ncu capture of k_trace (profiles/k_trace_procedural_500k.md): "
+                          f"{TRACE_DRAM_BYTES_PER_RAY:.1f} DRAM bytes per ray, times the rays of the average "
+                          "launch of this frame",
         "algorithmic_bytes_per_launch": bytes_alg / max(1, kcount["trace_closest"]),
         "bytes_per_ray": bytes_alg / max(1, prof["closest_rays"] if dom != "trace_shadow" else prof["shadow_rays"]),
         "nodes_per_ray": prof["node_visits"] / max(1, prof["closest_rays"]),
