@@ -41,6 +41,7 @@
 #include <string>
 #include <vector>
 
+#include "bvh_collapse.cuh"
 #include "bvh_gpu.h"
 
 namespace phc {
@@ -624,79 +625,9 @@ __global__ void __launch_bounds__(128) k_collapse(Collapse c, const uint2 *__res
 }
 
 // ---------------------------------------------------------------- stage 4a
-// The collapse's surface-area program.  cost(u, j), for j = 1..8: the least
-// expected cost of covering binary subtree u with at most j child slots of
-// its wide parent, each slot holding a descendant w of u as a leaf child
-// (area(w) x primitives x tri_cost, when it has at most max_leaf primitives)
-// or as a wide inner node (area(w) x 1 + the cheapest cover of w's two
-// subtrees by 8 slots); for j >= 2 u may also be opened, its two subtrees
-// sharing the j slots.  A binary leaf (one primitive) is always a one-
-// primitive leaf child.  One launch per clustering iteration's new nodes:
-// their children come from earlier iterations, so they are final.
-struct CollapseDp {
-  float *cost;     // 8 per internal node: cost(v, j + 1)
-  uint8_t *split;  // 8 per internal node, entry j for j + 1 slots: 0 = v fills one slot, k = v opened, k slots
-                   // for its left subtree
-  uchar4 *info;    // per internal node: x = the split of v as a wide inner node, y = 1 when v fills one slot as a
-                   // leaf child, z = its primitives (at most 255)
-};
-
-__device__ __forceinline__ float dp_cost(const CollapseDp &d, const float *nbox, uint32_t n, int u, int j, float ct)
-{
-  return uint32_t(u) < n ? node_area(nbox, u) * ct : d.cost[8 * size_t(uint32_t(u) - n) + j];
-}
-
-// The program's entries of internal node v (its children's are final).
-__device__ void collapse_dp_node(const CollapseDp &d, const float *__restrict__ nbox, const int2 *__restrict__ nchild,
-    uint32_t n, uint32_t v, float ct, int max_leaf)
-{
-  const int2 c = nchild[v];
-  float cl[8], cr[8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    cl[j] = dp_cost(d, nbox, n, c.x, j, ct);
-    cr[j] = dp_cost(d, nbox, n, c.y, j, ct);
-  }
-  const uint32_t pl = uint32_t(c.x) < n ? 1u : d.info[uint32_t(c.x) - n].z;
-  const uint32_t pr = uint32_t(c.y) < n ? 1u : d.info[uint32_t(c.y) - n].z;
-  const uint32_t p = min(pl + pr, 255u);
-  // open v: the cheapest share of j slots between its subtrees (j = 2..8)
-  float sc[8];
-  uint8_t sk[8];
-  sc[0] = 3.4e38f;
-  sk[0] = 0;
-#pragma unroll
-  for (int j = 2; j <= 8; ++j) {
-    float best = 3.4e38f;
-    int bk = 1;
-#pragma unroll
-    for (int k = 1; k < j; ++k) {
-      const float x = cl[k - 1] + cr[j - k - 1];
-      if (x < best) {
-        best = x;
-        bk = k;
-      }
-    }
-    sc[j - 1] = best;
-    sk[j - 1] = uint8_t(bk);
-  }
-  const float a = node_area(nbox, int(v));
-  const float c_inner = a + sc[7];
-  const bool leaf = p <= uint32_t(max_leaf) && a * float(p) * ct <= c_inner;
-  const float self = leaf ? a * float(p) * ct : c_inner;
-  float *co = d.cost + 8 * size_t(v - n);
-  uint8_t *sp = d.split + 8 * size_t(v - n);
-  co[0] = self;
-  sp[0] = 0;
-#pragma unroll
-  for (int j = 1; j < 8; ++j) {
-    const bool open = sc[j] < self;
-    co[j] = open ? sc[j] : self;
-    sp[j] = open ? sk[j] : 0;
-  }
-  d.info[v - n] = make_uchar4(sk[7], leaf ? 1 : 0, uint8_t(p), 0);
-}
-
+// The collapse's surface-area program (bvh_collapse.cuh), one launch per
+// clustering iteration's new nodes: their children come from earlier
+// iterations, so their entries are final.
 __global__ void __launch_bounds__(128) k_collapse_dp(CollapseDp d, const float *__restrict__ nbox,
     const int2 *__restrict__ nchild, uint32_t n, uint32_t lo, uint32_t hi, float ct, int max_leaf)
 {
@@ -859,10 +790,7 @@ __device__ void write_wide_node(const Collapse &c, uint32_t ni, const int *ch, c
 }
 
 // One wide node per thread, its children chosen by the surface-area program
-// (k_collapse_dp): the root's two subtrees share the 8 slots as the program
-// chose; each (subtree, slots) entry either fills one slot or, when the
-// program opened it for that many slots, becomes two entries whose slots add
-// up to its own, so at most 8 entries are ever pending.
+// (k_collapse_dp, then sah_children).
 struct CollapseSah {
   const uint8_t *split; // CollapseDp::split
   const uchar4 *info;   // CollapseDp::info
@@ -880,42 +808,16 @@ __global__ void __launch_bounds__(128) k_collapse_sah(Collapse c, CollapseSah p,
   int ch[8], lc[8];
   for (int i = 0; i < 8; ++i)
     ch[i] = lc[i] = 0;
-  int k = 0;
+  int k = 1;
   if (uint32_t(root) < p.n) { // a leaf root: one leaf child
-    ch[k] = root;
-    lc[k++] = 1;
+    ch[0] = root;
+    lc[0] = 1;
   } else {
-    int stk[8], slots[8], sp = 0;
-    const int split = min(max(int(p.info[uint32_t(root) - p.n].x), 1), 7);
-    stk[sp] = c.nchild[root].y;
-    slots[sp++] = 8 - split;
-    stk[sp] = c.nchild[root].x;
-    slots[sp++] = split;
-    while (sp > 0) {
-      --sp;
-      const int u = stk[sp], j = slots[sp];
-      const bool bin_leaf = uint32_t(u) < p.n;
-      const int open = bin_leaf || j < 2 ? 0 : int(p.split[8 * size_t(uint32_t(u) - p.n) + size_t(j - 1)]);
-      if (open >= 1 && open < j && sp + 2 <= 8) {
-        stk[sp] = c.nchild[u].y;
-        slots[sp++] = j - open;
-        stk[sp] = c.nchild[u].x;
-        slots[sp++] = open;
-        continue;
-      }
-      if (k == 8) { // cannot happen: the entries' slots add up to 8
-        atomicExch(&c.counters[3], 2u);
-        return;
-      }
-      ch[k] = u;
-      if (bin_leaf) {
-        lc[k] = 1;
-      } else {
-        const uchar4 in = p.info[uint32_t(u) - p.n];
-        lc[k] = in.y ? int(in.z) : 0;
-      }
-      ++k;
-    }
+    k = sah_children(c.nchild, p.split, p.info, p.n, root, ch, lc);
+  }
+  if (k < 0) {
+    atomicExch(&c.counters[3], 2u);
+    return;
   }
   write_wide_node(c, ni, ch, lc, k, qout);
 }
