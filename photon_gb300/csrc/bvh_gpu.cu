@@ -639,6 +639,9 @@ __global__ void __launch_bounds__(128) k_collapse_dp(CollapseDp d, const float *
 // One wide node from its k candidates ch[i] (lc[i] primitives as a leaf
 // child, 0 for an inner node): octant slots, quantised child boxes, the leaf
 // records and the queue entries of the inner children, as k_collapse does.
+// k_collapse keeps its own copy of these steps: a build that ran both rules
+// in one kernel, choosing by a flag, lost leaf children on the device while
+// its host compilation built correct nodes.
 __device__ void write_wide_node(const Collapse &c, uint32_t ni, const int *ch, const int *lc, int k, uint2 *qout)
 {
   int prims[3];
